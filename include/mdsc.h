@@ -1,0 +1,205 @@
+/*
+ * mdsc.h -- C ABI of the GB300 (sm_103a) MD-step library for polydisperse
+ * dipolar spherocylinders.  Drop-in for the hot path of mdSpherocyl.
+ *
+ * The reference's boundary is the set of free functions in
+ * v25/functions.hpp:15-54 that v25/main.cpp calls once per step from one
+ * host thread (force_sc, force_dipR, force_dipK, ext_field, self_ener,
+ * moveX, moveP, moveTher, neigh_list, check_list, clust_conf).  Each of
+ * them has an entry point below that does the same work on the GPU, and
+ * mdsc_step() runs the whole loop body (v25/main.cpp:558-708) as one
+ * captured CUDA graph.
+ *
+ * Plain C types only: pointers and sizes, no exceptions across the ABI.
+ * All state stays resident in GPU memory between calls; the host sees
+ * scalars, except when it uploads or downloads a system.
+ *
+ * One handle (mdsc_batch) holds one or many independent systems ("batch");
+ * every entry point works on all of them at once and returns per-system
+ * results in arrays indexed by system.  A batch of one system is the plain
+ * path.  Calls on one handle are not thread-safe; different handles are.
+ *
+ * Units and conventions are the reference's: sigma = epsilon = k_B = 1; O is
+ * the 3x3 orientation matrix stored row-major with rows = body axes in the
+ * lab frame (row 2 = rod axis, v25/classes.hpp:74); angular momentum l in
+ * the lab frame; dipoles are given in the body frame as (offset along the
+ * rod axis, direction x, y, z, moment) (v25/classes.cpp:148-173).
+ */
+#ifndef MDSC_H
+#define MDSC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MDSC_ABI_VERSION 1
+#define MDSC_MAX_DIPOLES 4 /* dipoles per particle */
+
+typedef enum {
+  MDSC_OK = 0,
+  MDSC_ERR_BAD_ARG = 1,
+  MDSC_ERR_CUDA = 2,
+  MDSC_ERR_OOM = 3,
+  /* force_sc's abort (v25/functions.cpp:1454-1473): a listed pair with
+     segment distance^2 < 0.49 sigma^2 or greater than its centre distance^2 */
+  MDSC_ERR_OVERLAP = 4,
+  MDSC_ERR_NAN = 5,
+  /* a dipole pair beyond the reference's table range r > 100.1 sigma
+     (v25/functions.cpp:1563,1608-1614; guarded by L_min <= 200 at
+     v25/main.cpp:420-425) */
+  MDSC_ERR_TABLE_RANGE = 6,
+  MDSC_ERR_LIST_OVERFLOW = 7,
+  MDSC_ERR_NO_DEVICE = 8,
+  MDSC_ERR_TOO_LARGE = 9,
+  MDSC_ERR_STATE = 10
+} mdsc_status;
+
+/* Everything that defines one system besides its particle state: the
+   input.txt parameters the hot path uses (v25/functions.cpp:10-87). */
+typedef struct {
+  int n;             /* particles */
+  int nd;            /* dipoles per particle, 0..MDSC_MAX_DIPOLES */
+  double box[3];     /* box edges L_x, L_y, L_z */
+  double alpha;      /* Ewald convergence parameter ("Convergence param(a)") */
+  int K_max;         /* k-vectors n_x, n_y, n_z in [0, K_max-1] ("No. of Kvectors") */
+  int ksq_max;       /* 0: the reference's full cube; > 0: keep |n|^2 <= ksq_max only */
+  double sr_cut;     /* "Cutoff dist(SRange)"; 0 -> L_min/2 - d_min (v25/main.cpp:398-399) */
+  double dt;         /* time step */
+  double temp;       /* thermostat temperature */
+  double Q;          /* thermostat mass */
+  double gamma;      /* thermostat "shear rate" (Langevin noise on xi); 0 = deterministic */
+  double xi0;        /* initial thermostat coordinate (0 in v25, 1 in v25/v251) */
+  double B[3];       /* external field */
+  double min_s;      /* cluster proximity distance ("proximity dist.") */
+  int cl_fr;         /* clustering frequency in steps; 0 = never */
+  unsigned long thermo_seed[2]; /* MT19937 seeds of the two thermostats (1, 2 in the driver) */
+  unsigned long cluster_seed;   /* MT19937 seed of the cluster generator (1 in the driver) */
+  unsigned long cluster_skip;   /* draws already taken from it (e.g. by initialisation) */
+} mdsc_system_desc;
+
+/* Host-side structure-of-arrays view of one system (FP64).  Shapes:
+   r, p, l, F, T: n*3; O: n*9; len, dia, mass: n; dip: n*nd*5; clust: n. */
+typedef struct {
+  double* r;
+  double* p;
+  double* O;
+  double* l;
+  double* F;
+  double* T;
+  const double* len;
+  const double* dia;
+  const double* mass;
+  const double* dip;
+  int* clust;
+} mdsc_host_state;
+
+/* Per-system results of the last step, as totals over the system (the
+   driver divides by N and V, v25/main.cpp:626-649). */
+typedef struct {
+  double K[2];      /* translational, rotational kinetic energy (moveP) */
+  double U_ss, W_ss;
+  double U_dipR, U_dipK, U_ext, U_self;
+  double PT_kin[9], PT_ss[9], PT_dipR[9], PT_dipK[9];
+  double xi[2];     /* thermostat coordinates after the step */
+  long long step;   /* steps taken so far */
+  int status;       /* mdsc_status of this system */
+  int n_clusters;   /* clusters found at the last clustering step */
+  int list_builds;  /* neighbour-list rebuilds so far */
+  int pad;
+} mdsc_observables;
+
+typedef struct mdsc_batch mdsc_batch;
+
+/* ---- lifetime -------------------------------------------------------- */
+/* Creates a batch of nsys systems on CUDA device `device` and allocates all
+   its GPU memory.  The per-system tables the reference builds once
+   (tabul, v25/functions.cpp:1680-1704; wave_v, :1963-1990) are set up here. */
+mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mdsc_batch** out);
+mdsc_status mdsc_destroy(mdsc_batch* b);
+int mdsc_num_systems(const mdsc_batch* b);
+/* bytes of GPU memory the batch holds */
+size_t mdsc_device_bytes(const mdsc_batch* b);
+/* GPU memory a batch of these systems would need, without creating it */
+size_t mdsc_estimate_bytes(const mdsc_system_desc* descs, int nsys);
+/* human-readable detail of the last error on this handle */
+mdsc_status mdsc_last_error(const mdsc_batch* b, char* buf, size_t len);
+
+/* ---- state transfer (host SoA <-> GPU) -------------------------------- */
+/* Uploads system `sys`.  Shape arrays (len, dia, mass, dip) are read on
+   every upload; F and T may be NULL (then zero).  Rebuilds the
+   neighbour list and the derived single-precision copies. */
+mdsc_status mdsc_upload(mdsc_batch* b, int sys, const mdsc_host_state* s);
+/* Downloads r, p, O, l, F, T and (if non-NULL) clust of system `sys`. */
+mdsc_status mdsc_download(mdsc_batch* b, int sys, mdsc_host_state* s);
+/* Uploads / downloads all systems with one host->device (device->host)
+   copy each way; arrays are the concatenation of every system's arrays. */
+mdsc_status mdsc_upload_all(mdsc_batch* b, const mdsc_host_state* packed);
+mdsc_status mdsc_download_all(mdsc_batch* b, mdsc_host_state* packed);
+/* Thermostat state: xi, stored normal (v25/classes.hpp:147-151). */
+mdsc_status mdsc_set_thermostat(mdsc_batch* b, int sys, const double xi[2], const double strn[2]);
+
+/* ---- the reference's hot-path functions, on every system --------------- */
+/* Zero F and T (v25/main.cpp:582-588). */
+mdsc_status mdsc_zero_forces(mdsc_batch* b);
+/* force_sc (v25/functions.hpp:35-36, v25/functions.cpp:1397-1553): WCA
+   core forces and torques over the neighbour list, accumulated into F, T.
+   U, W: nsys each; PT: nsys*9.  Returns MDSC_ERR_OVERLAP like the
+   reference's false. */
+mdsc_status mdsc_force_sc(mdsc_batch* b, double* U, double* W, double* PT);
+/* force_dipR (v25/functions.hpp:37-38, v25/functions.cpp:1555-1678):
+   real-space Ewald over all minimum-image dipole pairs, accumulated. */
+mdsc_status mdsc_force_dipR(mdsc_batch* b, double* U, double* PT);
+/* force_dipK (v25/functions.hpp:39-40, v25/functions.cpp:1706-1961):
+   reciprocal-space Ewald, accumulated. */
+mdsc_status mdsc_force_dipK(mdsc_batch* b, double* U, double* PT);
+/* ext_field (v25/functions.hpp:41, v25/functions.cpp:1992-2025): torques
+   accumulated, energies out. */
+mdsc_status mdsc_ext_field(mdsc_batch* b, double* U);
+/* self_ener (v25/functions.hpp:42, v25/functions.cpp:2027-2069). */
+mdsc_status mdsc_self_ener(mdsc_batch* b, double* U);
+/* moveX (v25/functions.hpp:47, v25/functions.cpp:2071-2092). */
+mdsc_status mdsc_moveX(mdsc_batch* b);
+/* moveP (v25/functions.hpp:48-49, v25/functions.cpp:2094-2184); xi: nsys*2
+   thermostat coordinates; K: nsys*2; PT: nsys*9. */
+mdsc_status mdsc_moveP(mdsc_batch* b, const double* xi, int last, double* K, double* PT);
+/* Spherocyl::renorm for every particle (v25/classes.cpp:307-325). */
+mdsc_status mdsc_renorm(mdsc_batch* b);
+/* neigh_list (v25/functions.hpp:28-29, v25/functions.cpp:1298-1334):
+   rebuild every system's Verlet list now. */
+mdsc_status mdsc_neigh_list(mdsc_batch* b);
+/* check_list (v25/functions.hpp:31-34, v25/functions.cpp:1356-1394):
+   rebuild[s] = 1 where the skin was crossed since the last build. */
+mdsc_status mdsc_check_list(mdsc_batch* b, int* rebuild);
+/* clust_conf (v25/functions.hpp:104-105, v25/functions.cpp:3282-3324):
+   labels of system `sys` with the reference's numbering, drawing from the
+   system's cluster generator.  labels: n ints (may be NULL). */
+mdsc_status mdsc_clust_conf(mdsc_batch* b, int sys, int* labels, int* n_clusters);
+
+/* ---- the fused step ---------------------------------------------------- */
+/* Advances every system by nsteps steps of the reference's loop body
+   (renorm every 100 steps, moveTher 0, moveP, moveTher 1, moveX, forces,
+   ext_field, moveP, moveTher 2, list check, clustering every cl_fr steps).
+   Observables of the last step go to obs (nsys entries; may be NULL).
+   Thermostat noise is drawn on the host from each system's MT19937 pair
+   exactly as moveTher does (v25/functions.cpp:2193-2213). */
+mdsc_status mdsc_step(mdsc_batch* b, int nsteps, mdsc_observables* obs);
+/* Observables of the last step without stepping. */
+mdsc_status mdsc_observe(mdsc_batch* b, mdsc_observables* obs);
+
+/* ---- instrumentation --------------------------------------------------- */
+/* Number of kernel launches the last mdsc_step issued per step, and the
+   CUDA stream the batch runs on (a cudaStream_t). */
+int mdsc_launches_per_step(const mdsc_batch* b);
+void* mdsc_stream(const mdsc_batch* b);
+/* Average device time (ms) per launch of each kernel over the last
+   mdsc_profile_steps call: names and times in the order of `names`. */
+mdsc_status mdsc_profile_steps(mdsc_batch* b, int nsteps, int max_kernels, char* names,
+                               size_t name_stride, double* ms_per_launch, int* n_kernels);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

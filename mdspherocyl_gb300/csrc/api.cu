@@ -1,0 +1,1133 @@
+// Host implementation of the C ABI in include/mdsc.h: batch layout, memory,
+// the CUDA-graph step, thermostat noise and cluster-label replay.
+#include <algorithm>
+#include <cmath>
+#include <cstddef>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "host_util.hpp"
+#include "mdsc.h"
+#include "mdsc_dev.cuh"
+
+namespace mdsc {
+void launch_real_pairs(const Batch& b, bool multi, cudaStream_t s);
+void launch_kspace(const Batch& b, int maxnd, const int4* kwork, int nkwork, const int2* kowner,
+                   double* kE, cudaStream_t s);
+void launch_derive(const Batch& b, cudaStream_t s);
+void launch_integrate_first(const Batch& b, cudaStream_t s);
+void launch_finalize(const Batch& b, int mode, cudaStream_t s);
+void launch_reduce_obs(const Batch& b, int mode, cudaStream_t s);
+void launch_movex(const Batch& b, cudaStream_t s);
+void launch_renorm(const Batch& b, cudaStream_t s);
+void launch_movep(const Batch& b, const double* xi, int last, cudaStream_t s);
+void launch_list_build(const Batch& b, int force_all, cudaStream_t s);
+void launch_wca(const Batch& b, cudaStream_t s);
+void launch_cluster_bonds(const Batch& b, cudaStream_t s);
+void launch_cluster_hook(const Batch& b, cudaStream_t s);
+void launch_cluster_compress(const Batch& b, cudaStream_t s);
+void launch_reset_iter(const Batch& b, cudaStream_t s);
+void launch_kspace_parts(const Batch& b, int maxnd, const int4* kwork, int nkwork, const int2* kowner,
+                         double* kE, int part, cudaStream_t s);
+}  // namespace mdsc
+
+using namespace mdsc;
+
+namespace {
+
+constexpr int kNoiseChunk = 256;  // steps of thermostat noise per upload
+// the reference's table covers r <= 0.5 * 200.2 (v25/functions.cpp:1563,1681)
+constexpr double kTableRmax = 0.5 * 200 * 1.001;
+constexpr double kLh = 0.5 * (200 * 1.001) / 32768;
+
+struct Layout {
+  std::vector<SysDev> sys;
+  std::vector<int4> tiles, kn, kwork;
+  std::vector<float4> kv;
+  std::vector<double> kval, kpre;
+  std::vector<int2> blk, kowner;
+  int ntot = 0, ndtot = 0, nktot = 0, maxnd = 0;
+  long long rpart = 0, kpart = 0;
+  bool multi = false;
+};
+
+// distinct +-k representatives of the reference's cube (v25/functions.cpp:1725-1744)
+void k_vectors(const mdsc_system_desc& d, std::vector<int4>& kn) {
+  const int K = d.K_max;
+  for (int nz = 0; nz < K; ++nz)
+    for (int ny = -(K - 1); ny < K; ++ny)
+      for (int nx = -(K - 1); nx < K; ++nx) {
+        const bool half = nz > 0 || (nz == 0 && ny > 0) || (nz == 0 && ny == 0 && nx > 0);
+        if (!half) continue;
+        if (d.ksq_max > 0 && nx * nx + ny * ny + nz * nz > d.ksq_max) continue;
+        kn.push_back(make_int4(nx, ny, nz, 0));
+      }
+}
+
+std::string check_desc(const mdsc_system_desc& d, int s) {
+  char buf[256];
+  if (d.n < 0 || d.nd < 0 || d.nd > MDSC_MAX_DIPOLES) {
+    snprintf(buf, sizeof buf, "system %d: n=%d nd=%d out of range", s, d.n, d.nd);
+    return buf;
+  }
+  for (int a = 0; a < 3; ++a)
+    if (!(d.box[a] > 0)) {
+      snprintf(buf, sizeof buf, "system %d: box edge %d not positive", s, a);
+      return buf;
+    }
+  if (d.K_max < 1 || d.alpha <= 0 || d.dt <= 0 || d.Q <= 0) {
+    snprintf(buf, sizeof buf, "system %d: K_max, alpha, dt and Q must be positive", s);
+    return buf;
+  }
+  const double hd = 0.5 * std::sqrt(d.box[0] * d.box[0] + d.box[1] * d.box[1] + d.box[2] * d.box[2]);
+  if (hd >= kTableRmax) {
+    snprintf(buf, sizeof buf,
+             "system %d: half box diagonal %.3f exceeds the reference's real-space table (r <= %.1f)",
+             s, hd, kTableRmax);
+    return buf;
+  }
+  return "";
+}
+
+void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
+  Lo.sys.resize(nsys);
+  int part = 0, dip = 0, blk = 0;
+  long long pp = 0, kp = 0;
+  for (int s = 0; s < nsys; ++s) {
+    const mdsc_system_desc& d = descs[s];
+    SysDev& P = Lo.sys[s];
+    memset(&P, 0, sizeof P);
+    P.n = d.n;
+    P.nd = d.nd;
+    P.ndip = d.n * d.nd;
+    P.part_off = part;
+    P.dip_off = dip;
+    P.nstrip = cdiv(P.ndip, kTile);
+    P.pp_off = pp;
+    pp += (long long)P.nstrip * P.nstrip * 6 * kTile;
+    P.tile_off = (int)Lo.tiles.size();
+    for (int I = 0; I < P.nstrip; ++I)
+      for (int J = I; J < P.nstrip; ++J) Lo.tiles.push_back(make_int4(s, I, J, 0));
+    P.ntile = (int)Lo.tiles.size() - P.tile_off;
+    // k-vectors and their prefactors (wave_v, v25/functions.cpp:1963-1990)
+    P.k_off = (int)Lo.kn.size();
+    std::vector<int4> kn;
+    if (d.nd > 0) k_vectors(d, kn);
+    const double V = d.box[0] * d.box[1] * d.box[2];
+    const double c = 4. * d.alpha * d.alpha;
+    const double a4 = 1. / (4. * d.alpha);
+    for (const int4& n : kn) {
+      const double kx = 2. * M_PI / d.box[0] * n.x, ky = 2. * M_PI / d.box[1] * n.y,
+                   kz = 2. * M_PI / d.box[2] * n.z;
+      const double ksq = kx * kx + ky * ky + kz * kz;
+      const double KK = 4. * M_PI * std::exp(-ksq / c) / ksq;
+      const double val = 2. * KK / V;
+      Lo.kn.push_back(n);
+      Lo.kv.push_back(make_float4((float)kx, (float)ky, (float)kz, (float)val));
+      Lo.kval.push_back(val);
+      Lo.kpre.push_back(2 * (a4 + 1. / ksq));  // pval (v25/functions.cpp:1715,1738)
+      Lo.kowner.push_back(make_int2(s, (int)(Lo.kn.size() - 1 - P.k_off)));
+    }
+    P.nk = (int)kn.size();
+    P.nkchunk = P.nk > 0 ? cdiv(d.n, kKChunk) : 0;
+    P.kchunk_off = (int)kp;
+    kp += (long long)P.nkchunk * P.nk;
+    for (int ch = 0; ch < P.nkchunk; ++ch)
+      for (int kt = 0; kt < cdiv(P.nk, kKBlock); ++kt) Lo.kwork.push_back(make_int4(s, ch, kt, 0));
+    P.blk_off = blk;
+    P.nblk = cdiv(d.n, kPartBlock);
+    for (int k = 0; k < P.nblk; ++k) Lo.blk.push_back(make_int2(s, part + k * kPartBlock));
+    blk += P.nblk;
+    P.cl_fr = d.cl_fr;
+    for (int a = 0; a < 3; ++a) {
+      P.L[a] = d.box[a];
+      P.invL[a] = 1.0 / d.box[a];
+      P.Lfix[a] = (float)(d.box[a] / 4294967296.0);
+      P.Lf[a] = (float)d.box[a];
+      P.B[a] = d.B[a];
+    }
+    P.V = V;
+    P.alpha = d.alpha;
+    P.dt = d.dt;
+    P.temp = d.temp;
+    P.Q = d.Q;
+    P.gamma = d.gamma;
+    P.ex1 = std::exp(-d.gamma * d.dt / 2);
+    P.cnoise = std::sqrt(2. * d.temp * d.gamma * d.dt / d.Q);
+    P.ntemp3 = 3. * d.n * d.temp;
+    P.min_s = d.min_s;
+    P.alphaf = (float)d.alpha;
+    P.alpha2x2 = (float)(2. * d.alpha * d.alpha);
+    P.gpref = (float)(2. * d.alpha / std::sqrt(M_PI));
+    P.alpha4x4 = (float)(4. * d.alpha * d.alpha * d.alpha * d.alpha);
+    P.invLh = (float)(1.0 / kLh);
+    P.halfLh2 = (float)(0.5 * kLh * kLh);
+    P.rmax_table = (float)kTableRmax;
+    part += d.n;
+    dip += P.ndip;
+    Lo.maxnd = std::max(Lo.maxnd, d.nd);
+    if (d.nd > 1) Lo.multi = true;
+  }
+  Lo.ntot = part;
+  Lo.ndtot = dip;
+  Lo.nktot = (int)Lo.kn.size();
+  Lo.rpart = pp;
+  Lo.kpart = kp;
+}
+
+struct Arena {
+  size_t off = 0;
+  char* base = nullptr;
+  template <class T>
+  T* take(size_t count) {
+    const size_t bytes = ((count * sizeof(T) + 255) / 256) * 256;
+    T* p = base ? reinterpret_cast<T*>(base + off) : nullptr;
+    off += bytes ? bytes : 256;
+    return p;
+  }
+};
+
+// carves every buffer of a batch out of one allocation (or only sizes it)
+void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** kowner,
+           double** noise2) {
+  const size_t n = std::max(Lo.ntot, 1), nd = std::max(Lo.ndtot, 1), nk = std::max(Lo.nktot, 1);
+  const size_t nt = std::max<size_t>(Lo.tiles.size(), 1), nb = std::max<size_t>(Lo.blk.size(), 1);
+  b.sys = A.take<SysDev>(nsys);
+  b.st = A.take<SysState>(nsys);
+  b.obs = A.take<SysObs>(nsys);
+  b.r = A.take<double>(3 * n);
+  b.p = A.take<double>(3 * n);
+  b.O = A.take<double>(9 * n);
+  b.l = A.take<double>(3 * n);
+  b.F = A.take<double>(3 * n);
+  b.T = A.take<double>(3 * n);
+  b.len = A.take<double>(n);
+  b.dia = A.take<double>(n);
+  b.mass = A.take<double>(n);
+  b.inert = A.take<double>(3 * n);
+  b.invm = A.take<double>(n);
+  b.invI = A.take<double>(3 * n);
+  b.psys = A.take<int>(n);
+  b.dpc = A.take<double>(nd);
+  b.dob = A.take<double>(3 * nd);
+  b.dmu = A.take<double>(nd);
+  b.downer = A.take<int>(nd);
+  b.pfx = A.take<uint32_t>(3 * n);
+  b.pax = A.take<float4>(n);
+  b.pdia = A.take<float>(n);
+  b.dfx = A.take<uint32_t>(3 * nd);
+  b.dm = A.take<float>(3 * nd);
+  b.rpart = A.take<float>(std::max<long long>(Lo.rpart, 1));
+  b.tileE = A.take<float>(10 * nt);
+  b.tiles = A.take<int4>(nt);
+  b.Fw = A.take<double>(3 * n);
+  b.Tw = A.take<double>(3 * n);
+  b.wcaE = A.take<double>(11 * nb);
+  b.kn = A.take<int4>(nk);
+  b.kv = A.take<float4>(nk);
+  b.kval = A.take<double>(nk);
+  b.kpre = A.take<double>(nk);
+  b.kpart = A.take<float>(10 * std::max<long long>(Lo.kpart, 1));
+  b.ksum = A.take<double>(10 * nk);
+  b.kS = A.take<float2>(nk);
+  b.kE = A.take<double>(10 * nk);
+  b.Fk = A.take<double>(3 * nd);
+  b.Gk = A.take<double>(3 * nd);
+  b.kin1 = A.take<double>(2 * nb);
+  b.kin2 = A.take<double>(9 * nb);
+  b.dmax = A.take<double>(nb);
+  b.blk = A.take<int2>(nb);
+  b.nb = A.take<int>(n * kMaxNb);
+  b.nbc = A.take<int>(n);
+  b.rsave = A.take<double>(3 * n);
+  b.usave = A.take<double>(3 * n);
+  b.comp = A.take<int>(n);
+  b.eflag = A.take<unsigned char>(n * kMaxNb);
+  b.flag = A.take<int>(1);
+  *kwork = A.take<int4>(std::max<size_t>(Lo.kwork.size(), 1));
+  *kowner = A.take<int2>(nk);
+  noise2[0] = A.take<double>((size_t)kNoiseChunk * nsys * 4);
+  noise2[1] = A.take<double>((size_t)kNoiseChunk * nsys * 4);
+}
+
+}  // namespace
+
+struct mdsc_batch {
+  int device = 0;
+  int nsys = 0;
+  cudaStream_t st = nullptr, s2 = nullptr, s3 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_j2 = nullptr, ev_j3 = nullptr;
+  std::vector<mdsc_system_desc> desc;
+  Layout lo;
+  Batch b{};
+  int4* kwork = nullptr;
+  int2* kowner = nullptr;
+  double* noise[2] = {nullptr, nullptr};
+  double* h_noise = nullptr;  // pinned
+  SysObs* h_obs = nullptr;    // pinned
+  char* arena = nullptr;
+  size_t arena_bytes = 0;
+  std::vector<Mt19937> thermo_rng;  // 2 per system
+  std::vector<Mt19937> clus_rng;    // 1 per system
+  std::vector<long long> step_h;
+  std::vector<std::vector<int>> labels;
+  std::vector<int> n_clusters;
+  std::vector<char> uploaded, built, have_forces;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  int launches = 0;
+  std::string err;
+};
+
+namespace {
+
+mdsc_status fail(mdsc_batch* b, mdsc_status code, const std::string& msg) {
+  if (b) b->err = msg;
+  return code;
+}
+
+#define CU(call)                                                                              \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      return fail(B, e_ == cudaErrorMemoryAllocation ? MDSC_ERR_OOM : MDSC_ERR_CUDA,          \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                        \
+  } while (0)
+
+mdsc_status status_from_bits(int bits) {
+  if (bits & kErrOverlap) return MDSC_ERR_OVERLAP;
+  if (bits & kErrNan) return MDSC_ERR_NAN;
+  if (bits & kErrListOverflow) return MDSC_ERR_LIST_OVERFLOW;
+  if (bits & kErrTable) return MDSC_ERR_TABLE_RANGE;
+  return MDSC_OK;
+}
+
+Batch batch_with_noise(const mdsc_batch* B, int which) {
+  Batch b = B->b;
+  b.noise = B->noise[which];
+  return b;
+}
+
+// every force term, F and T set from scratch, energies reduced
+mdsc_status eval_forces(mdsc_batch* B, int force_list) {
+  Batch b = batch_with_noise(B, 0);
+  launch_derive(b, B->st);
+  launch_list_build(b, force_list, B->st);
+  launch_wca(b, B->st);
+  launch_real_pairs(b, B->lo.multi, B->st);
+  launch_kspace(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, B->st);
+  launch_finalize(b, kMaskAll, B->st);
+  launch_reduce_obs(b, kRedEnergies, B->st);
+  CU(cudaGetLastError());
+  for (int s = 0; s < B->nsys; ++s) {
+    B->built[s] = 1;
+    B->have_forces[s] = 1;
+  }
+  return MDSC_OK;
+}
+
+mdsc_status capture_step(mdsc_batch* B, int which) {
+  Batch b = batch_with_noise(B, which);
+  cudaGraph_t g = nullptr;
+  CU(cudaStreamBeginCapture(B->st, cudaStreamCaptureModeThreadLocal));
+  int launches = 0;
+  launch_integrate_first(b, B->st);
+  ++launches;
+  cudaEventRecord(B->ev_fork, B->st);
+  cudaStreamWaitEvent(B->s2, B->ev_fork, 0);
+  cudaStreamWaitEvent(B->s3, B->ev_fork, 0);
+  launch_list_build(b, 0, B->st);
+  launch_wca(b, B->st);
+  launches += 2;
+  launch_real_pairs(b, B->lo.multi, B->s2);
+  launches += b.ntiles > 0;
+  launch_kspace(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, B->s3);
+  launches += b.nktot > 0 ? 3 : 0;
+  cudaEventRecord(B->ev_j2, B->s2);
+  cudaEventRecord(B->ev_j3, B->s3);
+  cudaStreamWaitEvent(B->st, B->ev_j2, 0);
+  cudaStreamWaitEvent(B->st, B->ev_j3, 0);
+  launch_finalize(b, kMaskAll | kFlagMoveP, B->st);
+  launch_reduce_obs(b, kRedStep, B->st);
+  launches += 2;
+  cudaError_t e = cudaStreamEndCapture(B->st, &g);
+  if (e != cudaSuccess) return fail(B, MDSC_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&B->graph[which], g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(B, MDSC_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  B->launches = launches;
+  return MDSC_OK;
+}
+
+// thermostat noise of `steps` steps for every system, drawn as moveTher
+// mode 0 draws it (v25/functions.cpp:2194-2197): two uniforms per
+// thermostat, Box-Muller, first value now, second stored for mode 2
+void draw_noise(mdsc_batch* B, int steps) {
+  double* h = B->h_noise;
+  for (int k = 0; k < steps; ++k)
+    for (int s = 0; s < B->nsys; ++s) {
+      double* o = h + ((size_t)k * B->nsys + s) * 4;
+      for (int t = 0; t < 2; ++t) {
+        Mt19937& g = B->thermo_rng[2 * s + t];
+        double r1 = g.uniform(), r2 = g.uniform();
+        box_muller(r1, r2);
+        o[2 * t] = r1;
+        o[2 * t + 1] = r2;
+      }
+    }
+}
+
+// connected components on the GPU, then the reference's labelling order on
+// the host: repeatedly draw u, take the floor(u * remaining)-th remaining
+// particle in index order, label its whole component (v25/functions.cpp:
+// 2950-2970,3282-3313)
+mdsc_status run_clusters(mdsc_batch* B, const std::vector<int>& systems) {
+  Batch b = B->b;
+  launch_cluster_bonds(b, B->st);
+  for (int it = 0; it < 64; ++it) {
+    CU(cudaMemsetAsync(b.flag, 0, sizeof(int), B->st));
+    launch_cluster_hook(b, B->st);
+    launch_cluster_compress(b, B->st);
+    int flag = 0;
+    CU(cudaMemcpyAsync(&flag, b.flag, sizeof(int), cudaMemcpyDeviceToHost, B->st));
+    CU(cudaStreamSynchronize(B->st));
+    if (!flag) break;
+  }
+  CU(cudaGetLastError());
+  for (int s : systems) {
+    const SysDev& P = B->lo.sys[s];
+    std::vector<int> comp(P.n);
+    if (P.n)
+      CU(cudaMemcpy(comp.data(), b.comp + P.part_off, sizeof(int) * P.n, cudaMemcpyDeviceToHost));
+    // members of each component, in index order
+    std::vector<int> head(P.n, -1), next(P.n, -1), tail(P.n, -1);
+    for (int i = 0; i < P.n; ++i) {
+      const int r = comp[i] - P.part_off;
+      if (head[r] < 0) head[r] = i;
+      else next[tail[r]] = i;
+      tail[r] = i;
+    }
+    Fenwick fw(P.n);
+    std::vector<int>& lab = B->labels[s];
+    lab.assign(P.n, -1);
+    int remaining = P.n, nc = 0;
+    Mt19937& g = B->clus_rng[s];
+    while (remaining > 0) {
+      const double u = g.uniform();
+      const int ip = (int)std::floor(u * remaining);
+      const int seed = fw.kth(ip);
+      const int r = comp[seed] - P.part_off;
+      for (int m = head[r]; m >= 0; m = next[m]) {
+        lab[m] = nc;
+        fw.remove(m);
+        --remaining;
+      }
+      ++nc;
+    }
+    B->n_clusters[s] = nc;
+  }
+  return MDSC_OK;
+}
+
+mdsc_status read_obs(mdsc_batch* B, mdsc_observables* out) {
+  CU(cudaMemcpyAsync(B->h_obs, B->b.obs, sizeof(SysObs) * B->nsys, cudaMemcpyDeviceToHost, B->st));
+  CU(cudaStreamSynchronize(B->st));
+  int bits = 0;
+  for (int s = 0; s < B->nsys; ++s) {
+    const SysObs& o = B->h_obs[s];
+    bits |= o.status;
+    if (!out) continue;
+    mdsc_observables& r = out[s];
+    memset(&r, 0, sizeof r);
+    r.K[0] = o.K[0];
+    r.K[1] = o.K[1];
+    r.U_ss = o.U_ss;
+    r.W_ss = o.W_ss;
+    r.U_dipR = o.U_dipR;
+    r.U_dipK = o.U_dipK;
+    r.U_ext = o.U_ext;
+    r.U_self = o.U_self;
+    for (int c = 0; c < 9; ++c) {
+      r.PT_kin[c] = o.PT_kin[c];
+      r.PT_ss[c] = o.PT_ss[c];
+      r.PT_dipR[c] = o.PT_dipR[c];
+      r.PT_dipK[c] = o.PT_dipK[c];
+    }
+    r.xi[0] = o.xi[0];
+    r.xi[1] = o.xi[1];
+    r.step = o.step;
+    r.status = status_from_bits(o.status);
+    r.n_clusters = B->n_clusters[s];
+    r.list_builds = o.list_builds;
+  }
+  const mdsc_status st = status_from_bits(bits);
+  if (st != MDSC_OK) return fail(B, st, "a system reported an error (see mdsc_observables.status)");
+  return MDSC_OK;
+}
+
+mdsc_status ensure_forces(mdsc_batch* B) {
+  for (int s = 0; s < B->nsys; ++s)
+    if (!B->uploaded[s]) return fail(B, MDSC_ERR_STATE, "system " + std::to_string(s) + " has no state yet");
+  bool need = false;
+  for (int s = 0; s < B->nsys; ++s) need |= !B->have_forces[s];
+  if (!need) return MDSC_OK;
+  return eval_forces(B, 0);
+}
+
+// host-side derived per-particle data of system s from its shape arrays
+void shapes_to_host(const mdsc_batch* B, int s, const mdsc_host_state* h, std::vector<double>& inert,
+                    std::vector<double>& invm, std::vector<double>& invI, std::vector<double>& dpc,
+                    std::vector<double>& dob, std::vector<double>& dmu, std::vector<int>& downer,
+                    double& Uself) {
+  const SysDev& P = B->lo.sys[s];
+  const int n = P.n, nd = P.nd;
+  inert.resize(3 * n);
+  invm.resize(n);
+  invI.resize(3 * n);
+  dpc.resize((size_t)n * nd);
+  dob.resize((size_t)3 * n * nd);
+  dmu.resize((size_t)n * nd);
+  downer.resize((size_t)n * nd);
+  Uself = 0.0;
+  for (int i = 0; i < n; ++i) {
+    spherocyl_inertia(h->len[i], h->dia[i], h->mass[i], &inert[3 * i]);
+    invm[i] = 1.0 / h->mass[i];
+    for (int a = 0; a < 3; ++a) invI[3 * i + a] = 1.0 / inert[3 * i + a];
+    for (int w = 0; w < nd; ++w) {
+      const double* d = h->dip + ((size_t)i * nd + w) * 5;
+      const size_t g = (size_t)i * nd + w;
+      dpc[g] = d[0];
+      dob[3 * g] = d[1];
+      dob[3 * g + 1] = d[2];
+      dob[3 * g + 2] = d[3];
+      dmu[g] = d[4];
+      downer[g] = P.part_off + i;
+    }
+    // self_ener (v25/functions.cpp:2027-2069): bare dipole-dipole energy of
+    // the particle's own dipoles; frame-independent, so the body frame serves
+    for (int v = 0; v + 1 < nd; ++v)
+      for (int w = v + 1; w < nd; ++w) {
+        const double* a = h->dip + ((size_t)i * nd + v) * 5;
+        const double* c = h->dip + ((size_t)i * nd + w) * 5;
+        const double rij[3] = {0., 0., a[0] - c[0]};
+        const double RIJSQ = rij[2] * rij[2];
+        const double RIJ = std::sqrt(RIJSQ);
+        const double SR2 = 1. / RIJSQ, SR3 = SR2 / RIJ;
+        const double UIUJ = a[1] * c[1] + a[2] * c[2] + a[3] * c[3];
+        const double UIR = a[3] * rij[2], UJR = c[3] * rij[2];
+        Uself += a[4] * c[4] * (UIUJ * SR3 - 3. * UIR * UJR * SR2 * SR3);
+      }
+  }
+}
+
+}  // namespace
+
+// ======================================================================
+// C ABI
+// ======================================================================
+extern "C" {
+
+size_t mdsc_estimate_bytes(const mdsc_system_desc* descs, int nsys) {
+  if (!descs || nsys <= 0) return 0;
+  Layout lo;
+  make_layout(descs, nsys, lo);
+  Arena A;
+  Batch b{};
+  int4* kw;
+  int2* ko;
+  double* nz[2];
+  carve(A, lo, nsys, b, &kw, &ko, nz);
+  return A.off;
+}
+
+mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mdsc_batch** out) {
+  if (!out || !descs || nsys <= 0) return MDSC_ERR_BAD_ARG;
+  *out = nullptr;
+  mdsc_batch* B = new mdsc_batch();
+  for (int s = 0; s < nsys; ++s) {
+    const std::string e = check_desc(descs[s], s);
+    if (!e.empty()) {
+      const bool table = e.find("table") != std::string::npos;
+      delete B;
+      fprintf(stderr, "mdsc_create: %s\n", e.c_str());
+      return table ? MDSC_ERR_TABLE_RANGE : MDSC_ERR_BAD_ARG;
+    }
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0 || device < 0 || device >= ndev) {
+    delete B;
+    return MDSC_ERR_NO_DEVICE;
+  }
+  B->device = device;
+  B->nsys = nsys;
+  B->desc.assign(descs, descs + nsys);
+  cudaSetDevice(device);
+  make_layout(descs, nsys, B->lo);
+  const Layout& lo = B->lo;
+  Arena A;
+  carve(A, lo, nsys, B->b, &B->kwork, &B->kowner, B->noise);
+  B->arena_bytes = A.off;
+  cudaError_t e = cudaMalloc(&B->arena, B->arena_bytes);
+  if (e != cudaSuccess) {
+    delete B;
+    return e == cudaErrorMemoryAllocation ? MDSC_ERR_OOM : MDSC_ERR_CUDA;
+  }
+  A.off = 0;
+  A.base = B->arena;
+  carve(A, lo, nsys, B->b, &B->kwork, &B->kowner, B->noise);
+  Batch& b = B->b;
+  b.nsys = nsys;
+  b.ntot = lo.ntot;
+  b.ndtot = lo.ndtot;
+  b.nktot = lo.nktot;
+  b.ntiles = (int)lo.tiles.size();
+  b.nblk = (int)lo.blk.size();
+  b.noise = B->noise[0];
+  if (cudaStreamCreateWithFlags(&B->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&B->s2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&B->s3, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&B->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&B->ev_j2, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&B->ev_j3, cudaEventDisableTiming) != cudaSuccess ||
+      cudaMallocHost(&B->h_noise, sizeof(double) * kNoiseChunk * nsys * 4) != cudaSuccess ||
+      cudaMallocHost(&B->h_obs, sizeof(SysObs) * nsys) != cudaSuccess) {
+    mdsc_destroy(B);
+    return MDSC_ERR_CUDA;
+  }
+  // constant tables
+  auto up = [&](void* dst, const void* src, size_t bytes) {
+    if (bytes) cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, B->st);
+  };
+  up((void*)b.sys, lo.sys.data(), sizeof(SysDev) * nsys);
+  up(b.tiles, lo.tiles.data(), sizeof(int4) * lo.tiles.size());
+  up(b.blk, lo.blk.data(), sizeof(int2) * lo.blk.size());
+  up(b.kn, lo.kn.data(), sizeof(int4) * lo.kn.size());
+  up(b.kv, lo.kv.data(), sizeof(float4) * lo.kv.size());
+  up(b.kval, lo.kval.data(), sizeof(double) * lo.kval.size());
+  up(b.kpre, lo.kpre.data(), sizeof(double) * lo.kpre.size());
+  up(B->kwork, lo.kwork.data(), sizeof(int4) * lo.kwork.size());
+  up(B->kowner, lo.kowner.data(), sizeof(int2) * lo.kowner.size());
+  std::vector<int> psys(std::max(lo.ntot, 1));
+  for (int s = 0; s < nsys; ++s)
+    for (int i = 0; i < lo.sys[s].n; ++i) psys[lo.sys[s].part_off + i] = s;
+  up(b.psys, psys.data(), sizeof(int) * lo.ntot);
+  std::vector<SysState> st(nsys);
+  memset(st.data(), 0, sizeof(SysState) * nsys);
+  for (int s = 0; s < nsys; ++s) {
+    st[s].xi[0] = st[s].xi[1] = descs[s].xi0;
+    st[s].force_list = 1;
+  }
+  up(b.st, st.data(), sizeof(SysState) * nsys);
+  cudaMemsetAsync(b.obs, 0, sizeof(SysObs) * nsys, B->st);
+  cudaMemsetAsync(b.rsave, 0, sizeof(double) * 3 * std::max(lo.ntot, 1), B->st);
+  cudaMemsetAsync(b.usave, 0, sizeof(double) * 3 * std::max(lo.ntot, 1), B->st);
+  cudaMemsetAsync(b.nbc, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
+  cudaMemsetAsync(b.F, 0, sizeof(double) * 3 * std::max(lo.ntot, 1), B->st);
+  cudaMemsetAsync(b.T, 0, sizeof(double) * 3 * std::max(lo.ntot, 1), B->st);
+  cudaMemsetAsync(B->noise[0], 0, sizeof(double) * kNoiseChunk * nsys * 4, B->st);
+  cudaMemsetAsync(B->noise[1], 0, sizeof(double) * kNoiseChunk * nsys * 4, B->st);
+  // rng streams
+  for (int s = 0; s < nsys; ++s) {
+    const unsigned long s0 = descs[s].thermo_seed[0] ? descs[s].thermo_seed[0] : 1;
+    const unsigned long s1 = descs[s].thermo_seed[1] ? descs[s].thermo_seed[1] : 2;
+    B->thermo_rng.emplace_back(s0);
+    B->thermo_rng.emplace_back(s1);
+    B->clus_rng.emplace_back(descs[s].cluster_seed ? descs[s].cluster_seed : 1);
+    B->clus_rng.back().discard(descs[s].cluster_skip);
+  }
+  B->step_h.assign(nsys, 0);
+  B->labels.assign(nsys, std::vector<int>());
+  for (int s = 0; s < nsys; ++s) B->labels[s].assign(descs[s].n, 0);
+  B->n_clusters.assign(nsys, 0);
+  B->uploaded.assign(nsys, 0);
+  B->built.assign(nsys, 0);
+  B->have_forces.assign(nsys, 0);
+  e = cudaStreamSynchronize(B->st);
+  if (e != cudaSuccess) {
+    mdsc_destroy(B);
+    return MDSC_ERR_CUDA;
+  }
+  *out = B;
+  return MDSC_OK;
+}
+
+mdsc_status mdsc_destroy(mdsc_batch* B) {
+  if (!B) return MDSC_OK;
+  cudaSetDevice(B->device);
+  if (B->st) cudaStreamSynchronize(B->st);
+  for (auto& g : B->graph)
+    if (g) cudaGraphExecDestroy(g);
+  if (B->arena) cudaFree(B->arena);
+  if (B->h_noise) cudaFreeHost(B->h_noise);
+  if (B->h_obs) cudaFreeHost(B->h_obs);
+  if (B->ev_fork) cudaEventDestroy(B->ev_fork);
+  if (B->ev_j2) cudaEventDestroy(B->ev_j2);
+  if (B->ev_j3) cudaEventDestroy(B->ev_j3);
+  if (B->st) cudaStreamDestroy(B->st);
+  if (B->s2) cudaStreamDestroy(B->s2);
+  if (B->s3) cudaStreamDestroy(B->s3);
+  delete B;
+  return MDSC_OK;
+}
+
+int mdsc_num_systems(const mdsc_batch* B) { return B ? B->nsys : 0; }
+size_t mdsc_device_bytes(const mdsc_batch* B) { return B ? B->arena_bytes : 0; }
+int mdsc_launches_per_step(const mdsc_batch* B) { return B ? B->launches : 0; }
+void* mdsc_stream(const mdsc_batch* B) { return B ? (void*)B->st : nullptr; }
+
+mdsc_status mdsc_last_error(const mdsc_batch* B, char* buf, size_t len) {
+  if (!B || !buf || !len) return MDSC_ERR_BAD_ARG;
+  snprintf(buf, len, "%s", B->err.c_str());
+  return MDSC_OK;
+}
+
+static mdsc_status upload_one(mdsc_batch* B, int s, const mdsc_host_state* h, bool sync) {
+  const SysDev& P = B->lo.sys[s];
+  const int n = P.n;
+  if (!h->r || !h->p || !h->O || !h->l) return fail(B, MDSC_ERR_BAD_ARG, "r, p, O, l are required");
+  const bool shapes = h->len && h->dia && h->mass && (P.nd == 0 || h->dip);
+  if (!shapes && !B->uploaded[s])
+    return fail(B, MDSC_ERR_BAD_ARG, "the first upload of a system needs len, dia, mass and dip");
+  Batch& b = B->b;
+  const int i0 = P.part_off;
+  auto up = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+    return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, B->st) : cudaSuccess;
+  };
+  CU(up(b.r + 3 * i0, h->r, sizeof(double) * 3 * n));
+  CU(up(b.p + 3 * i0, h->p, sizeof(double) * 3 * n));
+  CU(up(b.O + 9 * i0, h->O, sizeof(double) * 9 * n));
+  CU(up(b.l + 3 * i0, h->l, sizeof(double) * 3 * n));
+  if (h->F && h->T) {
+    CU(up(b.F + 3 * i0, h->F, sizeof(double) * 3 * n));
+    CU(up(b.T + 3 * i0, h->T, sizeof(double) * 3 * n));
+  }
+  if (shapes) {
+    std::vector<double> inert, invm, invI, dpc, dob, dmu;
+    std::vector<int> downer;
+    double Uself = 0;
+    shapes_to_host(B, s, h, inert, invm, invI, dpc, dob, dmu, downer, Uself);
+    CU(up(b.len + i0, h->len, sizeof(double) * n));
+    CU(up(b.dia + i0, h->dia, sizeof(double) * n));
+    CU(up(b.mass + i0, h->mass, sizeof(double) * n));
+    CU(up(b.inert + 3 * i0, inert.data(), sizeof(double) * 3 * n));
+    CU(up(b.invm + i0, invm.data(), sizeof(double) * n));
+    CU(up(b.invI + 3 * i0, invI.data(), sizeof(double) * 3 * n));
+    const int g0 = P.dip_off, nd = P.ndip;
+    CU(up(b.dpc + g0, dpc.data(), sizeof(double) * nd));
+    CU(up(b.dob + 3 * g0, dob.data(), sizeof(double) * 3 * nd));
+    CU(up(b.dmu + g0, dmu.data(), sizeof(double) * nd));
+    CU(up(b.downer + g0, downer.data(), sizeof(int) * nd));
+    // list radius: max(2^(1/6) sigma, sigma + min_s) + skin, skin = 0.9 d_min
+    // (the reference's r_list_max - r_list_min, v25/main.cpp:460-463)
+    double dmax = 0, dmin = 1e300;
+    for (int i = 0; i < n; ++i) {
+      dmax = std::max(dmax, h->dia[i]);
+      dmin = std::min(dmin, h->dia[i]);
+    }
+    if (n == 0) dmin = dmax = 1.0;
+    SysDev& Pm = B->lo.sys[s];
+    Pm.sig_max = dmax;
+    Pm.skin = 0.9 * dmin;
+    Pm.r_list = std::max(1.122462048309373 * dmax, dmax + B->desc[s].min_s) + Pm.skin;
+    Pm.Uself = Uself;
+    CU(up((void*)(b.sys + s), &Pm, sizeof(SysDev)));
+    if (B->uploaded[s]) {
+      // new shapes: the list must be rebuilt
+      const int one = 1;
+      CU(up((char*)(b.st + s) + offsetof(SysState, force_list), &one, sizeof(int)));
+    }
+  }
+  B->uploaded[s] = 1;
+  B->have_forces[s] = (h->F && h->T) ? 1 : 0;
+  if (sync) CU(cudaStreamSynchronize(B->st));
+  return MDSC_OK;
+}
+
+mdsc_status mdsc_upload(mdsc_batch* B, int sys, const mdsc_host_state* h) {
+  if (!B || !h || sys < 0 || sys >= B->nsys) return MDSC_ERR_BAD_ARG;
+  cudaSetDevice(B->device);
+  return upload_one(B, sys, h, true);
+}
+
+mdsc_status mdsc_upload_all(mdsc_batch* B, const mdsc_host_state* h) {
+  if (!B || !h) return MDSC_ERR_BAD_ARG;
+  cudaSetDevice(B->device);
+  bool first = false;
+  for (int s = 0; s < B->nsys; ++s) first |= !B->uploaded[s];
+  const bool shapes = h->len && h->dia && h->mass;
+  if (first || shapes) {
+    // per system (computes the host-side shape data)
+    for (int s = 0; s < B->nsys; ++s) {
+      const SysDev& P = B->lo.sys[s];
+      mdsc_host_state v = *h;
+      v.r = h->r + 3 * (size_t)P.part_off;
+      v.p = h->p + 3 * (size_t)P.part_off;
+      v.O = h->O + 9 * (size_t)P.part_off;
+      v.l = h->l + 3 * (size_t)P.part_off;
+      v.F = h->F ? h->F + 3 * (size_t)P.part_off : nullptr;
+      v.T = h->T ? h->T + 3 * (size_t)P.part_off : nullptr;
+      v.len = h->len ? h->len + P.part_off : nullptr;
+      v.dia = h->dia ? h->dia + P.part_off : nullptr;
+      v.mass = h->mass ? h->mass + P.part_off : nullptr;
+      v.dip = h->dip ? h->dip + 5 * (size_t)P.dip_off : nullptr;
+      mdsc_status st = upload_one(B, s, &v, false);
+      if (st != MDSC_OK) return st;
+    }
+    CU(cudaStreamSynchronize(B->st));
+    return MDSC_OK;
+  }
+  // state only: one copy per array for the whole batch
+  const size_t n = B->lo.ntot;
+  Batch& b = B->b;
+  CU(cudaMemcpyAsync(b.r, h->r, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->st));
+  CU(cudaMemcpyAsync(b.p, h->p, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->st));
+  CU(cudaMemcpyAsync(b.O, h->O, sizeof(double) * 9 * n, cudaMemcpyHostToDevice, B->st));
+  CU(cudaMemcpyAsync(b.l, h->l, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->st));
+  const bool forces = h->F && h->T;
+  if (forces) {
+    CU(cudaMemcpyAsync(b.F, h->F, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->st));
+    CU(cudaMemcpyAsync(b.T, h->T, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->st));
+  }
+  for (int s = 0; s < B->nsys; ++s) B->have_forces[s] = forces ? 1 : 0;
+  return MDSC_OK;
+}
+
+static mdsc_status download_range(mdsc_batch* B, int i0, int n, int s_first, int s_last,
+                                  mdsc_host_state* h) {
+  Batch& b = B->b;
+  auto dn = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+    return (dst && bytes) ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, B->st) : cudaSuccess;
+  };
+  CU(dn(h->r, b.r + 3 * i0, sizeof(double) * 3 * n));
+  CU(dn(h->p, b.p + 3 * i0, sizeof(double) * 3 * n));
+  CU(dn(h->O, b.O + 9 * i0, sizeof(double) * 9 * n));
+  CU(dn(h->l, b.l + 3 * i0, sizeof(double) * 3 * n));
+  CU(dn(h->F, b.F + 3 * i0, sizeof(double) * 3 * n));
+  CU(dn(h->T, b.T + 3 * i0, sizeof(double) * 3 * n));
+  CU(cudaStreamSynchronize(B->st));
+  if (h->clust) {
+    int off = 0;
+    for (int s = s_first; s <= s_last; ++s) {
+      const std::vector<int>& lab = B->labels[s];
+      std::copy(lab.begin(), lab.end(), h->clust + off);
+      off += (int)lab.size();
+    }
+  }
+  return MDSC_OK;
+}
+
+mdsc_status mdsc_download(mdsc_batch* B, int sys, mdsc_host_state* h) {
+  if (!B || !h || sys < 0 || sys >= B->nsys) return MDSC_ERR_BAD_ARG;
+  cudaSetDevice(B->device);
+  const SysDev& P = B->lo.sys[sys];
+  return download_range(B, P.part_off, P.n, sys, sys, h);
+}
+
+mdsc_status mdsc_download_all(mdsc_batch* B, mdsc_host_state* h) {
+  if (!B || !h) return MDSC_ERR_BAD_ARG;
+  cudaSetDevice(B->device);
+  return download_range(B, 0, B->lo.ntot, 0, B->nsys - 1, h);
+}
+
+mdsc_status mdsc_set_thermostat(mdsc_batch* B, int sys, const double xi[2], const double strn[2]) {
+  if (!B || sys < 0 || sys >= B->nsys || !xi) return MDSC_ERR_BAD_ARG;
+  cudaSetDevice(B->device);
+  SysState st;
+  CU(cudaMemcpy(&st, B->b.st + sys, sizeof st, cudaMemcpyDeviceToHost));
+  st.xi[0] = xi[0];
+  st.xi[1] = xi[1];
+  if (strn) {
+    st.strn[0] = strn[0];
+    st.strn[1] = strn[1];
+  }
+  CU(cudaMemcpy(B->b.st + sys, &st, sizeof st, cudaMemcpyHostToDevice));
+  return MDSC_OK;
+}
+
+// ---- function-level entry points --------------------------------------
+static mdsc_status need_state(mdsc_batch* B) {
+  if (!B) return MDSC_ERR_BAD_ARG;
+  cudaSetDevice(B->device);
+  for (int s = 0; s < B->nsys; ++s)
+    if (!B->uploaded[s]) return fail(B, MDSC_ERR_STATE, "system " + std::to_string(s) + " has no state yet");
+  return MDSC_OK;
+}
+
+mdsc_status mdsc_zero_forces(mdsc_batch* B) {
+  mdsc_status st = need_state(B);
+  if (st) return st;
+  CU(cudaMemsetAsync(B->b.F, 0, sizeof(double) * 3 * B->lo.ntot, B->st));
+  CU(cudaMemsetAsync(B->b.T, 0, sizeof(double) * 3 * B->lo.ntot, B->st));
+  CU(cudaStreamSynchronize(B->st));
+  return MDSC_OK;
+}
+
+mdsc_status mdsc_force_sc(mdsc_batch* B, double* U, double* W, double* PT) {
+  mdsc_status st = need_state(B);
+  if (st) return st;
+  launch_derive(B->b, B->st);
+  launch_list_build(B->b, 0, B->st);
+  launch_wca(B->b, B->st);
+  launch_finalize(B->b, kMaskWca | kFlagAccum, B->st);
+  launch_reduce_obs(B->b, kRedEnergies, B->st);
+  st = read_obs(B, nullptr);
+  for (int s = 0; s < B->nsys; ++s) {
+    const SysObs& o = B->h_obs[s];
+    if (U) U[s] = o.U_ss;
+    if (W) W[s] = o.W_ss;
+    if (PT) memcpy(PT + 9 * s, o.PT_ss, sizeof(double) * 9);
+  }
+  return st;
+}
+
+mdsc_status mdsc_force_dipR(mdsc_batch* B, double* U, double* PT) {
+  mdsc_status st = need_state(B);
+  if (st) return st;
+  launch_derive(B->b, B->st);
+  launch_real_pairs(B->b, B->lo.multi, B->st);
+  launch_finalize(B->b, kMaskReal | kFlagAccum, B->st);
+  launch_reduce_obs(B->b, kRedEnergies, B->st);
+  st = read_obs(B, nullptr);
+  for (int s = 0; s < B->nsys; ++s) {
+    const SysObs& o = B->h_obs[s];
+    if (U) U[s] = o.U_dipR;
+    if (PT) memcpy(PT + 9 * s, o.PT_dipR, sizeof(double) * 9);
+  }
+  return st;
+}
+
+mdsc_status mdsc_force_dipK(mdsc_batch* B, double* U, double* PT) {
+  mdsc_status st = need_state(B);
+  if (st) return st;
+  launch_derive(B->b, B->st);
+  launch_kspace(B->b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, B->b.kE, B->st);
+  launch_finalize(B->b, kMaskK | kFlagAccum, B->st);
+  launch_reduce_obs(B->b, kRedEnergies, B->st);
+  st = read_obs(B, nullptr);
+  for (int s = 0; s < B->nsys; ++s) {
+    const SysObs& o = B->h_obs[s];
+    if (U) U[s] = o.U_dipK;
+    if (PT) memcpy(PT + 9 * s, o.PT_dipK, sizeof(double) * 9);
+  }
+  return st;
+}
+
+mdsc_status mdsc_ext_field(mdsc_batch* B, double* U) {
+  mdsc_status st = need_state(B);
+  if (st) return st;
+  launch_derive(B->b, B->st);
+  launch_finalize(B->b, kMaskExt | kFlagAccum, B->st);
+  launch_reduce_obs(B->b, kRedEnergies, B->st);
+  st = read_obs(B, nullptr);
+  for (int s = 0; s < B->nsys; ++s)
+    if (U) U[s] = B->h_obs[s].U_ext;
+  return st;
+}
+
+mdsc_status mdsc_self_ener(mdsc_batch* B, double* U) {
+  mdsc_status st = need_state(B);
+  if (st) return st;
+  for (int s = 0; s < B->nsys; ++s)
+    if (U) U[s] = B->lo.sys[s].Uself;
+  return MDSC_OK;
+}
+
+mdsc_status mdsc_moveX(mdsc_batch* B) {
+  mdsc_status st = need_state(B);
+  if (st) return st;
+  launch_movex(B->b, B->st);
+  CU(cudaGetLastError());
+  CU(cudaStreamSynchronize(B->st));
+  return MDSC_OK;
+}
+
+mdsc_status mdsc_renorm(mdsc_batch* B) {
+  mdsc_status st = need_state(B);
+  if (st) return st;
+  launch_renorm(B->b, B->st);
+  launch_derive(B->b, B->st);
+  CU(cudaGetLastError());
+  CU(cudaStreamSynchronize(B->st));
+  return MDSC_OK;
+}
+
+mdsc_status mdsc_moveP(mdsc_batch* B, const double* xi, int last, double* K, double* PT) {
+  mdsc_status st = need_state(B);
+  if (st) return st;
+  if (!xi) return fail(B, MDSC_ERR_BAD_ARG, "xi is required");
+  // the noise buffer is free outside mdsc_step: stage xi there
+  CU(cudaMemcpyAsync(B->noise[1], xi, sizeof(double) * 2 * B->nsys, cudaMemcpyHostToDevice, B->st));
+  launch_movep(B->b, B->noise[1], last, B->st);
+  std::vector<double> part(9 * B->b.nblk);
+  CU(cudaMemcpyAsync(part.data(), B->b.kin2, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, B->st));
+  CU(cudaStreamSynchronize(B->st));
+  for (int s = 0; s < B->nsys; ++s) {
+    const SysDev& P = B->lo.sys[s];
+    double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < P.nblk; ++k)
+      for (int c = 0; c < 9; ++c) v[c] += part[9 * (P.blk_off + k) + c];
+    if (K) {
+      K[2 * s] = 0.5 * v[0];
+      K[2 * s + 1] = 0.5 * v[1];
+    }
+    if (PT) {
+      const int map[9] = {2, 3, 4, 3, 5, 6, 4, 6, 7};
+      for (int c = 0; c < 9; ++c) PT[9 * s + c] = last ? v[map[c]] : 0.0;
+    }
+  }
+  return MDSC_OK;
+}
+
+mdsc_status mdsc_neigh_list(mdsc_batch* B) {
+  mdsc_status st = need_state(B);
+  if (st) return st;
+  launch_derive(B->b, B->st);
+  launch_list_build(B->b, 1, B->st);
+  CU(cudaGetLastError());
+  CU(cudaStreamSynchronize(B->st));
+  for (int s = 0; s < B->nsys; ++s) B->built[s] = 1;
+  return MDSC_OK;
+}
+
+mdsc_status mdsc_check_list(mdsc_batch* B, int* rebuild) {
+  mdsc_status st = need_state(B);
+  if (st) return st;
+  launch_derive(B->b, B->st);
+  std::vector<double> dm(B->b.nblk);
+  CU(cudaMemcpyAsync(dm.data(), B->b.dmax, sizeof(double) * dm.size(), cudaMemcpyDeviceToHost, B->st));
+  CU(cudaStreamSynchronize(B->st));
+  for (int s = 0; s < B->nsys; ++s) {
+    const SysDev& P = B->lo.sys[s];
+    double m = 0;
+    for (int k = 0; k < P.nblk; ++k) m = std::max(m, dm[P.blk_off + k]);
+    if (rebuild) rebuild[s] = (!B->built[s] || 2.0 * m > P.skin) ? 1 : 0;
+  }
+  return MDSC_OK;
+}
+
+mdsc_status mdsc_clust_conf(mdsc_batch* B, int sys, int* labels, int* n_clusters) {
+  mdsc_status st = need_state(B);
+  if (st) return st;
+  if (sys < 0 || sys >= B->nsys) return MDSC_ERR_BAD_ARG;
+  launch_derive(B->b, B->st);
+  launch_list_build(B->b, 0, B->st);
+  st = run_clusters(B, std::vector<int>{sys});
+  if (st) return st;
+  if (labels) std::copy(B->labels[sys].begin(), B->labels[sys].end(), labels);
+  if (n_clusters) *n_clusters = B->n_clusters[sys];
+  return MDSC_OK;
+}
+
+// ---- the fused step ----------------------------------------------------
+mdsc_status mdsc_step(mdsc_batch* B, int nsteps, mdsc_observables* obs) {
+  if (!B || nsteps < 0) return MDSC_ERR_BAD_ARG;
+  cudaSetDevice(B->device);
+  mdsc_status st = ensure_forces(B);
+  if (st) return st;
+  for (int w = 0; w < 2; ++w)
+    if (!B->graph[w]) {
+      st = capture_step(B, w);
+      if (st) return st;
+    }
+  int which = 0;
+  int done = 0;
+  while (done < nsteps) {
+    // steps until the next clustering step of any system (inclusive)
+    int chunk = std::min(nsteps - done, kNoiseChunk);
+    for (int s = 0; s < B->nsys; ++s) {
+      const int fr = B->desc[s].cl_fr;
+      if (fr <= 0) continue;
+      const long long k0 = B->step_h[s];
+      const long long next = ((k0 + fr - 1) / fr) * fr;  // first k >= k0 with k % fr == 0
+      chunk = (int)std::min<long long>(chunk, next - k0 + 1);
+    }
+    // noise for this chunk; the other buffer may still be read by the GPU
+    CU(cudaStreamSynchronize(B->st));
+    draw_noise(B, chunk);
+    CU(cudaMemcpyAsync(B->noise[which], B->h_noise, sizeof(double) * chunk * B->nsys * 4,
+                       cudaMemcpyHostToDevice, B->st));
+    launch_reset_iter(B->b, B->st);
+    for (int k = 0; k < chunk; ++k) CU(cudaGraphLaunch(B->graph[which], B->st));
+    std::vector<int> due;
+    for (int s = 0; s < B->nsys; ++s) {
+      const int fr = B->desc[s].cl_fr;
+      const long long last = B->step_h[s] + chunk - 1;
+      if (fr > 0 && last % fr == 0) due.push_back(s);
+      B->step_h[s] += chunk;
+    }
+    if (!due.empty()) {
+      st = run_clusters(B, due);
+      if (st) return st;
+    }
+    done += chunk;
+    which ^= 1;
+  }
+  return read_obs(B, obs);
+}
+
+mdsc_status mdsc_observe(mdsc_batch* B, mdsc_observables* obs) {
+  if (!B) return MDSC_ERR_BAD_ARG;
+  cudaSetDevice(B->device);
+  mdsc_status st = ensure_forces(B);
+  if (st) return st;
+  return read_obs(B, obs);
+}
+
+mdsc_status mdsc_profile_steps(mdsc_batch* B, int nsteps, int max_kernels, char* names,
+                               size_t name_stride, double* ms, int* n_kernels) {
+  if (!B || nsteps <= 0) return MDSC_ERR_BAD_ARG;
+  cudaSetDevice(B->device);
+  mdsc_status st = ensure_forces(B);
+  if (st) return st;
+  const char* kn[9] = {"integrate_first", "list_build", "wca", "real_pairs", "kspace_sum",
+                       "kspace_combine", "kspace_gather", "finalize", "reduce_obs"};
+  const int nk = 9;
+  std::vector<cudaEvent_t> ev(nk + 1);
+  for (auto& e : ev) cudaEventCreate(&e);
+  std::vector<double> acc(nk, 0.0);
+  draw_noise(B, 1);
+  Batch b = batch_with_noise(B, 0);
+  for (int it = 0; it < nsteps; ++it) {
+    CU(cudaMemcpyAsync(B->noise[0], B->h_noise, sizeof(double) * B->nsys * 4, cudaMemcpyHostToDevice, B->st));
+    launch_reset_iter(b, B->st);
+    cudaEventRecord(ev[0], B->st);
+    launch_integrate_first(b, B->st);
+    cudaEventRecord(ev[1], B->st);
+    launch_list_build(b, 0, B->st);
+    cudaEventRecord(ev[2], B->st);
+    launch_wca(b, B->st);
+    cudaEventRecord(ev[3], B->st);
+    launch_real_pairs(b, B->lo.multi, B->st);
+    cudaEventRecord(ev[4], B->st);
+    // the three k-space kernels, timed one by one
+    launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 0, B->st);
+    cudaEventRecord(ev[5], B->st);
+    launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 1, B->st);
+    cudaEventRecord(ev[6], B->st);
+    launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 2, B->st);
+    cudaEventRecord(ev[7], B->st);
+    launch_finalize(b, kMaskAll | kFlagMoveP, B->st);
+    cudaEventRecord(ev[8], B->st);
+    launch_reduce_obs(b, kRedStep, B->st);
+    cudaEventRecord(ev[9], B->st);
+    CU(cudaStreamSynchronize(B->st));
+    for (int k = 0; k < nk; ++k) {
+      float t = 0;
+      cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+      acc[k] += t;
+    }
+    for (int s = 0; s < B->nsys; ++s) B->step_h[s] += 1;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  const int m = std::min(nk, max_kernels);
+  for (int k = 0; k < m; ++k) {
+    if (names) snprintf(names + k * name_stride, name_stride, "%s", kn[k]);
+    if (ms) ms[k] = acc[k] / nsteps;
+  }
+  if (n_kernels) *n_kernels = m;
+  CU(cudaGetLastError());
+  return MDSC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,619 @@
+// Integrator, force assembly and per-system reductions -- the GPU form of
+// moveTher / moveP / moveX / renorm / ext_field and of the driver's
+// bookkeeping (v25/functions.cpp:1992-2025,2071-2218; v25/classes.cpp:228-325;
+// v25/main.cpp:558-649).
+//
+// Precision: the master state (r, p, l, O, F, T) is FP64.  FP64 runs at a
+// small fraction of the FP32 rate on this GPU, so the free-rotor update
+// (five plane rotations in the body frame, J. Chem. Phys. 107, 5840, as
+// Spherocyl::rotate does) is composed in FP32 as M = I + D, with every
+// rotation entered as cos-1 = -2 sin^2(a/2) and sin a so that D keeps full
+// FP32 *relative* precision (|D| ~ 1e-3 -> ~1e-10 absolute), and is applied
+// to the FP64 orientation as O += D O.  Kicks, drifts and the thermostat
+// scalars stay in FP64.
+#include "mdsc_dev.cuh"
+#include "reduce.cuh"
+
+namespace mdsc {
+
+// ---------------------------------------------------------------------
+// working copies: fixed-point positions, FP32 axes and dipole vectors
+// ---------------------------------------------------------------------
+__device__ __forceinline__ void derive_particle(const Batch& b, const SysDev& P, int i,
+                                                const double* r, const double* O) {
+  const int N = b.ntot, ND = b.ndtot;
+  uint32_t u[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    u[a] = to_fix(r[a], P.invL[a]);
+    b.pfx[a * N + i] = u[a];
+  }
+  b.pax[i] = make_float4((float)O[6], (float)O[7], (float)O[8], (float)b.len[i]);
+  b.pdia[i] = (float)b.dia[i];
+  const int nd = P.nd;
+  const int g0 = P.dip_off + (i - P.part_off) * nd;
+  float Of[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) Of[k] = (float)O[k];
+  for (int w = 0; w < nd; ++w) {
+    const int g = g0 + w;
+    const double pc = b.dpc[g];
+    if (pc == 0.0) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) b.dfx[a * ND + g] = u[a];
+    } else {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) b.dfx[a * ND + g] = to_fix(r[a] + pc * O[6 + a], P.invL[a]);
+    }
+    // lab direction O^T o_body (Spherocyl::set_dip, v25/classes.cpp:166-170), times the moment
+    const float ox = (float)b.dob[3 * g], oy = (float)b.dob[3 * g + 1], oz = (float)b.dob[3 * g + 2];
+    const float mu = (float)b.dmu[g];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) b.dm[a * ND + g] = mu * (Of[a] * ox + Of[3 + a] * oy + Of[6 + a] * oz);
+  }
+}
+
+__device__ __forceinline__ float displacement(const Batch& b, int i, const double* r, const double* O) {
+  float dr2 = 0.f, du2 = 0.f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float d = (float)(r[a] - b.rsave[3 * i + a]);
+    const float e = (float)(O[6 + a] - b.usave[3 * i + a]);
+    dr2 += d * d;
+    du2 += e * e;
+  }
+  return sqrtf(dr2) + 0.5f * (float)b.len[i] * sqrtf(du2);
+}
+
+__global__ void __launch_bounds__(kPartBlock) derive_kernel(Batch b) {
+  __shared__ float shm[kPartBlock / 32];
+  const int2 bk = b.blk[blockIdx.x];
+  const SysDev& P = b.sys[bk.x];
+  const int i = bk.y + threadIdx.x;
+  float disp = 0.f;
+  if (i < P.part_off + P.n) {
+    double r[3], O[9];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) r[a] = b.r[3 * i + a];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) O[k] = b.O[9 * i + k];
+    derive_particle(b, P, i, r, O);
+    disp = displacement(b, i, r, O);
+  }
+  const float m = block_max<kPartBlock>(disp, shm);
+  if (threadIdx.x == 0) b.dmax[blockIdx.x] = (double)m;
+}
+
+// Spherocyl::renorm, v25/classes.cpp:307-325
+__device__ __forceinline__ void renorm_O(double* o) {
+  double norm = sqrt(o[6] * o[6] + o[7] * o[7] + o[8] * o[8]);
+  o[6] /= norm; o[7] /= norm; o[8] /= norm;
+  const double Up[3] = {o[6] + o[3], o[7] + o[4], o[8] + o[5]};
+  const double d = Up[0] * o[6] + Up[1] * o[7] + Up[2] * o[8];
+  o[3] = Up[0] - d * o[6];
+  o[4] = Up[1] - d * o[7];
+  o[5] = Up[2] - d * o[8];
+  norm = sqrt(o[3] * o[3] + o[4] * o[4] + o[5] * o[5]);
+  o[3] /= norm; o[4] /= norm; o[5] /= norm;
+  o[0] = o[4] * o[8] - o[7] * o[5];
+  o[1] = o[5] * o[6] - o[8] * o[3];
+  o[2] = o[3] * o[7] - o[6] * o[4];
+}
+
+// one plane rotation of the composition: rows/components (i, j) turn by a
+__device__ __forceinline__ void plane_rot(float a, int i, int j, float* lb, float* D) {
+  float sh, ch;
+  sincosf(0.5f * a, &sh, &ch);
+  const float s = 2.f * sh * ch;
+  const float cm1 = -2.f * sh * sh;  // cos a - 1 with full relative precision
+  const float li = lb[i], lj = lb[j];
+  lb[i] = li + (cm1 * li - s * lj);
+  lb[j] = lj + (s * li + cm1 * lj);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float di = D[3 * i + c], dj = D[3 * j + c];
+    float ni = di + (cm1 * di - s * dj);
+    float nj = dj + (s * di + cm1 * dj);
+    if (c == i) { ni += cm1; nj += s; }
+    if (c == j) { ni -= s; nj += cm1; }
+    D[3 * i + c] = ni;
+    D[3 * j + c] = nj;
+  }
+}
+
+// translate + rotate (Spherocyl::translate / rotate, v25/classes.cpp:228-304)
+__device__ __forceinline__ void move_x(const Batch& b, int i, double dt, double* r, const double* p,
+                                       double* O, const double* l) {
+  const double im = b.invm[i];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) r[a] += dt * p[a] * im;
+  const float iI0 = (float)b.invI[3 * i], iI1 = (float)b.invI[3 * i + 1], iI2 = (float)b.invI[3 * i + 2];
+  const float h = (float)(0.5 * dt), fdt = (float)dt;
+  float lb[3];
+  const float lf[3] = {(float)l[0], (float)l[1], (float)l[2]};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) lb[a] = (float)O[3 * a] * lf[0] + (float)O[3 * a + 1] * lf[1] + (float)O[3 * a + 2] * lf[2];
+  float D[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) D[k] = 0.f;
+  plane_rot(-lb[0] * h * iI0, 1, 2, lb, D);   // Rx
+  plane_rot(-lb[1] * h * iI1, 2, 0, lb, D);   // Ry
+  plane_rot(-lb[2] * fdt * iI2, 0, 1, lb, D); // Rz
+  plane_rot(-lb[1] * h * iI1, 2, 0, lb, D);   // Ry
+  plane_rot(-lb[0] * h * iI0, 1, 2, lb, D);   // Rx
+  double On[9];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      On[3 * a + c] = O[3 * a + c] + ((double)D[3 * a] * O[c] + (double)D[3 * a + 1] * O[3 + c] +
+                                      (double)D[3 * a + 2] * O[6 + c]);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) O[k] = On[k];
+}
+
+// K_r = l^T (O^T I^-1 O) l = sum_a (O l)_a^2 / I_a  (v25/functions.cpp:2123-2148)
+__device__ __forceinline__ double rot_kin(const Batch& b, int i, const double* O, const double* l) {
+  double kr = 0.0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const double lb = O[3 * a] * l[0] + O[3 * a + 1] * l[1] + O[3 * a + 2] * l[2];
+    kr += lb * lb * b.invI[3 * i + a];
+  }
+  return kr;
+}
+
+// ---------------------------------------------------------------------
+// first half of the step: moveTher(0), [renorm], moveP(first), moveX
+// ---------------------------------------------------------------------
+__global__ void __launch_bounds__(kPartBlock) integrate_first_kernel(Batch b) {
+  __shared__ double sh[2 * kPartBlock / 32];
+  __shared__ float shm[kPartBlock / 32];
+  __shared__ double sfac[2];
+  const int2 bk = b.blk[blockIdx.x];
+  const int s = bk.x;
+  const SysDev& P = b.sys[s];
+  const SysState& S = b.st[s];
+  const int i = bk.y + threadIdx.x;
+  const bool ok = i < P.part_off + P.n;
+  if (threadIdx.x == 0) {
+    // moveTher mode 0 (v25/functions.cpp:2193-2202); noise drawn on the host
+    const double* nz = b.noise + ((long long)S.iter * b.nsys + s) * 4;
+    const double xt = P.ex1 * S.xi[0] + P.cnoise * nz[0];
+    const double xr = P.ex1 * S.xi[1] + P.cnoise * nz[2];
+    sfac[0] = 1.0 / (1.0 + 0.5 * P.dt * xt);
+    sfac[1] = 1.0 / (1.0 + 0.5 * P.dt * xr);
+  }
+  __syncthreads();
+  double kin[2] = {0.0, 0.0};
+  float disp = 0.f;
+  if (ok) {
+    const double h = 0.5 * P.dt;
+    double r[3], p[3], l[3], O[9];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      r[a] = b.r[3 * i + a];
+      p[a] = b.p[3 * i + a];
+      l[a] = b.l[3 * i + a];
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) O[k] = b.O[9 * i + k];
+    if (S.step % 100 == 0) renorm_O(O);  // v25/main.cpp:556-563
+    // moveP first half (v25/functions.cpp:2129-2149)
+    double psq = 0.0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      p[a] = (p[a] + h * b.F[3 * i + a]) * sfac[0];
+      psq += p[a] * p[a];
+      l[a] = (l[a] + h * b.T[3 * i + a]) * sfac[1];
+    }
+    kin[0] = psq * b.invm[i];
+    kin[1] = rot_kin(b, i, O, l);
+    // moveX (v25/functions.cpp:2071-2092)
+    move_x(b, i, P.dt, r, p, O, l);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      b.r[3 * i + a] = r[a];
+      b.p[3 * i + a] = p[a];
+      b.l[3 * i + a] = l[a];
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) b.O[9 * i + k] = O[k];
+    derive_particle(b, P, i, r, O);
+    // how far the rod's ends may have moved since the last list build
+    disp = displacement(b, i, r, O);
+  }
+  double tot[2];
+  block_sum<2, kPartBlock>(kin, sh, tot);
+  const float m = block_max<kPartBlock>(disp, shm);
+  if (threadIdx.x == 0) {
+    b.kin1[2 * blockIdx.x] = tot[0];
+    b.kin1[2 * blockIdx.x + 1] = tot[1];
+    b.dmax[blockIdx.x] = (double)m;
+  }
+}
+
+// thermostat coordinates used by the second half kick: moveTher 0 then 1
+// (v25/functions.cpp:2193-2206), from the first-half kinetic energies
+__device__ __forceinline__ void xi_mid(const Batch& b, const SysDev& P, const SysState& S, int s,
+                                       double* xi2, double* Kf) {
+  double K0 = 0.0, K1 = 0.0;
+  for (int k = 0; k < P.nblk; ++k) {
+    K0 += b.kin1[2 * (P.blk_off + k)];
+    K1 += b.kin1[2 * (P.blk_off + k) + 1];
+  }
+  Kf[0] = 0.5 * K0;
+  Kf[1] = 0.5 * K1;
+  const double* nz = b.noise + ((long long)S.iter * b.nsys + s) * 4;
+  const double x1t = P.ex1 * S.xi[0] + P.cnoise * nz[0];
+  const double x1r = P.ex1 * S.xi[1] + P.cnoise * nz[2];
+  xi2[0] = x1t + P.dt * (2. * Kf[0] - P.ntemp3) / P.Q;
+  xi2[1] = x1r + P.dt * (2. * Kf[1] - P.ntemp3) / P.Q;
+}
+
+// ---------------------------------------------------------------------
+// force assembly (+ ext_field) and optionally moveP(last)
+// ---------------------------------------------------------------------
+__global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode) {
+  __shared__ double sh[9 * kPartBlock / 32];
+  __shared__ double sx[2];
+  const int2 bk = b.blk[blockIdx.x];
+  const int s = bk.x;
+  const SysDev& P = b.sys[s];
+  const SysState& S = b.st[s];
+  const int i = bk.y + threadIdx.x;
+  const bool ok = i < P.part_off + P.n;
+  if ((mode & kFlagMoveP) && threadIdx.x == 0) {
+    double xi2[2], Kf[2];
+    xi_mid(b, P, S, s, xi2, Kf);
+    sx[0] = xi2[0];
+    sx[1] = xi2[1];
+  }
+  __syncthreads();
+  double acc[9];
+#pragma unroll
+  for (int c = 0; c < 9; ++c) acc[c] = 0.0;
+  if (ok) {
+    double F[3], T[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      F[a] = (mode & kFlagAccum) ? b.F[3 * i + a] : 0.0;
+      T[a] = (mode & kFlagAccum) ? b.T[3 * i + a] : 0.0;
+    }
+    if (mode & kMaskWca) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        F[a] += b.Fw[3 * i + a];
+        T[a] += b.Tw[3 * i + a];
+      }
+    }
+    double ax[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) ax[a] = b.O[9 * i + 6 + a];
+    const int nd = P.nd, ND = b.ndtot;
+    const int loc0 = (i - P.part_off) * nd;
+    double uext = 0.0;
+    for (int w = 0; w < nd; ++w) {
+      const int loc = loc0 + w;
+      const int g = P.dip_off + loc;
+      double f[3] = {0.0, 0.0, 0.0}, t[3] = {0.0, 0.0, 0.0};
+      if (mode & kMaskReal) {
+        // sum of the tile partials of this dipole over all partner strips,
+        // float-float so that hundreds of strips add without loss
+        const int X = loc / kTile, lx = loc % kTile, ns = P.nstrip;
+        const float* base = b.rpart + P.pp_off + (long long)X * ns * 6 * kTile + lx;
+        FF acc6[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) acc6[c].hi = acc6[c].lo = 0.f;
+        for (int Y = 0; Y < ns; ++Y) {
+#pragma unroll
+          for (int c = 0; c < 6; ++c) {
+            FF v;
+            v.hi = base[((long long)Y * 6 + c) * kTile];
+            v.lo = 0.f;
+            acc6[c] = ff_add(acc6[c], v);
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          f[c] += (double)acc6[c].hi + (double)acc6[c].lo;
+          t[c] += (double)acc6[3 + c].hi + (double)acc6[3 + c].lo;
+        }
+      }
+      const double mx = b.dm[g], my = b.dm[ND + g], mz = b.dm[2 * ND + g];
+      if (mode & kMaskK) {
+        const double gx = b.Gk[3 * g], gy = b.Gk[3 * g + 1], gz = b.Gk[3 * g + 2];
+        f[0] += b.Fk[3 * g];
+        f[1] += b.Fk[3 * g + 1];
+        f[2] += b.Fk[3 * g + 2];
+        t[0] += my * gz - mz * gy;
+        t[1] += mz * gx - mx * gz;
+        t[2] += mx * gy - my * gx;
+      }
+      if (mode & kMaskExt) {
+        // ext_field: torque mu o x B, energy -mu o.B (v25/functions.cpp:2014-2020)
+        t[0] += my * P.B[2] - mz * P.B[1];
+        t[1] += mz * P.B[0] - mx * P.B[2];
+        t[2] += mx * P.B[1] - my * P.B[0];
+        uext -= mx * P.B[0] + my * P.B[1] + mz * P.B[2];
+      }
+      // lever arm of an off-centre dipole: d x f (v25/classes.hpp:135-136)
+      const double pc = b.dpc[g];
+      if (pc != 0.0) {
+        const double d[3] = {pc * ax[0], pc * ax[1], pc * ax[2]};
+        t[0] += d[1] * f[2] - d[2] * f[1];
+        t[1] += d[2] * f[0] - d[0] * f[2];
+        t[2] += d[0] * f[1] - d[1] * f[0];
+      }
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        F[a] += f[a];
+        T[a] += t[a];
+      }
+    }
+    acc[8] = uext;
+    double p[3], l[3];
+    if (mode & kFlagMoveP) {
+      // moveP last half (v25/functions.cpp:2150-2173)
+      const double h = 0.5 * P.dt;
+      const double ft = 1. - h * sx[0], fr = 1. - h * sx[1];
+      double psq = 0.0;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        p[a] = b.p[3 * i + a] * ft + h * F[a];
+        psq += p[a] * p[a];
+        l[a] = b.l[3 * i + a] * fr + h * T[a];
+        b.p[3 * i + a] = p[a];
+        b.l[3 * i + a] = l[a];
+      }
+      double O[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) O[k] = b.O[9 * i + k];
+      const double im = b.invm[i];
+      acc[0] = psq * im;
+      acc[1] = rot_kin(b, i, O, l);
+      acc[2] = p[0] * p[0] * im;
+      acc[3] = p[0] * p[1] * im;
+      acc[4] = p[0] * p[2] * im;
+      acc[5] = p[1] * p[1] * im;
+      acc[6] = p[1] * p[2] * im;
+      acc[7] = p[2] * p[2] * im;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      b.F[3 * i + a] = F[a];
+      b.T[3 * i + a] = T[a];
+    }
+  }
+  double tot[9];
+  block_sum<9, kPartBlock>(acc, sh, tot);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int c = 0; c < 9; ++c) b.kin2[9 * blockIdx.x + c] = tot[c];
+  }
+}
+
+// ---------------------------------------------------------------------
+// per-system sums (block per system) and the thermostat's last update
+// ---------------------------------------------------------------------
+__global__ void __launch_bounds__(128) reduce_obs_kernel(Batch b, int mode) {
+  __shared__ double sh[10 * 4];
+  const int s = blockIdx.x;
+  const SysDev& P = b.sys[s];
+  SysState& S = b.st[s];
+  SysObs& ob = b.obs[s];
+  double v[10], out[10];
+  // real-space tiles: U, PT
+#pragma unroll
+  for (int c = 0; c < 10; ++c) v[c] = 0.0;
+  for (int t = threadIdx.x; t < P.ntile; t += 128) {
+    const float* e = b.tileE + (long long)(P.tile_off + t) * 10;
+#pragma unroll
+    for (int c = 0; c < 10; ++c) v[c] += (double)e[c];
+  }
+  block_sum<10, 128>(v, sh, out);
+  if (threadIdx.x == 0) {
+    ob.U_dipR = out[0];
+    for (int c = 0; c < 9; ++c) ob.PT_dipR[c] = out[1 + c];
+  }
+  // k-space
+#pragma unroll
+  for (int c = 0; c < 10; ++c) v[c] = 0.0;
+  for (int k = threadIdx.x; k < P.nk; k += 128) {
+    const double* e = b.kE + (long long)(P.k_off + k) * 10;
+#pragma unroll
+    for (int c = 0; c < 10; ++c) v[c] += e[c];
+  }
+  block_sum<10, 128>(v, sh, out);
+  if (threadIdx.x == 0) {
+    ob.U_dipK = out[0];
+    for (int c = 0; c < 9; ++c) ob.PT_dipK[c] = out[1 + c];
+  }
+  // WCA: U, W, PT
+#pragma unroll
+  for (int c = 0; c < 10; ++c) v[c] = 0.0;
+  double w = 0.0;
+  for (int k = threadIdx.x; k < P.nblk; k += 128) {
+    const double* e = b.wcaE + (long long)(P.blk_off + k) * 11;
+    v[0] += e[0];
+    w += e[1];
+#pragma unroll
+    for (int c = 0; c < 9; ++c) v[1 + c] += e[2 + c];
+  }
+  block_sum<10, 128>(v, sh, out);
+  {
+    double wv[1] = {w}, wo[1];
+    block_sum<1, 128>(wv, sh, wo);
+    if (threadIdx.x == 0) {
+      ob.U_ss = out[0];
+      ob.W_ss = wo[0];
+      for (int c = 0; c < 9; ++c) ob.PT_ss[c] = out[1 + c];
+    }
+  }
+  // kinetic terms and the field energy
+#pragma unroll
+  for (int c = 0; c < 10; ++c) v[c] = 0.0;
+  for (int k = threadIdx.x; k < P.nblk; k += 128) {
+    const double* e = b.kin2 + (long long)(P.blk_off + k) * 9;
+#pragma unroll
+    for (int c = 0; c < 9; ++c) v[c] += e[c];
+  }
+  block_sum<10, 128>(v, sh, out);
+  if (threadIdx.x == 0) {
+    ob.U_ext = out[8];
+    ob.U_self = P.Uself;
+    if (mode & kRedStep) {
+      ob.K[0] = 0.5 * out[0];
+      ob.K[1] = 0.5 * out[1];
+      const double pt6[6] = {out[2], out[3], out[4], out[5], out[6], out[7]};
+      const int map[9] = {0, 1, 2, 1, 3, 4, 2, 4, 5};
+      for (int c = 0; c < 9; ++c) ob.PT_kin[c] = pt6[map[c]];
+      // moveTher mode 2 (v25/functions.cpp:2207-2213) closes the step
+      double xi2[2], Kf[2];
+      xi_mid(b, P, S, s, xi2, Kf);
+      const double* nz = b.noise + ((long long)S.iter * b.nsys + s) * 4;
+      S.xi[0] = P.ex1 * xi2[0] + P.cnoise * nz[1];
+      S.xi[1] = P.ex1 * xi2[1] + P.cnoise * nz[3];
+      S.strn[0] = nz[1];
+      S.strn[1] = nz[3];
+      S.K_first[0] = Kf[0];
+      S.K_first[1] = Kf[1];
+      S.step += 1;
+      S.iter += 1;
+      if (S.rebuild) S.list_builds += 1;
+      S.force_list = 0;
+    }
+    ob.xi[0] = S.xi[0];
+    ob.xi[1] = S.xi[1];
+    ob.step = S.step;
+    ob.status = S.status;
+    ob.list_builds = S.list_builds;
+  }
+}
+
+// ---------------------------------------------------------------------
+// function-level entry points
+// ---------------------------------------------------------------------
+__global__ void __launch_bounds__(kPartBlock) movex_kernel(Batch b) {
+  const int2 bk = b.blk[blockIdx.x];
+  const SysDev& P = b.sys[bk.x];
+  const int i = bk.y + threadIdx.x;
+  if (i >= P.part_off + P.n) return;
+  double r[3], p[3], l[3], O[9];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    r[a] = b.r[3 * i + a];
+    p[a] = b.p[3 * i + a];
+    l[a] = b.l[3 * i + a];
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) O[k] = b.O[9 * i + k];
+  move_x(b, i, P.dt, r, p, O, l);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) b.r[3 * i + a] = r[a];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) b.O[9 * i + k] = O[k];
+  derive_particle(b, P, i, r, O);
+}
+
+__global__ void __launch_bounds__(kPartBlock) renorm_kernel(Batch b) {
+  const int2 bk = b.blk[blockIdx.x];
+  const SysDev& P = b.sys[bk.x];
+  const int i = bk.y + threadIdx.x;
+  if (i >= P.part_off + P.n) return;
+  double O[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) O[k] = b.O[9 * i + k];
+  renorm_O(O);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) b.O[9 * i + k] = O[k];
+}
+
+// moveP with caller-given thermostat coordinates xi[2*sys]; partial sums
+// K_t, K_r, PT (6) per block into kin2
+__global__ void __launch_bounds__(kPartBlock) movep_kernel(Batch b, const double* __restrict__ xi,
+                                                          int last) {
+  __shared__ double sh[9 * kPartBlock / 32];
+  const int2 bk = b.blk[blockIdx.x];
+  const int s = bk.x;
+  const SysDev& P = b.sys[s];
+  const int i = bk.y + threadIdx.x;
+  double acc[9];
+#pragma unroll
+  for (int c = 0; c < 9; ++c) acc[c] = 0.0;
+  if (i < P.part_off + P.n) {
+    const double h = 0.5 * P.dt;
+    double p[3], l[3], O[9];
+    double psq = 0.0;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) O[k] = b.O[9 * i + k];
+    const double xt = xi[2 * s], xr = xi[2 * s + 1];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const double p0 = b.p[3 * i + a], l0 = b.l[3 * i + a];
+      const double f = b.F[3 * i + a], t = b.T[3 * i + a];
+      if (!last) {
+        p[a] = (p0 + h * f) / (1. + h * xt);
+        l[a] = (l0 + h * t) / (1. + h * xr);
+      } else {
+        p[a] = p0 * (1. - h * xt) + h * f;
+        l[a] = l0 * (1. - h * xr) + h * t;
+      }
+      psq += p[a] * p[a];
+      b.p[3 * i + a] = p[a];
+      b.l[3 * i + a] = l[a];
+    }
+    const double im = b.invm[i];
+    acc[0] = psq * im;
+    acc[1] = rot_kin(b, i, O, l);
+    if (last) {
+      acc[2] = p[0] * p[0] * im;
+      acc[3] = p[0] * p[1] * im;
+      acc[4] = p[0] * p[2] * im;
+      acc[5] = p[1] * p[1] * im;
+      acc[6] = p[1] * p[2] * im;
+      acc[7] = p[2] * p[2] * im;
+    }
+  }
+  double tot[9];
+  block_sum<9, kPartBlock>(acc, sh, tot);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int c = 0; c < 9; ++c) b.kin2[9 * blockIdx.x + c] = tot[c];
+  }
+}
+
+__global__ void reset_iter_kernel(Batch b) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < b.nsys) b.st[s].iter = 0;
+}
+
+// ---------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------
+void launch_reset_iter(const Batch& b, cudaStream_t s) {
+  if (b.nsys) reset_iter_kernel<<<cdiv(b.nsys, 128), 128, 0, s>>>(b);
+}
+void launch_derive(const Batch& b, cudaStream_t s) {
+  if (b.nblk) derive_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
+}
+void launch_integrate_first(const Batch& b, cudaStream_t s) {
+  if (b.nblk) integrate_first_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
+}
+void launch_finalize(const Batch& b, int mode, cudaStream_t s) {
+  if (b.nblk) finalize_kernel<<<b.nblk, kPartBlock, 0, s>>>(b, mode);
+}
+void launch_reduce_obs(const Batch& b, int mode, cudaStream_t s) {
+  if (b.nsys) reduce_obs_kernel<<<b.nsys, 128, 0, s>>>(b, mode);
+}
+void launch_movex(const Batch& b, cudaStream_t s) {
+  if (b.nblk) movex_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
+}
+void launch_renorm(const Batch& b, cudaStream_t s) {
+  if (b.nblk) renorm_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
+}
+void launch_movep(const Batch& b, const double* xi, int last, cudaStream_t s) {
+  if (b.nblk) movep_kernel<<<b.nblk, kPartBlock, 0, s>>>(b, xi, last);
+}
+
+}  // namespace mdsc

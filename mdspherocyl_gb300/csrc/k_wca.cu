@@ -1,0 +1,330 @@
+// Verlet list, WCA core forces and cluster bonds -- the GPU form of
+// neigh_list / check_list (v25/functions.cpp:1298-1394), force_sc
+// (:1397-1553) and the cluster criterion of clust_conf (:2987-3016).
+//
+// List: each particle keeps every partner (both directions, ascending
+// index) whose segment distance is below r_list = max(2^(1/6) sigma_max,
+// sigma_max + min_s) + skin.  It is rebuilt when any rod end may have moved
+// by more than skin/2 since the last build (centre displacement plus half
+// the length times the axis change); the reference's own test looks at the
+// centres only (v25/functions.cpp:1386-1387), which is not enough once the
+// list radius is tight.  The build scans every particle of the system in
+// FP32 (fixed-point separations, exact minimum image).
+//
+// WCA: the force is non-zero only for segment distance < 2^(1/6) sigma_ij.
+// A pair is first screened in FP32; pairs that pass are evaluated exactly as
+// the reference does, in FP64 and with the reference's segment-distance
+// routine and sentinels, always with the lower index as particle i so both
+// members of a pair see the same numbers.  Each particle sums its own pairs
+// in ascending partner order -- the order in which force_sc adds them.
+#include "mdsc_dev.cuh"
+#include "reduce.cuh"
+#include "seg_dist.cuh"
+
+namespace mdsc {
+
+__global__ void __launch_bounds__(kPartBlock) list_build_kernel(Batch b, int force_all) {
+  __shared__ uint32_t sx[kPartBlock], sy[kPartBlock], sz[kPartBlock];
+  __shared__ float4 sa[kPartBlock];
+  const int2 bk = b.blk[blockIdx.x];
+  const int s = bk.x;
+  const SysDev& P = b.sys[s];
+  SysState& S = b.st[s];
+  // rebuild decision, identical in every block of the system
+  bool need = force_all || S.force_list;
+  if (!need) {
+    double m = 0.0;
+    for (int k = 0; k < P.nblk; ++k) m = fmax(m, b.dmax[P.blk_off + k]);
+    need = 2.0 * m > P.skin;
+  }
+  if (blockIdx.x == P.blk_off) S.rebuild = need ? 1 : 0;
+  if (!need) return;
+  const int i = bk.y + threadIdx.x;
+  const bool ok = i < P.part_off + P.n;
+  const int N = b.ntot;
+  uint32_t ux = 0, uy = 0, uz = 0;
+  float4 ai = make_float4(0.f, 0.f, 1.f, 0.f);
+  if (ok) {
+    ux = b.pfx[i];
+    uy = b.pfx[N + i];
+    uz = b.pfx[2 * N + i];
+    ai = b.pax[i];
+  }
+  const float rl = (float)P.r_list;
+  const float rl2 = rl * rl;
+  int cnt = 0;
+  int* out = b.nb + (long long)i * kMaxNb;
+  for (int q0 = 0; q0 < P.n; q0 += kPartBlock) {
+    const int nq = min(kPartBlock, P.n - q0);
+    __syncthreads();
+    if (threadIdx.x < nq) {
+      const int q = P.part_off + q0 + threadIdx.x;
+      sx[threadIdx.x] = b.pfx[q];
+      sy[threadIdx.x] = b.pfx[N + q];
+      sz[threadIdx.x] = b.pfx[2 * N + q];
+      sa[threadIdx.x] = b.pax[q];
+    }
+    __syncthreads();
+    if (!ok) continue;
+    for (int k = 0; k < nq; ++k) {
+      const int q = P.part_off + q0 + k;
+      if (q == i) continue;
+      const float dx = fix_diff(ux, sx[k], P.Lfix[0]);
+      const float dy = fix_diff(uy, sy[k], P.Lfix[1]);
+      const float dz = fix_diff(uz, sz[k], P.Lfix[2]);
+      const float4 aj = sa[k];
+      const float reach = rl + 0.5f * (ai.w + aj.w);
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 >= reach * reach) continue;
+      const float d2 = seg_dist_fast(dx, dy, dz, ai.x, ai.y, ai.z, ai.w, aj.x, aj.y, aj.z, aj.w);
+      if (d2 < rl2) {
+        if (cnt < kMaxNb) out[cnt] = q;
+        ++cnt;
+      }
+    }
+  }
+  if (!ok) return;
+  if (cnt > kMaxNb) atomicOr(&S.status, kErrListOverflow);
+  b.nbc[i] = min(cnt, kMaxNb);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    b.rsave[3 * i + a] = b.r[3 * i + a];
+    b.usave[3 * i + a] = b.O[9 * i + 6 + a];
+  }
+}
+
+__device__ __forceinline__ void load_rod(const Batch& b, int i, RodD& R) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    R.r[a] = b.r[3 * i + a];
+    R.o[a] = b.O[9 * i + 6 + a];
+  }
+  R.len = b.len[i];
+}
+
+// WCA pair (v25/functions.cpp:1438-1540) for A < B; returns false when the
+// pair does not interact.  fA: force on A; tA, tB: torques.
+__device__ bool wca_pair(const Batch& b, const SysDev& P, int A, int B, double* fA, double* tA,
+                         double* tB, double& U, double& W, double* PT, int& err) {
+  RodD ra, rb;
+  load_rod(b, A, ra);
+  load_rod(b, B, rb);
+  const double shA0 = ra.len, shB0 = rb.len;
+  const double sigma = (b.dia[A] + b.dia[B]) / 2;
+  const double sig_sq = sigma * sigma;
+  const double srt = 1.122462048309373;   // 2^(1/6)
+  const double rsh = srt * srt * sig_sq;
+  double rij[3], rsq = 0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    rij[a] = ra.r[a] - rb.r[a];
+    rij[a] -= P.L[a] * floor(rij[a] / P.L[a] + 0.5);
+    rsq += rij[a] * rij[a];
+  }
+  double dij[3], st[2];
+  const double dsq = seg_dist_ref(ra, rb, P.L, rij, dij, st);
+  if (dsq < 0.49 * sig_sq || dsq > rsq * 1.00001) err |= kErrOverlap;
+  if (!(dsq < rsh)) return false;
+  const double SR2s = sig_sq / dsq;
+  const double SR6s = SR2s * SR2s * SR2s;
+  const double pot = 4 * SR6s * (SR6s - 1.);
+  const double ddr = rij[0] * dij[0] + rij[1] * dij[1] + rij[2] * dij[2];
+  U = pot + 1.;
+  W = 6 * (pot + 4 * SR6s * SR6s) * ddr / dsq;
+  const double FIJ = W / ddr;
+  if (!(fabs(FIJ) < 1e300)) err |= kErrNan;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) fA[a] = FIJ * dij[a];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) PT[3 * a + c] = rij[a] * fA[c];
+  const double *oi = ra.o, *oj = rb.o;
+  const double icroj[3] = {oi[1] * oj[2] - oi[2] * oj[1], oi[2] * oj[0] - oi[0] * oj[2],
+                           oi[0] * oj[1] - oi[1] * oj[0]};
+  const double icror[3] = {oi[1] * rij[2] - oi[2] * rij[1], oi[2] * rij[0] - oi[0] * rij[2],
+                           oi[0] * rij[1] - oi[1] * rij[0]};
+  const double jcror[3] = {oj[1] * rij[2] - oj[2] * rij[1], oj[2] * rij[0] - oj[0] * rij[2],
+                           oj[0] * rij[1] - oj[1] * rij[0]};
+  double fact1 = (st[0] - 0.5) * shA0;
+  double fact2 = -(st[1] - 0.5) * shB0;
+  if (st[0] == -1.e+6) fact1 = fact2 = 0.;
+  // as in the reference, -3e10 is tested twice (v25/functions.cpp:1526,1529),
+  // so the (-/+) end-point sentinel keeps the lever arms computed above
+  if (st[0] == -1.e+10) {
+    fact1 = 0.5 * shA0;
+    fact2 = 0.5 * shB0;
+  } else if (st[0] == -2.e+10) {
+    fact1 = -0.5 * shA0;
+    fact2 = -0.5 * shB0;
+  } else if (st[0] == -3.e+10) {
+    fact1 = 0.5 * shA0;
+    fact2 = -0.5 * shB0;
+  }
+  const double fmul = fact1 * fact2;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    tA[a] = FIJ * (fact1 * icror[a] + fmul * icroj[a]);
+    tB[a] = FIJ * (fact2 * jcror[a] - fmul * icroj[a]);
+  }
+  return true;
+}
+
+__global__ void __launch_bounds__(kPartBlock) wca_kernel(Batch b) {
+  __shared__ double sh[11 * kPartBlock / 32];
+  const int2 bk = b.blk[blockIdx.x];
+  const int s = bk.x;
+  const SysDev& P = b.sys[s];
+  const int i = bk.y + threadIdx.x;
+  const bool ok = i < P.part_off + P.n;
+  double acc[11];
+#pragma unroll
+  for (int c = 0; c < 11; ++c) acc[c] = 0.0;
+  int err = 0;
+  if (ok) {
+    const int N = b.ntot;
+    const uint32_t ux = b.pfx[i], uy = b.pfx[N + i], uz = b.pfx[2 * N + i];
+    const float4 ai = b.pax[i];
+    const float di = b.pdia[i];
+    double F[3] = {0, 0, 0}, T[3] = {0, 0, 0};
+    const int nc = b.nbc[i];
+    const int* lst = b.nb + (long long)i * kMaxNb;
+    for (int k = 0; k < nc; ++k) {
+      const int q = lst[k];
+      const float dx = fix_diff(ux, b.pfx[q], P.Lfix[0]);
+      const float dy = fix_diff(uy, b.pfx[N + q], P.Lfix[1]);
+      const float dz = fix_diff(uz, b.pfx[2 * N + q], P.Lfix[2]);
+      const float4 aj = b.pax[q];
+      const float sg = 0.5f * (di + b.pdia[q]);
+      const float d2 = seg_dist_fast(dx, dy, dz, ai.x, ai.y, ai.z, ai.w, aj.x, aj.y, aj.z, aj.w);
+      // 2^(1/3) sigma^2 with a margin for the FP32 screen
+      if (d2 >= 1.2599211f * sg * sg * 1.002f) continue;
+      const int A = min(i, q), B = max(i, q);
+      double fA[3], tA[3], tB[3], U, W, PT[9];
+      if (!wca_pair(b, P, A, B, fA, tA, tB, U, W, PT, err)) continue;
+      if (i == A) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          F[a] += fA[a];
+          T[a] += tA[a];
+        }
+        acc[0] += U;
+        acc[1] += W;
+#pragma unroll
+        for (int c = 0; c < 9; ++c) acc[2 + c] += PT[c];
+      } else {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          F[a] -= fA[a];
+          T[a] += tB[a];
+        }
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      b.Fw[3 * i + a] = F[a];
+      b.Tw[3 * i + a] = T[a];
+    }
+    if (err) atomicOr(&b.st[s].status, err);
+  }
+  double tot[11];
+  block_sum<11, kPartBlock>(acc, sh, tot);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int c = 0; c < 11; ++c) b.wcaE[11 * blockIdx.x + c] = tot[c];
+  }
+}
+
+// ---- clusters (v25/functions.cpp:2987-3016,3282-3324) ----------------
+// bond flags for list entries q > i: segment distance < (D_i + D_j)/2 + min_s,
+// evaluated in FP64 with the reference's routine (lower index first)
+__global__ void __launch_bounds__(kPartBlock) cluster_bonds_kernel(Batch b) {
+  const int2 bk = b.blk[blockIdx.x];
+  const SysDev& P = b.sys[bk.x];
+  const int i = bk.y + threadIdx.x;
+  if (i >= P.part_off + P.n) return;
+  const int nc = b.nbc[i];
+  const int* lst = b.nb + (long long)i * kMaxNb;
+  unsigned char* fl = b.eflag + (long long)i * kMaxNb;
+  b.comp[i] = i;
+  RodD ri;
+  load_rod(b, i, ri);
+  for (int k = 0; k < nc; ++k) {
+    const int q = lst[k];
+    unsigned char bond = 0;
+    if (q > i) {
+      RodD rq;
+      load_rod(b, q, rq);
+      const double sigma = (b.dia[i] + b.dia[q]) / 2 + P.min_s;
+      double rij[3], dij[3], st[2];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        rij[a] = ri.r[a] - rq.r[a];
+        rij[a] -= P.L[a] * floor(rij[a] / P.L[a] + 0.5);
+      }
+      const double dsq = seg_dist_ref(ri, rq, P.L, rij, dij, st);
+      bond = dsq < sigma * sigma ? 1 : 0;
+    }
+    fl[k] = bond;
+  }
+}
+
+__device__ __forceinline__ int find_root(const int* comp, int x) {
+  int p = comp[x];
+  while (p != x) {
+    x = p;
+    p = comp[x];
+  }
+  return x;
+}
+
+// hook: for every bond, attach the larger root to the smaller one
+__global__ void __launch_bounds__(kPartBlock) cluster_hook_kernel(Batch b) {
+  const int2 bk = b.blk[blockIdx.x];
+  const SysDev& P = b.sys[bk.x];
+  const int i = bk.y + threadIdx.x;
+  if (i >= P.part_off + P.n) return;
+  const int nc = b.nbc[i];
+  const int* lst = b.nb + (long long)i * kMaxNb;
+  const unsigned char* fl = b.eflag + (long long)i * kMaxNb;
+  for (int k = 0; k < nc; ++k) {
+    if (!fl[k]) continue;
+    int ra = find_root(b.comp, i), rb = find_root(b.comp, lst[k]);
+    while (ra != rb) {
+      const int hi = max(ra, rb), lo = min(ra, rb);
+      const int old = atomicMin(&b.comp[hi], lo);
+      if (old == hi) {
+        *b.flag = 1;
+        break;
+      }
+      ra = find_root(b.comp, old);
+      rb = find_root(b.comp, lo);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kPartBlock) cluster_compress_kernel(Batch b) {
+  const int2 bk = b.blk[blockIdx.x];
+  const SysDev& P = b.sys[bk.x];
+  const int i = bk.y + threadIdx.x;
+  if (i >= P.part_off + P.n) return;
+  b.comp[i] = find_root(b.comp, i);
+}
+
+void launch_list_build(const Batch& b, int force_all, cudaStream_t s) {
+  if (b.nblk) list_build_kernel<<<b.nblk, kPartBlock, 0, s>>>(b, force_all);
+}
+void launch_wca(const Batch& b, cudaStream_t s) {
+  if (b.nblk) wca_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
+}
+void launch_cluster_bonds(const Batch& b, cudaStream_t s) {
+  if (b.nblk) cluster_bonds_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
+}
+void launch_cluster_hook(const Batch& b, cudaStream_t s) {
+  if (b.nblk) cluster_hook_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
+}
+void launch_cluster_compress(const Batch& b, cudaStream_t s) {
+  if (b.nblk) cluster_compress_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
+}
+
+}  // namespace mdsc

@@ -1,0 +1,182 @@
+// Device-side layout of a batch of MD systems and the helpers the kernels
+// share.  Everything is concatenated over the systems of a batch and
+// addressed through per-system offset tables (SysDev).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mdsc {
+
+constexpr int kTile = 64;        // real-space tile edge, in dipoles
+constexpr int kMaxNb = 64;       // Verlet-list capacity per particle
+constexpr int kMaxD = 4;         // dipoles per particle (MDSC_MAX_DIPOLES)
+constexpr int kPartBlock = 128;  // threads per block of the per-particle kernels
+constexpr int kKBlock = 128;     // k-vectors per block of the k-space kernels
+constexpr int kKChunk = 256;     // particles per block of the structure-factor kernel
+constexpr int kWcaQueue = 32;    // FP64 contact batch per warp
+
+// status bits (OR-ed per system; mapped to mdsc_status on the host)
+enum : int {
+  kErrOverlap = 1,
+  kErrNan = 2,
+  kErrTable = 4,
+  kErrListOverflow = 8,
+};
+
+// modes of the force-assembly kernel
+enum : int {
+  kMaskWca = 1,
+  kMaskReal = 2,
+  kMaskK = 4,
+  kMaskExt = 8,
+  kMaskAll = 15,
+  kFlagAccum = 16,  // F, T += components (else F, T = components)
+  kFlagMoveP = 32,  // then the second half kick (moveP last)
+};
+// modes of the per-system reduction kernel
+enum : int { kRedEnergies = 1, kRedStep = 2 };
+
+// Per-system constants (read-only during a step).
+struct SysDev {
+  int n, nd, ndip;
+  int part_off;   // first particle of the system in the batch arrays
+  int dip_off;    // first dipole
+  int nstrip;     // ceil(ndip / kTile)
+  long long pp_off;  // real-space partials: nstrip*nstrip*6*kTile floats
+  int tile_off, ntile;  // tile list range
+  int k_off, nk;        // k-vector range
+  int kchunk_off, nkchunk;  // structure-factor partial range (chunks of kKChunk particles)
+  int blk_off, nblk;        // per-particle block range
+  int cl_fr;
+  double L[3];
+  double invL[3];
+  double V;
+  double ex1;      // exp(-gamma dt / 2)            (moveTher, v25/functions.cpp:2199)
+  double cnoise;   // sqrt(2 T gamma dt / Q)        (v25/functions.cpp:2200)
+  double ntemp3;   // 3 N T                          (v25/functions.cpp:2204)
+  double alpha;
+  double dt, temp, Q, gamma;
+  double B[3];
+  double r_list;   // Verlet-list radius on the segment distance
+  double skin;
+  double min_s;
+  double sig_max;  // largest pair sigma
+  double Uself;
+  float Lfix[3];   // L / 2^32: fixed-point units to length
+  float Lf[3];
+  // real-space Ewald constants (FP32)
+  float alphaf, alpha2x2;  // alpha, 2 alpha^2
+  float gpref;             // 2 alpha / sqrt(pi)
+  float alpha4x4;          // 4 alpha^4
+  float invLh, halfLh2;    // table spacing of the reference: Lh = 0.5*200.2/32768
+  float rmax_table;        // 100.1: the reference's table covers r <= 100.1
+  float pad;
+};
+
+// Per-system mutable state.
+struct SysState {
+  double xi[2];      // thermostat coordinates (trans, rot)
+  double strn[2];    // stored normals
+  long long step;    // steps since upload
+  int status;
+  int rebuild;       // the list was rebuilt this step
+  int list_builds;
+  int iter;          // step index within the current mdsc_step call (noise row)
+  int force_list;    // rebuild the Verlet list at the next check regardless of the skin
+  double K_first[2]; // kinetic energies after the first half kick
+  double xi_mid[2];  // xi used by the second half kick
+};
+
+// Per-system observables of the last step (mirrors mdsc_observables).
+struct SysObs {
+  double K[2];
+  double U_ss, W_ss, U_dipR, U_dipK, U_ext, U_self;
+  double PT_kin[9], PT_ss[9], PT_dipR[9], PT_dipK[9];
+  double xi[2];
+  long long step;
+  int status, n_clusters, list_builds, pad;
+};
+
+// One batch, device pointers.
+struct Batch {
+  int nsys, ntot, ndtot, nktot, ntiles, nblk;
+  const SysDev* sys;
+  SysState* st;
+  SysObs* obs;
+  // FP64 master state, AoS per particle
+  double* r;     // 3n
+  double* p;     // 3n
+  double* O;     // 9n
+  double* l;     // 3n
+  double* F;     // 3n   total force of the last evaluation
+  double* T;     // 3n
+  double* len;   // n
+  double* dia;   // n
+  double* mass;  // n
+  double* inert; // 3n principal moments (set_inertia)
+  double* invm;  // n  1 / mass
+  double* invI;  // 3n 1 / inertia
+  int* psys;     // n: system of each particle
+  // dipoles: body data and owner
+  double* dpc;   // ndip: offset along the axis
+  double* dob;   // 3 ndip: body-frame direction
+  double* dmu;   // ndip: moment
+  int* downer;   // ndip: particle (batch index)
+  // FP32 / fixed-point working copies written by the integrator
+  uint32_t* pfx; // 3n  particle positions, fixed point (x[n], y[n], z[n] blocks)
+  float4* pax;   // n   rod axis (xyz) and length
+  float* pdia;   // n
+  uint32_t* dfx; // 3 ndip dipole positions, fixed point (SoA blocks)
+  float* dm;     // 3 ndip dipole moment vectors mu*o (SoA blocks)
+  // force components
+  float* rpart;  // real-space partials
+  float* tileE;  // 10 per tile: U, PT[9]
+  int4* tiles;   // (sys, I, J, 0)
+  double* Fw;    // 3n WCA force
+  double* Tw;    // 3n WCA torque
+  double* wcaE;  // per block: U, W, PT[9] = 11
+  // k-space
+  int4* kn;      // (nx, ny, nz, 0) per k
+  float4* kv;    // (kx, ky, kz, val) per k
+  double* kval;  // val per k (FP64)
+  double* kpre;  // pval per k (2 (a4 + 1/k^2)) for the pressure tensor
+  float* kpart;  // structure-factor partials: 10 per (chunk, k)
+  double* ksum;  // 10 per k: uve (6), self, uvslf (3) -- FP64
+  float2* kS;    // val * S(k) per k, FP32 for the gather
+  double* kE;    // 10 per k: energy and pressure-tensor terms
+  double* Fk;    // 3 ndip
+  double* Gk;    // 3 ndip  (torque = m x Gk)
+  // integrator partials, per block
+  double* kin1;  // 2 per block
+  double* kin2;  // 9 per block: K_t, K_r, PTkin xx xy xz yy yz zz, U_ext
+  double* dmax;  // 1 per block: largest displacement measure since the last list build
+  int2* blk;     // (sys, first particle) per block
+  // neighbour list
+  int* nb;       // n * kMaxNb
+  int* nbc;      // n
+  double* rsave; // 3n positions at the last build
+  double* usave; // 3n axes at the last build
+  // clusters
+  int* comp;     // n component representative
+  unsigned char* eflag;  // n * kMaxNb: list entry is a cluster bond
+  int* flag;     // 1 changed flag
+  // thermostat noise: [iter][sys][4] = g0_t, g1_t, g0_r, g1_r
+  const double* noise;
+};
+
+// ---- small helpers ----------------------------------------------------
+__host__ __device__ inline int cdiv(int a, int b) { return (a + b - 1) / b; }
+
+// fixed-point image of a coordinate: fraction of the box in [0, 2^32)
+__device__ inline uint32_t to_fix(double x, double invL) {
+  double t = x * invL;
+  t -= floor(t);
+  return (uint32_t)(unsigned long long)(t * 4294967296.0);
+}
+
+// minimum-image difference of two fixed-point coordinates, in length units
+__device__ inline float fix_diff(uint32_t a, uint32_t b, float scale) {
+  return (float)(int32_t)(a - b) * scale;
+}
+
+}  // namespace mdsc

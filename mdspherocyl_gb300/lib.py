@@ -1,0 +1,340 @@
+"""ctypes binding of the C ABI (include/mdsc.h) and a thin Python front-end.
+
+The library is the in-tree build mdspherocyl_gb300/_lib/libmdsc.so.  There
+is no fallback: if it cannot be built or loaded, or no GPU is visible,
+every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import POINTER, c_char_p, c_double, c_int, c_longlong, c_size_t, c_ulong, c_void_p
+
+import numpy as np
+
+from . import build as _build
+from .systems import SystemSpec, SystemState
+
+_dp = POINTER(c_double)
+_ip = POINTER(c_int)
+
+MAX_DIPOLES = 4
+
+STATUS = {
+    0: "MDSC_OK", 1: "MDSC_ERR_BAD_ARG", 2: "MDSC_ERR_CUDA", 3: "MDSC_ERR_OOM",
+    4: "MDSC_ERR_OVERLAP", 5: "MDSC_ERR_NAN", 6: "MDSC_ERR_TABLE_RANGE",
+    7: "MDSC_ERR_LIST_OVERFLOW", 8: "MDSC_ERR_NO_DEVICE", 9: "MDSC_ERR_TOO_LARGE",
+    10: "MDSC_ERR_STATE",
+}
+
+# every entry point include/mdsc.h declares
+EXPORTS = [
+    "mdsc_create", "mdsc_destroy", "mdsc_num_systems", "mdsc_device_bytes", "mdsc_estimate_bytes",
+    "mdsc_last_error", "mdsc_upload", "mdsc_download", "mdsc_upload_all", "mdsc_download_all",
+    "mdsc_set_thermostat", "mdsc_zero_forces", "mdsc_force_sc", "mdsc_force_dipR",
+    "mdsc_force_dipK", "mdsc_ext_field", "mdsc_self_ener", "mdsc_moveX", "mdsc_moveP",
+    "mdsc_renorm", "mdsc_neigh_list", "mdsc_check_list", "mdsc_clust_conf", "mdsc_step",
+    "mdsc_observe", "mdsc_launches_per_step", "mdsc_stream", "mdsc_profile_steps",
+]
+
+
+class SystemDesc(ctypes.Structure):
+    _fields_ = [
+        ("n", c_int), ("nd", c_int), ("box", c_double * 3), ("alpha", c_double),
+        ("K_max", c_int), ("ksq_max", c_int), ("sr_cut", c_double), ("dt", c_double),
+        ("temp", c_double), ("Q", c_double), ("gamma", c_double), ("xi0", c_double),
+        ("B", c_double * 3), ("min_s", c_double), ("cl_fr", c_int),
+        ("thermo_seed", c_ulong * 2), ("cluster_seed", c_ulong), ("cluster_skip", c_ulong),
+    ]
+
+
+class HostState(ctypes.Structure):
+    _fields_ = [
+        ("r", _dp), ("p", _dp), ("O", _dp), ("l", _dp), ("F", _dp), ("T", _dp),
+        ("len", _dp), ("dia", _dp), ("mass", _dp), ("dip", _dp), ("clust", _ip),
+    ]
+
+
+class Observables(ctypes.Structure):
+    _fields_ = [
+        ("K", c_double * 2), ("U_ss", c_double), ("W_ss", c_double), ("U_dipR", c_double),
+        ("U_dipK", c_double), ("U_ext", c_double), ("U_self", c_double),
+        ("PT_kin", c_double * 9), ("PT_ss", c_double * 9), ("PT_dipR", c_double * 9),
+        ("PT_dipK", c_double * 9), ("xi", c_double * 2), ("step", c_longlong),
+        ("status", c_int), ("n_clusters", c_int), ("list_builds", c_int), ("pad", c_int),
+    ]
+
+    def as_dict(self) -> dict:
+        d = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            d[name] = list(v) if hasattr(v, "__len__") else v
+        return d
+
+
+class MdscError(RuntimeError):
+    def __init__(self, code: int, where: str, detail: str = ""):
+        self.code = code
+        super().__init__(f"{where}: {STATUS.get(code, code)} {detail}".strip())
+
+
+_LIB = None
+
+
+def load(build: bool = True) -> ctypes.CDLL:
+    """Load libmdsc.so (building it first if needed)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.build() if build else _build.LIB
+    if not os.path.exists(path):
+        raise RuntimeError(f"libmdsc.so not found at {path}")
+    lib = ctypes.CDLL(path)
+    P = POINTER
+    sig = {
+        "mdsc_create": (c_int, [P(SystemDesc), c_int, c_int, P(c_void_p)]),
+        "mdsc_destroy": (c_int, [c_void_p]),
+        "mdsc_num_systems": (c_int, [c_void_p]),
+        "mdsc_device_bytes": (c_size_t, [c_void_p]),
+        "mdsc_estimate_bytes": (c_size_t, [P(SystemDesc), c_int]),
+        "mdsc_last_error": (c_int, [c_void_p, c_char_p, c_size_t]),
+        "mdsc_upload": (c_int, [c_void_p, c_int, P(HostState)]),
+        "mdsc_download": (c_int, [c_void_p, c_int, P(HostState)]),
+        "mdsc_upload_all": (c_int, [c_void_p, P(HostState)]),
+        "mdsc_download_all": (c_int, [c_void_p, P(HostState)]),
+        "mdsc_set_thermostat": (c_int, [c_void_p, c_int, _dp, _dp]),
+        "mdsc_zero_forces": (c_int, [c_void_p]),
+        "mdsc_force_sc": (c_int, [c_void_p, _dp, _dp, _dp]),
+        "mdsc_force_dipR": (c_int, [c_void_p, _dp, _dp]),
+        "mdsc_force_dipK": (c_int, [c_void_p, _dp, _dp]),
+        "mdsc_ext_field": (c_int, [c_void_p, _dp]),
+        "mdsc_self_ener": (c_int, [c_void_p, _dp]),
+        "mdsc_moveX": (c_int, [c_void_p]),
+        "mdsc_moveP": (c_int, [c_void_p, _dp, c_int, _dp, _dp]),
+        "mdsc_renorm": (c_int, [c_void_p]),
+        "mdsc_neigh_list": (c_int, [c_void_p]),
+        "mdsc_check_list": (c_int, [c_void_p, _ip]),
+        "mdsc_clust_conf": (c_int, [c_void_p, c_int, _ip, _ip]),
+        "mdsc_step": (c_int, [c_void_p, c_int, P(Observables)]),
+        "mdsc_observe": (c_int, [c_void_p, P(Observables)]),
+        "mdsc_launches_per_step": (c_int, [c_void_p]),
+        "mdsc_stream": (c_void_p, [c_void_p]),
+        "mdsc_profile_steps": (c_int, [c_void_p, c_int, c_int, c_char_p, c_size_t, _dp, _ip]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def desc_from_spec(spec: SystemSpec, nd: int) -> SystemDesc:
+    d = SystemDesc()
+    d.n, d.nd = int(spec.n), int(nd)
+    for a in range(3):
+        d.box[a] = float(spec.box[a])
+        d.B[a] = float(spec.B[a])
+    d.alpha = float(spec.alpha)
+    d.K_max, d.ksq_max = int(spec.K_max), int(spec.ksq_max)
+    d.sr_cut = float(spec.sr_cut)
+    d.dt, d.temp, d.Q, d.gamma, d.xi0 = (float(spec.dt), float(spec.temp), float(spec.Q),
+                                          float(spec.gamma), float(spec.xi0))
+    d.min_s = float(spec.min_s)
+    d.cl_fr = int(spec.cl_fr)
+    d.thermo_seed[0], d.thermo_seed[1] = 1, 2
+    d.cluster_seed, d.cluster_skip = 1, 0
+    return d
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+class Batch:
+    """One handle of the library: nsys independent systems resident on the GPU.
+
+    Mirrors the reference's hot-path functions (force_sc, force_dipR,
+    force_dipK, ext_field, self_ener, moveX, moveP, renorm, neigh_list,
+    check_list, clust_conf) and adds the fused, graph-captured step.
+    """
+
+    def __init__(self, specs, states=None, device: int = 0, descs=None):
+        self.lib = load()
+        self.specs = list(specs)
+        if descs is None:
+            nds = [states[k].dip.shape[1] if states is not None else 1 for k in range(len(self.specs))]
+            descs = [desc_from_spec(s, nd) for s, nd in zip(self.specs, nds)]
+        self.nsys = len(descs)
+        self._descs = (SystemDesc * self.nsys)(*descs)
+        h = c_void_p()
+        self._check(self.lib.mdsc_create(self._descs, self.nsys, device, ctypes.byref(h)), "mdsc_create")
+        self.h = h
+        self.n = [d.n for d in descs]
+        self.nd = [d.nd for d in descs]
+        if states is not None:
+            for k, st in enumerate(states):
+                self.upload(k, st)
+
+    # -- plumbing --
+    def _err(self) -> str:
+        if not getattr(self, "h", None):
+            return ""
+        buf = ctypes.create_string_buffer(512)
+        self.lib.mdsc_last_error(self.h, buf, 512)
+        return buf.value.decode(errors="replace")
+
+    def _check(self, code: int, where: str) -> None:
+        if code != 0:
+            raise MdscError(code, where, self._err())
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.mdsc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def device_bytes(self) -> int:
+        return int(self.lib.mdsc_device_bytes(self.h))
+
+    @property
+    def launches_per_step(self) -> int:
+        return int(self.lib.mdsc_launches_per_step(self.h))
+
+    # -- state --
+    @staticmethod
+    def _hoststate(r, p, O, l, F=None, T=None, length=None, dia=None, mass=None, dip=None, clust=None):
+        hs = HostState()
+        hs.r, hs.p, hs.O, hs.l = _ptr(r), _ptr(p), _ptr(O), _ptr(l)
+        hs.F, hs.T = _ptr(F), _ptr(T)
+        hs.len, hs.dia, hs.mass, hs.dip = _ptr(length), _ptr(dia), _ptr(mass), _ptr(dip)
+        hs.clust = None if clust is None else clust.ctypes.data_as(_ip)
+        return hs
+
+    def upload(self, k: int, st: SystemState, F=None, T=None) -> None:
+        c = lambda a: np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
+        arrs = dict(r=c(st.r), p=c(st.p), O=c(st.O), l=c(st.l), length=c(st.length), dia=c(st.dia),
+                    mass=c(st.mass), dip=c(st.dip), F=None if F is None else c(F),
+                    T=None if T is None else c(T))
+        hs = self._hoststate(**arrs)
+        self._check(self.lib.mdsc_upload(self.h, k, ctypes.byref(hs)), "mdsc_upload")
+
+    def download(self, k: int, template: SystemState | None = None) -> dict:
+        n = self.n[k]
+        out = dict(r=np.zeros((n, 3)), p=np.zeros((n, 3)), O=np.zeros((n, 3, 3)), l=np.zeros((n, 3)),
+                   F=np.zeros((n, 3)), T=np.zeros((n, 3)), clust=np.zeros(n, np.int32))
+        hs = self._hoststate(out["r"], out["p"], out["O"], out["l"], out["F"], out["T"], clust=out["clust"])
+        self._check(self.lib.mdsc_download(self.h, k, ctypes.byref(hs)), "mdsc_download")
+        return out
+
+    def upload_all(self, r, p, O, l, F=None, T=None, length=None, dia=None, mass=None, dip=None) -> None:
+        hs = self._hoststate(r, p, O, l, F, T, length, dia, mass, dip)
+        self._check(self.lib.mdsc_upload_all(self.h, ctypes.byref(hs)), "mdsc_upload_all")
+
+    def download_all(self, r, p, O, l, F=None, T=None) -> None:
+        hs = self._hoststate(r, p, O, l, F, T)
+        self._check(self.lib.mdsc_download_all(self.h, ctypes.byref(hs)), "mdsc_download_all")
+
+    def set_thermostat(self, k: int, xi, strn=None) -> None:
+        x = np.ascontiguousarray(xi, dtype=np.float64)
+        s = None if strn is None else np.ascontiguousarray(strn, dtype=np.float64)
+        self._check(self.lib.mdsc_set_thermostat(self.h, k, _ptr(x), _ptr(s)), "mdsc_set_thermostat")
+
+    # -- the reference's functions --
+    def zero_forces(self):
+        self._check(self.lib.mdsc_zero_forces(self.h), "mdsc_zero_forces")
+
+    def force_sc(self):
+        U, W, PT = np.zeros(self.nsys), np.zeros(self.nsys), np.zeros((self.nsys, 9))
+        code = self.lib.mdsc_force_sc(self.h, _ptr(U), _ptr(W), _ptr(PT))
+        self._check(code, "mdsc_force_sc")
+        return U, W, PT.reshape(self.nsys, 3, 3)
+
+    def force_dipR(self):
+        U, PT = np.zeros(self.nsys), np.zeros((self.nsys, 9))
+        self._check(self.lib.mdsc_force_dipR(self.h, _ptr(U), _ptr(PT)), "mdsc_force_dipR")
+        return U, PT.reshape(self.nsys, 3, 3)
+
+    def force_dipK(self):
+        U, PT = np.zeros(self.nsys), np.zeros((self.nsys, 9))
+        self._check(self.lib.mdsc_force_dipK(self.h, _ptr(U), _ptr(PT)), "mdsc_force_dipK")
+        return U, PT.reshape(self.nsys, 3, 3)
+
+    def ext_field(self):
+        U = np.zeros(self.nsys)
+        self._check(self.lib.mdsc_ext_field(self.h, _ptr(U)), "mdsc_ext_field")
+        return U
+
+    def self_ener(self):
+        U = np.zeros(self.nsys)
+        self._check(self.lib.mdsc_self_ener(self.h, _ptr(U)), "mdsc_self_ener")
+        return U
+
+    def moveX(self):
+        self._check(self.lib.mdsc_moveX(self.h), "mdsc_moveX")
+
+    def moveP(self, xi, last: bool):
+        x = np.ascontiguousarray(np.broadcast_to(np.asarray(xi, dtype=np.float64), (self.nsys, 2)))
+        K, PT = np.zeros((self.nsys, 2)), np.zeros((self.nsys, 9))
+        self._check(self.lib.mdsc_moveP(self.h, _ptr(x), int(last), _ptr(K), _ptr(PT)), "mdsc_moveP")
+        return K, PT.reshape(self.nsys, 3, 3)
+
+    def renorm(self):
+        self._check(self.lib.mdsc_renorm(self.h), "mdsc_renorm")
+
+    def neigh_list(self):
+        self._check(self.lib.mdsc_neigh_list(self.h), "mdsc_neigh_list")
+
+    def check_list(self):
+        out = np.zeros(self.nsys, np.int32)
+        self._check(self.lib.mdsc_check_list(self.h, out.ctypes.data_as(_ip)), "mdsc_check_list")
+        return out.astype(bool)
+
+    def clust_conf(self, k: int):
+        lab = np.zeros(self.n[k], np.int32)
+        nc = c_int(0)
+        self._check(self.lib.mdsc_clust_conf(self.h, k, lab.ctypes.data_as(_ip), ctypes.byref(nc)),
+                    "mdsc_clust_conf")
+        return lab, nc.value
+
+    # -- fused step --
+    def step(self, nsteps: int = 1):
+        obs = (Observables * self.nsys)()
+        self._check(self.lib.mdsc_step(self.h, int(nsteps), obs), "mdsc_step")
+        return [o.as_dict() for o in obs]
+
+    def observe(self):
+        obs = (Observables * self.nsys)()
+        self._check(self.lib.mdsc_observe(self.h, obs), "mdsc_observe")
+        return [o.as_dict() for o in obs]
+
+    def profile(self, nsteps: int):
+        nmax, stride = 16, 32
+        names = ctypes.create_string_buffer(nmax * stride)
+        ms = np.zeros(nmax)
+        nk = c_int(0)
+        self._check(self.lib.mdsc_profile_steps(self.h, nsteps, nmax, names, stride, _ptr(ms),
+                                                ctypes.byref(nk)), "mdsc_profile_steps")
+        out = {}
+        for k in range(nk.value):
+            nm = names.raw[k * stride:(k + 1) * stride].split(b"\0")[0].decode()
+            out[nm] = float(ms[k])
+        return out
+
+
+def estimate_bytes(descs) -> int:
+    lib = load()
+    arr = (SystemDesc * len(descs))(*descs)
+    return int(lib.mdsc_estimate_bytes(arr, len(descs)))
