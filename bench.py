@@ -1,0 +1,331 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 MD step on the 256-replica mix.
+
+Workload (default "replica_mix"): 256 independent dipolar-spherocylinder
+systems, N log-uniform in [128, 2048] (182,573 particles in all), packing
+fraction U[0.05, 0.25], mu^2 U[0.5, 4], T U[0.8, 1.5], lengths U[2, 4],
+alpha = 6/L_box, |n|^2 <= 36, real space over all minimum-image pairs,
+Nose thermostat Q = 1, dt = 1e-3; seeded synthetic configurations.  One
+"step" advances every system by one MD step in one CUDA-graph launch.
+
+Metric: aggregate particle-steps/s.  `value` is device-timed with the
+state resident in HBM (CUDA events around each step, L2 flushed between
+steps); `e2e` goes through the C ABI with host buffers: every step uploads
+the packed state (r, p, O, l, F, T) from pinned memory, steps once and
+downloads it again.
+
+  python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+
+--impl reference times the reference's CPU routines (the C restatement in
+oracle/, all host threads) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "particle-steps/s batched/served vs plain GPU at <=1e-5 force err; job p50/p99"
+UNIT = "particle-steps/s"
+# real-space Ewald pair: FLOP per dipole pair of the tile kernel
+# (minimum image 9, r^2 5, rsqrt 1, erfc + exp ~30, A B C 12, table
+# correction 15, three dot products 15, energy 4, force 21, torques 36,
+# pressure tensor 18, accumulation 13 -> ~180, the figure of the survey)
+FLOP_PER_PAIR = 180.0
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def build_mix(seed: int, nsys: int):
+    from mdspherocyl_gb300 import systems as S
+
+    ds = S.replica_mix_specs(n_systems=nsys, seed=seed)
+    return [S.replica_system(d) for d in ds], ds
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def cpu_sample(states, threads: int, budget_s: float = 20.0, stride: int = 16):
+    """Times the oracle's MD step (the reference's routines restated in C,
+    OpenMP over `threads` host threads) on every `stride`-th system of the
+    mix -- a sample that spans the mix's N distribution -- one step each,
+    until `budget_s` is spent.  Returns particle-steps/s and the sample."""
+    import oracle
+
+    orc = oracle.Oracle()
+    orc.set_threads(threads)
+    done_p, t_tot, used = 0, 0.0, []
+    for k in range(0, len(states), stride):
+        spec, st = states[k]
+        o = oracle.System(st.r, st.p, st.O, st.l, st.length, st.dia, st.mass, st.dip, spec.box)
+        md = oracle.MDOracle(orc, o, dt=spec.dt, temp=spec.temp, Q=spec.Q, gamma=spec.gamma, xi0=spec.xi0,
+                             sr_cut=3.0, K_max=spec.K_max, ksq_max=spec.ksq_max, alpha=spec.alpha, B=spec.B)
+        t0 = time.perf_counter()
+        md.step()
+        t_tot += time.perf_counter() - t0
+        done_p += spec.n
+        used.append(spec.n)
+        md.close()
+        if t_tot > budget_s:
+            break
+    return done_p / t_tot, used, t_tot
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    states, _ = build_mix(args.seed, args.systems)
+    vals = []
+    used, tt = [], 0.0
+    for it in range(args.warmup + args.steps):
+        v, used, tt = cpu_sample(states, threads, budget_s=args.cpu_budget / max(args.steps, 1))
+        if it >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    sample = (f"oracle MD step (reference routines restated in C, OpenMP) on {len(used)} of "
+              f"{len(states)} systems (every 16th, N={min(used)}..{max(used)}, {sum(used)} particles), "
+              f"one step each per timed step")
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * tt, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "replica_mix", "systems": len(states),
+                   "particles": int(sum(s.n for s, _ in states)), "ksq_max": 36,
+                   "real_space": "all minimum-image pairs"},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def run_ours(args):
+    ws, rank, local = dist_env()
+    import torch
+
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    device = local if torch.cuda.is_available() else 0
+    torch.cuda.set_device(device)
+    from mdspherocyl_gb300 import lib as L
+
+    t0 = time.time()
+    states, _ = build_mix(args.seed + 1000 * rank, args.systems)
+    specs = [s for s, _ in states]
+    sts = [st for _, st in states]
+    ntot = int(sum(s.n for s in specs))
+    log(f"[rank {rank}] workload built in {time.time() - t0:.1f}s: {len(specs)} systems, {ntot} particles")
+    bt = L.Batch(specs, sts, device=device)
+    stream = torch.cuda.ExternalStream(bt.lib.mdsc_stream(bt.h), device=device)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{device}")
+
+    # ---- device-resident throughput ----
+    bt.step(max(args.warmup, 3))
+    torch.cuda.synchronize()
+    clk = ClockSampler(device)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clk.start()
+    ms = []
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()  # L2 (129 MB) flushed between timed steps, outside the timed region
+        code = bt.lib.mdsc_step(bt.h, 1, None)  # CUDA events on the library's stream around the step
+        if code != 0:
+            raise L.MdscError(code, "mdsc_step", bt._err())
+        ms.append(bt.lib.mdsc_last_device_ms(bt.h))
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    t_dev = sum(ms) / 1e3
+    if ws > 1:
+        tt = torch.tensor([t_dev], device=f"cuda:{device}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_dev = float(tt.item())
+    value = ntot * ws * args.steps / t_dev
+    obs = bt.observe()
+    st_ok = all(o["status"] == 0 for o in obs)
+
+    # ---- kernel times (events per kernel, serialised) ----
+    prof = bt.profile(max(2, min(5, args.steps)))
+    pairs = sum(s.n * (s.n - 1) // 2 for s in specs)
+    rp_ms = prof.get("real_pairs", float("nan"))
+    achieved = FLOP_PER_PAIR * pairs / (rp_ms * 1e-3) / 1e12
+    peaks, src = measured_peaks()
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    fp32_peak = 2 * 128 * 152 * sm_max * 1e6 / 1e12
+
+    # ---- end to end through the C ABI with host buffers ----
+    nd = sts[0].dip.shape[1]
+    pin = lambda *shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()  # noqa: E731
+    h = {k: pin(ntot, 3) for k in ("r", "p", "l", "F", "T")}
+    h["O"] = pin(ntot, 3, 3)
+    bt.download_all(h["r"], h["p"], h["O"], h["l"], h["F"], h["T"])
+    bytes_h2d = sum(v.nbytes for v in h.values())
+    bytes_d2h = bytes_h2d
+    for _ in range(2):
+        bt.upload_all(h["r"], h["p"], h["O"], h["l"], h["F"], h["T"])
+        bt.lib.mdsc_step(bt.h, 1, None)
+        bt.download_all(h["r"], h["p"], h["O"], h["l"], h["F"], h["T"])
+    e2e_steps = max(3, min(args.steps, 20))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        bt.upload_all(h["r"], h["p"], h["O"], h["l"], h["F"], h["T"])
+        bt.lib.mdsc_step(bt.h, 1, None)
+        bt.download_all(h["r"], h["p"], h["O"], h["l"], h["F"], h["T"])
+    torch.cuda.synchronize()
+    t_e2e = time.perf_counter() - t0
+    if ws > 1:
+        tt = torch.tensor([t_e2e], device=f"cuda:{device}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    e2e = ntot * ws * e2e_steps / t_e2e
+    launches = bt.launches_per_step + 1  # + the per-call reset of the noise row
+
+    out = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu and ws == 1:
+            threads = os.cpu_count() or 1
+            v, used, tt = cpu_sample(states, threads, budget_s=args.cpu_budget)
+            cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": (f"oracle MD step (reference routines restated in C, OpenMP, {threads} threads) "
+                              f"on every 16th system of the mix ({len(used)} systems, N={min(used)}..{max(used)}, "
+                              f"{sum(used)} particles), one step each, {tt:.1f}s")}
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair/k-space arithmetic, f64 state and sums",
+            "data": "synthetic",
+            "config": {"workload": "replica_mix", "systems": len(specs), "particles": ntot,
+                       "N_range": [min(s.n for s in specs), max(s.n for s in specs)], "ksq_max": 36,
+                       "alpha": "6/L_box", "real_space": "all minimum-image pairs", "dt": 1e-3,
+                       "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{ws}",
+                       "graph": "one CUDA graph per step"},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": bytes_h2d,
+                    "d2h_bytes_per_step": bytes_d2h},
+            "gpu_launches": launches * args.steps,
+            "roofline": {"bound": "fp32", "kernel": "real_pairs", "achieved": achieved, "peak": fp32_peak,
+                         "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
+                         "peak_source": (f"nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 FLOP at "
+                                         f"{sm_max:.0f} MHz ({src} max SM clock); MEASURED_PEAKS.json has "
+                                         f"HBM and bf16 tensor figures only"),
+                         "flop_per_pair": FLOP_PER_PAIR, "pairs_per_launch": pairs,
+                         "kernel_ms": rp_ms},
+            "kernel_ms": prof,
+            "clocks": clocks,
+            "status_ok": st_ok,
+        }
+        if cpu is not None:
+            out["cpu_baseline"] = cpu
+        print(json.dumps(out), flush=True)
+    bt.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--systems", type=int, default=256)
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

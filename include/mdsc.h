@@ -194,10 +194,24 @@ mdsc_status mdsc_observe(mdsc_batch* b, mdsc_observables* obs);
    CUDA stream the batch runs on (a cudaStream_t). */
 int mdsc_launches_per_step(const mdsc_batch* b);
 void* mdsc_stream(const mdsc_batch* b);
+/* Device time (ms) of the last mdsc_step call: CUDA events on the batch's
+   stream around its noise upload and graph launches. */
+double mdsc_last_device_ms(const mdsc_batch* b);
 /* Average device time (ms) per launch of each kernel over the last
    mdsc_profile_steps call: names and times in the order of `names`. */
 mdsc_status mdsc_profile_steps(mdsc_batch* b, int nsteps, int max_kernels, char* names,
                                size_t name_stride, double* ms_per_launch, int* n_kernels);
+
+/* ---- utility ------------------------------------------------------------ */
+/* Seeded random non-overlapping placement of n rods in a periodic box
+   (sequential rejection on the segment distance, gap added to
+   (D_i + D_j)/2): centres r (n*3) and orientation matrices O (n*9).  Host
+   code, no GPU.  No counterpart on the reference's hot path: the reference
+   starts from a lattice plus cluster pivots (v25/functions.cpp:491-1156,
+   3328-3409), which stays out of scope.  Returns MDSC_ERR_TOO_LARGE when
+   max_attempts + 100 n proposals do not place every rod. */
+int mdsc_place_rods(int n, const double* len, const double* dia, const double* box,
+                    unsigned long long seed, double gap, int max_attempts, double* r, double* O);
 
 #ifdef __cplusplus
 }

@@ -18,7 +18,7 @@ INCLUDE = os.path.join(ROOT, "include")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libmdsc.so")
 
-SOURCES = ["k_real.cu", "k_kspace.cu", "k_int.cu", "k_wca.cu", "api.cu"]
+SOURCES = ["k_real.cu", "k_kspace.cu", "k_int.cu", "k_wca.cu", "api.cu", "gen.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
            "--expt-relaxed-constexpr", "-I", CSRC, "-I", INCLUDE]
@@ -58,7 +58,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
     flags = NVFLAGS + (extra_flags or [])
 
     def one(src):
-        obj = os.path.join(objdir, src.replace(".cu", ".o"))
+        obj = os.path.join(objdir, os.path.splitext(src)[0] + ".o")
         cmd = [cc] + ARCH + flags + ["-c", os.path.join(CSRC, src), "-o", obj]
         if src == "k_wca.cu":
             # the exact FP64 pair path keeps the reference's rounding: no FMA contraction

@@ -276,6 +276,8 @@ struct mdsc_batch {
   std::vector<int> n_clusters;
   std::vector<char> uploaded, built, have_forces;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  cudaEvent_t t_beg = nullptr, t_end = nullptr;  // device time of the last mdsc_step
+  double last_ms = 0.0;
   int launches = 0;
   std::string err;
 };
@@ -590,6 +592,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
       cudaEventCreateWithFlags(&B->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&B->ev_j2, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&B->ev_j3, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreate(&B->t_beg) != cudaSuccess || cudaEventCreate(&B->t_end) != cudaSuccess ||
       cudaMallocHost(&B->h_noise, sizeof(double) * kNoiseChunk * nsys * 4) != cudaSuccess ||
       cudaMallocHost(&B->h_obs, sizeof(SysObs) * nsys) != cudaSuccess) {
     mdsc_destroy(B);
@@ -664,6 +667,8 @@ mdsc_status mdsc_destroy(mdsc_batch* B) {
   if (B->ev_fork) cudaEventDestroy(B->ev_fork);
   if (B->ev_j2) cudaEventDestroy(B->ev_j2);
   if (B->ev_j3) cudaEventDestroy(B->ev_j3);
+  if (B->t_beg) cudaEventDestroy(B->t_beg);
+  if (B->t_end) cudaEventDestroy(B->t_end);
   if (B->st) cudaStreamDestroy(B->st);
   if (B->s2) cudaStreamDestroy(B->s2);
   if (B->s3) cudaStreamDestroy(B->s3);
@@ -1032,6 +1037,7 @@ mdsc_status mdsc_step(mdsc_batch* B, int nsteps, mdsc_observables* obs) {
     }
   int which = 0;
   int done = 0;
+  double dev_ms = 0.0;
   while (done < nsteps) {
     // steps until the next clustering step of any system (inclusive)
     int chunk = std::min(nsteps - done, kNoiseChunk);
@@ -1045,10 +1051,18 @@ mdsc_status mdsc_step(mdsc_batch* B, int nsteps, mdsc_observables* obs) {
     // noise for this chunk; the other buffer may still be read by the GPU
     CU(cudaStreamSynchronize(B->st));
     draw_noise(B, chunk);
+    CU(cudaEventRecord(B->t_beg, B->st));
     CU(cudaMemcpyAsync(B->noise[which], B->h_noise, sizeof(double) * chunk * B->nsys * 4,
                        cudaMemcpyHostToDevice, B->st));
     launch_reset_iter(B->b, B->st);
     for (int k = 0; k < chunk; ++k) CU(cudaGraphLaunch(B->graph[which], B->st));
+    CU(cudaEventRecord(B->t_end, B->st));
+    {
+      CU(cudaEventSynchronize(B->t_end));
+      float t = 0.f;
+      CU(cudaEventElapsedTime(&t, B->t_beg, B->t_end));
+      dev_ms += t;
+    }
     std::vector<int> due;
     for (int s = 0; s < B->nsys; ++s) {
       const int fr = B->desc[s].cl_fr;
@@ -1063,8 +1077,11 @@ mdsc_status mdsc_step(mdsc_batch* B, int nsteps, mdsc_observables* obs) {
     done += chunk;
     which ^= 1;
   }
+  B->last_ms = dev_ms;
   return read_obs(B, obs);
 }
+
+double mdsc_last_device_ms(const mdsc_batch* B) { return B ? B->last_ms : 0.0; }
 
 mdsc_status mdsc_observe(mdsc_batch* B, mdsc_observables* obs) {
   if (!B) return MDSC_ERR_BAD_ARG;

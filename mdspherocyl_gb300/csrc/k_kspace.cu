@@ -28,8 +28,10 @@ namespace mdsc {
 __device__ __forceinline__ void phase_exp(uint32_t ux, uint32_t uy, uint32_t uz, int4 n, float& c,
                                           float& s) {
   const uint32_t ph = (uint32_t)n.x * ux + (uint32_t)n.y * uy + (uint32_t)n.z * uz;
-  const float t = (float)(int32_t)ph * 4.656612873077393e-10f;  // 2^-31: phase / pi in [-1, 1)
-  sincospif(t, &s, &c);
+  // (int)ph * 2^-31 * pi: the phase, already reduced to [-pi, pi); the
+  // hardware sine/cosine is accurate to ~4e-7 absolute on that range
+  const float x = (float)(int32_t)ph * 1.4629180792671596e-09f;
+  __sincosf(x, &s, &c);
 }
 
 // grid: one block per (system, particle chunk, k tile); work list kwork

@@ -170,26 +170,35 @@ __device__ bool wca_pair(const Batch& b, const SysDev& P, int A, int B, double* 
   return true;
 }
 
+// Two phases per warp.  (1) Each lane screens its particle's list in FP32
+// and keeps the candidate partners (ascending index) in shared memory.  (2)
+// The warp's candidates, concatenated owner by owner, are evaluated 32 at a
+// time in FP64 with every lane busy; each owner then adds its own entries in
+// order.  FP64 runs at a small fraction of the FP32 rate on this GPU, so
+// only pairs that can touch reach the FP64 pipe, densely packed.
+constexpr int kMaxC = 24;  // contact candidates per particle
+
 __global__ void __launch_bounds__(kPartBlock) wca_kernel(Batch b) {
+  __shared__ int cand[kPartBlock][kMaxC];
+  __shared__ double res[kPartBlock / 32][32][6];
+  __shared__ int soff[kPartBlock / 32][32];
   __shared__ double sh[11 * kPartBlock / 32];
   const int2 bk = b.blk[blockIdx.x];
   const int s = bk.x;
   const SysDev& P = b.sys[s];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int i = bk.y + threadIdx.x;
   const bool ok = i < P.part_off + P.n;
-  double acc[11];
-#pragma unroll
-  for (int c = 0; c < 11; ++c) acc[c] = 0.0;
+  const int N = b.ntot;
   int err = 0;
+  int nc = 0;
   if (ok) {
-    const int N = b.ntot;
     const uint32_t ux = b.pfx[i], uy = b.pfx[N + i], uz = b.pfx[2 * N + i];
     const float4 ai = b.pax[i];
     const float di = b.pdia[i];
-    double F[3] = {0, 0, 0}, T[3] = {0, 0, 0};
-    const int nc = b.nbc[i];
+    const int nl = b.nbc[i];
     const int* lst = b.nb + (long long)i * kMaxNb;
-    for (int k = 0; k < nc; ++k) {
+    for (int k = 0; k < nl; ++k) {
       const int q = lst[k];
       const float dx = fix_diff(ux, b.pfx[q], P.Lfix[0]);
       const float dy = fix_diff(uy, b.pfx[N + q], P.Lfix[1]);
@@ -197,36 +206,89 @@ __global__ void __launch_bounds__(kPartBlock) wca_kernel(Batch b) {
       const float4 aj = b.pax[q];
       const float sg = 0.5f * (di + b.pdia[q]);
       const float d2 = seg_dist_fast(dx, dy, dz, ai.x, ai.y, ai.z, ai.w, aj.x, aj.y, aj.z, aj.w);
-      // 2^(1/3) sigma^2 with a margin for the FP32 screen
+      // 2^(1/3) sigma^2, with a margin for the FP32 screen
       if (d2 >= 1.2599211f * sg * sg * 1.002f) continue;
-      const int A = min(i, q), B = max(i, q);
+      if (nc < kMaxC) cand[threadIdx.x][nc] = q;
+      ++nc;
+    }
+    if (nc > kMaxC) {
+      err |= kErrListOverflow;
+      nc = kMaxC;
+    }
+  }
+  // exclusive scan of the candidate counts over the warp
+  int off = nc;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, off, d);
+    if (lane >= d) off += v;
+  }
+  const int total = __shfl_sync(0xffffffffu, off, 31);
+  off -= nc;
+  soff[warp][lane] = off;
+  __syncwarp();
+
+  double F[3] = {0, 0, 0}, T[3] = {0, 0, 0};
+  double acc[11];
+#pragma unroll
+  for (int c = 0; c < 11; ++c) acc[c] = 0.0;
+  for (int base = 0; base < total; base += 32) {
+    const int e = base + lane;
+    double r6[6] = {0, 0, 0, 0, 0, 0};
+    if (e < total) {
+      // owner: the last lane whose offset is <= e
+      int lo = 0, hi = 31;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (soff[warp][mid] <= e) lo = mid;
+        else hi = mid - 1;
+      }
+      const int o = lo;
+      const int p = bk.y + warp * 32 + o;
+      const int q = cand[warp * 32 + o][e - soff[warp][o]];
+      const int A = min(p, q), B = max(p, q);
       double fA[3], tA[3], tB[3], U, W, PT[9];
-      if (!wca_pair(b, P, A, B, fA, tA, tB, U, W, PT, err)) continue;
-      if (i == A) {
+      if (wca_pair(b, P, A, B, fA, tA, tB, U, W, PT, err)) {
+        if (p == A) {
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          F[a] += fA[a];
-          T[a] += tA[a];
-        }
-        acc[0] += U;
-        acc[1] += W;
+          for (int a = 0; a < 3; ++a) {
+            r6[a] = fA[a];
+            r6[3 + a] = tA[a];
+          }
+          acc[0] += U;
+          acc[1] += W;
 #pragma unroll
-        for (int c = 0; c < 9; ++c) acc[2 + c] += PT[c];
-      } else {
+          for (int c = 0; c < 9; ++c) acc[2 + c] += PT[c];
+        } else {
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          F[a] -= fA[a];
-          T[a] += tB[a];
+          for (int a = 0; a < 3; ++a) {
+            r6[a] = -fA[a];
+            r6[3 + a] = tB[a];
+          }
         }
       }
     }
+#pragma unroll
+    for (int c = 0; c < 6; ++c) res[warp][lane][c] = r6[c];
+    __syncwarp();
+    const int e0 = max(off, base), e1 = min(off + nc, base + 32);
+    for (int k = e0; k < e1; ++k) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        F[a] += res[warp][k - base][a];
+        T[a] += res[warp][k - base][3 + a];
+      }
+    }
+    __syncwarp();
+  }
+  if (ok) {
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
       b.Fw[3 * i + a] = F[a];
       b.Tw[3 * i + a] = T[a];
     }
-    if (err) atomicOr(&b.st[s].status, err);
   }
+  if (err) atomicOr(&b.st[s].status, err);
   double tot[11];
   block_sum<11, kPartBlock>(acc, sh, tot);
   if (threadIdx.x == 0) {

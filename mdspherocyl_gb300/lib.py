@@ -35,6 +35,7 @@ EXPORTS = [
     "mdsc_force_dipK", "mdsc_ext_field", "mdsc_self_ener", "mdsc_moveX", "mdsc_moveP",
     "mdsc_renorm", "mdsc_neigh_list", "mdsc_check_list", "mdsc_clust_conf", "mdsc_step",
     "mdsc_observe", "mdsc_launches_per_step", "mdsc_stream", "mdsc_profile_steps",
+    "mdsc_place_rods", "mdsc_last_device_ms",
 ]
 
 
@@ -119,7 +120,9 @@ def load(build: bool = True) -> ctypes.CDLL:
         "mdsc_observe": (c_int, [c_void_p, P(Observables)]),
         "mdsc_launches_per_step": (c_int, [c_void_p]),
         "mdsc_stream": (c_void_p, [c_void_p]),
+        "mdsc_last_device_ms": (c_double, [c_void_p]),
         "mdsc_profile_steps": (c_int, [c_void_p, c_int, c_int, c_char_p, c_size_t, _dp, _ip]),
+        "mdsc_place_rods": (c_int, [c_int, _dp, _dp, _dp, ctypes.c_ulonglong, c_double, c_int, _dp, _dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -332,6 +335,22 @@ class Batch:
             nm = names.raw[k * stride:(k + 1) * stride].split(b"\0")[0].decode()
             out[nm] = float(ms[k])
         return out
+
+
+def place_rods(lengths, dia, box, seed: int, gap: float = 0.0):
+    """Seeded non-overlapping placement (host routine of the library)."""
+    lib = load()
+    n = len(lengths)
+    ln = np.ascontiguousarray(lengths, dtype=np.float64)
+    dd = np.ascontiguousarray(dia, dtype=np.float64)
+    bx = np.ascontiguousarray(box, dtype=np.float64)
+    r = np.zeros((n, 3))
+    O = np.zeros((n, 3, 3))
+    code = lib.mdsc_place_rods(n, _ptr(ln), _ptr(dd), _ptr(bx), int(seed) & ((1 << 64) - 1), float(gap),
+                               2000000, _ptr(r), _ptr(O))
+    if code != 0:
+        raise MdscError(code, "mdsc_place_rods")
+    return r, O
 
 
 def estimate_bytes(descs) -> int:

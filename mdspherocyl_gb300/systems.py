@@ -203,7 +203,9 @@ def make_system(*, n, phi, lengths, mu, temp=1.0, seed=0, dia=None, mass=None,
     V = vol.sum() / phi
     Lz = (V / (aspect[0] * aspect[1])) ** (1.0 / 3.0)
     box = np.array([aspect[0] * Lz, aspect[1] * Lz, Lz])
-    r, O = place_rods(rng, lengths, dia, box, min_gap=min_gap)
+    from .lib import place_rods as _place
+
+    r, O = _place(lengths, dia, box, seed=int(rng.integers(1 << 62)), gap=min_gap)
     I = inertia(lengths, dia, mass)
     p, l = maxwell_boltzmann(rng, mass, I, O, temp)
     dip = np.zeros((n, 1, 5))

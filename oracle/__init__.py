@@ -292,6 +292,8 @@ class MDOracle:
                       c_int, c_int, c_double, _dp, c_int, c_double])
         self._step = _bind(lib, "mdsc_or_md_step", c_int, [c_void_p, _SP])
         self._free = _bind(lib, "mdsc_or_md_free", None, [c_void_p])
+        self._obs = _bind(lib, "mdsc_or_md_obs", None, [c_void_p, _dp])
+        self._setth = _bind(lib, "mdsc_or_md_set_thermo", None, [c_void_p, _dp, _dp])
         Bc = np.ascontiguousarray(B, dtype=np.float64)
         ok = init(self._buf, ctypes.byref(self._cs), dt, temp, Q, gamma, xi0, sr_cut, K_max,
                   ksq_max, alpha, Bc.ctypes.data_as(_dp), cl_fr, min_s)
@@ -300,6 +302,18 @@ class MDOracle:
 
     def step(self) -> bool:
         return bool(self._step(self._buf, ctypes.byref(self._cs)))
+
+    def set_thermostat(self, xi, strn) -> None:
+        x = np.ascontiguousarray(xi, dtype=np.float64)
+        s = np.ascontiguousarray(strn, dtype=np.float64)
+        self._setth(self._buf, x.ctypes.data_as(_dp), s.ctypes.data_as(_dp))
+
+    def obs(self) -> dict:
+        o = np.zeros(48)
+        self._obs(self._buf, o.ctypes.data_as(_dp))
+        return dict(K=o[0:2].copy(), Uss=o[2], Wss=o[3], UdipR=o[4], UdipK=o[5], Uext=o[6], Uself=o[7],
+                    xi=o[8:10].copy(), step=int(o[10]), list_builds=int(o[11]), PTkin=o[12:21].reshape(3, 3),
+                    PTss=o[21:30].reshape(3, 3), PTdipR=o[30:39].reshape(3, 3), PTdipK=o[39:48].reshape(3, 3))
 
     def close(self):
         if self._buf is not None:

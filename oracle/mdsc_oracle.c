@@ -1259,6 +1259,35 @@ int mdsc_or_md_step(mdsc_or_md* md, mdsc_oracle_state* s) {
   return 1;
 }
 
+void mdsc_or_md_obs(const mdsc_or_md* md, double* out) {
+  /* K_t, K_r, Uss, Wss, UdipR, UdipK, Uext, Uself, xi_t, xi_r, steps, list builds */
+  out[0] = md->K[0];
+  out[1] = md->K[1];
+  out[2] = md->Uss;
+  out[3] = md->Wss;
+  out[4] = md->UdipR;
+  out[5] = md->UdipK;
+  out[6] = md->Uext;
+  out[7] = md->Uself;
+  out[8] = md->thermo.xi[0];
+  out[9] = md->thermo.xi[1];
+  out[10] = (double)md->step;
+  out[11] = (double)md->list_builds;
+  for (int k = 0; k < 9; ++k) {
+    out[12 + k] = md->PTkin[k];
+    out[21 + k] = md->PTss[k];
+    out[30 + k] = md->PTdipR[k];
+    out[39 + k] = md->PTdipK[k];
+  }
+}
+
+void mdsc_or_md_set_thermo(mdsc_or_md* md, const double xi[2], const double strn[2]) {
+  md->thermo.xi[0] = xi[0];
+  md->thermo.xi[1] = xi[1];
+  md->thermo.strn[0] = strn[0];
+  md->thermo.strn[1] = strn[1];
+}
+
 void mdsc_or_md_free(mdsc_or_md* md) {
   free(md->tab);
   free(md->kvec);

@@ -131,6 +131,11 @@ int mdsc_or_md_init(mdsc_or_md* md, mdsc_oracle_state* s, double dt, double temp
                     const double B[3], int cl_fr, double min_s);
 int mdsc_or_md_step(mdsc_or_md* md, mdsc_oracle_state* s);
 void mdsc_or_md_free(mdsc_or_md* md);
+/* observables of the last step: K_t, K_r, Uss, Wss, UdipR, UdipK, Uext,
+   Uself, xi_t, xi_r, steps, list builds, then PTkin, PTss, PTdipR, PTdipK
+   (9 each) -- 48 doubles */
+void mdsc_or_md_obs(const mdsc_or_md* md, double* out);
+void mdsc_or_md_set_thermo(mdsc_or_md* md, const double xi[2], const double strn[2]);
 
 /* number of OpenMP threads the routines may use (1 = serial, bit-exact) */
 void mdsc_or_set_threads(int n);

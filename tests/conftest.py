@@ -1,0 +1,46 @@
+import glob
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+GOLDEN = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "golden_*.npz")))
+REFERENCE = os.environ.get("MDSC_REFERENCE", "/root/reference")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+@pytest.fixture(scope="session")
+def orc():
+    import oracle
+
+    return oracle.Oracle()
+
+
+@pytest.fixture(scope="session")
+def ref():
+    import oracle
+
+    if not os.path.isdir(os.path.join(REFERENCE, "v25")):
+        pytest.skip("reference sources not present")
+    if not os.path.exists(oracle.REF_SO):
+        oracle.build_ref()
+    return oracle.Ref()
+
+
+def rms_rel(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    den = np.sqrt(np.mean(b ** 2))
+    return float(np.sqrt(np.mean((a - b) ** 2)) / den) if den > 0 else float(np.abs(a).max())
+
+
+def load_golden(path):
+    return dict(np.load(path))
