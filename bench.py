@@ -231,6 +231,28 @@ def run_ours(args):
     obs = bt.observe()
     st_ok = all(o["status"] == 0 for o in obs)
 
+    # ---- the plain path: one system per launch sequence, one after another ----
+    plain = None
+    if not args.no_plain:
+        singles = [L.Batch([sp], [st], device=device) for sp, st in zip(specs, sts)]
+        for b1 in singles:
+            b1.step(2)
+        dev_ms, t0 = 0.0, time.perf_counter()
+        for _ in range(args.plain_steps):
+            for b1 in singles:
+                code = b1.lib.mdsc_step(b1.h, 1, None)
+                if code != 0:
+                    raise L.MdscError(code, "mdsc_step (plain)", b1._err())
+                dev_ms += b1.lib.mdsc_last_device_ms(b1.h)
+        wall = time.perf_counter() - t0
+        for b1 in singles:
+            b1.close()
+        pv_dev = ntot * args.plain_steps / (dev_ms / 1e3)
+        pv_wall = ntot * args.plain_steps / wall
+        plain = {"value_device": pv_dev, "value_wall": pv_wall, "unit": UNIT, "steps": args.plain_steps,
+                 "how": "each system its own handle and launch sequence, stepped one after another",
+                 "batched_over_plain_device": value / pv_dev, "batched_over_plain_wall": value / pv_wall}
+
     # ---- kernel times (events per kernel, serialised) ----
     prof = bt.profile(max(2, min(5, args.steps)))
     pairs = sum(s.n * (s.n - 1) // 2 for s in specs)
@@ -299,6 +321,7 @@ def run_ours(args):
                          "flop_per_pair": FLOP_PER_PAIR, "pairs_per_launch": pairs,
                          "kernel_ms": rp_ms},
             "kernel_ms": prof,
+            "plain_gpu": plain,
             "clocks": clocks,
             "status_ok": st_ok,
         }
@@ -321,6 +344,8 @@ def main():
     ap.add_argument("--systems", type=int, default=256)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--plain-steps", type=int, default=3)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -46,7 +46,7 @@ struct Layout {
   std::vector<SysDev> sys;
   std::vector<int4> tiles, kn, kwork;
   std::vector<float4> kv;
-  std::vector<double> kval, kpre;
+  std::vector<double> kval, kpre, kvec;
   std::vector<int2> blk, kowner;
   int ntot = 0, ndtot = 0, nktot = 0, maxnd = 0;
   long long rpart = 0, kpart = 0;
@@ -127,6 +127,9 @@ void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
       Lo.kn.push_back(n);
       Lo.kv.push_back(make_float4((float)kx, (float)ky, (float)kz, (float)val));
       Lo.kval.push_back(val);
+      Lo.kvec.push_back(kx);
+      Lo.kvec.push_back(ky);
+      Lo.kvec.push_back(kz);
       Lo.kpre.push_back(2 * (a4 + 1. / ksq));  // pval (v25/functions.cpp:1715,1738)
       Lo.kowner.push_back(make_int2(s, (int)(Lo.kn.size() - 1 - P.k_off)));
     }
@@ -165,6 +168,7 @@ void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
     P.invLh = (float)(1.0 / kLh);
     P.halfLh2 = (float)(0.5 * kLh * kLh);
     P.rmax_table = (float)kTableRmax;
+    P.sixthLh3 = (float)(kLh * kLh * kLh / 6.0);
     part += d.n;
     dip += P.ndip;
     Lo.maxnd = std::max(Lo.maxnd, d.nd);
@@ -225,9 +229,13 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   b.Fw = A.take<double>(3 * n);
   b.Tw = A.take<double>(3 * n);
   b.wcaE = A.take<double>(11 * nb);
+  b.wcand = A.take<int>(n * kMaxC);
+  b.wcnt = A.take<int>(n);
+  b.wrec = A.take<double>(n * kMaxC * 6);
   b.kn = A.take<int4>(nk);
   b.kv = A.take<float4>(nk);
   b.kval = A.take<double>(nk);
+  b.kvec = A.take<double>(3 * nk);
   b.kpre = A.take<double>(nk);
   b.kpart = A.take<float>(10 * std::max<long long>(Lo.kpart, 1));
   b.ksum = A.take<double>(10 * nk);
@@ -608,6 +616,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   up(b.kn, lo.kn.data(), sizeof(int4) * lo.kn.size());
   up(b.kv, lo.kv.data(), sizeof(float4) * lo.kv.size());
   up(b.kval, lo.kval.data(), sizeof(double) * lo.kval.size());
+  up(b.kvec, lo.kvec.data(), sizeof(double) * lo.kvec.size());
   up(b.kpre, lo.kpre.data(), sizeof(double) * lo.kpre.size());
   up(B->kwork, lo.kwork.data(), sizeof(int4) * lo.kwork.size());
   up(B->kowner, lo.kowner.data(), sizeof(int2) * lo.kowner.size());
@@ -626,6 +635,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   cudaMemsetAsync(b.rsave, 0, sizeof(double) * 3 * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.usave, 0, sizeof(double) * 3 * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.nbc, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
+  cudaMemsetAsync(b.wcnt, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.F, 0, sizeof(double) * 3 * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.T, 0, sizeof(double) * 3 * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(B->noise[0], 0, sizeof(double) * kNoiseChunk * nsys * 4, B->st);

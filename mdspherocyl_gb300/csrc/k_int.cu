@@ -286,11 +286,30 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
         F[a] += b.Fw[3 * i + a];
         T[a] += b.Tw[3 * i + a];
       }
+      // shares of the pairs this particle forms with lower-index partners,
+      // left by the WCA kernel in the partner's records (ascending partner)
+      const int nl = b.nbc[i];
+      const int* lst = b.nb + (long long)i * kMaxNb;
+      for (int k = 0; k < nl; ++k) {
+        const int q = lst[k];
+        if (q >= i) break;
+        const int nc = b.wcnt[q];
+        const int* cq = b.wcand + (long long)q * kMaxC;
+        for (int c = 0; c < nc; ++c) {
+          if (cq[c] != i) continue;
+          const double* rec = b.wrec + ((long long)q * kMaxC + c) * 6;
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            F[a] += rec[a];
+            T[a] += rec[3 + a];
+          }
+        }
+      }
     }
     double ax[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) ax[a] = b.O[9 * i + 6 + a];
-    const int nd = P.nd, ND = b.ndtot;
+    const int nd = P.nd;
     const int loc0 = (i - P.part_off) * nd;
     double uext = 0.0;
     for (int w = 0; w < nd; ++w) {
@@ -320,7 +339,15 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
           t[c] += (double)acc6[3 + c].hi + (double)acc6[3 + c].lo;
         }
       }
-      const double mx = b.dm[g], my = b.dm[ND + g], mz = b.dm[2 * ND + g];
+      // dipole vector mu O^T o_body in FP64 (the FP32 copy is 6e-8 off)
+      double mx, my, mz;
+      {
+        const double* O = b.O + 9 * i;
+        const double ox = b.dob[3 * g], oy = b.dob[3 * g + 1], oz = b.dob[3 * g + 2], mu = b.dmu[g];
+        mx = mu * (O[0] * ox + O[3] * oy + O[6] * oz);
+        my = mu * (O[1] * ox + O[4] * oy + O[7] * oz);
+        mz = mu * (O[2] * ox + O[5] * oy + O[8] * oz);
+      }
       if (mode & kMaskK) {
         const double gx = b.Gk[3 * g], gy = b.Gk[3 * g + 1], gz = b.Gk[3 * g + 2];
         f[0] += b.Fk[3 * g];

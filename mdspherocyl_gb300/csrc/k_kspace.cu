@@ -113,11 +113,7 @@ __global__ void kcombine_kernel(Batch b, const int2* __restrict__ kowner, double
   double* ks = b.ksum + (long long)k * 10;
 #pragma unroll
   for (int c = 0; c < 10; ++c) ks[c] = s[c];
-  const float4 kvf = b.kv[k];
-  const int4 n = b.kn[k];
-  const double kx = 2.0 * M_PI * n.x / P.L[0], ky = 2.0 * M_PI * n.y / P.L[1],
-               kz = 2.0 * M_PI * n.z / P.L[2];
-  (void)kvf;
+  const double kx = b.kvec[3 * k], ky = b.kvec[3 * k + 1], kz = b.kvec[3 * k + 2];
   const double Sr = kx * s[0] + ky * s[2] + kz * s[4];
   const double Si = kx * s[1] + ky * s[3] + kz * s[5];
   const double val = b.kval[k];

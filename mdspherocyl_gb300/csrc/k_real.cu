@@ -19,10 +19,13 @@
 // (v25/functions.cpp:1563,1606-1614,1680-1697), which differs from the
 // analytic B(r), C(r) by up to ~5e-5 near contact.  The kernel evaluates the
 // analytic terms and adds the table's own interpolation error to second
-// order, h f''(r) with h = (r - r0)(r1 - r)/2, using the closed forms
-//   A'' = 4B + C,  B'' = 6(5B + C)/r^2 + 2a^2 C,  C'' = 2a^2 C (2a^2 r^2 - 1)
-// (A, B, C as the reference's table columns), which matches the table to
-// ~2e-7 without reading it.
+// and third order, h2 f''(r) + h3 f'''(r) with a = r - r0, b = r1 - r,
+// h2 = ab/2, h3 = ab(b - a)/6, using the closed forms (A, B, C as the
+// reference's table columns, s = 5B + C)
+//   A'' = 4B + C,                A''' = -4s/r - 2a^2 r C
+//   B'' = 6s/r^2 + 2a^2 C,       B''' = -42s/r^3 - 12a^2 C/r - 4a^4 r C
+//   C'' = 2a^2 C (2a^2 r^2 - 1), C''' = 4a^4 r C (3 - 2a^2 r^2)
+// which matches the table to ~2e-9 without reading it.
 #include "mdsc_dev.cuh"
 
 namespace mdsc {
@@ -49,17 +52,23 @@ __device__ __forceinline__ void dip_pair(const SysDev& P, float dx, float dy, fl
   float A = E * rinv3 + G * rinv2;
   float B = (3.f * E * rinv3 + G * (P.alpha2x2 + 3.f * rinv2)) * rinv2;
   float C = P.alpha4x4 * G;
-  // the reference table's linear-interpolation error, to second order
+  // the reference table's linear-interpolation error to third order:
+  // h2 f'' + h3 f''' with a = r - r0, b = r1 - r, h2 = ab/2, h3 = ab(b - a)/6
   const float uu = r * P.invLh;
   const float fr = uu - floorf(uu);
-  const float h = P.halfLh2 * fr * (1.f - fr);
+  const float ab = fr * (1.f - fr);
+  const float h2 = P.halfLh2 * ab;
+  const float h3 = P.sixthLh3 * ab * (1.f - 2.f * fr);
   const float s5 = 5.f * B + C;
-  const float hA = h * (4.f * B + C);
-  const float hB = h * (6.f * s5 * rinv2 + P.alpha2x2 * C);
-  const float hC = h * (P.alpha2x2 * C * (P.alpha2x2 * r2 - 1.f));
-  A += hA;
-  B += hB;
-  C += hC;
+  const float a2 = P.alpha2x2;
+  const float a2C = a2 * C;
+  const float a2rC = a2C * r;
+  const float dA = h2 * (4.f * B + C) - h3 * (4.f * s5 * rinv + a2rC);
+  const float dB = h2 * (6.f * s5 * rinv2 + a2C) - h3 * (42.f * s5 * rinv3 + 6.f * a2C * rinv + a2 * a2rC);
+  const float dC = h2 * (a2C * (a2 * r2 - 1.f)) + h3 * (a2 * a2rC * (3.f - a2 * r2));
+  A += dA;
+  B += dB;
+  C += dC;
 
   const float mimj = mix * mjx + miy * mjy + miz * mjz;
   const float mir = mix * dx + miy * dy + miz * dz;

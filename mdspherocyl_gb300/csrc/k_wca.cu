@@ -118,7 +118,7 @@ __device__ bool wca_pair(const Batch& b, const SysDev& P, int A, int B, double* 
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     rij[a] = ra.r[a] - rb.r[a];
-    rij[a] -= P.L[a] * floor(rij[a] / P.L[a] + 0.5);
+    rij[a] -= P.L[a] * floor(rij[a] * P.invL[a] + 0.5);
     rsq += rij[a] * rij[a];
   }
   double dij[3], st[2];
@@ -170,14 +170,14 @@ __device__ bool wca_pair(const Batch& b, const SysDev& P, int A, int B, double* 
   return true;
 }
 
-// Two phases per warp.  (1) Each lane screens its particle's list in FP32
-// and keeps the candidate partners (ascending index) in shared memory.  (2)
-// The warp's candidates, concatenated owner by owner, are evaluated 32 at a
-// time in FP64 with every lane busy; each owner then adds its own entries in
-// order.  FP64 runs at a small fraction of the FP32 rate on this GPU, so
-// only pairs that can touch reach the FP64 pipe, densely packed.
-constexpr int kMaxC = 24;  // contact candidates per particle
-
+// Two phases per warp.  (1) Each lane screens its particle's partners of
+// higher index (each pair once) in FP32 and keeps the candidates (ascending
+// index).  (2) The warp's candidates, concatenated owner by owner, are
+// evaluated 32 at a time in FP64 with every lane busy; the owner (the lower
+// index) adds its share in order, and the partner's share goes to a record
+// that the finalize kernel gathers.  FP64 runs at a small fraction of the
+// FP32 rate on this GPU, so only pairs that can touch reach the FP64 pipe,
+// once each and densely packed.
 __global__ void __launch_bounds__(kPartBlock) wca_kernel(Batch b) {
   __shared__ int cand[kPartBlock][kMaxC];
   __shared__ double res[kPartBlock / 32][32][6];
@@ -200,6 +200,7 @@ __global__ void __launch_bounds__(kPartBlock) wca_kernel(Batch b) {
     const int* lst = b.nb + (long long)i * kMaxNb;
     for (int k = 0; k < nl; ++k) {
       const int q = lst[k];
+      if (q < i) continue;
       const float dx = fix_diff(ux, b.pfx[q], P.Lfix[0]);
       const float dy = fix_diff(uy, b.pfx[N + q], P.Lfix[1]);
       const float dz = fix_diff(uz, b.pfx[2 * N + q], P.Lfix[2]);
@@ -208,13 +209,17 @@ __global__ void __launch_bounds__(kPartBlock) wca_kernel(Batch b) {
       const float d2 = seg_dist_fast(dx, dy, dz, ai.x, ai.y, ai.z, ai.w, aj.x, aj.y, aj.z, aj.w);
       // 2^(1/3) sigma^2, with a margin for the FP32 screen
       if (d2 >= 1.2599211f * sg * sg * 1.002f) continue;
-      if (nc < kMaxC) cand[threadIdx.x][nc] = q;
+      if (nc < kMaxC) {
+        cand[threadIdx.x][nc] = q;
+        b.wcand[(long long)i * kMaxC + nc] = q;
+      }
       ++nc;
     }
     if (nc > kMaxC) {
       err |= kErrListOverflow;
       nc = kMaxC;
     }
+    b.wcnt[i] = nc;
   }
   // exclusive scan of the candidate counts over the warp
   int off = nc;
@@ -244,29 +249,27 @@ __global__ void __launch_bounds__(kPartBlock) wca_kernel(Batch b) {
         else hi = mid - 1;
       }
       const int o = lo;
+      const int kk = e - soff[warp][o];
       const int p = bk.y + warp * 32 + o;
-      const int q = cand[warp * 32 + o][e - soff[warp][o]];
-      const int A = min(p, q), B = max(p, q);
+      const int q = cand[warp * 32 + o][kk];
       double fA[3], tA[3], tB[3], U, W, PT[9];
-      if (wca_pair(b, P, A, B, fA, tA, tB, U, W, PT, err)) {
-        if (p == A) {
+      double rec[6] = {0, 0, 0, 0, 0, 0};
+      if (wca_pair(b, P, p, q, fA, tA, tB, U, W, PT, err)) {
 #pragma unroll
-          for (int a = 0; a < 3; ++a) {
-            r6[a] = fA[a];
-            r6[3 + a] = tA[a];
-          }
-          acc[0] += U;
-          acc[1] += W;
-#pragma unroll
-          for (int c = 0; c < 9; ++c) acc[2 + c] += PT[c];
-        } else {
-#pragma unroll
-          for (int a = 0; a < 3; ++a) {
-            r6[a] = -fA[a];
-            r6[3 + a] = tB[a];
-          }
+        for (int a = 0; a < 3; ++a) {
+          r6[a] = fA[a];
+          r6[3 + a] = tA[a];
+          rec[a] = -fA[a];
+          rec[3 + a] = tB[a];
         }
+        acc[0] += U;
+        acc[1] += W;
+#pragma unroll
+        for (int c = 0; c < 9; ++c) acc[2 + c] += PT[c];
       }
+      double* out = b.wrec + ((long long)p * kMaxC + kk) * 6;
+#pragma unroll
+      for (int c = 0; c < 6; ++c) out[c] = rec[c];
     }
 #pragma unroll
     for (int c = 0; c < 6; ++c) res[warp][lane][c] = r6[c];

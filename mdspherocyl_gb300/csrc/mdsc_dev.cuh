@@ -13,7 +13,7 @@ constexpr int kMaxD = 4;         // dipoles per particle (MDSC_MAX_DIPOLES)
 constexpr int kPartBlock = 128;  // threads per block of the per-particle kernels
 constexpr int kKBlock = 128;     // k-vectors per block of the k-space kernels
 constexpr int kKChunk = 256;     // particles per block of the structure-factor kernel
-constexpr int kWcaQueue = 32;    // FP64 contact batch per warp
+constexpr int kMaxC = 16;        // WCA contact candidates of higher index per particle
 
 // status bits (OR-ed per system; mapped to mdsc_status on the host)
 enum : int {
@@ -70,7 +70,7 @@ struct SysDev {
   float alpha4x4;          // 4 alpha^4
   float invLh, halfLh2;    // table spacing of the reference: Lh = 0.5*200.2/32768
   float rmax_table;        // 100.1: the reference's table covers r <= 100.1
-  float pad;
+  float sixthLh3;          // Lh^3 / 6
 };
 
 // Per-system mutable state.
@@ -135,10 +135,14 @@ struct Batch {
   double* Fw;    // 3n WCA force
   double* Tw;    // 3n WCA torque
   double* wcaE;  // per block: U, W, PT[9] = 11
+  int* wcand;    // n * kMaxC contact candidates (higher index) of each particle
+  int* wcnt;     // n
+  double* wrec;  // n * kMaxC * 6: the partner's force and torque of each candidate
   // k-space
   int4* kn;      // (nx, ny, nz, 0) per k
   float4* kv;    // (kx, ky, kz, val) per k
   double* kval;  // val per k (FP64)
+  double* kvec;  // 3 per k: the k vector in FP64
   double* kpre;  // pval per k (2 (a4 + 1/k^2)) for the pressure tensor
   float* kpart;  // structure-factor partials: 10 per (chunk, k)
   double* ksum;  // 10 per k: uve (6), self, uvslf (3) -- FP64
