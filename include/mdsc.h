@@ -202,6 +202,28 @@ double mdsc_last_device_ms(const mdsc_batch* b);
 mdsc_status mdsc_profile_steps(mdsc_batch* b, int nsteps, int max_kernels, char* names,
                                size_t name_stride, double* ms_per_launch, int* n_kernels);
 
+/* ---- allocation-free variant ------------------------------------------- */
+/* Real-space Ewald forces, torques (without lever arms), energy and
+   pressure tensor of one system of ndip dipoles, one per particle, for
+   callers that cannot allocate GPU memory at the point of the call (a host
+   with a fixed device-memory budget, a real-time loop, a plugin whose host
+   owns every buffer).  Inputs and outputs are device pointers the caller
+   owns: d_pos, d_mom (ndip*3 doubles each: dipole positions and moment
+   vectors mu*o), d_F, d_T (ndip*3 doubles), d_UPT (10 doubles: the energy,
+   then the pressure tensor row by row); box, alpha on the host; stream is a
+   cudaStream_t (NULL: the default stream).  The call allocates nothing: its
+   scratch is a fixed array of this library's device memory (about 6.5 MB
+   on every GPU that loads the library, held until the process exits), so
+   ndip may not exceed 4096 (MDSC_ERR_TOO_LARGE otherwise).  The first call
+   on a device looks up that array's device address; make it before any
+   stream capture.  Calls share the array and overwrite what they read, so
+   calls whose work overlaps on the GPU race.  No counterpart in the
+   reference: it is the GPU form of force_dipR's arithmetic for callers
+   without an allocator. */
+mdsc_status mdsc_force_dipR_noalloc(int ndip, const double* d_pos, const double* d_mom,
+                                    const double box[3], double alpha, double* d_F, double* d_T,
+                                    double* d_UPT, void* stream);
+
 /* ---- utility ------------------------------------------------------------ */
 /* Seeded random non-overlapping placement of n rods in a periodic box
    (sequential rejection on the segment distance, gap added to

@@ -35,7 +35,7 @@ EXPORTS = [
     "mdsc_force_dipK", "mdsc_ext_field", "mdsc_self_ener", "mdsc_moveX", "mdsc_moveP",
     "mdsc_renorm", "mdsc_neigh_list", "mdsc_check_list", "mdsc_clust_conf", "mdsc_step",
     "mdsc_observe", "mdsc_launches_per_step", "mdsc_stream", "mdsc_profile_steps",
-    "mdsc_place_rods", "mdsc_last_device_ms",
+    "mdsc_place_rods", "mdsc_last_device_ms", "mdsc_force_dipR_noalloc",
 ]
 
 
@@ -121,6 +121,8 @@ def load(build: bool = True) -> ctypes.CDLL:
         "mdsc_launches_per_step": (c_int, [c_void_p]),
         "mdsc_stream": (c_void_p, [c_void_p]),
         "mdsc_last_device_ms": (c_double, [c_void_p]),
+        "mdsc_force_dipR_noalloc": (c_int, [c_int, c_void_p, c_void_p, _dp, c_double, c_void_p, c_void_p,
+                                            c_void_p, c_void_p]),
         "mdsc_profile_steps": (c_int, [c_void_p, c_int, c_int, c_char_p, c_size_t, _dp, _ip]),
         "mdsc_place_rods": (c_int, [c_int, _dp, _dp, _dp, ctypes.c_ulonglong, c_double, c_int, _dp, _dp]),
     }
