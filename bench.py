@@ -182,6 +182,33 @@ def run_reference(args):
     return 0
 
 
+def run_serving(args, device: int) -> dict:
+    """Poisson stream of jobs (one system each) through the continuous-
+    batching server; job configurations are generated before the clock
+    starts (they are the clients' inputs)."""
+    import multiprocessing as mp
+
+    from mdspherocyl_gb300 import serve
+    from mdspherocyl_gb300 import systems as S
+
+    arr = serve.poisson_arrivals(args.jobs, args.rate, seed=args.seed + 7)
+    t0 = time.time()
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+        made = pool.map(S.serving_job, range(args.jobs), chunksize=1)
+    log(f"serving: {args.jobs} jobs generated in {time.time() - t0:.1f}s")
+    jobs = [serve.Job(k, spec, st, spec.steps, arrival=float(arr[k])) for k, (spec, st) in enumerate(made)]
+    srv = serve.Server(hbm_budget_bytes=120e9, tick_steps=args.tick, device=device)
+    t0 = time.perf_counter()
+    stats = srv.run(jobs)
+    wall = time.perf_counter() - t0
+    out = serve.summarize(stats, wall)
+    out.update({"rate_per_s": args.rate, "hbm_budget_bytes": 120e9, "tick_steps": args.tick,
+                "jobs_spec": "N log-U[64,8192], steps U[500,5000], phi U[.05,.25], mu^2 U[.5,5], T U[.8,1.5], "
+                             "L ~ N(3, 0.3); alpha = 6/L_box, |n|^2 <= 36",
+                "note": f"{args.jobs} jobs of the 2000-job stream's distribution, same arrival rate"})
+    return out
+
+
 def run_ours(args):
     ws, rank, local = dist_env()
     import torch
@@ -289,6 +316,8 @@ def run_ours(args):
         t_e2e = float(tt.item())
     e2e = ntot * ws * e2e_steps / t_e2e
     launches = bt.launches_per_step + 1  # + the per-call reset of the noise row
+    bt.close()
+    serving = run_serving(args, device) if (args.jobs > 0 and ws == 1) else None
 
     out = None
     if rank == 0:
@@ -322,13 +351,13 @@ def run_ours(args):
                          "kernel_ms": rp_ms},
             "kernel_ms": prof,
             "plain_gpu": plain,
+            "serving": serving,
             "clocks": clocks,
             "status_ok": st_ok,
         }
         if cpu is not None:
             out["cpu_baseline"] = cpu
         print(json.dumps(out), flush=True)
-    bt.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
     return 0
@@ -346,6 +375,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=3)
+    ap.add_argument("--jobs", type=int, default=200, help="serving leg: jobs (0 = skip)")
+    ap.add_argument("--rate", type=float, default=40.0, help="serving leg: arrivals per second")
+    ap.add_argument("--tick", type=int, default=50, help="serving leg: steps between admissions")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

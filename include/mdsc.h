@@ -178,6 +178,13 @@ mdsc_status mdsc_check_list(mdsc_batch* b, int* rebuild);
    system's cluster generator.  labels: n ints (may be NULL). */
 mdsc_status mdsc_clust_conf(mdsc_batch* b, int sys, int* labels, int* n_clusters);
 
+/* Moves system ssys of batch src into slot dsys of batch dst (same device,
+   same n and nd) without leaving the GPU: particle state, forces, shapes,
+   thermostat and generator states, step count and cluster labels.  The
+   continuous-batching server uses it to repack running systems when jobs
+   finish or arrive.  No counterpart in the reference (one system per run). */
+mdsc_status mdsc_transfer(mdsc_batch* dst, int dsys, mdsc_batch* src, int ssys);
+
 /* ---- the fused step ---------------------------------------------------- */
 /* Advances every system by nsteps steps of the reference's loop body
    (renorm every 100 steps, moveTher 0, moveP, moveTher 1, moveX, forces,

@@ -1034,6 +1034,67 @@ mdsc_status mdsc_clust_conf(mdsc_batch* B, int sys, int* labels, int* n_clusters
   return MDSC_OK;
 }
 
+// ---- moving a system between batches (continuous batching) -------------
+mdsc_status mdsc_transfer(mdsc_batch* D, int dsys, mdsc_batch* S, int ssys) {
+  if (!D || !S || dsys < 0 || dsys >= D->nsys || ssys < 0 || ssys >= S->nsys) return MDSC_ERR_BAD_ARG;
+  mdsc_batch* B = D;
+  const SysDev& Ps = S->lo.sys[ssys];
+  SysDev& Pd = D->lo.sys[dsys];
+  if (Ps.n != Pd.n || Ps.nd != Pd.nd || S->device != D->device)
+    return fail(D, MDSC_ERR_BAD_ARG, "mdsc_transfer: systems differ in size or device");
+  if (!S->uploaded[ssys]) return fail(D, MDSC_ERR_STATE, "mdsc_transfer: source system has no state");
+  cudaSetDevice(D->device);
+  CU(cudaStreamSynchronize(S->st));
+  const int n = Ps.n, nd = Ps.ndip;
+  const int is = Ps.part_off, id = Pd.part_off, gs = Ps.dip_off, gd = Pd.dip_off;
+  const Batch& a = S->b;
+  const Batch& b = D->b;
+  auto cp = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+    return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, D->st) : cudaSuccess;
+  };
+  CU(cp(b.r + 3 * id, a.r + 3 * is, sizeof(double) * 3 * n));
+  CU(cp(b.p + 3 * id, a.p + 3 * is, sizeof(double) * 3 * n));
+  CU(cp(b.O + 9 * id, a.O + 9 * is, sizeof(double) * 9 * n));
+  CU(cp(b.l + 3 * id, a.l + 3 * is, sizeof(double) * 3 * n));
+  CU(cp(b.F + 3 * id, a.F + 3 * is, sizeof(double) * 3 * n));
+  CU(cp(b.T + 3 * id, a.T + 3 * is, sizeof(double) * 3 * n));
+  CU(cp(b.len + id, a.len + is, sizeof(double) * n));
+  CU(cp(b.dia + id, a.dia + is, sizeof(double) * n));
+  CU(cp(b.mass + id, a.mass + is, sizeof(double) * n));
+  CU(cp(b.inert + 3 * id, a.inert + 3 * is, sizeof(double) * 3 * n));
+  CU(cp(b.invm + id, a.invm + is, sizeof(double) * n));
+  CU(cp(b.invI + 3 * id, a.invI + 3 * is, sizeof(double) * 3 * n));
+  CU(cp(b.dpc + gd, a.dpc + gs, sizeof(double) * nd));
+  CU(cp(b.dob + 3 * gd, a.dob + 3 * gs, sizeof(double) * 3 * nd));
+  CU(cp(b.dmu + gd, a.dmu + gs, sizeof(double) * nd));
+  std::vector<int> owner(nd);
+  for (int g = 0; g < nd; ++g) owner[g] = id + g / std::max(Ps.nd, 1);
+  CU(cudaMemcpyAsync(b.downer + gd, owner.data(), sizeof(int) * nd, cudaMemcpyHostToDevice, D->st));
+  // per-system constants set at upload, and the mutable state
+  Pd.sig_max = Ps.sig_max;
+  Pd.skin = Ps.skin;
+  Pd.r_list = Ps.r_list;
+  Pd.Uself = Ps.Uself;
+  CU(cudaMemcpyAsync((void*)(b.sys + dsys), &Pd, sizeof(SysDev), cudaMemcpyHostToDevice, D->st));
+  SysState st;
+  CU(cudaMemcpy(&st, a.st + ssys, sizeof st, cudaMemcpyDeviceToHost));
+  st.force_list = 1;
+  st.rebuild = 0;
+  st.iter = 0;
+  CU(cudaMemcpyAsync(b.st + dsys, &st, sizeof st, cudaMemcpyHostToDevice, D->st));
+  CU(cudaStreamSynchronize(D->st));
+  D->thermo_rng[2 * dsys] = S->thermo_rng[2 * ssys];
+  D->thermo_rng[2 * dsys + 1] = S->thermo_rng[2 * ssys + 1];
+  D->clus_rng[dsys] = S->clus_rng[ssys];
+  D->step_h[dsys] = S->step_h[ssys];
+  D->labels[dsys] = S->labels[ssys];
+  D->n_clusters[dsys] = S->n_clusters[ssys];
+  D->uploaded[dsys] = 1;
+  D->built[dsys] = 0;
+  D->have_forces[dsys] = S->have_forces[ssys];
+  return MDSC_OK;
+}
+
 // ---- the fused step ----------------------------------------------------
 mdsc_status mdsc_step(mdsc_batch* B, int nsteps, mdsc_observables* obs) {
   if (!B || nsteps < 0) return MDSC_ERR_BAD_ARG;

@@ -35,7 +35,7 @@ EXPORTS = [
     "mdsc_force_dipK", "mdsc_ext_field", "mdsc_self_ener", "mdsc_moveX", "mdsc_moveP",
     "mdsc_renorm", "mdsc_neigh_list", "mdsc_check_list", "mdsc_clust_conf", "mdsc_step",
     "mdsc_observe", "mdsc_launches_per_step", "mdsc_stream", "mdsc_profile_steps",
-    "mdsc_place_rods", "mdsc_last_device_ms", "mdsc_force_dipR_noalloc",
+    "mdsc_place_rods", "mdsc_last_device_ms", "mdsc_force_dipR_noalloc", "mdsc_transfer",
 ]
 
 
@@ -121,6 +121,7 @@ def load(build: bool = True) -> ctypes.CDLL:
         "mdsc_launches_per_step": (c_int, [c_void_p]),
         "mdsc_stream": (c_void_p, [c_void_p]),
         "mdsc_last_device_ms": (c_double, [c_void_p]),
+        "mdsc_transfer": (c_int, [c_void_p, c_int, c_void_p, c_int]),
         "mdsc_force_dipR_noalloc": (c_int, [c_int, c_void_p, c_void_p, _dp, c_double, c_void_p, c_void_p,
                                             c_void_p, c_void_p]),
         "mdsc_profile_steps": (c_int, [c_void_p, c_int, c_int, c_char_p, c_size_t, _dp, _ip]),
@@ -313,6 +314,10 @@ class Batch:
         self._check(self.lib.mdsc_clust_conf(self.h, k, lab.ctypes.data_as(_ip), ctypes.byref(nc)),
                     "mdsc_clust_conf")
         return lab, nc.value
+
+    def transfer_from(self, k: int, src: "Batch", ks: int) -> None:
+        """Move system ks of src into slot k of this batch, on the GPU."""
+        self._check(self.lib.mdsc_transfer(self.h, k, src.h, ks), "mdsc_transfer")
 
     # -- fused step --
     def step(self, nsteps: int = 1):
