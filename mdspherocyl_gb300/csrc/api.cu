@@ -48,7 +48,7 @@ struct Layout {
   std::vector<float4> kv;
   std::vector<double> kval, kpre, kvec;
   std::vector<int2> blk, kowner;
-  int ntot = 0, ndtot = 0, nktot = 0, maxnd = 0;
+  int ntot = 0, ndtot = 0, nktot = 0, maxnd = 0, nchunks = 0;
   long long rpart = 0, kpart = 0;
   bool multi = false;
 };
@@ -137,6 +137,8 @@ void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
     P.nkchunk = P.nk > 0 ? cdiv(d.n, kKChunk) : 0;
     P.kchunk_off = (int)kp;
     kp += (long long)P.nkchunk * P.nk;
+    P.gch_off = Lo.nchunks;
+    Lo.nchunks += P.nkchunk;
     for (int ch = 0; ch < P.nkchunk; ++ch)
       for (int kt = 0; kt < cdiv(P.nk, kKBlock); ++kt) Lo.kwork.push_back(make_int4(s, ch, kt, 0));
     P.blk_off = blk;
@@ -241,6 +243,7 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   b.ksum = A.take<double>(10 * nk);
   b.kS = A.take<float2>(nk);
   b.kE = A.take<double>(10 * nk);
+  b.kG = A.take<double>(6 * (size_t)std::max(Lo.nchunks, 1));
   b.Fk = A.take<double>(3 * nd);
   b.Gk = A.take<double>(3 * nd);
   b.kin1 = A.take<double>(2 * nb);

@@ -324,6 +324,7 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
         FF acc6[6];
 #pragma unroll
         for (int c = 0; c < 6; ++c) acc6[c].hi = acc6[c].lo = 0.f;
+#pragma unroll 4
         for (int Y = 0; Y < ns; ++Y) {
 #pragma unroll
           for (int c = 0; c < 6; ++c) {

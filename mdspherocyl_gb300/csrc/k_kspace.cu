@@ -22,6 +22,7 @@
 // thread), kcombine (chunks -> FP64 sums per k, energy and pressure-tensor
 // terms per k), kgather (per particle over all k: force and torque).
 #include "mdsc_dev.cuh"
+#include "reduce.cuh"
 
 namespace mdsc {
 
@@ -34,11 +35,16 @@ __device__ __forceinline__ void phase_exp(uint32_t ux, uint32_t uy, uint32_t uz,
   __sincosf(x, &s, &c);
 }
 
-// grid: one block per (system, particle chunk, k tile); work list kwork
+// grid: one block per (system, particle chunk, k tile); work list kwork.
+// With one dipole per particle the per-particle self terms need no per-k
+// work: |S_i(k)|^2 = (m_i.k)^2 and Re(conj(S_i) U_ic) = (m_i.k) m_ic, so
+// self(k) = k^T G k and uvslf(k) = G k with G = sum_i m_i m_i^T, which the
+// first k tile of every chunk sums once.
 template <int ND>
 __global__ void __launch_bounds__(kKBlock) ksum_kernel(Batch b, const int4* __restrict__ kwork) {
   __shared__ uint32_t sx[kKChunk * ND], sy[kKChunk * ND], sz[kKChunk * ND];
   __shared__ float smx[kKChunk * ND], smy[kKChunk * ND], smz[kKChunk * ND];
+  __shared__ double shG[6 * kKBlock / 32];
   const int4 w = kwork[blockIdx.x];
   const SysDev& P = b.sys[w.x];
   const int chunk = w.y;
@@ -57,63 +63,108 @@ __global__ void __launch_bounds__(kKBlock) ksum_kernel(Batch b, const int4* __re
     smz[q] = b.dm[2 * ND_all + g];
   }
   __syncthreads();
+  if (ND == 1 && w.z == 0) {
+    double gl[6] = {0, 0, 0, 0, 0, 0};
+    for (int q = threadIdx.x; q < np; q += kKBlock) {
+      const double mx = smx[q], my = smy[q], mz = smz[q];
+      gl[0] += mx * mx; gl[1] += mx * my; gl[2] += mx * mz;
+      gl[3] += my * my; gl[4] += my * mz; gl[5] += mz * mz;
+    }
+    double tot[6];
+    block_sum<6, kKBlock>(gl, shG, tot);
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) b.kG[((long long)P.gch_off + chunk) * 6 + c] = tot[c];
+    }
+  }
   if (kl >= P.nk) return;
   const int4 n = b.kn[P.k_off + kl];
   const float4 kv = b.kv[P.k_off + kl];
   float acc[10];
 #pragma unroll
   for (int c = 0; c < 10; ++c) acc[c] = 0.f;
-  for (int p = 0; p < np; ++p) {
-    float Sr = 0.f, Si = 0.f, Ur[3] = {0.f, 0.f, 0.f}, Ui[3] = {0.f, 0.f, 0.f};
+  if (ND == 1) {
+    for (int p = 0; p < np; ++p) {
+      float c, s;
+      phase_exp(sx[p], sy[p], sz[p], n, c, s);
+      // E = exp(-i k.r) = (c, -s); U_c += m_c E
+      const float mx = smx[p], my = smy[p], mz = smz[p];
+      acc[0] += mx * c; acc[1] -= mx * s;
+      acc[2] += my * c; acc[3] -= my * s;
+      acc[4] += mz * c; acc[5] -= mz * s;
+    }
+  } else {
+    for (int p = 0; p < np; ++p) {
+      float Sr = 0.f, Si = 0.f, Ur[3] = {0.f, 0.f, 0.f}, Ui[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-    for (int d = 0; d < ND; ++d) {
-      if (d < nd) {
-        const int q = p * nd + d;
-        float c, s;
-        phase_exp(sx[q], sy[q], sz[q], n, c, s);
-        // E = exp(-i k.r) = (c, -s)
-        const float mx = smx[q], my = smy[q], mz = smz[q];
-        const float a = mx * kv.x + my * kv.y + mz * kv.z;
-        Sr += a * c;
-        Si -= a * s;
-        Ur[0] += mx * c; Ui[0] -= mx * s;
-        Ur[1] += my * c; Ui[1] -= my * s;
-        Ur[2] += mz * c; Ui[2] -= mz * s;
+      for (int d = 0; d < ND; ++d) {
+        if (d < nd) {
+          const int q = p * nd + d;
+          float c, s;
+          phase_exp(sx[q], sy[q], sz[q], n, c, s);
+          const float mx = smx[q], my = smy[q], mz = smz[q];
+          const float a = mx * kv.x + my * kv.y + mz * kv.z;
+          Sr += a * c;
+          Si -= a * s;
+          Ur[0] += mx * c; Ui[0] -= mx * s;
+          Ur[1] += my * c; Ui[1] -= my * s;
+          Ur[2] += mz * c; Ui[2] -= mz * s;
+        }
       }
-    }
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      acc[2 * c] += Ur[c];
-      acc[2 * c + 1] += Ui[c];
-      acc[7 + c] += Sr * Ur[c] + Si * Ui[c];
+      for (int c = 0; c < 3; ++c) {
+        acc[2 * c] += Ur[c];
+        acc[2 * c + 1] += Ui[c];
+        acc[7 + c] += Sr * Ur[c] + Si * Ui[c];
+      }
+      acc[6] += Sr * Sr + Si * Si;
     }
-    acc[6] += Sr * Sr + Si * Si;
   }
   float* out = b.kpart + ((long long)P.kchunk_off + (long long)chunk * P.nk + kl) * 10;
+  const int nout = ND == 1 ? 6 : 10;
 #pragma unroll
-  for (int c = 0; c < 10; ++c) out[c] = acc[c];
+  for (int c = 0; c < 10; ++c)
+    if (c < nout) out[c] = acc[c];
 }
 
 // one thread per k over the whole batch: chunk sums in FP64, S(k), and the
 // energy and pressure-tensor terms of that k (v25/functions.cpp:1839-1952)
+template <int ND>
 __global__ void kcombine_kernel(Batch b, const int2* __restrict__ kowner, double* __restrict__ kE) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= b.nktot) return;
   const int2 ow = kowner[k];  // (system, k index within the system)
   const SysDev& P = b.sys[ow.x];
   const int kl = ow.y;
+  const int nv = ND == 1 ? 6 : 10;
   double s[10];
 #pragma unroll
   for (int c = 0; c < 10; ++c) s[c] = 0.0;
   for (int ch = 0; ch < P.nkchunk; ++ch) {
     const float* in = b.kpart + ((long long)P.kchunk_off + (long long)ch * P.nk + kl) * 10;
 #pragma unroll
-    for (int c = 0; c < 10; ++c) s[c] += (double)in[c];
+    for (int c = 0; c < 10; ++c)
+      if (c < nv) s[c] += (double)in[c];
+  }
+  const double kx = b.kvec[3 * k], ky = b.kvec[3 * k + 1], kz = b.kvec[3 * k + 2];
+  if (ND == 1) {
+    double G[6] = {0, 0, 0, 0, 0, 0};
+    for (int ch = 0; ch < P.nkchunk; ++ch) {
+      const double* g = b.kG + ((long long)P.gch_off + ch) * 6;
+#pragma unroll
+      for (int c = 0; c < 6; ++c) G[c] += g[c];
+    }
+    const double gx = G[0] * kx + G[1] * ky + G[2] * kz;
+    const double gy = G[1] * kx + G[3] * ky + G[4] * kz;
+    const double gz = G[2] * kx + G[4] * ky + G[5] * kz;
+    s[6] = kx * gx + ky * gy + kz * gz;
+    s[7] = gx;
+    s[8] = gy;
+    s[9] = gz;
   }
   double* ks = b.ksum + (long long)k * 10;
 #pragma unroll
   for (int c = 0; c < 10; ++c) ks[c] = s[c];
-  const double kx = b.kvec[3 * k], ky = b.kvec[3 * k + 1], kz = b.kvec[3 * k + 2];
   const double Sr = kx * s[0] + ky * s[2] + kz * s[4];
   const double Si = kx * s[1] + ky * s[3] + kz * s[5];
   const double val = b.kval[k];
@@ -248,7 +299,7 @@ static void launch_kspace_nd(const Batch& b, const int4* kwork, int nkwork, cons
                              double* kE, cudaStream_t s) {
   if (b.nktot == 0) return;
   if (nkwork > 0) ksum_kernel<ND><<<nkwork, kKBlock, 0, s>>>(b, kwork);
-  kcombine_kernel<<<cdiv(b.nktot, 128), 128, 0, s>>>(b, kowner, kE);
+  kcombine_kernel<ND><<<cdiv(b.nktot, 128), 128, 0, s>>>(b, kowner, kE);
   kgather_kernel<ND><<<b.nblk, kPartBlock, 0, s>>>(b);
 }
 
@@ -257,7 +308,7 @@ static void kspace_part_nd(const Batch& b, const int4* kwork, int nkwork, const 
                            double* kE, int part, cudaStream_t s) {
   if (b.nktot == 0) return;
   if (part == 0 && nkwork > 0) ksum_kernel<ND><<<nkwork, kKBlock, 0, s>>>(b, kwork);
-  if (part == 1) kcombine_kernel<<<cdiv(b.nktot, 128), 128, 0, s>>>(b, kowner, kE);
+  if (part == 1) kcombine_kernel<ND><<<cdiv(b.nktot, 128), 128, 0, s>>>(b, kowner, kE);
   if (part == 2) kgather_kernel<ND><<<b.nblk, kPartBlock, 0, s>>>(b);
 }
 

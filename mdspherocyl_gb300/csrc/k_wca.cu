@@ -122,16 +122,21 @@ __device__ bool wca_pair(const Batch& b, const SysDev& P, int A, int B, double* 
     rsq += rij[a] * rij[a];
   }
   double dij[3], st[2];
-  const double dsq = seg_dist_ref(ra, rb, P.L, rij, dij, st);
+  const double dsq = seg_dist_ref<false>(ra, rb, P.L, rij, dij, st);
   if (dsq < 0.49 * sig_sq || dsq > rsq * 1.00001) err |= kErrOverlap;
   if (!(dsq < rsh)) return false;
-  const double SR2s = sig_sq / dsq;
+  // one reciprocal instead of the reference's three divisions (FP64
+  // division is a long instruction sequence here); FIJ = W / ddr reduces to
+  // 6 (pot + 4 SR6^2) / dsq, NaN where ddr = 0 as in the reference
+  const double inv_dsq = 1.0 / dsq;
+  const double SR2s = sig_sq * inv_dsq;
   const double SR6s = SR2s * SR2s * SR2s;
   const double pot = 4 * SR6s * (SR6s - 1.);
   const double ddr = rij[0] * dij[0] + rij[1] * dij[1] + rij[2] * dij[2];
   U = pot + 1.;
-  W = 6 * (pot + 4 * SR6s * SR6s) * ddr / dsq;
-  const double FIJ = W / ddr;
+  const double fw = 6 * (pot + 4 * SR6s * SR6s) * inv_dsq;
+  W = fw * ddr;
+  const double FIJ = (ddr != 0.0) ? fw : __longlong_as_double(0x7ff8000000000000LL);
   if (!(fabs(FIJ) < 1e300)) err |= kErrNan;
 #pragma unroll
   for (int a = 0; a < 3; ++a) fA[a] = FIJ * dij[a];
@@ -327,7 +332,7 @@ __global__ void __launch_bounds__(kPartBlock) cluster_bonds_kernel(Batch b) {
         rij[a] = ri.r[a] - rq.r[a];
         rij[a] -= P.L[a] * floor(rij[a] / P.L[a] + 0.5);
       }
-      const double dsq = seg_dist_ref(ri, rq, P.L, rij, dij, st);
+      const double dsq = seg_dist_ref<true>(ri, rq, P.L, rij, dij, st);
       bond = dsq < sigma * sigma ? 1 : 0;
     }
     fl[k] = bond;

@@ -46,6 +46,7 @@ struct SysDev {
   int tile_off, ntile;  // tile list range
   int k_off, nk;        // k-vector range
   int kchunk_off, nkchunk;  // structure-factor partial range (chunks of kKChunk particles)
+  int gch_off, pad_g;       // first chunk of the system in the G-tensor partials
   int blk_off, nblk;        // per-particle block range
   int cl_fr;
   double L[3];
@@ -148,6 +149,7 @@ struct Batch {
   double* ksum;  // 10 per k: uve (6), self, uvslf (3) -- FP64
   float2* kS;    // val * S(k) per k, FP32 for the gather
   double* kE;    // 10 per k: energy and pressure-tensor terms
+  double* kG;    // 6 per particle chunk: sum of m m^T (one dipole per particle)
   double* Fk;    // 3 ndip
   double* Gk;    // 3 ndip  (torque = m x Gk)
   // integrator partials, per block

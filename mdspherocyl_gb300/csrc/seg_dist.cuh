@@ -25,7 +25,11 @@ __device__ inline double ddot(const double* a, const double* b) {
 }
 __device__ inline double dmimg(double x, double L) { return x - L * floor(x / L + 0.5); }
 
-// returns d^2; dAB = closest-approach vector (from B to A); st = (s, t)
+// returns d^2; dAB = closest-approach vector (from B to A); st = (s, t).
+// EXACT: divide by det as the reference does (the cluster test, whose labels
+// must equal the reference's); otherwise multiply by one reciprocal (the WCA
+// forces, within ~1e-16 of the reference).
+template <bool EXACT>
 __device__ inline double seg_dist_ref(const RodD& A, const RodD& B, const double L[3],
                                       const double rAB[3], double dAB[3], double st[2]) {
   const double *oA = A.o, *oB = B.o;
@@ -47,7 +51,8 @@ __device__ inline double seg_dist_ref(const RodD& A, const RodD& B, const double
   };
   if (det > 1.e-12) {
     double dis[3];
-    double s0 = s / det, t0 = t / det;
+    const double inv_det = EXACT ? 0.0 : 1.0 / det;
+    double s0 = EXACT ? s / det : s * inv_det, t0 = EXACT ? t / det : t * inv_det;
     seg(s0, t0, dis);
     double dsq0 = ddot(dis, dis);
     if (dsq0 < 1.e-12) {
@@ -157,8 +162,8 @@ __device__ inline double seg_dist_ref(const RodD& A, const RodD& B, const double
           break;
         }
         default:  // 5
-          s /= det;
-          t /= det;
+          s = s0;
+          t = t0;
           seg(s, t, dAB);
           break;
       }
