@@ -11,6 +11,17 @@
 // fixed slots of a partial buffer, which the finalize kernel adds in a
 // fixed order -- the result is deterministic.
 //
+// Packed arithmetic: a lane's two i-dipoles meet the same j at each step,
+// so the two pair evaluations run side by side in the two halves of
+// float2 values with Blackwell's paired FP32 instructions (__ffma2_rn,
+// __fmul2_rn, __fadd2_rn: two FP32 operations per issued instruction).
+// Only the special-function steps (rsqrt, exp2, reciprocal, floor) and the
+// integer minimum image stay scalar.  Pairs that must be skipped (the lower
+// triangle and self pairs of diagonal tiles, ragged strips, dipoles of one
+// particle) are zeroed by scaling the i-moment by 0 -- every output is
+// linear in it -- so the warp never diverges; tiles with no such pairs run
+// a loop without the masks.
+//
 // Arithmetic: FP32.  Pair separations come from 32-bit fixed-point box
 // fractions, so the minimum image is an exact integer wrap and the
 // separation keeps ~1e-7 relative precision at any box size.  The
@@ -26,87 +37,223 @@
 //   B'' = 6s/r^2 + 2a^2 C,       B''' = -42s/r^3 - 12a^2 C/r - 4a^4 r C
 //   C'' = 2a^2 C (2a^2 r^2 - 1), C''' = 4a^4 r C (3 - 2a^2 r^2)
 // which matches the table to ~2e-9 without reading it.
+//
+// erfc(x) = exp(-x^2) t Q(t), t = 1/(1 + x/2), with Q a degree-9 polynomial
+// fitted to erfcx(x)/t by weighted least squares on Chebyshev nodes over
+// 0 <= x <= 9.5 (fit_erfcx.py beside this file; relative error 5e-8 with
+// FP32 coefficients).  exp(-x^2) is shared with the Gaussian term.  Beyond
+// x = 9.35 exp(-x^2) is below the FP32 range and both terms are 0, as the
+// reference's table is there to FP32 precision.
 #include "mdsc_dev.cuh"
 
 namespace mdsc {
 
-struct PairOut {
-  float fx, fy, fz;     // force on i (j gets -f)
-  float tix, tiy, tiz;  // torque on i without lever arm
-  float tjx, tjy, tjz;  // torque on j without lever arm
-  float u;              // pair energy
-};
+namespace {
 
-// One dipole pair: d = r_i - r_j (minimum image), moment vectors mi, mj.
-__device__ __forceinline__ void dip_pair(const SysDev& P, float dx, float dy, float dz, float mix,
-                                         float miy, float miz, float mjx, float mjy, float mjz,
-                                         PairOut& o) {
-  const float r2 = dx * dx + dy * dy + dz * dz;
-  const float rinv = rsqrtf(r2);
-  const float r = r2 * rinv;
-  const float rinv2 = rinv * rinv;
-  const float x = P.alphaf * r;
-  const float E = erfcf(x);
-  const float G = P.gpref * expf(-x * x);
-  const float rinv3 = rinv2 * rinv;
-  float A = E * rinv3 + G * rinv2;
-  float B = (3.f * E * rinv3 + G * (P.alpha2x2 + 3.f * rinv2)) * rinv2;
-  float C = P.alpha4x4 * G;
-  // the reference table's linear-interpolation error to third order:
-  // h2 f'' + h3 f''' with a = r - r0, b = r1 - r, h2 = ab/2, h3 = ab(b - a)/6
-  const float uu = r * P.invLh;
-  const float fr = uu - floorf(uu);
-  const float ab = fr * (1.f - fr);
-  const float h2 = P.halfLh2 * ab;
-  const float h3 = P.sixthLh3 * ab * (1.f - 2.f * fr);
-  const float s5 = 5.f * B + C;
-  const float a2 = P.alpha2x2;
-  const float a2C = a2 * C;
-  const float a2rC = a2C * r;
-  const float dA = h2 * (4.f * B + C) - h3 * (4.f * s5 * rinv + a2rC);
-  const float dB = h2 * (6.f * s5 * rinv2 + a2C) - h3 * (42.f * s5 * rinv3 + 6.f * a2C * rinv + a2 * a2rC);
-  const float dC = h2 * (a2C * (a2 * r2 - 1.f)) + h3 * (a2 * a2rC * (3.f - a2 * r2));
-  A += dA;
-  B += dB;
-  C += dC;
+using f2 = float2;
+__device__ __forceinline__ f2 b2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ f2 add2(f2 a, f2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ f2 neg2(f2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) { return __fadd2_rn(a, neg2(b)); }
 
-  const float mimj = mix * mjx + miy * mjy + miz * mjz;
-  const float mir = mix * dx + miy * dy + miz * dz;
-  const float mjr = mjx * dx + mjy * dy + mjz * dz;
-  const float pr = mir * mjr;
-  o.u = mimj * A - pr * B;
-  const float q = pr * rinv2;
-  const float fact = (mimj - 5.f * q) * B - q * C;
-  o.fx = fact * dx + (mir * mjx + mjr * mix) * B;
-  o.fy = fact * dy + (mir * mjy + mjr * miy) * B;
-  o.fz = fact * dz + (mir * mjz + mjr * miz) * B;
-  // mi x mj scaled by A
-  const float wx = A * (miy * mjz - miz * mjy);
-  const float wy = A * (miz * mjx - mix * mjz);
-  const float wz = A * (mix * mjy - miy * mjx);
-  const float bj = mjr * B, bi = mir * B;
-  o.tix = bj * (miy * dz - miz * dy) - wx;
-  o.tiy = bj * (miz * dx - mix * dz) - wy;
-  o.tiz = bj * (mix * dy - miy * dx) - wz;
-  o.tjx = bi * (mjy * dz - mjz * dy) + wx;
-  o.tjy = bi * (mjz * dx - mjx * dz) + wy;
-  o.tjz = bi * (mjx * dy - mjy * dx) + wz;
+__device__ __forceinline__ float ex2_approx(float y) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(y));
+  return r;
+}
+__device__ __forceinline__ float rcp_approx(float y) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(y));
+  return r;
+}
+__device__ __forceinline__ float rsqrt_approx(float y) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(y));
+  return r;
+}
+// minimum-image separation of two fixed-point coordinates: the integer
+// difference times L / 2^32, the scale carried as hi + lo so that its FP32
+// rounding does not bias every separation of the system the same way
+__device__ __forceinline__ f2 fix_diff2(uint32_t a0, uint32_t a1, uint32_t bj, f2 hi, f2 lo) {
+  const f2 k = make_float2((float)(int32_t)(a0 - bj), (float)(int32_t)(a1 - bj));
+  return fma2(k, hi, mul2(k, lo));
 }
 
-struct IDip {
-  uint32_t x, y, z;
-  float mx, my, mz;
-  int own;
-  bool ok;
-  float f[3], t[3];
+// Q(t) coefficients, constant term first (fit_erfcx.py)
+constexpr float kQ0 = 2.820587754e-01f, kQ1 = 2.829789221e-01f, kQ2 = 2.375463843e-01f,
+                kQ3 = 2.310565114e-01f, kQ4 = -1.153462157e-01f, kQ5 = 4.548966587e-01f,
+                kQ6 = -7.125887275e-01f, kQ7 = 4.623427987e-01f, kQ8 = -1.380545348e-01f,
+                kQ9 = 1.510943193e-02f;
+constexpr double kSqrtLog2e = 1.2011224087864498;  // sqrt(log2(e))
+
+// per-system constants, the same value in both halves
+struct PairConst {
+  f2 xh, xlo;    // alpha sqrt(log2 e) as a float-float pair: 2^(-(x r)^2) = exp(-alpha^2 r^2)
+  f2 ahalf;      // alpha / 2
+  f2 gpref;      // 2 alpha / sqrt(pi)
+  f2 a2, a4x4;   // 2 alpha^2, 4 alpha^4
+  f2 invLh, halfLh2, nsixthLh3;
+  f2 Lhx, Lhy, Lhz, Llx, Lly, Llz;  // L / 2^32 per axis as float-float pairs
 };
+
+struct Lane2 {
+  uint32_t x0, x1, y0, y1, z0, z1;  // fixed-point positions of the two i-dipoles
+  f2 mx, my, mz;                    // their moments (0 for a missing dipole)
+  int own0, own1;
+  bool ok0, ok1;
+  f2 F[3], T[3], pt[9], U, Uc;
+};
+
+// one step of the tile loop: the lane's two i-dipoles against j = lj
+template <bool MASKED, bool MULTI>
+__device__ __forceinline__ void tile_step(const PairConst& K, Lane2& s, const uint4 jp, const float4 jm,
+                                          bool diag, int lane, int lj, int jvalid, float4& ja4, float2& ja2) {
+  f2 mix = s.mx, miy = s.my, miz = s.mz;
+  bool a0 = true, a1 = true;
+  if (MASKED) {
+    const bool jv = lj < jvalid;
+    a0 = s.ok0 && jv && (!diag || lj > lane);
+    a1 = s.ok1 && jv && (!diag || lj > lane + 32);
+    if (MULTI) {
+      a0 = a0 && (s.own0 != (int)jp.w);
+      a1 = a1 && (s.own1 != (int)jp.w);
+    }
+    const f2 on = make_float2(a0 ? 1.f : 0.f, a1 ? 1.f : 0.f);
+    mix = mul2(mix, on);
+    miy = mul2(miy, on);
+    miz = mul2(miz, on);
+  }
+  const f2 dx = fix_diff2(s.x0, s.x1, jp.x, K.Lhx, K.Llx);
+  const f2 dy = fix_diff2(s.y0, s.y1, jp.y, K.Lhy, K.Lly);
+  const f2 dz = fix_diff2(s.z0, s.z1, jp.z, K.Lhz, K.Llz);
+  f2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+  if (MASKED) {
+    r2.x = a0 ? r2.x : 1.f;
+    r2.y = a1 ? r2.y : 1.f;
+  }
+  const f2 rinv = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
+  const f2 r = mul2(r2, rinv);
+  const f2 rinv2 = mul2(rinv, rinv);
+  const f2 rinv3 = mul2(rinv2, rinv);
+
+  // exp(-x^2) and erfc(x), x = alpha r; the exponent from a once-rounded
+  // product (x up to ~5 puts it near -40, where a biased constant would
+  // shift every far pair's weight alike)
+  const f2 xr = fma2(r, K.xh, mul2(r, K.xlo));
+  const f2 y = mul2(xr, xr);
+  const f2 ex = make_float2(ex2_approx(-y.x), ex2_approx(-y.y));
+  const f2 den = fma2(r, K.ahalf, b2(1.f));
+  const f2 tt = make_float2(rcp_approx(den.x), rcp_approx(den.y));
+  f2 q = fma2(b2(kQ9), tt, b2(kQ8));
+  q = fma2(q, tt, b2(kQ7));
+  q = fma2(q, tt, b2(kQ6));
+  q = fma2(q, tt, b2(kQ5));
+  q = fma2(q, tt, b2(kQ4));
+  q = fma2(q, tt, b2(kQ3));
+  q = fma2(q, tt, b2(kQ2));
+  q = fma2(q, tt, b2(kQ1));
+  q = fma2(q, tt, b2(kQ0));
+  const f2 E = mul2(mul2(ex, tt), q);
+  const f2 G = mul2(ex, K.gpref);
+  const f2 Er3 = mul2(E, rinv3);
+  const f2 A = fma2(G, rinv2, Er3);
+  const f2 B = mul2(fma2(G, fma2(b2(3.f), rinv2, K.a2), mul2(b2(3.f), Er3)), rinv2);
+  const f2 C = mul2(G, K.a4x4);
+
+  // the table's interpolation error, second and third order
+  const f2 uu = mul2(r, K.invLh);
+  const f2 fr = sub2(uu, make_float2(floorf(uu.x), floorf(uu.y)));
+  const f2 ab = mul2(fr, fma2(fr, b2(-1.f), b2(1.f)));
+  const f2 h2 = mul2(ab, K.halfLh2);
+  const f2 nh3 = mul2(mul2(ab, K.nsixthLh3), fma2(fr, b2(-2.f), b2(1.f)));  // -h3
+  const f2 s5 = fma2(b2(5.f), B, C);
+  const f2 a2C = mul2(K.a2, C);
+  const f2 a2rC = mul2(a2C, r);
+  const f2 a2a2rC = mul2(K.a2, a2rC);
+  const f2 a2r2 = mul2(K.a2, r2);
+  const f2 Ac = fma2(h2, fma2(b2(4.f), B, C), fma2(nh3, fma2(mul2(b2(4.f), s5), rinv, a2rC), A));
+  const f2 Bc = fma2(h2, fma2(mul2(b2(6.f), s5), rinv2, a2C),
+                     fma2(nh3, fma2(mul2(b2(42.f), s5), rinv3, fma2(mul2(b2(6.f), a2C), rinv, a2a2rC)), B));
+  const f2 Cc = fma2(h2, mul2(a2C, add2(a2r2, b2(-1.f))), fma2(nh3, mul2(a2a2rC, add2(a2r2, b2(-3.f))), C));
+
+  // dipole-dipole energy, force on i, torques without lever arm
+  const f2 mjx = b2(jm.x), mjy = b2(jm.y), mjz = b2(jm.z);
+  const f2 mimj = fma2(miz, mjz, fma2(miy, mjy, mul2(mix, mjx)));
+  const f2 mir = fma2(miz, dz, fma2(miy, dy, mul2(mix, dx)));
+  const f2 mjr = fma2(mjz, dz, fma2(mjy, dy, mul2(mjx, dx)));
+  const f2 pr = mul2(mir, mjr);
+  const f2 u = fma2(neg2(pr), Bc, mul2(mimj, Ac));
+  const f2 qq = mul2(pr, rinv2);
+  const f2 fact = fma2(neg2(qq), Cc, mul2(fma2(b2(-5.f), qq, mimj), Bc));
+  const f2 mirB = mul2(mir, Bc), mjrB = mul2(mjr, Bc);
+  const f2 fx = fma2(fact, dx, fma2(mirB, mjx, mul2(mjrB, mix)));
+  const f2 fy = fma2(fact, dy, fma2(mirB, mjy, mul2(mjrB, miy)));
+  const f2 fz = fma2(fact, dz, fma2(mirB, mjz, mul2(mjrB, miz)));
+  const f2 wx = mul2(Ac, fma2(miy, mjz, mul2(neg2(miz), mjy)));
+  const f2 wy = mul2(Ac, fma2(miz, mjx, mul2(neg2(mix), mjz)));
+  const f2 wz = mul2(Ac, fma2(mix, mjy, mul2(neg2(miy), mjx)));
+  const f2 tix = fma2(mjrB, fma2(miy, dz, mul2(neg2(miz), dy)), neg2(wx));
+  const f2 tiy = fma2(mjrB, fma2(miz, dx, mul2(neg2(mix), dz)), neg2(wy));
+  const f2 tiz = fma2(mjrB, fma2(mix, dy, mul2(neg2(miy), dx)), neg2(wz));
+  const f2 tjx = fma2(mirB, fma2(mjy, dz, mul2(neg2(mjz), dy)), wx);
+  const f2 tjy = fma2(mirB, fma2(mjz, dx, mul2(neg2(mjx), dz)), wy);
+  const f2 tjz = fma2(mirB, fma2(mjx, dy, mul2(neg2(mjy), dx)), wz);
+
+  s.F[0] = add2(s.F[0], fx);
+  s.F[1] = add2(s.F[1], fy);
+  s.F[2] = add2(s.F[2], fz);
+  s.T[0] = add2(s.T[0], tix);
+  s.T[1] = add2(s.T[1], tiy);
+  s.T[2] = add2(s.T[2], tiz);
+  ja4.x -= fx.x + fx.y;
+  ja4.y -= fy.x + fy.y;
+  ja4.z -= fz.x + fz.y;
+  ja4.w += tjx.x + tjx.y;
+  ja2.x += tjy.x + tjy.y;
+  ja2.y += tjz.x + tjz.y;
+  // Kahan: U += u
+  const f2 yk = sub2(u, s.Uc);
+  const f2 tk = add2(s.U, yk);
+  s.Uc = sub2(sub2(tk, s.U), yk);
+  s.U = tk;
+  s.pt[0] = fma2(dx, fx, s.pt[0]);
+  s.pt[1] = fma2(dx, fy, s.pt[1]);
+  s.pt[2] = fma2(dx, fz, s.pt[2]);
+  s.pt[3] = fma2(dy, fx, s.pt[3]);
+  s.pt[4] = fma2(dy, fy, s.pt[4]);
+  s.pt[5] = fma2(dy, fz, s.pt[5]);
+  s.pt[6] = fma2(dz, fx, s.pt[6]);
+  s.pt[7] = fma2(dz, fy, s.pt[7]);
+  s.pt[8] = fma2(dz, fz, s.pt[8]);
+}
+
+template <bool MASKED, bool MULTI>
+__device__ __forceinline__ void tile_loop(const PairConst& K, Lane2& s, const uint4* sj, const float4* smj,
+                                          float4* sa4, float2* sa2, bool diag, int lane, int jvalid) {
+#pragma unroll 1
+  for (int t = 0; t < kTile; ++t) {
+    const int lj = (lane + t) & (kTile - 1);
+    const uint4 jp = sj[lj];
+    const float4 jm = smj[lj];
+    float4 ja4 = sa4[lj];
+    float2 ja2 = sa2[lj];
+    tile_step<MASKED, MULTI>(K, s, jp, jm, diag, lane, lj, jvalid, ja4, ja2);
+    sa4[lj] = ja4;
+    sa2[lj] = ja2;
+    __syncwarp();
+  }
+}
+
+}  // namespace
 
 template <bool MULTI>
 __global__ void __launch_bounds__(32) real_pairs_kernel(Batch b) {
-  __shared__ uint32_t sx[kTile], sy[kTile], sz[kTile];
-  __shared__ float smx[kTile], smy[kTile], smz[kTile];
-  __shared__ int sown[kTile];
-  __shared__ float sacc[6][kTile];
+  __shared__ uint4 sj[kTile];    // fixed-point x, y, z and owner of the j-dipoles
+  __shared__ float4 smj[kTile];  // their moments
+  __shared__ float4 sa4[kTile];  // j-side sums: F x, y, z and T x
+  __shared__ float2 sa2[kTile];  // T y, z
 
   const int4 tl = b.tiles[blockIdx.x];
   const SysDev& P = b.sys[tl.x];
@@ -115,89 +262,75 @@ __global__ void __launch_bounds__(32) real_pairs_kernel(Batch b) {
   const int lane = threadIdx.x;
   const int ndip = P.ndip;
   const int ND = b.ndtot;
-  const float sxs = P.Lfix[0], sys_ = P.Lfix[1], szs = P.Lfix[2];
+
+  PairConst K;
+  {
+    const double xa = P.alpha * kSqrtLog2e;
+    const float xh = (float)xa;
+    K.xh = b2(xh);
+    K.xlo = b2((float)(xa - (double)xh));
+    const double inv32 = 1.0 / 4294967296.0;
+    float h = (float)(P.L[0] * inv32);
+    K.Lhx = b2(h);
+    K.Llx = b2((float)(P.L[0] * inv32 - (double)h));
+    h = (float)(P.L[1] * inv32);
+    K.Lhy = b2(h);
+    K.Lly = b2((float)(P.L[1] * inv32 - (double)h));
+    h = (float)(P.L[2] * inv32);
+    K.Lhz = b2(h);
+    K.Llz = b2((float)(P.L[2] * inv32 - (double)h));
+  }
+  K.ahalf = b2(0.5f * P.alphaf);
+  K.gpref = b2(P.gpref);
+  K.a2 = b2(P.alpha2x2);
+  K.a4x4 = b2(P.alpha4x4);
+  K.invLh = b2(P.invLh);
+  K.halfLh2 = b2(P.halfLh2);
+  K.nsixthLh3 = b2(-P.sixthLh3);
 
   for (int k = lane; k < kTile; k += 32) {
     const int jj = J * kTile + k;
     const bool v = jj < ndip;
     const int g = P.dip_off + (v ? jj : 0);
-    sx[k] = b.dfx[g];
-    sy[k] = b.dfx[ND + g];
-    sz[k] = b.dfx[2 * ND + g];
-    smx[k] = v ? b.dm[g] : 0.f;
-    smy[k] = v ? b.dm[ND + g] : 0.f;
-    smz[k] = v ? b.dm[2 * ND + g] : 0.f;
-    sown[k] = v ? b.downer[g] : -1;
-#pragma unroll
-    for (int c = 0; c < 6; ++c) sacc[c][k] = 0.f;
+    sj[k] = make_uint4(b.dfx[g], b.dfx[ND + g], b.dfx[2 * ND + g], v ? (uint32_t)b.downer[g] : 0xffffffffu);
+    smj[k] = v ? make_float4(b.dm[g], b.dm[ND + g], b.dm[2 * ND + g], 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+    sa4[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    sa2[k] = make_float2(0.f, 0.f);
   }
 
-  IDip id[2];
+  Lane2 s;
+  {
+    const int i0 = I * kTile + lane, i1 = i0 + 32;
+    s.ok0 = i0 < ndip;
+    s.ok1 = i1 < ndip;
+    const int g0 = P.dip_off + (s.ok0 ? i0 : 0), g1 = P.dip_off + (s.ok1 ? i1 : 0);
+    s.x0 = b.dfx[g0];
+    s.y0 = b.dfx[ND + g0];
+    s.z0 = b.dfx[2 * ND + g0];
+    s.x1 = b.dfx[g1];
+    s.y1 = b.dfx[ND + g1];
+    s.z1 = b.dfx[2 * ND + g1];
+    const float z0 = s.ok0 ? 1.f : 0.f, z1 = s.ok1 ? 1.f : 0.f;
+    s.mx = make_float2(z0 * b.dm[g0], z1 * b.dm[g1]);
+    s.my = make_float2(z0 * b.dm[ND + g0], z1 * b.dm[ND + g1]);
+    s.mz = make_float2(z0 * b.dm[2 * ND + g0], z1 * b.dm[2 * ND + g1]);
+    s.own0 = b.downer[g0];
+    s.own1 = b.downer[g1];
 #pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    const int ii = I * kTile + lane + 32 * h;
-    id[h].ok = ii < ndip;
-    const int g = P.dip_off + (id[h].ok ? ii : 0);
-    id[h].x = b.dfx[g];
-    id[h].y = b.dfx[ND + g];
-    id[h].z = b.dfx[2 * ND + g];
-    id[h].mx = b.dm[g];
-    id[h].my = b.dm[ND + g];
-    id[h].mz = b.dm[2 * ND + g];
-    id[h].own = b.downer[g];
+    for (int c = 0; c < 3; ++c) s.F[c] = s.T[c] = b2(0.f);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) id[h].f[c] = id[h].t[c] = 0.f;
+    for (int c = 0; c < 9; ++c) s.pt[c] = b2(0.f);
+    s.U = s.Uc = b2(0.f);
   }
-  float U = 0.f, Uc = 0.f;  // Kahan-compensated pair-energy sum
-  float pt[9];
-#pragma unroll
-  for (int c = 0; c < 9; ++c) pt[c] = 0.f;
   __syncwarp();
 
   const int jvalid = min(kTile, ndip - J * kTile);
-  for (int t = 0; t < kTile; ++t) {
-    const int lj = (lane + t) & (kTile - 1);
-    const bool jv = lj < jvalid;
-    const uint32_t jx = sx[lj], jy = sy[lj], jz = sz[lj];
-    const float mjx = smx[lj], mjy = smy[lj], mjz = smz[lj];
-    const int jown = sown[lj];
-    float ja[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int li = lane + 32 * h;
-      bool act = id[h].ok && jv && (!diag || lj > li);
-      if (MULTI) act = act && (id[h].own != jown);
-      if (act) {
-        const float dx = fix_diff(id[h].x, jx, sxs);
-        const float dy = fix_diff(id[h].y, jy, sys_);
-        const float dz = fix_diff(id[h].z, jz, szs);
-        PairOut o;
-        dip_pair(P, dx, dy, dz, id[h].mx, id[h].my, id[h].mz, mjx, mjy, mjz, o);
-        id[h].f[0] += o.fx;
-        id[h].f[1] += o.fy;
-        id[h].f[2] += o.fz;
-        id[h].t[0] += o.tix;
-        id[h].t[1] += o.tiy;
-        id[h].t[2] += o.tiz;
-        ja[0] -= o.fx;
-        ja[1] -= o.fy;
-        ja[2] -= o.fz;
-        ja[3] += o.tjx;
-        ja[4] += o.tjy;
-        ja[5] += o.tjz;
-        // Kahan: U += o.u
-        const float yk = o.u - Uc;
-        const float tk = U + yk;
-        Uc = (tk - U) - yk;
-        U = tk;
-        pt[0] += dx * o.fx; pt[1] += dx * o.fy; pt[2] += dx * o.fz;
-        pt[3] += dy * o.fx; pt[4] += dy * o.fy; pt[5] += dy * o.fz;
-        pt[6] += dz * o.fx; pt[7] += dz * o.fy; pt[8] += dz * o.fz;
-      }
-    }
-#pragma unroll
-    for (int c = 0; c < 6; ++c) sacc[c][lj] += ja[c];
-  }
+  // no pair of this tile is skipped: the fast loop without masks
+  const bool full = !MULTI && !diag && jvalid == kTile;
+  if (full)
+    tile_loop<false, MULTI>(K, s, sj, smj, sa4, sa2, diag, lane, jvalid);
+  else
+    tile_loop<true, MULTI>(K, s, sj, smj, sa4, sa2, diag, lane, jvalid);
   __syncwarp();
 
   // partial slots: (strip X, strip Y, component c, local index)
@@ -207,28 +340,45 @@ __global__ void __launch_bounds__(32) real_pairs_kernel(Batch b) {
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     const int li = lane + 32 * h;
+    float fv[3], tv[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      float fv = id[h].f[c], tv = id[h].t[c];
-      if (diag) {
-        fv += sacc[c][li];
-        tv += sacc[3 + c][li];
-      }
-      base_ij[c * kTile + li] = fv;
-      base_ij[(3 + c) * kTile + li] = tv;
+      fv[c] = h ? s.F[c].y : s.F[c].x;
+      tv[c] = h ? s.T[c].y : s.T[c].x;
+    }
+    if (diag) {
+      const float4 a4 = sa4[li];
+      const float2 a2 = sa2[li];
+      fv[0] += a4.x;
+      fv[1] += a4.y;
+      fv[2] += a4.z;
+      tv[0] += a4.w;
+      tv[1] += a2.x;
+      tv[2] += a2.y;
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      base_ij[c * kTile + li] = fv[c];
+      base_ij[(3 + c) * kTile + li] = tv[c];
     }
   }
   if (!diag) {
     for (int k = lane; k < kTile; k += 32) {
-#pragma unroll
-      for (int c = 0; c < 6; ++c) base_ji[c * kTile + k] = sacc[c][k];
+      const float4 a4 = sa4[k];
+      const float2 a2 = sa2[k];
+      base_ji[0 * kTile + k] = a4.x;
+      base_ji[1 * kTile + k] = a4.y;
+      base_ji[2 * kTile + k] = a4.z;
+      base_ji[3 * kTile + k] = a4.w;
+      base_ji[4 * kTile + k] = a2.x;
+      base_ji[5 * kTile + k] = a2.y;
     }
   }
   // tile energy and pressure tensor
   float red[10];
-  red[0] = U + (-Uc);
+  red[0] = (s.U.x + (-s.Uc.x)) + (s.U.y + (-s.Uc.y));
 #pragma unroll
-  for (int c = 0; c < 9; ++c) red[1 + c] = pt[c];
+  for (int c = 0; c < 9; ++c) red[1 + c] = s.pt[c].x + s.pt[c].y;
 #pragma unroll
   for (int c = 0; c < 10; ++c) {
 #pragma unroll
