@@ -103,9 +103,12 @@ __device__ __forceinline__ void load_rod(const Batch& b, int i, RodD& R) {
 }
 
 // WCA pair (v25/functions.cpp:1438-1540) for A < B; returns false when the
-// pair does not interact.  fA: force on A; tA, tB: torques.
+// pair does not interact.  fA: force on A; tA, tB: torques; ev: U, W and
+// the pressure tensor.  This file is compiled without FMA contraction (the
+// cluster test must repeat the reference's roundings); the force path asks
+// for its FMAs explicitly.
 __device__ bool wca_pair(const Batch& b, const SysDev& P, int A, int B, double* fA, double* tA,
-                         double* tB, double& U, double& W, double* PT, int& err) {
+                         double* tB, double* ev, int& err) {
   RodD ra, rb;
   load_rod(b, A, ra);
   load_rod(b, B, rb);
@@ -114,43 +117,42 @@ __device__ bool wca_pair(const Batch& b, const SysDev& P, int A, int B, double* 
   const double sig_sq = sigma * sigma;
   const double srt = 1.122462048309373;   // 2^(1/6)
   const double rsh = srt * srt * sig_sq;
-  double rij[3], rsq = 0;
+  double rij[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     rij[a] = ra.r[a] - rb.r[a];
-    rij[a] -= P.L[a] * floor(rij[a] * P.invL[a] + 0.5);
-    rsq += rij[a] * rij[a];
+    rij[a] = fma(-P.L[a], floor(fma(rij[a], P.invL[a], 0.5)), rij[a]);
   }
+  const double rsq = fma(rij[2], rij[2], fma(rij[1], rij[1], rij[0] * rij[0]));
   double dij[3], st[2];
-  const double dsq = seg_dist_ref<false>(ra, rb, P.L, rij, dij, st);
+  const double dsq = seg_dist_wca(ra, rb, P.L, rij, dij, st);
   if (dsq < 0.49 * sig_sq || dsq > rsq * 1.00001) err |= kErrOverlap;
   if (!(dsq < rsh)) return false;
-  // one reciprocal instead of the reference's three divisions (FP64
-  // division is a long instruction sequence here); FIJ = W / ddr reduces to
-  // 6 (pot + 4 SR6^2) / dsq, NaN where ddr = 0 as in the reference
+  // one reciprocal instead of the reference's three divisions; FIJ = W / ddr
+  // reduces to 6 (pot + 4 SR6^2) / dsq, NaN where ddr = 0 as in the reference
   const double inv_dsq = 1.0 / dsq;
   const double SR2s = sig_sq * inv_dsq;
   const double SR6s = SR2s * SR2s * SR2s;
-  const double pot = 4 * SR6s * (SR6s - 1.);
-  const double ddr = rij[0] * dij[0] + rij[1] * dij[1] + rij[2] * dij[2];
-  U = pot + 1.;
-  const double fw = 6 * (pot + 4 * SR6s * SR6s) * inv_dsq;
-  W = fw * ddr;
+  const double pot = fma(4 * SR6s, SR6s, -4 * SR6s);
+  const double ddr = fma(rij[2], dij[2], fma(rij[1], dij[1], rij[0] * dij[0]));
+  const double fw = 6 * fma(4 * SR6s, SR6s, pot) * inv_dsq;
   const double FIJ = (ddr != 0.0) ? fw : __longlong_as_double(0x7ff8000000000000LL);
   if (!(fabs(FIJ) < 1e300)) err |= kErrNan;
+  ev[0] = pot + 1.;
+  ev[1] = fw * ddr;
 #pragma unroll
   for (int a = 0; a < 3; ++a) fA[a] = FIJ * dij[a];
 #pragma unroll
   for (int a = 0; a < 3; ++a)
 #pragma unroll
-    for (int c = 0; c < 3; ++c) PT[3 * a + c] = rij[a] * fA[c];
+    for (int c = 0; c < 3; ++c) ev[2 + 3 * a + c] = rij[a] * fA[c];
   const double *oi = ra.o, *oj = rb.o;
-  const double icroj[3] = {oi[1] * oj[2] - oi[2] * oj[1], oi[2] * oj[0] - oi[0] * oj[2],
-                           oi[0] * oj[1] - oi[1] * oj[0]};
-  const double icror[3] = {oi[1] * rij[2] - oi[2] * rij[1], oi[2] * rij[0] - oi[0] * rij[2],
-                           oi[0] * rij[1] - oi[1] * rij[0]};
-  const double jcror[3] = {oj[1] * rij[2] - oj[2] * rij[1], oj[2] * rij[0] - oj[0] * rij[2],
-                           oj[0] * rij[1] - oj[1] * rij[0]};
+  const double icroj[3] = {fma(oi[1], oj[2], -oi[2] * oj[1]), fma(oi[2], oj[0], -oi[0] * oj[2]),
+                           fma(oi[0], oj[1], -oi[1] * oj[0])};
+  const double icror[3] = {fma(oi[1], rij[2], -oi[2] * rij[1]), fma(oi[2], rij[0], -oi[0] * rij[2]),
+                           fma(oi[0], rij[1], -oi[1] * rij[0])};
+  const double jcror[3] = {fma(oj[1], rij[2], -oj[2] * rij[1]), fma(oj[2], rij[0], -oj[0] * rij[2]),
+                           fma(oj[0], rij[1], -oj[1] * rij[0])};
   double fact1 = (st[0] - 0.5) * shA0;
   double fact2 = -(st[1] - 0.5) * shB0;
   if (st[0] == -1.e+6) fact1 = fact2 = 0.;
@@ -169,30 +171,33 @@ __device__ bool wca_pair(const Batch& b, const SysDev& P, int A, int B, double* 
   const double fmul = fact1 * fact2;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    tA[a] = FIJ * (fact1 * icror[a] + fmul * icroj[a]);
-    tB[a] = FIJ * (fact2 * jcror[a] - fmul * icroj[a]);
+    tA[a] = FIJ * fma(fact1, icror[a], fmul * icroj[a]);
+    tB[a] = FIJ * fma(fact2, jcror[a], -fmul * icroj[a]);
   }
   return true;
 }
 
-// Two phases per warp.  (1) Each lane screens its particle's partners of
-// higher index (each pair once) in FP32 and keeps the candidates (ascending
-// index).  (2) The warp's candidates, concatenated owner by owner, are
-// evaluated 32 at a time in FP64 with every lane busy; the owner (the lower
-// index) adds its share in order, and the partner's share goes to a record
-// that the finalize kernel gathers.  FP64 runs at a small fraction of the
-// FP32 rate on this GPU, so only pairs that can touch reach the FP64 pipe,
-// once each and densely packed.
+// Two phases per block of particles.  (1) Each thread screens its
+// particle's partners of higher index (each pair once) in FP32 and keeps
+// the candidates (ascending index).  (2) The block's candidates,
+// concatenated owner by owner, are evaluated in FP64 one per thread, in
+// rounds of one block-width; warps with no candidate left skip the round.
+// The owner (the lower index) adds its share in candidate order, the
+// partner's share goes to a record that the finalize kernel gathers, and
+// eleven threads add the round's energies and virials in candidate order.
+// FP64 runs at 1/64 of the FP32 instruction rate on this GPU, so only pairs
+// that can touch reach the FP64 pipe, once each and densely packed.
 __global__ void __launch_bounds__(kPartBlock) wca_kernel(Batch b) {
   __shared__ int cand[kPartBlock][kMaxC];
-  __shared__ double res[kPartBlock / 32][32][6];
-  __shared__ int soff[kPartBlock / 32][32];
-  __shared__ double sh[11 * kPartBlock / 32];
+  __shared__ int soff[kPartBlock + 1];
+  __shared__ int swarp[kPartBlock / 32];
+  __shared__ double res[kPartBlock][6];
+  __shared__ double sev[kPartBlock][11];
   const int2 bk = b.blk[blockIdx.x];
   const int s = bk.x;
   const SysDev& P = b.sys[s];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int i = bk.y + threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int i = bk.y + tid;
   const bool ok = i < P.part_off + P.n;
   const int N = b.ntot;
   int err = 0;
@@ -215,7 +220,7 @@ __global__ void __launch_bounds__(kPartBlock) wca_kernel(Batch b) {
       // 2^(1/3) sigma^2, with a margin for the FP32 screen
       if (d2 >= 1.2599211f * sg * sg * 1.002f) continue;
       if (nc < kMaxC) {
-        cand[threadIdx.x][nc] = q;
+        cand[tid][nc] = q;
         b.wcand[(long long)i * kMaxC + nc] = q;
       }
       ++nc;
@@ -226,68 +231,74 @@ __global__ void __launch_bounds__(kPartBlock) wca_kernel(Batch b) {
     }
     b.wcnt[i] = nc;
   }
-  // exclusive scan of the candidate counts over the warp
-  int off = nc;
+  // exclusive scan of the candidate counts over the block
+  int inc = nc;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
-    const int v = __shfl_up_sync(0xffffffffu, off, d);
-    if (lane >= d) off += v;
+    const int v = __shfl_up_sync(0xffffffffu, inc, d);
+    if (lane >= d) inc += v;
   }
-  const int total = __shfl_sync(0xffffffffu, off, 31);
-  off -= nc;
-  soff[warp][lane] = off;
-  __syncwarp();
+  if (lane == 31) swarp[warp] = inc;
+  __syncthreads();
+  int wbase = 0;
+#pragma unroll
+  for (int w = 0; w < kPartBlock / 32; ++w) wbase += (w < warp) ? swarp[w] : 0;
+  const int off = wbase + inc - nc;
+  soff[tid] = off;
+  if (tid == kPartBlock - 1) soff[kPartBlock] = off + nc;
+  __syncthreads();
+  const int total = soff[kPartBlock];
 
   double F[3] = {0, 0, 0}, T[3] = {0, 0, 0};
-  double acc[11];
-#pragma unroll
-  for (int c = 0; c < 11; ++c) acc[c] = 0.0;
-  for (int base = 0; base < total; base += 32) {
-    const int e = base + lane;
-    double r6[6] = {0, 0, 0, 0, 0, 0};
+  double esum = 0.0;  // thread c < 11: component c of the block's energies
+  for (int base = 0; base < total; base += kPartBlock) {
+    const int e = base + tid;
     if (e < total) {
-      // owner: the last lane whose offset is <= e
-      int lo = 0, hi = 31;
+      // owner: the last thread whose offset is <= e
+      int lo = 0, hi = kPartBlock - 1;
       while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (soff[warp][mid] <= e) lo = mid;
+        if (soff[mid] <= e) lo = mid;
         else hi = mid - 1;
       }
-      const int o = lo;
-      const int kk = e - soff[warp][o];
-      const int p = bk.y + warp * 32 + o;
-      const int q = cand[warp * 32 + o][kk];
-      double fA[3], tA[3], tB[3], U, W, PT[9];
-      double rec[6] = {0, 0, 0, 0, 0, 0};
-      if (wca_pair(b, P, p, q, fA, tA, tB, U, W, PT, err)) {
+      const int kk = e - soff[lo];
+      const int p = bk.y + lo;
+      const int q = cand[lo][kk];
+      double fA[3], tA[3], tB[3], ev[11];
+      if (!wca_pair(b, P, p, q, fA, tA, tB, ev, err)) {
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          r6[a] = fA[a];
-          r6[3 + a] = tA[a];
-          rec[a] = -fA[a];
-          rec[3 + a] = tB[a];
-        }
-        acc[0] += U;
-        acc[1] += W;
+        for (int a = 0; a < 3; ++a) fA[a] = tA[a] = tB[a] = 0.0;
 #pragma unroll
-        for (int c = 0; c < 9; ++c) acc[2 + c] += PT[c];
+        for (int c = 0; c < 11; ++c) ev[c] = 0.0;
       }
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        res[tid][a] = fA[a];
+        res[tid][3 + a] = tA[a];
+      }
+#pragma unroll
+      for (int c = 0; c < 11; ++c) sev[tid][c] = ev[c];
       double* out = b.wrec + ((long long)p * kMaxC + kk) * 6;
 #pragma unroll
-      for (int c = 0; c < 6; ++c) out[c] = rec[c];
+      for (int a = 0; a < 3; ++a) {
+        out[a] = -fA[a];
+        out[3 + a] = tB[a];
+      }
     }
-#pragma unroll
-    for (int c = 0; c < 6; ++c) res[warp][lane][c] = r6[c];
-    __syncwarp();
-    const int e0 = max(off, base), e1 = min(off + nc, base + 32);
+    __syncthreads();
+    const int e0 = max(off, base), e1 = min(off + nc, base + kPartBlock);
     for (int k = e0; k < e1; ++k) {
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
-        F[a] += res[warp][k - base][a];
-        T[a] += res[warp][k - base][3 + a];
+        F[a] += res[k - base][a];
+        T[a] += res[k - base][3 + a];
       }
     }
-    __syncwarp();
+    if (tid < 11) {
+      const int m = min(kPartBlock, total - base);
+      for (int k = 0; k < m; ++k) esum += sev[k][tid];
+    }
+    __syncthreads();
   }
   if (ok) {
 #pragma unroll
@@ -297,12 +308,7 @@ __global__ void __launch_bounds__(kPartBlock) wca_kernel(Batch b) {
     }
   }
   if (err) atomicOr(&b.st[s].status, err);
-  double tot[11];
-  block_sum<11, kPartBlock>(acc, sh, tot);
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int c = 0; c < 11; ++c) b.wcaE[11 * blockIdx.x + c] = tot[c];
-  }
+  if (tid < 11) b.wcaE[11 * blockIdx.x + tid] = esum;
 }
 
 // ---- clusters (v25/functions.cpp:2987-3016,3282-3324) ----------------

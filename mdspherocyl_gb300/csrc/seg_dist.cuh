@@ -195,6 +195,79 @@ __device__ inline double seg_dist_ref(const RodD& A, const RodD& B, const double
   return dsq;
 }
 
+// seg_dist_ref<false> without divergence, for the WCA forces.  The
+// reference's nine regions reduce to three candidate points: the interior
+// solution (s0, t0); s held at an end, S = 1 if s > det else 0, with
+// t = clamp((e + b S)/c); t held at an end, T = 1 if t > det else 0, with
+// s = clamp((b T - d)/a).  Regions 2/8 take the s-held point, 4/6 the
+// t-held one, 5 the interior one, and the corners 1/3/7/9 the nearer of the
+// two held points, ties going as in the reference (1/3 keep the s-held
+// point, 7/9 the t-held one).  Every lane computes all three and selects,
+// so a warp of contacts in different regions runs one instruction stream.
+// Parallel axes (det <= 1e-12) and intersecting axis lines fall back to
+// seg_dist_ref<false>.  Products are contracted to FMAs and the three
+// divisions share one reciprocal: the closest points agree with the
+// reference's to a few ulps.
+__device__ inline double seg_dist_wca(const RodD& A, const RodD& B, const double L[3],
+                                      const double rAB[3], double dAB[3], double st[2]) {
+  const double *oA = A.o, *oB = B.o;
+  const double lA = A.len, lB = B.len;
+  const double doto = fma(oA[2], oB[2], fma(oA[1], oB[1], oA[0] * oB[0]));
+  const double dotrA = fma(rAB[2], oA[2], fma(rAB[1], oA[1], rAB[0] * oA[0]));
+  const double dotrB = fma(rAB[2], oB[2], fma(rAB[1], oB[1], rAB[0] * oB[0]));
+  const double a = lA * lA;
+  const double b = doto * lA * lB;
+  const double c = lB * lB;
+  const double d = fma(dotrA, lA, -0.5 * a) + 0.5 * b;
+  const double e = fma(dotrB, lB, 0.5 * c) - 0.5 * b;
+  const double det = fma(a, c, -b * b);
+  const double s = fma(b, e, -c * d);
+  const double t = fma(a, e, -b * d);
+  const bool par = !(det > 1.e-12);
+  const double dets = par ? 1.0 : det;
+  const double ac = a * c;
+  const double inv = 1.0 / (dets * ac);
+  const double inv_det = inv * ac, inv_a = inv * dets * c, inv_c = inv * dets * a;
+  double laA[3], lbB[3];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    laA[q] = lA * oA[q];
+    lbB[q] = lB * oB[q];
+  }
+  auto seg = [&](double sv, double tv, double* out) {
+    const double sm = sv - 0.5, tm = 0.5 - tv;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) out[q] = fma(tm, lbB[q], fma(sm, laA[q], rAB[q]));
+    return fma(out[2], out[2], fma(out[1], out[1], out[0] * out[0]));
+  };
+  const double s0 = s * inv_det, t0 = t * inv_det;
+  double vI[3];
+  const double dI = seg(s0, t0, vI);
+  if (par || dI < 1.e-12) return seg_dist_ref<false>(A, B, L, rAB, dAB, st);
+  const bool sneg = s < 0.0, sbig = s > det, tneg = t < 0.0, tbig = t > det;
+  const double S = sbig ? 1.0 : 0.0, T = tbig ? 1.0 : 0.0;
+  double tS = fma(b, S, e) * inv_c;
+  tS = tS > 1.0 ? 1.0 : (tS < 0.0 ? 0.0 : tS);
+  double sT = fma(b, T, -d) * inv_a;
+  sT = sT > 1.0 ? 1.0 : (sT < 0.0 ? 0.0 : sT);
+  double vS[3], vT[3];
+  const double dS = seg(S, tS, vS);
+  const double dT = seg(sT, T, vT);
+  const bool sout = sneg || sbig, tout = tneg || tbig;
+  // 0: interior, 1: s held, 2: t held
+  int pick;
+  if (!sout && !tout) pick = 0;
+  else if (!tout) pick = 1;
+  else if (!sout) pick = 2;
+  else if (sbig) pick = (dT < dS) ? 2 : 1;
+  else pick = (dS < dT) ? 1 : 2;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) dAB[q] = pick == 0 ? vI[q] : (pick == 1 ? vS[q] : vT[q]);
+  st[0] = pick == 0 ? s0 : (pick == 1 ? S : sT);
+  st[1] = pick == 0 ? t0 : (pick == 1 ? tS : T);
+  return pick == 0 ? dI : (pick == 1 ? dS : dT);
+}
+
 // FP32 closest distance^2 of two segments c_A + s lA oA, c_B + t lB oB
 // (s, t in [-1/2, 1/2]); r = c_A - c_B.  Pre-filter only.
 __device__ __forceinline__ float seg_dist_fast(float rx, float ry, float rz, float ax, float ay,
