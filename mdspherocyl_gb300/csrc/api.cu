@@ -176,6 +176,13 @@ void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
     Lo.maxnd = std::max(Lo.maxnd, d.nd);
     if (d.nd > 1) Lo.multi = true;
   }
+  // launch the particle blocks of the largest systems first: their blocks
+  // run longest (real-space partials over more strips), so they must not
+  // be the last wave on the GPU.  Kernels find a block's partial-sum slot
+  // from its particle range (blk_slot), so results do not depend on this
+  // order.
+  std::stable_sort(Lo.blk.begin(), Lo.blk.end(),
+                   [&](const int2& u, const int2& v) { return descs[u.x].n > descs[v.x].n; });
   Lo.ntot = part;
   Lo.ndtot = dip;
   Lo.nktot = (int)Lo.kn.size();
@@ -244,6 +251,8 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   b.kS = A.take<float2>(nk);
   b.kE = A.take<double>(10 * nk);
   b.kG = A.take<double>(6 * (size_t)std::max(Lo.nchunks, 1));
+  b.kGs = A.take<double>(6 * (size_t)std::max(nsys, 1));
+  b.kgcnt = A.take<int>(std::max(nsys, 1));
   b.Fk = A.take<double>(3 * nd);
   b.Gk = A.take<double>(3 * nd);
   b.kin1 = A.take<double>(2 * nb);
@@ -639,6 +648,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   cudaMemsetAsync(b.usave, 0, sizeof(double) * 3 * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.nbc, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.wcnt, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
+  cudaMemsetAsync(b.kgcnt, 0, sizeof(int) * std::max(nsys, 1), B->st);
   cudaMemsetAsync(b.F, 0, sizeof(double) * 3 * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.T, 0, sizeof(double) * 3 * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(B->noise[0], 0, sizeof(double) * kNoiseChunk * nsys * 4, B->st);

@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(kPartBlock) derive_kernel(Batch b) {
     disp = displacement(b, i, r, O);
   }
   const float m = block_max<kPartBlock>(disp, shm);
-  if (threadIdx.x == 0) b.dmax[blockIdx.x] = (double)m;
+  if (threadIdx.x == 0) b.dmax[blk_slot(P, bk)] = (double)m;
 }
 
 // Spherocyl::renorm, v25/classes.cpp:307-325
@@ -227,9 +227,10 @@ __global__ void __launch_bounds__(kPartBlock) integrate_first_kernel(Batch b) {
   block_sum<2, kPartBlock>(kin, sh, tot);
   const float m = block_max<kPartBlock>(disp, shm);
   if (threadIdx.x == 0) {
-    b.kin1[2 * blockIdx.x] = tot[0];
-    b.kin1[2 * blockIdx.x + 1] = tot[1];
-    b.dmax[blockIdx.x] = (double)m;
+    const int lb = blk_slot(P, bk);
+    b.kin1[2 * lb] = tot[0];
+    b.kin1[2 * lb + 1] = tot[1];
+    b.dmax[lb] = (double)m;
   }
 }
 
@@ -417,7 +418,7 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
   block_sum<9, kPartBlock>(acc, sh, tot);
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int c = 0; c < 9; ++c) b.kin2[9 * blockIdx.x + c] = tot[c];
+    for (int c = 0; c < 9; ++c) b.kin2[9 * blk_slot(P, bk) + c] = tot[c];
   }
 }
 
@@ -607,7 +608,7 @@ __global__ void __launch_bounds__(kPartBlock) movep_kernel(Batch b, const double
   block_sum<9, kPartBlock>(acc, sh, tot);
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int c = 0; c < 9; ++c) b.kin2[9 * blockIdx.x + c] = tot[c];
+    for (int c = 0; c < 9; ++c) b.kin2[9 * blk_slot(P, bk) + c] = tot[c];
   }
 }
 

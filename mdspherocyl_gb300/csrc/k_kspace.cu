@@ -127,6 +127,97 @@ __global__ void __launch_bounds__(kKBlock) ksum_kernel(Batch b, const int4* __re
     if (c < nout) out[c] = acc[c];
 }
 
+// Single-dipole systems: as ksum_kernel<1>, with each thread taking two
+// k-vectors (kl and kl + 64 of the block's k tile) in the halves of float2
+// values, so every particle read from shared memory serves two k's and the
+// six multiply-adds of U(k) issue once for both.
+__global__ void __launch_bounds__(kKBlock / 2) ksum1_kernel(Batch b, const int4* __restrict__ kwork) {
+  __shared__ uint32_t sx[kKChunk], sy[kKChunk], sz[kKChunk];
+  __shared__ float4 sm[kKChunk];
+  __shared__ double shG[6 * (kKBlock / 2) / 32];
+  const int4 w = kwork[blockIdx.x];
+  const SysDev& P = b.sys[w.x];
+  const int chunk = w.y;
+  const int t = threadIdx.x;
+  const int kl0 = w.z * kKBlock + t, kl1 = kl0 + kKBlock / 2;
+  const int ND_all = b.ndtot;
+  const int p0 = chunk * kKChunk;
+  const int np = min(kKChunk, P.n - p0);
+  for (int q = t; q < np; q += kKBlock / 2) {
+    const int g = P.dip_off + p0 + q;
+    sx[q] = b.dfx[g];
+    sy[q] = b.dfx[ND_all + g];
+    sz[q] = b.dfx[2 * ND_all + g];
+    sm[q] = make_float4(b.dm[g], b.dm[ND_all + g], b.dm[2 * ND_all + g], 0.f);
+  }
+  __syncthreads();
+  if (w.z == 0) {
+    double gl[6] = {0, 0, 0, 0, 0, 0};
+    for (int q = t; q < np; q += kKBlock / 2) {
+      const double mx = sm[q].x, my = sm[q].y, mz = sm[q].z;
+      gl[0] += mx * mx; gl[1] += mx * my; gl[2] += mx * mz;
+      gl[3] += my * my; gl[4] += my * mz; gl[5] += mz * mz;
+    }
+    double tot[6];
+    block_sum<6, kKBlock / 2>(gl, shG, tot);
+    if (t == 0) {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) b.kG[((long long)P.gch_off + chunk) * 6 + c] = tot[c];
+      // the last chunk of the system to finish adds all chunks in chunk
+      // order (the same bits whichever block it is) and rearms the counter
+      __threadfence();
+      if (atomicAdd(&b.kgcnt[w.x], 1) == P.nkchunk - 1) {
+        __threadfence();
+        double g[6] = {0, 0, 0, 0, 0, 0};
+        for (int ch = 0; ch < P.nkchunk; ++ch)
+#pragma unroll
+          for (int c = 0; c < 6; ++c) g[c] += __ldcg(&b.kG[((long long)P.gch_off + ch) * 6 + c]);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) b.kGs[6 * w.x + c] = g[c];
+        b.kgcnt[w.x] = 0;
+      }
+    }
+  }
+  const bool v0 = kl0 < P.nk, v1 = kl1 < P.nk;
+  if (!v0) return;
+  const int4 n0 = b.kn[P.k_off + kl0];
+  const int4 n1 = v1 ? b.kn[P.k_off + kl1] : n0;
+  float2 acc[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) acc[c] = make_float2(0.f, 0.f);
+#pragma unroll 2
+  for (int p = 0; p < np; ++p) {
+    float c0, s0, c1, s1;
+    phase_exp(sx[p], sy[p], sz[p], n0, c0, s0);
+    phase_exp(sx[p], sy[p], sz[p], n1, c1, s1);
+    const float2 c = make_float2(c0, c1), sn = make_float2(-s0, -s1);
+    // E = exp(-i k.r) = (c, -s); U_c += m_c E
+    const float4 m = sm[p];
+    acc[0] = __ffma2_rn(make_float2(m.x, m.x), c, acc[0]);
+    acc[1] = __ffma2_rn(make_float2(m.x, m.x), sn, acc[1]);
+    acc[2] = __ffma2_rn(make_float2(m.y, m.y), c, acc[2]);
+    acc[3] = __ffma2_rn(make_float2(m.y, m.y), sn, acc[3]);
+    acc[4] = __ffma2_rn(make_float2(m.z, m.z), c, acc[4]);
+    acc[5] = __ffma2_rn(make_float2(m.z, m.z), sn, acc[5]);
+  }
+  float* out0 = b.kpart + ((long long)P.kchunk_off + (long long)chunk * P.nk + kl0) * 10;
+#pragma unroll
+  for (int c = 0; c < 6; ++c) out0[c] = acc[c].x;
+  if (v1) {
+    float* out1 = b.kpart + ((long long)P.kchunk_off + (long long)chunk * P.nk + kl1) * 10;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) out1[c] = acc[c].y;
+  }
+}
+
+template <int ND>
+static void launch_ksum(const Batch& b, const int4* kwork, int nkwork, cudaStream_t s) {
+  if (ND == 1)
+    ksum1_kernel<<<nkwork, kKBlock / 2, 0, s>>>(b, kwork);
+  else
+    ksum_kernel<ND><<<nkwork, kKBlock, 0, s>>>(b, kwork);
+}
+
 // one thread per k over the whole batch: chunk sums in FP64, S(k), and the
 // energy and pressure-tensor terms of that k (v25/functions.cpp:1839-1952)
 template <int ND>
@@ -137,23 +228,27 @@ __global__ void kcombine_kernel(Batch b, const int2* __restrict__ kowner, double
   const SysDev& P = b.sys[ow.x];
   const int kl = ow.y;
   const int nv = ND == 1 ? 6 : 10;
-  double s[10];
+  // chunk sums in float-float (FP32 instructions; ~48 bits), then FP64
+  FF sf[10];
 #pragma unroll
-  for (int c = 0; c < 10; ++c) s[c] = 0.0;
+  for (int c = 0; c < 10; ++c) sf[c].hi = sf[c].lo = 0.f;
   for (int ch = 0; ch < P.nkchunk; ++ch) {
     const float* in = b.kpart + ((long long)P.kchunk_off + (long long)ch * P.nk + kl) * 10;
 #pragma unroll
     for (int c = 0; c < 10; ++c)
-      if (c < nv) s[c] += (double)in[c];
+      if (c < nv) {
+        FF v;
+        v.hi = in[c];
+        v.lo = 0.f;
+        sf[c] = ff_add(sf[c], v);
+      }
   }
+  double s[10];
+#pragma unroll
+  for (int c = 0; c < 10; ++c) s[c] = c < nv ? (double)sf[c].hi + (double)sf[c].lo : 0.0;
   const double kx = b.kvec[3 * k], ky = b.kvec[3 * k + 1], kz = b.kvec[3 * k + 2];
   if (ND == 1) {
-    double G[6] = {0, 0, 0, 0, 0, 0};
-    for (int ch = 0; ch < P.nkchunk; ++ch) {
-      const double* g = b.kG + ((long long)P.gch_off + ch) * 6;
-#pragma unroll
-      for (int c = 0; c < 6; ++c) G[c] += g[c];
-    }
+    const double* G = b.kGs + 6 * ow.x;
     const double gx = G[0] * kx + G[1] * ky + G[2] * kz;
     const double gy = G[1] * kx + G[3] * ky + G[4] * kz;
     const double gz = G[2] * kx + G[4] * ky + G[5] * kz;
@@ -294,22 +389,126 @@ __global__ void __launch_bounds__(kPartBlock) kgather_kernel(Batch b) {
   }
 }
 
+// Single-dipole systems: a thread takes two particles, i and i + 64 of its
+// block, and runs them side by side in the halves of float2 values with
+// the paired FP32 instructions, so every k read from shared memory serves
+// two particles and the force/torque arithmetic issues once for both.
+// With D = conj(val S) - val conj(S_i) (S_i = a e^{-ik.r}, a = m.k) the
+// k-term is Z = e^{-ik.r} D; fF = -a Im Z, fT = -Re Z, written below with
+// Dr = Re(val S) - val a cos, Dn = Im(val S) + val a sin.
+namespace {
+__device__ __forceinline__ float2 pk(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 bc(float a) { return make_float2(a, a); }
+}  // namespace
+
+__global__ void __launch_bounds__(kPartBlock / 2) kgather1_kernel(Batch b) {
+  __shared__ int4 skn[kKBlock];
+  __shared__ float4 skv[kKBlock];
+  __shared__ float2 sks[kKBlock];
+  const int2 bk = b.blk[blockIdx.x];
+  const SysDev& P = b.sys[bk.x];
+  const int t = threadIdx.x;
+  const int i0 = bk.y + t, i1 = i0 + kPartBlock / 2;
+  const int iend = P.part_off + P.n;
+  const bool ok0 = i0 < iend, ok1 = i1 < iend;
+  const int ND_all = b.ndtot;
+  // single dipole: dipole index = dip_off + (particle - part_off)
+  const int g0 = ok0 ? P.dip_off + (i0 - P.part_off) : 0;
+  const int g1 = ok1 ? P.dip_off + (i1 - P.part_off) : 0;
+  const uint32_t ux0 = b.dfx[g0], uy0 = b.dfx[ND_all + g0], uz0 = b.dfx[2 * ND_all + g0];
+  const uint32_t ux1 = b.dfx[g1], uy1 = b.dfx[ND_all + g1], uz1 = b.dfx[2 * ND_all + g1];
+  const float2 mx = pk(ok0 ? b.dm[g0] : 0.f, ok1 ? b.dm[g1] : 0.f);
+  const float2 my = pk(ok0 ? b.dm[ND_all + g0] : 0.f, ok1 ? b.dm[ND_all + g1] : 0.f);
+  const float2 mz = pk(ok0 ? b.dm[2 * ND_all + g0] : 0.f, ok1 ? b.dm[2 * ND_all + g1] : 0.f);
+  // outer accumulators (Kahan-compensated) of the per-tile sums
+  float2 fo[6], fc[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) fo[c] = fc[c] = bc(0.f);
+
+  for (int k0 = 0; k0 < P.nk; k0 += kKBlock) {
+    const int nk = min(kKBlock, P.nk - k0);
+    __syncthreads();
+    for (int q = t; q < nk; q += kPartBlock / 2) {
+      skn[q] = b.kn[P.k_off + k0 + q];
+      skv[q] = b.kv[P.k_off + k0 + q];
+      sks[q] = b.kS[P.k_off + k0 + q];
+    }
+    __syncthreads();
+    float2 ft[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) ft[c] = bc(0.f);
+#pragma unroll 2
+    for (int q = 0; q < nk; ++q) {
+      const int4 n = skn[q];
+      const float4 kv = skv[q];  // kx, ky, kz, val
+      const float2 vS = sks[q];  // val * S(k)
+      float c0, s0, c1, s1;
+      phase_exp(ux0, uy0, uz0, n, c0, s0);
+      phase_exp(ux1, uy1, uz1, n, c1, s1);
+      const float2 c = pk(c0, c1), sn = pk(s0, s1);
+      const float2 a = __ffma2_rn(mz, bc(kv.z), __ffma2_rn(my, bc(kv.y), __fmul2_rn(mx, bc(kv.x))));
+      const float2 va = __fmul2_rn(bc(kv.w), a);
+      const float2 Dr = __ffma2_rn(pk(-va.x, -va.y), c, bc(vS.x));
+      const float2 Dn = __ffma2_rn(va, sn, bc(vS.y));
+      const float2 fF = __fmul2_rn(a, __ffma2_rn(c, Dn, __fmul2_rn(sn, Dr)));
+      const float2 fT = __ffma2_rn(sn, Dn, __fmul2_rn(pk(-c.x, -c.y), Dr));
+      ft[0] = __ffma2_rn(fF, bc(kv.x), ft[0]);
+      ft[1] = __ffma2_rn(fF, bc(kv.y), ft[1]);
+      ft[2] = __ffma2_rn(fF, bc(kv.z), ft[2]);
+      ft[3] = __ffma2_rn(fT, bc(kv.x), ft[3]);
+      ft[4] = __ffma2_rn(fT, bc(kv.y), ft[4]);
+      ft[5] = __ffma2_rn(fT, bc(kv.z), ft[5]);
+    }
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      const float2 y = __fadd2_rn(ft[c], pk(-fc[c].x, -fc[c].y));
+      const float2 tt = __fadd2_rn(fo[c], y);
+      fc[c] = __fadd2_rn(__fadd2_rn(tt, pk(-fo[c].x, -fo[c].y)), pk(-y.x, -y.y));
+      fo[c] = tt;
+    }
+  }
+  if (ok0) {
+    b.Fk[3 * g0 + 0] = (double)fo[0].x - (double)fc[0].x;
+    b.Fk[3 * g0 + 1] = (double)fo[1].x - (double)fc[1].x;
+    b.Fk[3 * g0 + 2] = (double)fo[2].x - (double)fc[2].x;
+    b.Gk[3 * g0 + 0] = (double)fo[3].x - (double)fc[3].x;
+    b.Gk[3 * g0 + 1] = (double)fo[4].x - (double)fc[4].x;
+    b.Gk[3 * g0 + 2] = (double)fo[5].x - (double)fc[5].x;
+  }
+  if (ok1) {
+    b.Fk[3 * g1 + 0] = (double)fo[0].y - (double)fc[0].y;
+    b.Fk[3 * g1 + 1] = (double)fo[1].y - (double)fc[1].y;
+    b.Fk[3 * g1 + 2] = (double)fo[2].y - (double)fc[2].y;
+    b.Gk[3 * g1 + 0] = (double)fo[3].y - (double)fc[3].y;
+    b.Gk[3 * g1 + 1] = (double)fo[4].y - (double)fc[4].y;
+    b.Gk[3 * g1 + 2] = (double)fo[5].y - (double)fc[5].y;
+  }
+}
+
+template <int ND>
+static void launch_kgather(const Batch& b, cudaStream_t s) {
+  if (ND == 1)
+    kgather1_kernel<<<b.nblk, kPartBlock / 2, 0, s>>>(b);
+  else
+    kgather_kernel<ND><<<b.nblk, kPartBlock, 0, s>>>(b);
+}
+
 template <int ND>
 static void launch_kspace_nd(const Batch& b, const int4* kwork, int nkwork, const int2* kowner,
                              double* kE, cudaStream_t s) {
   if (b.nktot == 0) return;
-  if (nkwork > 0) ksum_kernel<ND><<<nkwork, kKBlock, 0, s>>>(b, kwork);
+  if (nkwork > 0) launch_ksum<ND>(b, kwork, nkwork, s);
   kcombine_kernel<ND><<<cdiv(b.nktot, 128), 128, 0, s>>>(b, kowner, kE);
-  kgather_kernel<ND><<<b.nblk, kPartBlock, 0, s>>>(b);
+  launch_kgather<ND>(b, s);
 }
 
 template <int ND>
 static void kspace_part_nd(const Batch& b, const int4* kwork, int nkwork, const int2* kowner,
                            double* kE, int part, cudaStream_t s) {
   if (b.nktot == 0) return;
-  if (part == 0 && nkwork > 0) ksum_kernel<ND><<<nkwork, kKBlock, 0, s>>>(b, kwork);
+  if (part == 0 && nkwork > 0) launch_ksum<ND>(b, kwork, nkwork, s);
   if (part == 1) kcombine_kernel<ND><<<cdiv(b.nktot, 128), 128, 0, s>>>(b, kowner, kE);
-  if (part == 2) kgather_kernel<ND><<<b.nblk, kPartBlock, 0, s>>>(b);
+  if (part == 2) launch_kgather<ND>(b, s);
 }
 
 // one of the three k-space kernels (0: ksum, 1: kcombine, 2: kgather)

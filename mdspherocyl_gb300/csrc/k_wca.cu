@@ -37,7 +37,7 @@ __global__ void __launch_bounds__(kPartBlock) list_build_kernel(Batch b, int for
     for (int k = 0; k < P.nblk; ++k) m = fmax(m, b.dmax[P.blk_off + k]);
     need = 2.0 * m > P.skin;
   }
-  if (blockIdx.x == P.blk_off) S.rebuild = need ? 1 : 0;
+  if (blk_slot(P, bk) == P.blk_off) S.rebuild = need ? 1 : 0;
   if (!need) return;
   const int i = bk.y + threadIdx.x;
   const bool ok = i < P.part_off + P.n;
@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(kPartBlock) wca_kernel(Batch b) {
     }
   }
   if (err) atomicOr(&b.st[s].status, err);
-  if (tid < 11) b.wcaE[11 * blockIdx.x + tid] = esum;
+  if (tid < 11) b.wcaE[11 * blk_slot(P, bk) + tid] = esum;
 }
 
 // ---- clusters (v25/functions.cpp:2987-3016,3282-3324) ----------------

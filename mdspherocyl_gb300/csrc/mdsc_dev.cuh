@@ -150,6 +150,8 @@ struct Batch {
   float2* kS;    // val * S(k) per k, FP32 for the gather
   double* kE;    // 10 per k: energy and pressure-tensor terms
   double* kG;    // 6 per particle chunk: sum of m m^T (one dipole per particle)
+  double* kGs;   // 6 per system: the chunk sums added in chunk order
+  int* kgcnt;    // per system: chunks done this step (the last one adds them)
   double* Fk;    // 3 ndip
   double* Gk;    // 3 ndip  (torque = m x Gk)
   // integrator partials, per block
@@ -181,6 +183,13 @@ __device__ inline uint32_t to_fix(double x, double invL) {
 }
 
 // minimum-image difference of two fixed-point coordinates, in length units
+// slot of a particle block in the per-block partial arrays: blocks are
+// launched largest system first, but each system's partials sit in order
+// at blk_off .. blk_off + nblk - 1
+__device__ __forceinline__ int blk_slot(const SysDev& P, int2 bk) {
+  return P.blk_off + (bk.y - P.part_off) / kPartBlock;
+}
+
 __device__ inline float fix_diff(uint32_t a, uint32_t b, float scale) {
   return (float)(int32_t)(a - b) * scale;
 }
