@@ -149,6 +149,7 @@ void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
     for (int a = 0; a < 3; ++a) {
       P.L[a] = d.box[a];
       P.invL[a] = 1.0 / d.box[a];
+      P.invL32[a] = P.invL[a] * 4294967296.0;
       P.Lfix[a] = (float)(d.box[a] / 4294967296.0);
       P.Lf[a] = (float)d.box[a];
       P.B[a] = d.B[a];
@@ -253,16 +254,16 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   b.kG = A.take<double>(6 * (size_t)std::max(Lo.nchunks, 1));
   b.kGs = A.take<double>(6 * (size_t)std::max(nsys, 1));
   b.kgcnt = A.take<int>(std::max(nsys, 1));
-  b.Fk = A.take<double>(3 * nd);
-  b.Gk = A.take<double>(3 * nd);
+  b.Fk = A.take<float2>(3 * nd);
+  b.Tk = A.take<float2>(3 * nd);
   b.kin1 = A.take<double>(2 * nb);
   b.kin2 = A.take<double>(9 * nb);
   b.dmax = A.take<double>(nb);
   b.blk = A.take<int2>(nb);
   b.nb = A.take<int>(n * kMaxNb);
   b.nbc = A.take<int>(n);
-  b.rsave = A.take<double>(3 * n);
-  b.usave = A.take<double>(3 * n);
+  b.fsave = A.take<uint32_t>(3 * n);
+  b.usave = A.take<float>(3 * n);
   b.comp = A.take<int>(n);
   b.eflag = A.take<unsigned char>(n * kMaxNb);
   b.flag = A.take<int>(1);
@@ -644,8 +645,8 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   }
   up(b.st, st.data(), sizeof(SysState) * nsys);
   cudaMemsetAsync(b.obs, 0, sizeof(SysObs) * nsys, B->st);
-  cudaMemsetAsync(b.rsave, 0, sizeof(double) * 3 * std::max(lo.ntot, 1), B->st);
-  cudaMemsetAsync(b.usave, 0, sizeof(double) * 3 * std::max(lo.ntot, 1), B->st);
+  cudaMemsetAsync(b.fsave, 0, sizeof(uint32_t) * 3 * std::max(lo.ntot, 1), B->st);
+  cudaMemsetAsync(b.usave, 0, sizeof(float) * 3 * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.nbc, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.wcnt, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.kgcnt, 0, sizeof(int) * std::max(nsys, 1), B->st);

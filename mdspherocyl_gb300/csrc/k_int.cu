@@ -20,12 +20,11 @@ namespace mdsc {
 // working copies: fixed-point positions, FP32 axes and dipole vectors
 // ---------------------------------------------------------------------
 __device__ __forceinline__ void derive_particle(const Batch& b, const SysDev& P, int i,
-                                                const double* r, const double* O) {
+                                                const double* r, const double* O, uint32_t* u) {
   const int N = b.ntot, ND = b.ndtot;
-  uint32_t u[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    u[a] = to_fix(r[a], P.invL[a]);
+    u[a] = to_fix(r[a], P.invL32[a]);
     b.pfx[a * N + i] = u[a];
   }
   b.pax[i] = make_float4((float)O[6], (float)O[7], (float)O[8], (float)b.len[i]);
@@ -43,7 +42,7 @@ __device__ __forceinline__ void derive_particle(const Batch& b, const SysDev& P,
       for (int a = 0; a < 3; ++a) b.dfx[a * ND + g] = u[a];
     } else {
 #pragma unroll
-      for (int a = 0; a < 3; ++a) b.dfx[a * ND + g] = to_fix(r[a] + pc * O[6 + a], P.invL[a]);
+      for (int a = 0; a < 3; ++a) b.dfx[a * ND + g] = to_fix(r[a] + pc * O[6 + a], P.invL32[a]);
     }
     // lab direction O^T o_body (Spherocyl::set_dip, v25/classes.cpp:166-170), times the moment
     const float ox = (float)b.dob[3 * g], oy = (float)b.dob[3 * g + 1], oz = (float)b.dob[3 * g + 2];
@@ -53,12 +52,16 @@ __device__ __forceinline__ void derive_particle(const Batch& b, const SysDev& P,
   }
 }
 
-__device__ __forceinline__ float displacement(const Batch& b, int i, const double* r, const double* O) {
+// how far the rod's ends may have moved since the last list build: the
+// centre's move from the fixed-point coordinates (exact minimum image, no
+// FP64 arithmetic) plus half the length times the axis change
+__device__ __forceinline__ float displacement(const Batch& b, const SysDev& P, int i, const uint32_t* u,
+                                              const double* O) {
   float dr2 = 0.f, du2 = 0.f;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    const float d = (float)(r[a] - b.rsave[3 * i + a]);
-    const float e = (float)(O[6 + a] - b.usave[3 * i + a]);
+    const float d = fix_diff(u[a], b.fsave[3 * i + a], P.Lfix[a]);
+    const float e = (float)O[6 + a] - b.usave[3 * i + a];
     dr2 += d * d;
     du2 += e * e;
   }
@@ -77,8 +80,9 @@ __global__ void __launch_bounds__(kPartBlock) derive_kernel(Batch b) {
     for (int a = 0; a < 3; ++a) r[a] = b.r[3 * i + a];
 #pragma unroll
     for (int k = 0; k < 9; ++k) O[k] = b.O[9 * i + k];
-    derive_particle(b, P, i, r, O);
-    disp = displacement(b, i, r, O);
+    uint32_t u[3];
+    derive_particle(b, P, i, r, O, u);
+    disp = displacement(b, P, i, u, O);
   }
   const float m = block_max<kPartBlock>(disp, shm);
   if (threadIdx.x == 0) b.dmax[blk_slot(P, bk)] = (double)m;
@@ -129,10 +133,12 @@ __device__ __forceinline__ void move_x(const Batch& b, int i, double dt, double*
   for (int a = 0; a < 3; ++a) r[a] += dt * p[a] * im;
   const float iI0 = (float)b.invI[3 * i], iI1 = (float)b.invI[3 * i + 1], iI2 = (float)b.invI[3 * i + 2];
   const float h = (float)(0.5 * dt), fdt = (float)dt;
-  float lb[3];
+  float lb[3], Of[9];
   const float lf[3] = {(float)l[0], (float)l[1], (float)l[2]};
 #pragma unroll
-  for (int a = 0; a < 3; ++a) lb[a] = (float)O[3 * a] * lf[0] + (float)O[3 * a + 1] * lf[1] + (float)O[3 * a + 2] * lf[2];
+  for (int k = 0; k < 9; ++k) Of[k] = (float)O[k];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) lb[a] = Of[3 * a] * lf[0] + Of[3 * a + 1] * lf[1] + Of[3 * a + 2] * lf[2];
   float D[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) D[k] = 0.f;
@@ -141,15 +147,15 @@ __device__ __forceinline__ void move_x(const Batch& b, int i, double dt, double*
   plane_rot(-lb[2] * fdt * iI2, 0, 1, lb, D); // Rz
   plane_rot(-lb[1] * h * iI1, 2, 0, lb, D);   // Ry
   plane_rot(-lb[0] * h * iI0, 1, 2, lb, D);   // Rx
-  double On[9];
+  // O += D O: the increment (|D| ~ 1e-3) in FP32, ~1e-10 absolute like D
+  // itself, added to the FP64 orientation
+  float inc[9];
 #pragma unroll
   for (int a = 0; a < 3; ++a)
 #pragma unroll
-    for (int c = 0; c < 3; ++c)
-      On[3 * a + c] = O[3 * a + c] + ((double)D[3 * a] * O[c] + (double)D[3 * a + 1] * O[3 + c] +
-                                      (double)D[3 * a + 2] * O[6 + c]);
+    for (int c = 0; c < 3; ++c) inc[3 * a + c] = D[3 * a] * Of[c] + D[3 * a + 1] * Of[3 + c] + D[3 * a + 2] * Of[6 + c];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) O[k] = On[k];
+  for (int k = 0; k < 9; ++k) O[k] += (double)inc[k];
 }
 
 // K_r = l^T (O^T I^-1 O) l = sum_a (O l)_a^2 / I_a  (v25/functions.cpp:2123-2148)
@@ -219,9 +225,9 @@ __global__ void __launch_bounds__(kPartBlock) integrate_first_kernel(Batch b) {
     }
 #pragma unroll
     for (int k = 0; k < 9; ++k) b.O[9 * i + k] = O[k];
-    derive_particle(b, P, i, r, O);
-    // how far the rod's ends may have moved since the last list build
-    disp = displacement(b, i, r, O);
+    uint32_t u[3];
+    derive_particle(b, P, i, r, O, u);
+    disp = displacement(b, P, i, u, O);
   }
   double tot[2];
   block_sum<2, kPartBlock>(kin, sh, tot);
@@ -271,9 +277,9 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
     sx[1] = xi2[1];
   }
   __syncthreads();
-  double acc[9];
+  FF acc[9];
 #pragma unroll
-  for (int c = 0; c < 9; ++c) acc[c] = 0.0;
+  for (int c = 0; c < 9; ++c) acc[c].hi = acc[c].lo = 0.f;
   if (ok) {
     double F[3], T[3];
 #pragma unroll
@@ -312,55 +318,54 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
     for (int a = 0; a < 3; ++a) ax[a] = b.O[9 * i + 6 + a];
     const int nd = P.nd;
     const int loc0 = (i - P.part_off) * nd;
+    // the field term needs the FP64 moment; without a field it adds nothing
+    const bool ext = (mode & kMaskExt) && (P.B[0] != 0.0 || P.B[1] != 0.0 || P.B[2] != 0.0);
     double uext = 0.0;
     for (int w = 0; w < nd; ++w) {
       const int loc = loc0 + w;
       const int g = P.dip_off + loc;
-      double f[3] = {0.0, 0.0, 0.0}, t[3] = {0.0, 0.0, 0.0};
+      // real- and reciprocal-space force and torque of this dipole in
+      // float-float (FP32 instructions), one conversion to FP64 at the end
+      FF acc6[6];
+#pragma unroll
+      for (int c = 0; c < 6; ++c) acc6[c].hi = acc6[c].lo = 0.f;
       if (mode & kMaskReal) {
-        // sum of the tile partials of this dipole over all partner strips,
-        // float-float so that hundreds of strips add without loss
+        // sum of the tile partials of this dipole over all partner strips
         const int X = loc / kTile, lx = loc % kTile, ns = P.nstrip;
         const float* base = b.rpart + P.pp_off + (long long)X * ns * 6 * kTile + lx;
-        FF acc6[6];
-#pragma unroll
-        for (int c = 0; c < 6; ++c) acc6[c].hi = acc6[c].lo = 0.f;
 #pragma unroll 4
         for (int Y = 0; Y < ns; ++Y) {
 #pragma unroll
-          for (int c = 0; c < 6; ++c) {
-            FF v;
-            v.hi = base[((long long)Y * 6 + c) * kTile];
-            v.lo = 0.f;
-            acc6[c] = ff_add(acc6[c], v);
-          }
+          for (int c = 0; c < 6; ++c) acc6[c] = ff_add(acc6[c], ff_of(base[((long long)Y * 6 + c) * kTile]));
         }
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          f[c] += (double)acc6[c].hi + (double)acc6[c].lo;
-          t[c] += (double)acc6[3 + c].hi + (double)acc6[3 + c].lo;
-        }
-      }
-      // dipole vector mu O^T o_body in FP64 (the FP32 copy is 6e-8 off)
-      double mx, my, mz;
-      {
-        const double* O = b.O + 9 * i;
-        const double ox = b.dob[3 * g], oy = b.dob[3 * g + 1], oz = b.dob[3 * g + 2], mu = b.dmu[g];
-        mx = mu * (O[0] * ox + O[3] * oy + O[6] * oz);
-        my = mu * (O[1] * ox + O[4] * oy + O[7] * oz);
-        mz = mu * (O[2] * ox + O[5] * oy + O[8] * oz);
       }
       if (mode & kMaskK) {
-        const double gx = b.Gk[3 * g], gy = b.Gk[3 * g + 1], gz = b.Gk[3 * g + 2];
-        f[0] += b.Fk[3 * g];
-        f[1] += b.Fk[3 * g + 1];
-        f[2] += b.Fk[3 * g + 2];
-        t[0] += my * gz - mz * gy;
-        t[1] += mz * gx - mx * gz;
-        t[2] += mx * gy - my * gx;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const float2 fk = b.Fk[3 * g + c], tk = b.Tk[3 * g + c];
+          FF v;
+          v.hi = fk.x;
+          v.lo = fk.y;
+          acc6[c] = ff_add(acc6[c], v);
+          v.hi = tk.x;
+          v.lo = tk.y;
+          acc6[3 + c] = ff_add(acc6[3 + c], v);
+        }
       }
-      if (mode & kMaskExt) {
-        // ext_field: torque mu o x B, energy -mu o.B (v25/functions.cpp:2014-2020)
+      double f[3], t[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        f[c] = (double)acc6[c].hi + (double)acc6[c].lo;
+        t[c] = (double)acc6[3 + c].hi + (double)acc6[3 + c].lo;
+      }
+      if (ext) {
+        // ext_field: torque mu o x B, energy -mu o.B (v25/functions.cpp:2014-2020),
+        // with the dipole vector mu O^T o_body in FP64
+        const double* O = b.O + 9 * i;
+        const double ox = b.dob[3 * g], oy = b.dob[3 * g + 1], oz = b.dob[3 * g + 2], mu = b.dmu[g];
+        const double mx = mu * (O[0] * ox + O[3] * oy + O[6] * oz);
+        const double my = mu * (O[1] * ox + O[4] * oy + O[7] * oz);
+        const double mz = mu * (O[2] * ox + O[5] * oy + O[8] * oz);
         t[0] += my * P.B[2] - mz * P.B[1];
         t[1] += mz * P.B[0] - mx * P.B[2];
         t[2] += mx * P.B[1] - my * P.B[0];
@@ -380,7 +385,7 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
         T[a] += t[a];
       }
     }
-    acc[8] = uext;
+    acc[8] = ff_from(uext);
     double p[3], l[3];
     if (mode & kFlagMoveP) {
       // moveP last half (v25/functions.cpp:2150-2173)
@@ -399,14 +404,17 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
 #pragma unroll
       for (int k = 0; k < 9; ++k) O[k] = b.O[9 * i + k];
       const double im = b.invm[i];
-      acc[0] = psq * im;
-      acc[1] = rot_kin(b, i, O, l);
-      acc[2] = p[0] * p[0] * im;
-      acc[3] = p[0] * p[1] * im;
-      acc[4] = p[0] * p[2] * im;
-      acc[5] = p[1] * p[1] * im;
-      acc[6] = p[1] * p[2] * im;
-      acc[7] = p[2] * p[2] * im;
+      acc[0] = ff_from(psq * im);
+      acc[1] = ff_from(rot_kin(b, i, O, l));
+      // kinetic pressure tensor p_a p_b / m: FP32 products, float-float sums
+      const float pf[3] = {(float)p[0], (float)p[1], (float)p[2]};
+      const float imf = (float)im;
+      acc[2] = ff_of(pf[0] * pf[0] * imf);
+      acc[3] = ff_of(pf[0] * pf[1] * imf);
+      acc[4] = ff_of(pf[0] * pf[2] * imf);
+      acc[5] = ff_of(pf[1] * pf[1] * imf);
+      acc[6] = ff_of(pf[1] * pf[2] * imf);
+      acc[7] = ff_of(pf[2] * pf[2] * imf);
     }
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -542,7 +550,8 @@ __global__ void __launch_bounds__(kPartBlock) movex_kernel(Batch b) {
   for (int a = 0; a < 3; ++a) b.r[3 * i + a] = r[a];
 #pragma unroll
   for (int k = 0; k < 9; ++k) b.O[9 * i + k] = O[k];
-  derive_particle(b, P, i, r, O);
+  uint32_t u[3];
+  derive_particle(b, P, i, r, O, u);
 }
 
 __global__ void __launch_bounds__(kPartBlock) renorm_kernel(Batch b) {

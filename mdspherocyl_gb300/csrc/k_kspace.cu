@@ -282,6 +282,20 @@ __global__ void kcombine_kernel(Batch b, const int2* __restrict__ kowner, double
   }
 }
 
+// k-space results of one dipole from its Kahan sums (sum = fo - fc): the
+// force as float-float, and the torque m x G (G the second triple) with the
+// FP32 moment -- as accurate as the FP32 sums it is built from
+__device__ __forceinline__ void store_kout(const Batch& b, int g, const float* fo, const float* fc,
+                                           float mx, float my, float mz) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) b.Fk[3 * g + c] = make_float2(fo[c], -fc[c]);
+  const float gx = fo[3], gy = fo[4], gz = fo[5];
+  const float lx = -fc[3], ly = -fc[4], lz = -fc[5];
+  b.Tk[3 * g + 0] = make_float2(my * gz - mz * gy, my * lz - mz * ly);
+  b.Tk[3 * g + 1] = make_float2(mz * gx - mx * gz, mz * lx - mx * lz);
+  b.Tk[3 * g + 2] = make_float2(mx * gy - my * gx, mx * ly - my * lx);
+}
+
 // per particle over all k of its system: force and torque (:1853-1925)
 template <int ND>
 __global__ void __launch_bounds__(kPartBlock) kgather_kernel(Batch b) {
@@ -376,17 +390,8 @@ __global__ void __launch_bounds__(kPartBlock) kgather_kernel(Batch b) {
   }
   if (!ok) return;
 #pragma unroll
-  for (int d = 0; d < ND; ++d) {
-    if (d < nd) {
-      const int g = gd0 + d;
-      b.Fk[3 * g + 0] = (double)fo[d][0] - (double)fc[d][0];
-      b.Fk[3 * g + 1] = (double)fo[d][1] - (double)fc[d][1];
-      b.Fk[3 * g + 2] = (double)fo[d][2] - (double)fc[d][2];
-      b.Gk[3 * g + 0] = (double)fo[d][3] - (double)fc[d][3];
-      b.Gk[3 * g + 1] = (double)fo[d][4] - (double)fc[d][4];
-      b.Gk[3 * g + 2] = (double)fo[d][5] - (double)fc[d][5];
-    }
-  }
+  for (int d = 0; d < ND; ++d)
+    if (d < nd) store_kout(b, gd0 + d, fo[d], fc[d], mx[d], my[d], mz[d]);
 }
 
 // Single-dipole systems: a thread takes two particles, i and i + 64 of its
@@ -467,21 +472,17 @@ __global__ void __launch_bounds__(kPartBlock / 2) kgather1_kernel(Batch b) {
       fo[c] = tt;
     }
   }
-  if (ok0) {
-    b.Fk[3 * g0 + 0] = (double)fo[0].x - (double)fc[0].x;
-    b.Fk[3 * g0 + 1] = (double)fo[1].x - (double)fc[1].x;
-    b.Fk[3 * g0 + 2] = (double)fo[2].x - (double)fc[2].x;
-    b.Gk[3 * g0 + 0] = (double)fo[3].x - (double)fc[3].x;
-    b.Gk[3 * g0 + 1] = (double)fo[4].x - (double)fc[4].x;
-    b.Gk[3 * g0 + 2] = (double)fo[5].x - (double)fc[5].x;
-  }
-  if (ok1) {
-    b.Fk[3 * g1 + 0] = (double)fo[0].y - (double)fc[0].y;
-    b.Fk[3 * g1 + 1] = (double)fo[1].y - (double)fc[1].y;
-    b.Fk[3 * g1 + 2] = (double)fo[2].y - (double)fc[2].y;
-    b.Gk[3 * g1 + 0] = (double)fo[3].y - (double)fc[3].y;
-    b.Gk[3 * g1 + 1] = (double)fo[4].y - (double)fc[4].y;
-    b.Gk[3 * g1 + 2] = (double)fo[5].y - (double)fc[5].y;
+  if (ok0 || ok1) {
+    float a0[6], c0[6], a1[6], c1[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      a0[c] = fo[c].x;
+      c0[c] = fc[c].x;
+      a1[c] = fo[c].y;
+      c1[c] = fc[c].y;
+    }
+    if (ok0) store_kout(b, g0, a0, c0, mx.x, my.x, mz.x);
+    if (ok1) store_kout(b, g1, a1, c1, mx.y, my.y, mz.y);
   }
 }
 

@@ -88,8 +88,8 @@ __global__ void __launch_bounds__(kPartBlock) list_build_kernel(Batch b, int for
   b.nbc[i] = min(cnt, kMaxNb);
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    b.rsave[3 * i + a] = b.r[3 * i + a];
-    b.usave[3 * i + a] = b.O[9 * i + 6 + a];
+    b.fsave[3 * i + a] = b.pfx[a * N + i];
+    b.usave[3 * i + a] = a == 0 ? ai.x : (a == 1 ? ai.y : ai.z);
   }
 }
 

@@ -51,6 +51,7 @@ struct SysDev {
   int cl_fr;
   double L[3];
   double invL[3];
+  double invL32[3];  // 2^32 / L: coordinate to fixed-point box fraction
   double V;
   double ex1;      // exp(-gamma dt / 2)            (moveTher, v25/functions.cpp:2199)
   double cnoise;   // sqrt(2 T gamma dt / Q)        (v25/functions.cpp:2200)
@@ -152,8 +153,8 @@ struct Batch {
   double* kG;    // 6 per particle chunk: sum of m m^T (one dipole per particle)
   double* kGs;   // 6 per system: the chunk sums added in chunk order
   int* kgcnt;    // per system: chunks done this step (the last one adds them)
-  double* Fk;    // 3 ndip
-  double* Gk;    // 3 ndip  (torque = m x Gk)
+  float2* Fk;    // 3 ndip: k-space force on each dipole, float-float (hi, lo)
+  float2* Tk;    // 3 ndip: k-space torque m x G, float-float
   // integrator partials, per block
   double* kin1;  // 2 per block
   double* kin2;  // 9 per block: K_t, K_r, PTkin xx xy xz yy yz zz, U_ext
@@ -162,8 +163,8 @@ struct Batch {
   // neighbour list
   int* nb;       // n * kMaxNb
   int* nbc;      // n
-  double* rsave; // 3n positions at the last build
-  double* usave; // 3n axes at the last build
+  uint32_t* fsave; // 3n fixed-point positions at the last build
+  float* usave;     // 3n axes at the last build
   // clusters
   int* comp;     // n component representative
   unsigned char* eflag;  // n * kMaxNb: list entry is a cluster bond
@@ -175,14 +176,13 @@ struct Batch {
 // ---- small helpers ----------------------------------------------------
 __host__ __device__ inline int cdiv(int a, int b) { return (a + b - 1) / b; }
 
-// fixed-point image of a coordinate: fraction of the box in [0, 2^32)
-__device__ inline uint32_t to_fix(double x, double invL) {
-  double t = x * invL;
-  t -= floor(t);
-  return (uint32_t)(unsigned long long)(t * 4294967296.0);
+// fixed-point image of a coordinate: fraction of the box in [0, 2^32),
+// floor(x 2^32 / L) modulo 2^32 (invL32 = 2^32 / L; the product is the
+// exactly scaled x / L, so this equals frac(x / L) 2^32 truncated)
+__device__ inline uint32_t to_fix(double x, double invL32) {
+  return (uint32_t)(unsigned long long)__double2ll_rd(x * invL32);
 }
 
-// minimum-image difference of two fixed-point coordinates, in length units
 // slot of a particle block in the per-block partial arrays: blocks are
 // launched largest system first, but each system's partials sit in order
 // at blk_off .. blk_off + nblk - 1
@@ -190,6 +190,7 @@ __device__ __forceinline__ int blk_slot(const SysDev& P, int2 bk) {
   return P.blk_off + (bk.y - P.part_off) / kPartBlock;
 }
 
+// minimum-image difference of two fixed-point coordinates, in length units
 __device__ inline float fix_diff(uint32_t a, uint32_t b, float scale) {
   return (float)(int32_t)(a - b) * scale;
 }

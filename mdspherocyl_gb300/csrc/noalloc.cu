@@ -79,6 +79,7 @@ __global__ void noalloc_prep_kernel(unsigned char* scr, int ndip, const double* 
     for (int a = 0; a < 3; ++a) {
       d.L[a] = L[a];
       d.invL[a] = 1.0 / L[a];
+      d.invL32[a] = d.invL[a] * 4294967296.0;
       d.Lfix[a] = (float)(L[a] / 4294967296.0);
       d.Lf[a] = (float)L[a];
     }
@@ -104,7 +105,7 @@ __global__ void noalloc_prep_kernel(unsigned char* scr, int ndip, const double* 
   }
   if (t < ndip) {
     for (int a = 0; a < 3; ++a) {
-      fx[a * ndip + t] = to_fix(pos[3 * t + a], 1.0 / L[a]);
+      fx[a * ndip + t] = to_fix(pos[3 * t + a], 4294967296.0 / L[a]);
       m[a * ndip + t] = (float)mom[3 * t + a];
     }
     own[t] = t;

@@ -63,6 +63,35 @@ __device__ __forceinline__ void block_sum(const double (&v)[NV], double* sh, dou
   __syncthreads();
 }
 
+// Same, for values already in float-float form (an FP32 value x enters as
+// {x, 0} and costs no FP64 instruction).
+template <int NV, int NT>
+__device__ __forceinline__ void block_sum(const FF (&v)[NV], double* sh, double* out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < NV; ++c) {
+    FF w = ff_warp_sum(v[c]);
+    if (lane == 0) sh[c * (NT / 32) + warp] = (double)w.hi + (double)w.lo;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+      double s = 0.0;
+      for (int k = 0; k < NT / 32; ++k) s += sh[c * (NT / 32) + k];
+      out[c] = s;
+    }
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ FF ff_of(float x) {
+  FF r;
+  r.hi = x;
+  r.lo = 0.f;
+  return r;
+}
+
 // Same, for a per-block maximum of non-negative values.
 template <int NT>
 __device__ __forceinline__ float block_max(float v, float* sh) {
