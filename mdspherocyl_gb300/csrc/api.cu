@@ -376,7 +376,7 @@ mdsc_status capture_step(mdsc_batch* B, int which) {
   launches += 2;
   cudaError_t e = cudaStreamEndCapture(B->st, &g);
   if (e != cudaSuccess) return fail(B, MDSC_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-  e = cudaGraphInstantiate(&B->graph[which], g, 0);
+  e = cudaGraphInstantiate(&B->graph[which], g, cudaGraphInstantiateFlagUseNodePriority);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return fail(B, MDSC_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
   B->launches = launches;
@@ -607,9 +607,16 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   b.ntiles = (int)lo.tiles.size();
   b.nblk = (int)lo.blk.size();
   b.noise = B->noise[0];
-  if (cudaStreamCreateWithFlags(&B->st, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&B->s2, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&B->s3, cudaStreamNonBlocking) != cudaSuccess ||
+  // The step graph forks the real-space tiles (stream s2) from the WCA and
+  // k-space chains (st, s3).  The tiles keep the FP32 pipe busy while the
+  // others wait on FP64, memory and special functions, so the others run at
+  // the higher priority: their blocks are placed first and the tiles fill
+  // the SMs around them.
+  int prio_lo = 0, prio_hi = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+  if (cudaStreamCreateWithPriority(&B->st, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&B->s2, cudaStreamNonBlocking, prio_lo) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&B->s3, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
       cudaEventCreateWithFlags(&B->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&B->ev_j2, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&B->ev_j3, cudaEventDisableTiming) != cudaSuccess ||

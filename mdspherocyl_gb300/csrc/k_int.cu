@@ -431,100 +431,96 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
 }
 
 // ---------------------------------------------------------------------
-// per-system sums (block per system) and the thermostat's last update
-// ---------------------------------------------------------------------
-__global__ void __launch_bounds__(128) reduce_obs_kernel(Batch b, int mode) {
-  __shared__ double sh[10 * 4];
-  const int s = blockIdx.x;
+// per-system sums and the thermostat's last update.  Four blocks per
+// system, one per group of sums (real-space tiles, k-vectors, WCA blocks,
+// kinetic terms), each in float-float with a fixed order; the kinetic block
+// also closes the step's thermostat and bookkeeping.
+constexpr int kRedThreads = 128;
+__global__ void __launch_bounds__(kRedThreads) reduce_obs_kernel(Batch b, int mode) {
+  __shared__ double sh[11 * kRedThreads / 32];
+  const int s = blockIdx.x >> 2, grp = blockIdx.x & 3;
   const SysDev& P = b.sys[s];
   SysState& S = b.st[s];
   SysObs& ob = b.obs[s];
-  double v[10], out[10];
-  // real-space tiles: U, PT
+  FF v[11];
 #pragma unroll
-  for (int c = 0; c < 10; ++c) v[c] = 0.0;
-  for (int t = threadIdx.x; t < P.ntile; t += 128) {
-    const float* e = b.tileE + (long long)(P.tile_off + t) * 10;
+  for (int c = 0; c < 11; ++c) v[c].hi = v[c].lo = 0.f;
+  double out[11];
+  if (grp == 0) {
+    // real-space tiles: U, PT (FP32 per tile)
+    for (int t = threadIdx.x; t < P.ntile; t += kRedThreads) {
+      const float* e = b.tileE + (long long)(P.tile_off + t) * 10;
 #pragma unroll
-    for (int c = 0; c < 10; ++c) v[c] += (double)e[c];
-  }
-  block_sum<10, 128>(v, sh, out);
-  if (threadIdx.x == 0) {
-    ob.U_dipR = out[0];
-    for (int c = 0; c < 9; ++c) ob.PT_dipR[c] = out[1 + c];
-  }
-  // k-space
+      for (int c = 0; c < 10; ++c) v[c] = ff_add(v[c], ff_of(e[c]));
+    }
+    block_sum<11, kRedThreads>(v, sh, out);
+    if (threadIdx.x == 0) {
+      ob.U_dipR = out[0];
+      for (int c = 0; c < 9; ++c) ob.PT_dipR[c] = out[1 + c];
+    }
+  } else if (grp == 1) {
+    // k-space: U, PT per k
+    for (int k = threadIdx.x; k < P.nk; k += kRedThreads) {
+      const double* e = b.kE + (long long)(P.k_off + k) * 10;
 #pragma unroll
-  for (int c = 0; c < 10; ++c) v[c] = 0.0;
-  for (int k = threadIdx.x; k < P.nk; k += 128) {
-    const double* e = b.kE + (long long)(P.k_off + k) * 10;
+      for (int c = 0; c < 10; ++c) v[c] = ff_add(v[c], ff_from(e[c]));
+    }
+    block_sum<11, kRedThreads>(v, sh, out);
+    if (threadIdx.x == 0) {
+      ob.U_dipK = out[0];
+      for (int c = 0; c < 9; ++c) ob.PT_dipK[c] = out[1 + c];
+    }
+  } else if (grp == 2) {
+    // WCA: U, W, PT per particle block
+    for (int k = threadIdx.x; k < P.nblk; k += kRedThreads) {
+      const double* e = b.wcaE + (long long)(P.blk_off + k) * 11;
 #pragma unroll
-    for (int c = 0; c < 10; ++c) v[c] += e[c];
-  }
-  block_sum<10, 128>(v, sh, out);
-  if (threadIdx.x == 0) {
-    ob.U_dipK = out[0];
-    for (int c = 0; c < 9; ++c) ob.PT_dipK[c] = out[1 + c];
-  }
-  // WCA: U, W, PT
-#pragma unroll
-  for (int c = 0; c < 10; ++c) v[c] = 0.0;
-  double w = 0.0;
-  for (int k = threadIdx.x; k < P.nblk; k += 128) {
-    const double* e = b.wcaE + (long long)(P.blk_off + k) * 11;
-    v[0] += e[0];
-    w += e[1];
-#pragma unroll
-    for (int c = 0; c < 9; ++c) v[1 + c] += e[2 + c];
-  }
-  block_sum<10, 128>(v, sh, out);
-  {
-    double wv[1] = {w}, wo[1];
-    block_sum<1, 128>(wv, sh, wo);
+      for (int c = 0; c < 11; ++c) v[c] = ff_add(v[c], ff_from(e[c]));
+    }
+    block_sum<11, kRedThreads>(v, sh, out);
     if (threadIdx.x == 0) {
       ob.U_ss = out[0];
-      ob.W_ss = wo[0];
-      for (int c = 0; c < 9; ++c) ob.PT_ss[c] = out[1 + c];
+      ob.W_ss = out[1];
+      for (int c = 0; c < 9; ++c) ob.PT_ss[c] = out[2 + c];
     }
-  }
-  // kinetic terms and the field energy
+  } else {
+    // kinetic terms and the field energy
+    for (int k = threadIdx.x; k < P.nblk; k += kRedThreads) {
+      const double* e = b.kin2 + (long long)(P.blk_off + k) * 9;
 #pragma unroll
-  for (int c = 0; c < 10; ++c) v[c] = 0.0;
-  for (int k = threadIdx.x; k < P.nblk; k += 128) {
-    const double* e = b.kin2 + (long long)(P.blk_off + k) * 9;
-#pragma unroll
-    for (int c = 0; c < 9; ++c) v[c] += e[c];
-  }
-  block_sum<10, 128>(v, sh, out);
-  if (threadIdx.x == 0) {
-    ob.U_ext = out[8];
-    ob.U_self = P.Uself;
-    if (mode & kRedStep) {
-      ob.K[0] = 0.5 * out[0];
-      ob.K[1] = 0.5 * out[1];
-      const double pt6[6] = {out[2], out[3], out[4], out[5], out[6], out[7]};
-      const int map[9] = {0, 1, 2, 1, 3, 4, 2, 4, 5};
-      for (int c = 0; c < 9; ++c) ob.PT_kin[c] = pt6[map[c]];
-      // moveTher mode 2 (v25/functions.cpp:2207-2213) closes the step
-      double xi2[2], Kf[2];
-      xi_mid(b, P, S, s, xi2, Kf);
-      const double* nz = b.noise + ((long long)S.iter * b.nsys + s) * 4;
-      S.xi[0] = P.ex1 * xi2[0] + P.cnoise * nz[1];
-      S.xi[1] = P.ex1 * xi2[1] + P.cnoise * nz[3];
-      S.strn[0] = nz[1];
-      S.strn[1] = nz[3];
-      S.K_first[0] = Kf[0];
-      S.K_first[1] = Kf[1];
-      S.step += 1;
-      S.iter += 1;
-      if (S.rebuild) S.list_builds += 1;
-      S.force_list = 0;
+      for (int c = 0; c < 9; ++c) v[c] = ff_add(v[c], ff_from(e[c]));
     }
-    ob.xi[0] = S.xi[0];
-    ob.xi[1] = S.xi[1];
-    ob.step = S.step;
-    ob.status = S.status;
-    ob.list_builds = S.list_builds;
+    block_sum<11, kRedThreads>(v, sh, out);
+    if (threadIdx.x == 0) {
+      ob.U_ext = out[8];
+      ob.U_self = P.Uself;
+      if (mode & kRedStep) {
+        ob.K[0] = 0.5 * out[0];
+        ob.K[1] = 0.5 * out[1];
+        const double pt6[6] = {out[2], out[3], out[4], out[5], out[6], out[7]};
+        const int map[9] = {0, 1, 2, 1, 3, 4, 2, 4, 5};
+        for (int c = 0; c < 9; ++c) ob.PT_kin[c] = pt6[map[c]];
+        // moveTher mode 2 (v25/functions.cpp:2207-2213) closes the step
+        double xi2[2], Kf[2];
+        xi_mid(b, P, S, s, xi2, Kf);
+        const double* nz = b.noise + ((long long)S.iter * b.nsys + s) * 4;
+        S.xi[0] = P.ex1 * xi2[0] + P.cnoise * nz[1];
+        S.xi[1] = P.ex1 * xi2[1] + P.cnoise * nz[3];
+        S.strn[0] = nz[1];
+        S.strn[1] = nz[3];
+        S.K_first[0] = Kf[0];
+        S.K_first[1] = Kf[1];
+        S.step += 1;
+        S.iter += 1;
+        if (S.rebuild) S.list_builds += 1;
+        S.force_list = 0;
+      }
+      ob.xi[0] = S.xi[0];
+      ob.xi[1] = S.xi[1];
+      ob.step = S.step;
+      ob.status = S.status;
+      ob.list_builds = S.list_builds;
+    }
   }
 }
 
@@ -642,7 +638,7 @@ void launch_finalize(const Batch& b, int mode, cudaStream_t s) {
   if (b.nblk) finalize_kernel<<<b.nblk, kPartBlock, 0, s>>>(b, mode);
 }
 void launch_reduce_obs(const Batch& b, int mode, cudaStream_t s) {
-  if (b.nsys) reduce_obs_kernel<<<b.nsys, 128, 0, s>>>(b, mode);
+  if (b.nsys) reduce_obs_kernel<<<4 * b.nsys, kRedThreads, 0, s>>>(b, mode);
 }
 void launch_movex(const Batch& b, cudaStream_t s) {
   if (b.nblk) movex_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
