@@ -3,7 +3,7 @@
  * dipolar spherocylinders.  Drop-in for the hot path of mdSpherocyl.
  *
  * The reference's boundary is the set of free functions in
- * v25/functions.hpp:15-54 that v25/main.cpp calls once per step from one
+ * v25/functions.hpp:30-54,107-108 that v25/main.cpp calls once per step from one
  * host thread (force_sc, force_dipR, force_dipK, ext_field, self_ener,
  * moveX, moveP, moveTher, neigh_list, check_list, clust_conf).  Each of
  * them has an entry point below that does the same work on the GPU, and
@@ -144,36 +144,36 @@ mdsc_status mdsc_set_thermostat(mdsc_batch* b, int sys, const double xi[2], cons
 /* ---- the reference's hot-path functions, on every system --------------- */
 /* Zero F and T (v25/main.cpp:582-588). */
 mdsc_status mdsc_zero_forces(mdsc_batch* b);
-/* force_sc (v25/functions.hpp:35-36, v25/functions.cpp:1397-1553): WCA
+/* force_sc (v25/functions.hpp:38-39, v25/functions.cpp:1397-1553): WCA
    core forces and torques over the neighbour list, accumulated into F, T.
    U, W: nsys each; PT: nsys*9.  Returns MDSC_ERR_OVERLAP like the
    reference's false. */
 mdsc_status mdsc_force_sc(mdsc_batch* b, double* U, double* W, double* PT);
-/* force_dipR (v25/functions.hpp:37-38, v25/functions.cpp:1555-1678):
+/* force_dipR (v25/functions.hpp:40-41, v25/functions.cpp:1555-1678):
    real-space Ewald over all minimum-image dipole pairs, accumulated. */
 mdsc_status mdsc_force_dipR(mdsc_batch* b, double* U, double* PT);
-/* force_dipK (v25/functions.hpp:39-40, v25/functions.cpp:1706-1961):
+/* force_dipK (v25/functions.hpp:42-43, v25/functions.cpp:1706-1961):
    reciprocal-space Ewald, accumulated. */
 mdsc_status mdsc_force_dipK(mdsc_batch* b, double* U, double* PT);
-/* ext_field (v25/functions.hpp:41, v25/functions.cpp:1992-2025): torques
+/* ext_field (v25/functions.hpp:44, v25/functions.cpp:1992-2025): torques
    accumulated, energies out. */
 mdsc_status mdsc_ext_field(mdsc_batch* b, double* U);
-/* self_ener (v25/functions.hpp:42, v25/functions.cpp:2027-2069). */
+/* self_ener (v25/functions.hpp:45, v25/functions.cpp:2027-2069). */
 mdsc_status mdsc_self_ener(mdsc_batch* b, double* U);
-/* moveX (v25/functions.hpp:47, v25/functions.cpp:2071-2092). */
+/* moveX (v25/functions.hpp:50, v25/functions.cpp:2071-2092). */
 mdsc_status mdsc_moveX(mdsc_batch* b);
-/* moveP (v25/functions.hpp:48-49, v25/functions.cpp:2094-2184); xi: nsys*2
+/* moveP (v25/functions.hpp:51-52, v25/functions.cpp:2094-2184); xi: nsys*2
    thermostat coordinates; K: nsys*2; PT: nsys*9. */
 mdsc_status mdsc_moveP(mdsc_batch* b, const double* xi, int last, double* K, double* PT);
 /* Spherocyl::renorm for every particle (v25/classes.cpp:307-325). */
 mdsc_status mdsc_renorm(mdsc_batch* b);
-/* neigh_list (v25/functions.hpp:28-29, v25/functions.cpp:1298-1334):
+/* neigh_list (v25/functions.hpp:30-31, v25/functions.cpp:1298-1334):
    rebuild every system's Verlet list now. */
 mdsc_status mdsc_neigh_list(mdsc_batch* b);
-/* check_list (v25/functions.hpp:31-34, v25/functions.cpp:1356-1394):
+/* check_list (v25/functions.hpp:33-36, v25/functions.cpp:1356-1394):
    rebuild[s] = 1 where the skin was crossed since the last build. */
 mdsc_status mdsc_check_list(mdsc_batch* b, int* rebuild);
-/* clust_conf (v25/functions.hpp:104-105, v25/functions.cpp:3282-3324):
+/* clust_conf (v25/functions.hpp:107-108, v25/functions.cpp:3282-3324):
    labels of system `sys` with the reference's numbering, drawing from the
    system's cluster generator.  labels: n ints (may be NULL). */
 mdsc_status mdsc_clust_conf(mdsc_batch* b, int sys, int* labels, int* n_clusters);
