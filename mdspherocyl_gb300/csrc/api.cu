@@ -91,6 +91,20 @@ std::string check_desc(const mdsc_system_desc& d, int s) {
   return "";
 }
 
+// constants of the real-space tiles as float-float pairs: the exponent's
+// alpha sqrt(log2 e) and the fixed-point scale L / 2^32, split on the host so
+// that the tiles do no FP64 work
+void set_pair_consts(SysDev& P) {
+  const double xa = P.alpha * 1.2011224087864498;  // sqrt(log2 e)
+  P.xh = (float)xa;
+  P.xlo = (float)(xa - (double)P.xh);
+  for (int a = 0; a < 3; ++a) {
+    const double h = P.L[a] / 4294967296.0;
+    P.Lhi[a] = (float)h;
+    P.Llo[a] = (float)(h - (double)P.Lhi[a]);
+  }
+}
+
 void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
   Lo.sys.resize(nsys);
   int part = 0, dip = 0, blk = 0;
@@ -172,6 +186,7 @@ void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
     P.halfLh2 = (float)(0.5 * kLh * kLh);
     P.rmax_table = (float)kTableRmax;
     P.sixthLh3 = (float)(kLh * kLh * kLh / 6.0);
+    set_pair_consts(P);
     part += d.n;
     dip += P.ndip;
     Lo.maxnd = std::max(Lo.maxnd, d.nd);

@@ -27,13 +27,14 @@ __device__ __forceinline__ void derive_particle(const Batch& b, const SysDev& P,
     u[a] = to_fix(r[a], P.invL32[a]);
     b.pfx[a * N + i] = u[a];
   }
-  b.pax[i] = make_float4((float)O[6], (float)O[7], (float)O[8], (float)b.len[i]);
-  b.pdia[i] = (float)b.dia[i];
-  const int nd = P.nd;
-  const int g0 = P.dip_off + (i - P.part_off) * nd;
+  // FP32 copies by integer instructions (the FP64 unit is the scarce one)
   float Of[9];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) Of[k] = (float)O[k];
+  for (int k = 0; k < 9; ++k) Of[k] = soft_d2f_rn(O[k]);
+  b.pax[i] = make_float4(Of[6], Of[7], Of[8], soft_d2f_rn(b.len[i]));
+  b.pdia[i] = soft_d2f_rn(b.dia[i]);
+  const int nd = P.nd;
+  const int g0 = P.dip_off + (i - P.part_off) * nd;
   for (int w = 0; w < nd; ++w) {
     const int g = g0 + w;
     const double pc = b.dpc[g];
@@ -45,8 +46,9 @@ __device__ __forceinline__ void derive_particle(const Batch& b, const SysDev& P,
       for (int a = 0; a < 3; ++a) b.dfx[a * ND + g] = to_fix(r[a] + pc * O[6 + a], P.invL32[a]);
     }
     // lab direction O^T o_body (Spherocyl::set_dip, v25/classes.cpp:166-170), times the moment
-    const float ox = (float)b.dob[3 * g], oy = (float)b.dob[3 * g + 1], oz = (float)b.dob[3 * g + 2];
-    const float mu = (float)b.dmu[g];
+    const float ox = soft_d2f_rn(b.dob[3 * g]), oy = soft_d2f_rn(b.dob[3 * g + 1]),
+                oz = soft_d2f_rn(b.dob[3 * g + 2]);
+    const float mu = soft_d2f_rn(b.dmu[g]);
 #pragma unroll
     for (int a = 0; a < 3; ++a) b.dm[a * ND + g] = mu * (Of[a] * ox + Of[3 + a] * oy + Of[6 + a] * oz);
   }
@@ -61,11 +63,11 @@ __device__ __forceinline__ float displacement(const Batch& b, const SysDev& P, i
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     const float d = fix_diff(u[a], b.fsave[3 * i + a], P.Lfix[a]);
-    const float e = (float)O[6 + a] - b.usave[3 * i + a];
+    const float e = soft_d2f_rn(O[6 + a]) - b.usave[3 * i + a];
     dr2 += d * d;
     du2 += e * e;
   }
-  return sqrtf(dr2) + 0.5f * (float)b.len[i] * sqrtf(du2);
+  return sqrtf(dr2) + 0.5f * soft_d2f_rn(b.len[i]) * sqrtf(du2);
 }
 
 __global__ void __launch_bounds__(kPartBlock) derive_kernel(Batch b) {
@@ -85,7 +87,7 @@ __global__ void __launch_bounds__(kPartBlock) derive_kernel(Batch b) {
     disp = displacement(b, P, i, u, O);
   }
   const float m = block_max<kPartBlock>(disp, shm);
-  if (threadIdx.x == 0) b.dmax[blk_slot(P, bk)] = (double)m;
+  if (threadIdx.x == 0) b.dmax[blk_slot(P, bk)] = soft_f2d(m);
 }
 
 // Spherocyl::renorm, v25/classes.cpp:307-325
@@ -131,12 +133,13 @@ __device__ __forceinline__ void move_x(const Batch& b, int i, double dt, double*
   const double im = b.invm[i];
 #pragma unroll
   for (int a = 0; a < 3; ++a) r[a] += dt * p[a] * im;
-  const float iI0 = (float)b.invI[3 * i], iI1 = (float)b.invI[3 * i + 1], iI2 = (float)b.invI[3 * i + 2];
-  const float h = (float)(0.5 * dt), fdt = (float)dt;
+  const float iI0 = soft_d2f_rn(b.invI[3 * i]), iI1 = soft_d2f_rn(b.invI[3 * i + 1]),
+              iI2 = soft_d2f_rn(b.invI[3 * i + 2]);
+  const float fdt = soft_d2f_rn(dt), h = 0.5f * fdt;
   float lb[3], Of[9];
-  const float lf[3] = {(float)l[0], (float)l[1], (float)l[2]};
+  const float lf[3] = {soft_d2f_rn(l[0]), soft_d2f_rn(l[1]), soft_d2f_rn(l[2])};
 #pragma unroll
-  for (int k = 0; k < 9; ++k) Of[k] = (float)O[k];
+  for (int k = 0; k < 9; ++k) Of[k] = soft_d2f_rn(O[k]);
 #pragma unroll
   for (int a = 0; a < 3; ++a) lb[a] = Of[3 * a] * lf[0] + Of[3 * a + 1] * lf[1] + Of[3 * a + 2] * lf[2];
   float D[9];
@@ -155,7 +158,7 @@ __device__ __forceinline__ void move_x(const Batch& b, int i, double dt, double*
 #pragma unroll
     for (int c = 0; c < 3; ++c) inc[3 * a + c] = D[3 * a] * Of[c] + D[3 * a + 1] * Of[3 + c] + D[3 * a + 2] * Of[6 + c];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) O[k] += (double)inc[k];
+  for (int k = 0; k < 9; ++k) O[k] += soft_f2d(inc[k]);
 }
 
 // K_r = l^T (O^T I^-1 O) l = sum_a (O l)_a^2 / I_a  (v25/functions.cpp:2123-2148)
@@ -236,7 +239,7 @@ __global__ void __launch_bounds__(kPartBlock) integrate_first_kernel(Batch b) {
     const int lb = blk_slot(P, bk);
     b.kin1[2 * lb] = tot[0];
     b.kin1[2 * lb + 1] = tot[1];
-    b.dmax[lb] = (double)m;
+    b.dmax[lb] = soft_f2d(m);
   }
 }
 
@@ -355,8 +358,8 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
       double f[3], t[3];
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        f[c] = (double)acc6[c].hi + (double)acc6[c].lo;
-        t[c] = (double)acc6[3 + c].hi + (double)acc6[3 + c].lo;
+        f[c] = soft_f2d(acc6[c].hi) + soft_f2d(acc6[c].lo);
+        t[c] = soft_f2d(acc6[3 + c].hi) + soft_f2d(acc6[3 + c].lo);
       }
       if (ext) {
         // ext_field: torque mu o x B, energy -mu o.B (v25/functions.cpp:2014-2020),
@@ -407,8 +410,8 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
       acc[0] = ff_from(psq * im);
       acc[1] = ff_from(rot_kin(b, i, O, l));
       // kinetic pressure tensor p_a p_b / m: FP32 products, float-float sums
-      const float pf[3] = {(float)p[0], (float)p[1], (float)p[2]};
-      const float imf = (float)im;
+      const float pf[3] = {soft_d2f_rn(p[0]), soft_d2f_rn(p[1]), soft_d2f_rn(p[2])};
+      const float imf = soft_d2f_rn(im);
       acc[2] = ff_of(pf[0] * pf[0] * imf);
       acc[3] = ff_of(pf[0] * pf[1] * imf);
       acc[4] = ff_of(pf[0] * pf[2] * imf);

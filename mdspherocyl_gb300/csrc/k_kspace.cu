@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(kKBlock / 2) ksum1_kernel(Batch b, const int4*
   if (w.z == 0) {
     double gl[6] = {0, 0, 0, 0, 0, 0};
     for (int q = t; q < np; q += kKBlock / 2) {
-      const double mx = sm[q].x, my = sm[q].y, mz = sm[q].z;
+      const double mx = soft_f2d(sm[q].x), my = soft_f2d(sm[q].y), mz = soft_f2d(sm[q].z);
       gl[0] += mx * mx; gl[1] += mx * my; gl[2] += mx * mz;
       gl[3] += my * my; gl[4] += my * mz; gl[5] += mz * mz;
     }
@@ -245,7 +245,7 @@ __global__ void kcombine_kernel(Batch b, const int2* __restrict__ kowner, double
   }
   double s[10];
 #pragma unroll
-  for (int c = 0; c < 10; ++c) s[c] = c < nv ? (double)sf[c].hi + (double)sf[c].lo : 0.0;
+  for (int c = 0; c < 10; ++c) s[c] = c < nv ? soft_f2d(sf[c].hi) + soft_f2d(sf[c].lo) : 0.0;
   const double kx = b.kvec[3 * k], ky = b.kvec[3 * k + 1], kz = b.kvec[3 * k + 2];
   if (ND == 1) {
     const double* G = b.kGs + 6 * ow.x;
@@ -266,7 +266,7 @@ __global__ void kcombine_kernel(Batch b, const int2* __restrict__ kowner, double
   const double nrm = Sr * Sr + Si * Si;
   const double self = s[6];
   const double en = val * 0.5 * (nrm - self);
-  b.kS[k] = make_float2((float)(val * Sr), (float)(val * Si));
+  b.kS[k] = make_float2(soft_d2f_rn(val * Sr), soft_d2f_rn(val * Si));
   const double pval = b.kpre[k];
   const double kk[3] = {kx, ky, kz};
   double* e = kE + (long long)k * 10;

@@ -86,7 +86,6 @@ constexpr float kQ0 = 2.820587754e-01f, kQ1 = 2.829789221e-01f, kQ2 = 2.37546384
                 kQ3 = 2.310565114e-01f, kQ4 = -1.153462157e-01f, kQ5 = 4.548966587e-01f,
                 kQ6 = -7.125887275e-01f, kQ7 = 4.623427987e-01f, kQ8 = -1.380545348e-01f,
                 kQ9 = 1.510943193e-02f;
-constexpr double kSqrtLog2e = 1.2011224087864498;  // sqrt(log2(e))
 
 // per-system constants, the same value in both halves
 struct PairConst {
@@ -264,22 +263,14 @@ __global__ void __launch_bounds__(32) real_pairs_kernel(Batch b) {
   const int ND = b.ndtot;
 
   PairConst K;
-  {
-    const double xa = P.alpha * kSqrtLog2e;
-    const float xh = (float)xa;
-    K.xh = b2(xh);
-    K.xlo = b2((float)(xa - (double)xh));
-    const double inv32 = 1.0 / 4294967296.0;
-    float h = (float)(P.L[0] * inv32);
-    K.Lhx = b2(h);
-    K.Llx = b2((float)(P.L[0] * inv32 - (double)h));
-    h = (float)(P.L[1] * inv32);
-    K.Lhy = b2(h);
-    K.Lly = b2((float)(P.L[1] * inv32 - (double)h));
-    h = (float)(P.L[2] * inv32);
-    K.Lhz = b2(h);
-    K.Llz = b2((float)(P.L[2] * inv32 - (double)h));
-  }
+  K.xh = b2(P.xh);
+  K.xlo = b2(P.xlo);
+  K.Lhx = b2(P.Lhi[0]);
+  K.Llx = b2(P.Llo[0]);
+  K.Lhy = b2(P.Lhi[1]);
+  K.Lly = b2(P.Llo[1]);
+  K.Lhz = b2(P.Lhi[2]);
+  K.Llz = b2(P.Llo[2]);
   K.ahalf = b2(0.5f * P.alphaf);
   K.gpref = b2(P.gpref);
   K.a2 = b2(P.alpha2x2);

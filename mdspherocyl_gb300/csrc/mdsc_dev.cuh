@@ -5,6 +5,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "softcvt.cuh"
+
 namespace mdsc {
 
 constexpr int kTile = 64;        // real-space tile edge, in dipoles
@@ -73,6 +75,8 @@ struct SysDev {
   float invLh, halfLh2;    // table spacing of the reference: Lh = 0.5*200.2/32768
   float rmax_table;        // 100.1: the reference's table covers r <= 100.1
   float sixthLh3;          // Lh^3 / 6
+  float xh, xlo;           // alpha sqrt(log2 e) as a float-float pair
+  float Lhi[3], Llo[3];    // L / 2^32 per axis as float-float pairs
 };
 
 // Per-system mutable state.
@@ -180,7 +184,7 @@ __host__ __device__ inline int cdiv(int a, int b) { return (a + b - 1) / b; }
 // floor(x 2^32 / L) modulo 2^32 (invL32 = 2^32 / L; the product is the
 // exactly scaled x / L, so this equals frac(x / L) 2^32 truncated)
 __device__ inline uint32_t to_fix(double x, double invL32) {
-  return (uint32_t)(unsigned long long)__double2ll_rd(x * invL32);
+  return soft_floor_u32(x * invL32);
 }
 
 // slot of a particle block in the per-block partial arrays: blocks are

@@ -6,16 +6,18 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "softcvt.cuh"
+
 namespace mdsc {
 
 struct FF {
   float hi, lo;
 };
 
+// x as a float-float pair (48 bits), by integer instructions
 __device__ __forceinline__ FF ff_from(double x) {
   FF r;
-  r.hi = (float)x;
-  r.lo = (float)(x - (double)r.hi);
+  soft_split(x, r.hi, r.lo);
   return r;
 }
 
@@ -49,7 +51,7 @@ __device__ __forceinline__ void block_sum(const double (&v)[NV], double* sh, dou
 #pragma unroll
   for (int c = 0; c < NV; ++c) {
     FF w = ff_warp_sum(ff_from(v[c]));
-    if (lane == 0) sh[c * (NT / 32) + warp] = (double)w.hi + (double)w.lo;
+    if (lane == 0) sh[c * (NT / 32) + warp] = soft_f2d(w.hi) + soft_f2d(w.lo);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -71,7 +73,7 @@ __device__ __forceinline__ void block_sum(const FF (&v)[NV], double* sh, double*
 #pragma unroll
   for (int c = 0; c < NV; ++c) {
     FF w = ff_warp_sum(v[c]);
-    if (lane == 0) sh[c * (NT / 32) + warp] = (double)w.hi + (double)w.lo;
+    if (lane == 0) sh[c * (NT / 32) + warp] = soft_f2d(w.hi) + soft_f2d(w.lo);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
