@@ -251,8 +251,10 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   b.rpart = A.take<float>(std::max<long long>(Lo.rpart, 1));
   b.tileE = A.take<float>(10 * nt);
   b.tiles = A.take<int4>(nt);
-  b.Fw = A.take<double>(3 * n);
-  b.Tw = A.take<double>(3 * n);
+  b.wlist = A.take<int2>(n * kMaxC);
+  b.wlist_n = A.take<int>(1);
+  b.wown = A.take<double>(n * kMaxC * 6);
+  b.wev = A.take<double>(n * kMaxC * 11);
   b.wcaE = A.take<double>(11 * nb);
   b.wcand = A.take<int>(n * kMaxC);
   b.wcnt = A.take<int>(n);
@@ -377,7 +379,7 @@ mdsc_status capture_step(mdsc_batch* B, int which) {
   cudaStreamWaitEvent(B->s3, B->ev_fork, 0);
   launch_list_build(b, 0, B->st);
   launch_wca(b, B->st);
-  launches += 2;
+  launches += 3;
   launch_real_pairs(b, B->lo.multi, B->s2);
   launches += b.ntiles > 0;
   launch_kspace(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, B->s3);

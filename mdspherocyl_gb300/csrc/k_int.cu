@@ -265,7 +265,7 @@ __device__ __forceinline__ void xi_mid(const Batch& b, const SysDev& P, const Sy
 // force assembly (+ ext_field) and optionally moveP(last)
 // ---------------------------------------------------------------------
 __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode) {
-  __shared__ double sh[9 * kPartBlock / 32];
+  __shared__ double sh[20 * kPartBlock / 32];
   __shared__ double sx[2];
   const int2 bk = b.blk[blockIdx.x];
   const int s = bk.x;
@@ -280,9 +280,11 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
     sx[1] = xi2[1];
   }
   __syncthreads();
-  FF acc[9];
+  // block sums: K_t, K_r, PT_kin (6), U_ext, then the WCA terms U, W, PT (9)
+  // of this block's own candidate pairs
+  FF acc[20];
 #pragma unroll
-  for (int c = 0; c < 9; ++c) acc[c].hi = acc[c].lo = 0.f;
+  for (int c = 0; c < 20; ++c) acc[c].hi = acc[c].lo = 0.f;
   if (ok) {
     double F[3], T[3];
 #pragma unroll
@@ -291,10 +293,21 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
       T[a] = (mode & kFlagAccum) ? b.T[3 * i + a] : 0.0;
     }
     if (mode & kMaskWca) {
+      // its own shares of its candidate pairs (higher-index partners), in
+      // slot order, as force_sc adds them
+      {
+        const int nc = b.wcnt[i];
+        const double* own = b.wown + (long long)i * kMaxC * 6;
+        const double* ev = b.wev + (long long)i * kMaxC * 11;
+        for (int c = 0; c < nc; ++c) {
 #pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        F[a] += b.Fw[3 * i + a];
-        T[a] += b.Tw[3 * i + a];
+          for (int a = 0; a < 3; ++a) {
+            F[a] += own[6 * c + a];
+            T[a] += own[6 * c + 3 + a];
+          }
+#pragma unroll
+          for (int q = 0; q < 11; ++q) acc[9 + q] = ff_add(acc[9 + q], ff_from(ev[11 * c + q]));
+        }
       }
       // shares of the pairs this particle forms with lower-index partners,
       // left by the WCA kernel in the partner's records (ascending partner)
@@ -425,11 +438,15 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
       b.T[3 * i + a] = T[a];
     }
   }
-  double tot[9];
-  block_sum<9, kPartBlock>(acc, sh, tot);
+  double tot[20];
+  block_sum<20, kPartBlock>(acc, sh, tot);
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int c = 0; c < 9; ++c) b.kin2[9 * blk_slot(P, bk) + c] = tot[c];
+    if (mode & kMaskWca) {
+#pragma unroll
+      for (int c = 0; c < 11; ++c) b.wcaE[11 * blk_slot(P, bk) + c] = tot[9 + c];
+    }
   }
 }
 
@@ -474,7 +491,7 @@ __global__ void __launch_bounds__(kRedThreads) reduce_obs_kernel(Batch b, int mo
       for (int c = 0; c < 9; ++c) ob.PT_dipK[c] = out[1 + c];
     }
   } else if (grp == 2) {
-    // WCA: U, W, PT per particle block
+    // WCA: U, W, PT per particle block (summed by the finalize kernel)
     for (int k = threadIdx.x; k < P.nblk; k += kRedThreads) {
       const double* e = b.wcaE + (long long)(P.blk_off + k) * 11;
 #pragma unroll

@@ -177,27 +177,25 @@ __device__ bool wca_pair(const Batch& b, const SysDev& P, int A, int B, double* 
   return true;
 }
 
-// Two phases per block of particles.  (1) Each thread screens its
-// particle's partners of higher index (each pair once) in FP32 and keeps
-// the candidates (ascending index).  (2) The block's candidates,
-// concatenated owner by owner, are evaluated in FP64 one per thread, in
-// rounds of one block-width; warps with no candidate left skip the round.
-// The owner (the lower index) adds its share in candidate order, the
-// partner's share goes to a record that the finalize kernel gathers, and
-// eleven threads add the round's energies and virials in candidate order.
-// FP64 runs at 1/64 of the FP32 instruction rate on this GPU, so only pairs
-// that can touch reach the FP64 pipe, once each and densely packed.
-__global__ void __launch_bounds__(kPartBlock) wca_kernel(Batch b) {
-  __shared__ int cand[kPartBlock][kMaxC];
-  __shared__ int soff[kPartBlock + 1];
-  __shared__ int swarp[kPartBlock / 32];
-  __shared__ double res[kPartBlock][6];
-  __shared__ double sev[kPartBlock][11];
+// WCA in two kernels.  (1) wca_screen: each thread screens its particle's
+// partners of higher index (each pair once) in FP32, keeps the candidates in
+// ascending index in its slots (wcand) and appends (slot, system) items to
+// a work list, one atomic per warp.  (2) wca_eval: every thread of a fixed
+// grid takes list items and evaluates them in FP64 -- only pairs that can
+// touch reach the FP64 unit (1/64 of the FP32 rate on this GPU), densely
+// packed, with no block-wide synchronisation.  Each item writes its own
+// share (force and torque on the lower index), its partner's share and its
+// energy/virial terms to the candidate's slot.  The finalize kernel adds a
+// particle's own shares in slot order and its partners' shares in partner
+// order, and the per-system reduction adds the slots' energies in particle
+// and slot order, so the list order (which depends on warp timing) does not
+// reach any result.
+__global__ void __launch_bounds__(kPartBlock) wca_screen_kernel(Batch b) {
   const int2 bk = b.blk[blockIdx.x];
   const int s = bk.x;
   const SysDev& P = b.sys[s];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int i = bk.y + tid;
+  const int lane = threadIdx.x & 31;
+  const int i = bk.y + threadIdx.x;
   const bool ok = i < P.part_off + P.n;
   const int N = b.ntot;
   int err = 0;
@@ -219,10 +217,7 @@ __global__ void __launch_bounds__(kPartBlock) wca_kernel(Batch b) {
       const float d2 = seg_dist_fast(dx, dy, dz, ai.x, ai.y, ai.z, ai.w, aj.x, aj.y, aj.z, aj.w);
       // 2^(1/3) sigma^2, with a margin for the FP32 screen
       if (d2 >= 1.2599211f * sg * sg * 1.002f) continue;
-      if (nc < kMaxC) {
-        cand[tid][nc] = q;
-        b.wcand[(long long)i * kMaxC + nc] = q;
-      }
+      if (nc < kMaxC) b.wcand[(long long)i * kMaxC + nc] = q;
       ++nc;
     }
     if (nc > kMaxC) {
@@ -231,84 +226,52 @@ __global__ void __launch_bounds__(kPartBlock) wca_kernel(Batch b) {
     }
     b.wcnt[i] = nc;
   }
-  // exclusive scan of the candidate counts over the block
+  // room on the work list for the warp's candidates: one atomic per warp
   int inc = nc;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
     const int v = __shfl_up_sync(0xffffffffu, inc, d);
     if (lane >= d) inc += v;
   }
-  if (lane == 31) swarp[warp] = inc;
-  __syncthreads();
-  int wbase = 0;
-#pragma unroll
-  for (int w = 0; w < kPartBlock / 32; ++w) wbase += (w < warp) ? swarp[w] : 0;
-  const int off = wbase + inc - nc;
-  soff[tid] = off;
-  if (tid == kPartBlock - 1) soff[kPartBlock] = off + nc;
-  __syncthreads();
-  const int total = soff[kPartBlock];
+  const int wtot = __shfl_sync(0xffffffffu, inc, 31);
+  int base = 0;
+  if (lane == 31 && wtot > 0) base = atomicAdd(b.wlist_n, wtot);
+  base = __shfl_sync(0xffffffffu, base, 31);
+  const int off = base + inc - nc;
+  for (int kk = 0; kk < nc; ++kk) b.wlist[off + kk] = make_int2(i * kMaxC + kk, s);
+  if (err) atomicOr(&b.st[s].status, err);
+}
 
-  double F[3] = {0, 0, 0}, T[3] = {0, 0, 0};
-  double esum = 0.0;  // thread c < 11: component c of the block's energies
-  for (int base = 0; base < total; base += kPartBlock) {
-    const int e = base + tid;
-    if (e < total) {
-      // owner: the last thread whose offset is <= e
-      int lo = 0, hi = kPartBlock - 1;
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (soff[mid] <= e) lo = mid;
-        else hi = mid - 1;
-      }
-      const int kk = e - soff[lo];
-      const int p = bk.y + lo;
-      const int q = cand[lo][kk];
-      double fA[3], tA[3], tB[3], ev[11];
-      if (!wca_pair(b, P, p, q, fA, tA, tB, ev, err)) {
+__global__ void __launch_bounds__(128) wca_eval_kernel(Batch b) {
+  const int n = *(volatile const int*)b.wlist_n;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const int2 it = b.wlist[e];
+    const int slot = it.x, s = it.y;
+    const int p = slot / kMaxC;
+    const SysDev& P = b.sys[s];
+    const int q = b.wcand[slot];
+    int err = 0;
+    double fA[3], tA[3], tB[3], ev[11];
+    if (!wca_pair(b, P, p, q, fA, tA, tB, ev, err)) {
 #pragma unroll
-        for (int a = 0; a < 3; ++a) fA[a] = tA[a] = tB[a] = 0.0;
+      for (int a = 0; a < 3; ++a) fA[a] = tA[a] = tB[a] = 0.0;
 #pragma unroll
-        for (int c = 0; c < 11; ++c) ev[c] = 0.0;
-      }
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        res[tid][a] = fA[a];
-        res[tid][3 + a] = tA[a];
-      }
-#pragma unroll
-      for (int c = 0; c < 11; ++c) sev[tid][c] = ev[c];
-      double* out = b.wrec + ((long long)p * kMaxC + kk) * 6;
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        out[a] = -fA[a];
-        out[3 + a] = tB[a];
-      }
+      for (int c = 0; c < 11; ++c) ev[c] = 0.0;
     }
-    __syncthreads();
-    const int e0 = max(off, base), e1 = min(off + nc, base + kPartBlock);
-    for (int k = e0; k < e1; ++k) {
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        F[a] += res[k - base][a];
-        T[a] += res[k - base][3 + a];
-      }
-    }
-    if (tid < 11) {
-      const int m = min(kPartBlock, total - base);
-      for (int k = 0; k < m; ++k) esum += sev[k][tid];
-    }
-    __syncthreads();
-  }
-  if (ok) {
+    double* own = b.wown + (long long)slot * 6;
+    double* rec = b.wrec + (long long)slot * 6;
+    double* evo = b.wev + (long long)slot * 11;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-      b.Fw[3 * i + a] = F[a];
-      b.Tw[3 * i + a] = T[a];
+      own[a] = fA[a];
+      own[3 + a] = tA[a];
+      rec[a] = -fA[a];
+      rec[3 + a] = tB[a];
     }
+#pragma unroll
+    for (int c = 0; c < 11; ++c) evo[c] = ev[c];
+    if (err) atomicOr(&b.st[s].status, err);
   }
-  if (err) atomicOr(&b.st[s].status, err);
-  if (tid < 11) b.wcaE[11 * blk_slot(P, bk) + tid] = esum;
 }
 
 // ---- clusters (v25/functions.cpp:2987-3016,3282-3324) ----------------
@@ -390,8 +353,14 @@ __global__ void __launch_bounds__(kPartBlock) cluster_compress_kernel(Batch b) {
 void launch_list_build(const Batch& b, int force_all, cudaStream_t s) {
   if (b.nblk) list_build_kernel<<<b.nblk, kPartBlock, 0, s>>>(b, force_all);
 }
+// eval grid: enough 128-thread blocks to fill every SM's FP64 unit; each
+// thread loops over the work list
+constexpr int kWcaEvalBlocks = 152 * 8;
 void launch_wca(const Batch& b, cudaStream_t s) {
-  if (b.nblk) wca_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
+  if (!b.nblk) return;
+  cudaMemsetAsync(b.wlist_n, 0, sizeof(int), s);
+  wca_screen_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
+  wca_eval_kernel<<<kWcaEvalBlocks, 128, 0, s>>>(b);
 }
 void launch_cluster_bonds(const Batch& b, cudaStream_t s) {
   if (b.nblk) cluster_bonds_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);

@@ -138,9 +138,11 @@ struct Batch {
   float* rpart;  // real-space partials
   float* tileE;  // 10 per tile: U, PT[9]
   int4* tiles;   // (sys, I, J, 0)
-  double* Fw;    // 3n WCA force
-  double* Tw;    // 3n WCA torque
-  double* wcaE;  // per block: U, W, PT[9] = 11
+  int2* wlist;   // WCA work list: (candidate slot, system), n * kMaxC at most
+  int* wlist_n;  // its length this step
+  double* wown;  // n * kMaxC * 6: the lower index's force and torque of each candidate
+  double* wev;   // n * kMaxC * 11: U, W, PT of each candidate
+  double* wcaE;  // per particle block: U, W, PT (11) of its own candidates
   int* wcand;    // n * kMaxC contact candidates (higher index) of each particle
   int* wcnt;     // n
   double* wrec;  // n * kMaxC * 6: the partner's force and torque of each candidate

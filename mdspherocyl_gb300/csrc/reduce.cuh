@@ -1,8 +1,9 @@
-// Deterministic reductions.  FP64 arithmetic runs at a small fraction of
-// the FP32 rate on this GPU, so warp-level sums of FP64 values are done in
-// float-float (a hi/lo pair of FP32 numbers combined with error-free
-// TwoSum, ~48 significant bits) and only the per-warp results are added in
-// FP64.  The tree shape is fixed, so results are bitwise reproducible.
+// Deterministic reductions.  FP64 arithmetic and FP64 conversions run at
+// 1/64 of the FP32 rate on this GPU, so block-level sums of FP64 values are
+// done in float-float (a hi/lo pair of FP32 numbers combined with
+// error-free TwoSum, ~48 significant bits), entered and left by integer
+// conversions, with one FP64 addition per value at the end.  The tree shape
+// is fixed, so results are bitwise reproducible.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -43,48 +44,39 @@ __device__ __forceinline__ FF ff_warp_sum(FF v) {
   return v;
 }
 
-// Sums NV FP64 values over a block of NT threads; thread 0 gets the totals
-// in out[].  sh must hold NV * NT/32 doubles.
+// Sums NV float-float values over a block of NT threads (an FP32 value x
+// enters as {x, 0}); thread 0 gets the totals in out[].  The warps' sums are
+// added in float-float too, so each value costs one FP64 addition, at the
+// end.  sh must hold NV * NT/32 doubles.
 template <int NV, int NT>
-__device__ __forceinline__ void block_sum(const double (&v)[NV], double* sh, double* out) {
+__device__ __forceinline__ void block_sum(const FF (&v)[NV], double* sh, double* out) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  FF* shf = reinterpret_cast<FF*>(sh);
 #pragma unroll
   for (int c = 0; c < NV; ++c) {
-    FF w = ff_warp_sum(ff_from(v[c]));
-    if (lane == 0) sh[c * (NT / 32) + warp] = soft_f2d(w.hi) + soft_f2d(w.lo);
+    FF w = ff_warp_sum(v[c]);
+    if (lane == 0) shf[c * (NT / 32) + warp] = w;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int c = 0; c < NV; ++c) {
-      double s = 0.0;
-      for (int k = 0; k < NT / 32; ++k) s += sh[c * (NT / 32) + k];
-      out[c] = s;
+      FF s = shf[c * (NT / 32)];
+      for (int k = 1; k < NT / 32; ++k) s = ff_add(s, shf[c * (NT / 32) + k]);
+      out[c] = soft_f2d(s.hi) + soft_f2d(s.lo);
     }
   }
   __syncthreads();
 }
 
-// Same, for values already in float-float form (an FP32 value x enters as
-// {x, 0} and costs no FP64 instruction).
+// Same, for FP64 values (split into float-float by integer instructions,
+// 48 bits).
 template <int NV, int NT>
-__device__ __forceinline__ void block_sum(const FF (&v)[NV], double* sh, double* out) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+__device__ __forceinline__ void block_sum(const double (&v)[NV], double* sh, double* out) {
+  FF f[NV];
 #pragma unroll
-  for (int c = 0; c < NV; ++c) {
-    FF w = ff_warp_sum(v[c]);
-    if (lane == 0) sh[c * (NT / 32) + warp] = soft_f2d(w.hi) + soft_f2d(w.lo);
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int c = 0; c < NV; ++c) {
-      double s = 0.0;
-      for (int k = 0; k < NT / 32; ++k) s += sh[c * (NT / 32) + k];
-      out[c] = s;
-    }
-  }
-  __syncthreads();
+  for (int c = 0; c < NV; ++c) f[c] = ff_from(v[c]);
+  block_sum<NV, NT>(f, sh, out);
 }
 
 __device__ __forceinline__ FF ff_of(float x) {
@@ -94,7 +86,7 @@ __device__ __forceinline__ FF ff_of(float x) {
   return r;
 }
 
-// Same, for a per-block maximum of non-negative values.
+// Per-block maximum of non-negative values.
 template <int NT>
 __device__ __forceinline__ float block_max(float v, float* sh) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
