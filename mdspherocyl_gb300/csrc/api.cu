@@ -14,6 +14,7 @@
 
 namespace mdsc {
 void launch_real_pairs(const Batch& b, bool multi, cudaStream_t s);
+void launch_real_sum(const Batch& b, cudaStream_t s);
 void launch_kspace(const Batch& b, int maxnd, const int4* kwork, int nkwork, const int2* kowner,
                    double* kE, cudaStream_t s);
 void launch_derive(const Batch& b, cudaStream_t s);
@@ -249,6 +250,7 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   b.dfx = A.take<uint32_t>(3 * nd);
   b.dm = A.take<float>(3 * nd);
   b.rpart = A.take<float>(std::max<long long>(Lo.rpart, 1));
+  b.rsum = A.take<float2>(6 * (size_t)std::max(Lo.ndtot, 1));
   b.tileE = A.take<float>(10 * nt);
   b.tiles = A.take<int4>(nt);
   b.wlist = A.take<int2>(n * kMaxC);
@@ -271,6 +273,7 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   b.kG = A.take<double>(6 * (size_t)std::max(Lo.nchunks, 1));
   b.kGs = A.take<double>(6 * (size_t)std::max(nsys, 1));
   b.kgcnt = A.take<int>(std::max(nsys, 1));
+  b.icnt = A.take<int>(std::max(nsys, 1));
   b.Fk = A.take<float2>(3 * nd);
   b.Tk = A.take<float2>(3 * nd);
   b.kin1 = A.take<double>(2 * nb);
@@ -356,6 +359,7 @@ mdsc_status eval_forces(mdsc_batch* B, int force_list) {
   launch_list_build(b, force_list, B->st);
   launch_wca(b, B->st);
   launch_real_pairs(b, B->lo.multi, B->st);
+  launch_real_sum(b, B->st);
   launch_kspace(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, B->st);
   launch_finalize(b, kMaskAll, B->st);
   launch_reduce_obs(b, kRedEnergies, B->st);
@@ -381,7 +385,8 @@ mdsc_status capture_step(mdsc_batch* B, int which) {
   launch_wca(b, B->st);
   launches += 3;
   launch_real_pairs(b, B->lo.multi, B->s2);
-  launches += b.ntiles > 0;
+  launch_real_sum(b, B->s2);
+  launches += b.ntiles > 0 ? 2 : 0;
   launch_kspace(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, B->s3);
   launches += b.nktot > 0 ? 3 : 0;
   cudaEventRecord(B->ev_j2, B->s2);
@@ -674,6 +679,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   cudaMemsetAsync(b.nbc, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.wcnt, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.kgcnt, 0, sizeof(int) * std::max(nsys, 1), B->st);
+  cudaMemsetAsync(b.icnt, 0, sizeof(int) * std::max(nsys, 1), B->st);
   cudaMemsetAsync(b.F, 0, sizeof(double) * 3 * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.T, 0, sizeof(double) * 3 * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(B->noise[0], 0, sizeof(double) * kNoiseChunk * nsys * 4, B->st);
@@ -939,6 +945,7 @@ mdsc_status mdsc_force_dipR(mdsc_batch* B, double* U, double* PT) {
   if (st) return st;
   launch_derive(B->b, B->st);
   launch_real_pairs(B->b, B->lo.multi, B->st);
+  launch_real_sum(B->b, B->st);
   launch_finalize(B->b, kMaskReal | kFlagAccum, B->st);
   launch_reduce_obs(B->b, kRedEnergies, B->st);
   st = read_obs(B, nullptr);
@@ -1206,9 +1213,9 @@ mdsc_status mdsc_profile_steps(mdsc_batch* B, int nsteps, int max_kernels, char*
   cudaSetDevice(B->device);
   mdsc_status st = ensure_forces(B);
   if (st) return st;
-  const char* kn[9] = {"integrate_first", "list_build", "wca", "real_pairs", "kspace_sum",
-                       "kspace_combine", "kspace_gather", "finalize", "reduce_obs"};
-  const int nk = 9;
+  const char* kn[10] = {"integrate_first", "list_build", "wca", "real_pairs", "real_sum", "kspace_sum",
+                        "kspace_combine", "kspace_gather", "finalize", "reduce_obs"};
+  const int nk = 10;
   std::vector<cudaEvent_t> ev(nk + 1);
   for (auto& e : ev) cudaEventCreate(&e);
   std::vector<double> acc(nk, 0.0);
@@ -1226,17 +1233,19 @@ mdsc_status mdsc_profile_steps(mdsc_batch* B, int nsteps, int max_kernels, char*
     cudaEventRecord(ev[3], B->st);
     launch_real_pairs(b, B->lo.multi, B->st);
     cudaEventRecord(ev[4], B->st);
+    launch_real_sum(b, B->st);
+    cudaEventRecord(ev[5], B->st);
     // the three k-space kernels, timed one by one
     launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 0, B->st);
-    cudaEventRecord(ev[5], B->st);
-    launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 1, B->st);
     cudaEventRecord(ev[6], B->st);
-    launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 2, B->st);
+    launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 1, B->st);
     cudaEventRecord(ev[7], B->st);
-    launch_finalize(b, kMaskAll | kFlagMoveP, B->st);
+    launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 2, B->st);
     cudaEventRecord(ev[8], B->st);
-    launch_reduce_obs(b, kRedStep, B->st);
+    launch_finalize(b, kMaskAll | kFlagMoveP, B->st);
     cudaEventRecord(ev[9], B->st);
+    launch_reduce_obs(b, kRedStep, B->st);
+    cudaEventRecord(ev[10], B->st);
     CU(cudaStreamSynchronize(B->st));
     for (int k = 0; k < nk; ++k) {
       float t = 0;

@@ -172,6 +172,25 @@ __device__ __forceinline__ double rot_kin(const Batch& b, int i, const double* O
   return kr;
 }
 
+// thermostat coordinates used by the second half kick: moveTher 0 then 1
+// (v25/functions.cpp:2193-2206), from the first-half kinetic energies of
+// every block of the system (read from L2: other blocks wrote them)
+__device__ __forceinline__ void xi_mid(const Batch& b, const SysDev& P, const SysState& S, int s,
+                                       double* xi2, double* Kf) {
+  double K0 = 0.0, K1 = 0.0;
+  for (int k = 0; k < P.nblk; ++k) {
+    K0 += __ldcg(&b.kin1[2 * (P.blk_off + k)]);
+    K1 += __ldcg(&b.kin1[2 * (P.blk_off + k) + 1]);
+  }
+  Kf[0] = 0.5 * K0;
+  Kf[1] = 0.5 * K1;
+  const double* nz = b.noise + ((long long)S.iter * b.nsys + s) * 4;
+  const double x1t = P.ex1 * S.xi[0] + P.cnoise * nz[0];
+  const double x1r = P.ex1 * S.xi[1] + P.cnoise * nz[2];
+  xi2[0] = x1t + P.dt * (2. * Kf[0] - P.ntemp3) / P.Q;
+  xi2[1] = x1r + P.dt * (2. * Kf[1] - P.ntemp3) / P.Q;
+}
+
 // ---------------------------------------------------------------------
 // first half of the step: moveTher(0), [renorm], moveP(first), moveX
 // ---------------------------------------------------------------------
@@ -240,46 +259,36 @@ __global__ void __launch_bounds__(kPartBlock) integrate_first_kernel(Batch b) {
     b.kin1[2 * lb] = tot[0];
     b.kin1[2 * lb + 1] = tot[1];
     b.dmax[lb] = soft_f2d(m);
+    // the system's last block to finish computes the second-half thermostat
+    // coordinates once (blocks' sums in block order: the same bits whichever
+    // block is last) and rearms the counter
+    __threadfence();
+    if (atomicAdd(&b.icnt[s], 1) == P.nblk - 1) {
+      __threadfence();
+      SysState& Sw = b.st[s];
+      double xi2[2], Kf[2];
+      xi_mid(b, P, Sw, s, xi2, Kf);
+      Sw.xi_mid[0] = xi2[0];
+      Sw.xi_mid[1] = xi2[1];
+      Sw.K_first[0] = Kf[0];
+      Sw.K_first[1] = Kf[1];
+      b.icnt[s] = 0;
+    }
   }
 }
 
-// thermostat coordinates used by the second half kick: moveTher 0 then 1
-// (v25/functions.cpp:2193-2206), from the first-half kinetic energies
-__device__ __forceinline__ void xi_mid(const Batch& b, const SysDev& P, const SysState& S, int s,
-                                       double* xi2, double* Kf) {
-  double K0 = 0.0, K1 = 0.0;
-  for (int k = 0; k < P.nblk; ++k) {
-    K0 += b.kin1[2 * (P.blk_off + k)];
-    K1 += b.kin1[2 * (P.blk_off + k) + 1];
-  }
-  Kf[0] = 0.5 * K0;
-  Kf[1] = 0.5 * K1;
-  const double* nz = b.noise + ((long long)S.iter * b.nsys + s) * 4;
-  const double x1t = P.ex1 * S.xi[0] + P.cnoise * nz[0];
-  const double x1r = P.ex1 * S.xi[1] + P.cnoise * nz[2];
-  xi2[0] = x1t + P.dt * (2. * Kf[0] - P.ntemp3) / P.Q;
-  xi2[1] = x1r + P.dt * (2. * Kf[1] - P.ntemp3) / P.Q;
-}
 
 // ---------------------------------------------------------------------
 // force assembly (+ ext_field) and optionally moveP(last)
 // ---------------------------------------------------------------------
 __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode) {
   __shared__ double sh[20 * kPartBlock / 32];
-  __shared__ double sx[2];
   const int2 bk = b.blk[blockIdx.x];
   const int s = bk.x;
   const SysDev& P = b.sys[s];
   const SysState& S = b.st[s];
   const int i = bk.y + threadIdx.x;
   const bool ok = i < P.part_off + P.n;
-  if ((mode & kFlagMoveP) && threadIdx.x == 0) {
-    double xi2[2], Kf[2];
-    xi_mid(b, P, S, s, xi2, Kf);
-    sx[0] = xi2[0];
-    sx[1] = xi2[1];
-  }
-  __syncthreads();
   // block sums: K_t, K_r, PT_kin (6), U_ext, then the WCA terms U, W, PT (9)
   // of this block's own candidate pairs
   FF acc[20];
@@ -346,13 +355,13 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
 #pragma unroll
       for (int c = 0; c < 6; ++c) acc6[c].hi = acc6[c].lo = 0.f;
       if (mode & kMaskReal) {
-        // sum of the tile partials of this dipole over all partner strips
-        const int X = loc / kTile, lx = loc % kTile, ns = P.nstrip;
-        const float* base = b.rpart + P.pp_off + (long long)X * ns * 6 * kTile + lx;
-#pragma unroll 4
-        for (int Y = 0; Y < ns; ++Y) {
+        // this dipole's tile partials summed over all partner strips
+        // (real_sum_kernel)
 #pragma unroll
-          for (int c = 0; c < 6; ++c) acc6[c] = ff_add(acc6[c], ff_of(base[((long long)Y * 6 + c) * kTile]));
+        for (int c = 0; c < 6; ++c) {
+          const float2 v = b.rsum[(long long)c * b.ndtot + g];
+          acc6[c].hi = v.x;
+          acc6[c].lo = v.y;
         }
       }
       if (mode & kMaskK) {
@@ -406,7 +415,8 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
     if (mode & kFlagMoveP) {
       // moveP last half (v25/functions.cpp:2150-2173)
       const double h = 0.5 * P.dt;
-      const double ft = 1. - h * sx[0], fr = 1. - h * sx[1];
+      // xi after moveTher 0 and 1, set by the first-half kernel
+      const double ft = 1. - h * S.xi_mid[0], fr = 1. - h * S.xi_mid[1];
       double psq = 0.0;
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
@@ -521,15 +531,11 @@ __global__ void __launch_bounds__(kRedThreads) reduce_obs_kernel(Batch b, int mo
         const int map[9] = {0, 1, 2, 1, 3, 4, 2, 4, 5};
         for (int c = 0; c < 9; ++c) ob.PT_kin[c] = pt6[map[c]];
         // moveTher mode 2 (v25/functions.cpp:2207-2213) closes the step
-        double xi2[2], Kf[2];
-        xi_mid(b, P, S, s, xi2, Kf);
         const double* nz = b.noise + ((long long)S.iter * b.nsys + s) * 4;
-        S.xi[0] = P.ex1 * xi2[0] + P.cnoise * nz[1];
-        S.xi[1] = P.ex1 * xi2[1] + P.cnoise * nz[3];
+        S.xi[0] = P.ex1 * S.xi_mid[0] + P.cnoise * nz[1];
+        S.xi[1] = P.ex1 * S.xi_mid[1] + P.cnoise * nz[3];
         S.strn[0] = nz[1];
         S.strn[1] = nz[3];
-        S.K_first[0] = Kf[0];
-        S.K_first[1] = Kf[1];
         S.step += 1;
         S.iter += 1;
         if (S.rebuild) S.list_builds += 1;

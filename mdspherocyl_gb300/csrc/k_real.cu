@@ -381,6 +381,44 @@ __global__ void __launch_bounds__(32) real_pairs_kernel(Batch b) {
   }
 }
 
+// Each dipole's real-space force and torque: the sum of its tile partials
+// over all partner strips, in strip order, in float-float.  One thread per
+// (dipole, component) of a particle block, component-major so that a warp
+// reads 32 consecutive dipoles of one component (coalesced) and the block
+// has six times as many independent load streams as dipoles.
+__global__ void __launch_bounds__(256) real_sum_kernel(Batch b) {
+  const int2 bk = b.blk[blockIdx.x];
+  const SysDev& P = b.sys[bk.x];
+  const int nd = P.nd;
+  const int p0 = bk.y - P.part_off;
+  const int np = min(kPartBlock, P.n - p0);
+  const int nloc = np * nd, loc0 = p0 * nd;
+  const int ns = P.nstrip;
+  const int ND = b.ndtot;
+  for (int it = threadIdx.x; it < 6 * nloc; it += blockDim.x) {
+    const int c = it / nloc, loc = loc0 + (it - c * nloc);
+    const int X = loc / kTile, lx = loc % kTile;
+    const float* base = b.rpart + P.pp_off + (long long)X * ns * 6 * kTile + c * kTile + lx;
+    float hi = 0.f, lo = 0.f;
+#pragma unroll 8
+    for (int Y = 0; Y < ns; ++Y) {
+      // float-float accumulation (TwoSum)
+      const float v = base[(long long)Y * 6 * kTile];
+      const float sum = hi + v;
+      const float bb = sum - hi;
+      lo += (hi - (sum - bb)) + (v - bb);
+      hi = sum;
+    }
+    const float r = hi + lo;
+    b.rsum[(long long)c * ND + P.dip_off + loc] = make_float2(r, lo - (r - hi));
+  }
+}
+
+void launch_real_sum(const Batch& b, cudaStream_t s) {
+  if (b.ntiles == 0 || b.nblk == 0) return;
+  real_sum_kernel<<<b.nblk, 256, 0, s>>>(b);
+}
+
 void launch_real_pairs(const Batch& b, bool multi, cudaStream_t s) {
   if (b.ntiles == 0) return;
   if (multi)

@@ -136,6 +136,7 @@ struct Batch {
   float* dm;     // 3 ndip dipole moment vectors mu*o (SoA blocks)
   // force components
   float* rpart;  // real-space partials
+  float2* rsum;  // 6 * ndtot: each dipole's real-space force and torque over all strips, float-float, component-major
   float* tileE;  // 10 per tile: U, PT[9]
   int4* tiles;   // (sys, I, J, 0)
   int2* wlist;   // WCA work list: (candidate slot, system), n * kMaxC at most
@@ -159,6 +160,7 @@ struct Batch {
   double* kG;    // 6 per particle chunk: sum of m m^T (one dipole per particle)
   double* kGs;   // 6 per system: the chunk sums added in chunk order
   int* kgcnt;    // per system: chunks done this step (the last one adds them)
+  int* icnt;     // per system: first-half blocks done this step (the last one sets xi_mid)
   float2* Fk;    // 3 ndip: k-space force on each dipole, float-float (hi, lo)
   float2* Tk;    // 3 ndip: k-space torque m x G, float-float
   // integrator partials, per block
