@@ -281,6 +281,9 @@ def run_ours(args):
                  "batched_over_plain_device": value / pv_dev, "batched_over_plain_wall": value / pv_wall}
 
     # ---- kernel times (events per kernel, serialised) ----
+    tun = bt.tuning()
+    tuning = {k: tun[k] for k in ("rp_warps", "rsum_threads", "wca_blocks", "kg_scalar")}
+    tuning["chosen_by"] = "autotuner (mdsc_autotune)" if tun["tuned"] else "defaults"
     prof = bt.profile(max(2, min(5, args.steps)))
     pairs = sum(s.n * (s.n - 1) // 2 for s in specs)
     rp_ms = prof.get("real_pairs", float("nan"))
@@ -338,7 +341,7 @@ def run_ours(args):
                        "N_range": [min(s.n for s in specs), max(s.n for s in specs)], "ksq_max": 36,
                        "alpha": "6/L_box", "real_space": "all minimum-image pairs", "dt": 1e-3,
                        "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{ws}",
-                       "graph": "one CUDA graph per step"},
+                       "graph": "one CUDA graph per step", "launch_mappings": tuning},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": bytes_h2d,
                     "d2h_bytes_per_step": bytes_d2h},
             "gpu_launches": launches * args.steps,

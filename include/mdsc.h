@@ -209,6 +209,23 @@ double mdsc_last_device_ms(const mdsc_batch* b);
 mdsc_status mdsc_profile_steps(mdsc_batch* b, int nsteps, int max_kernels, char* names,
                                size_t name_stride, double* ms_per_launch, int* n_kernels);
 
+/* ---- autotuner -------------------------------------------------------- */
+/* Chooses the launch mappings (real-space tiles per block, strip-sum block
+   size, grid of the FP64 WCA evaluation, k-space gather form) by timing each
+   candidate on the batch's current state, and keeps the fastest.  Only
+   mappings that leave every result bit-identical are candidates, so a
+   system's trajectory does not depend on the choice or on the batch it is
+   in.  mdsc_step runs it before its first step unless the environment sets
+   MDSC_AUTOTUNE=0; choices are cached per process by the batch's size class
+   (force = 1 times again regardless).  No counterpart in the reference. */
+mdsc_status mdsc_autotune(mdsc_batch* b, int force);
+/* The mappings in use: values[0..4] = tiles per block, strip-sum threads,
+   WCA evaluation blocks, gather form (0 packed, 1 one particle per thread),
+   tuned (1 once chosen); log: the last tuning's timings (may be NULL). */
+mdsc_status mdsc_tuning(const mdsc_batch* b, int* values, char* log, size_t len);
+/* Sets the mappings by hand (values[0..3] as above) instead of tuning. */
+mdsc_status mdsc_set_tuning(mdsc_batch* b, const int* values);
+
 /* ---- allocation-free variant ------------------------------------------- */
 /* Real-space Ewald forces, torques (without lever arms), energy and
    pressure tensor of one system of ndip dipoles, one per particle, for

@@ -4,8 +4,12 @@
 #include <cmath>
 #include <cstddef>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "host_util.hpp"
@@ -320,6 +324,8 @@ struct mdsc_batch {
   cudaEvent_t t_beg = nullptr, t_end = nullptr;  // device time of the last mdsc_step
   double last_ms = 0.0;
   int launches = 0;
+  int tuned = 0;          // launch mappings chosen (autotuner or cache)
+  std::string tune_log;   // the autotuner's timings, for mdsc_tuning
   std::string err;
 };
 
@@ -367,6 +373,108 @@ mdsc_status eval_forces(mdsc_batch* B, int force_list) {
   for (int s = 0; s < B->nsys; ++s) {
     B->built[s] = 1;
     B->have_forces[s] = 1;
+  }
+  return MDSC_OK;
+}
+
+mdsc_status ensure_forces(mdsc_batch* B);
+
+// ---------------------------------------------------------------------
+// autotuner: launch mappings timed on the batch's own state
+// ---------------------------------------------------------------------
+// Only mappings that leave every result unchanged are tuned (Tuning,
+// mdsc_dev.cuh), so a system gives the same bits whatever batch it runs in
+// and whatever the tuner picks.  Choices are cached per process by a size
+// class of the batch (tiles, particles, k-vectors: half-octaves), so a
+// server that repacks batches of similar size tunes once.
+struct TuneKey {
+  int tiles, parts, ks, maxnd;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(tiles, parts, ks, maxnd) < std::tie(o.tiles, o.parts, o.ks, o.maxnd);
+  }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, Tuning> g_tune_cache;
+
+TuneKey tune_key(const mdsc_batch* B) {
+  auto cls = [](long long x) { return x <= 0 ? -1 : (int)std::lround(2.0 * std::log2((double)x)); };
+  return TuneKey{cls(B->b.ntiles), cls(B->lo.ntot), cls(B->b.nktot), B->lo.maxnd};
+}
+
+// average device time (ms) of `launch` over `reps` runs after one warm-up
+template <class F>
+double time_launches(mdsc_batch* B, int reps, F&& launch) {
+  launch();
+  cudaEventRecord(B->t_beg, B->st);
+  for (int r = 0; r < reps; ++r) launch();
+  cudaEventRecord(B->t_end, B->st);
+  cudaEventSynchronize(B->t_end);
+  float t = 0.f;
+  cudaEventElapsedTime(&t, B->t_beg, B->t_end);
+  return t / reps;
+}
+
+mdsc_status autotune(mdsc_batch* B, int force, int reps) {
+  const TuneKey key = tune_key(B);
+  if (!force) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      B->b.tune = it->second;
+      B->tuned = 1;
+      return MDSC_OK;
+    }
+  }
+  mdsc_status st = ensure_forces(B);
+  if (st) return st;
+  Batch b = batch_with_noise(B, 0);
+  Tuning best = b.tune;
+  B->tune_log.clear();
+  char line[160];
+  auto pick = [&](const char* what, const int* cand, int nc, int& field, auto&& launch) {
+    double tbest = 1e30;
+    int vbest = field;
+    for (int k = 0; k < nc; ++k) {
+      field = cand[k];
+      const double t = time_launches(B, reps, launch);
+      snprintf(line, sizeof line, "%s=%d %.4f ms; ", what, cand[k], t);
+      B->tune_log += line;
+      if (t < tbest) {
+        tbest = t;
+        vbest = cand[k];
+      }
+    }
+    field = vbest;
+  };
+  // WCA evaluation grid (the screen runs with it: it refills the work list)
+  {
+    const int cand[4] = {152 * 2, 152 * 4, 152 * 8, 152 * 16};
+    pick("wca_blocks", cand, 4, b.tune.wca_blocks, [&] { launch_wca(b, B->st); });
+  }
+  // real-space tiles per block, then the strip-sum block size
+  if (b.ntiles > 0) {
+    const int cand[3] = {1, 2, 4};
+    pick("rp_warps", cand, 3, b.tune.rp_warps, [&] { launch_real_pairs(b, B->lo.multi, B->st); });
+    const int cand2[3] = {128, 256, 512};
+    pick("rsum_threads", cand2, 3, b.tune.rsum_threads, [&] { launch_real_sum(b, B->st); });
+  }
+  // k-space gather form (single-dipole systems)
+  if (b.nktot > 0 && B->lo.maxnd <= 1) {
+    launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 0, B->st);
+    launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 1, B->st);
+    const int cand[2] = {0, 1};
+    pick("kg_scalar", cand, 2, b.tune.kg_scalar, [&] {
+      launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 2, B->st);
+    });
+  }
+  CU(cudaStreamSynchronize(B->st));
+  CU(cudaGetLastError());
+  best = b.tune;
+  B->b.tune = best;
+  B->tuned = 1;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = best;
   }
   return MDSC_OK;
 }
@@ -1146,6 +1254,16 @@ mdsc_status mdsc_step(mdsc_batch* B, int nsteps, mdsc_observables* obs) {
   cudaSetDevice(B->device);
   mdsc_status st = ensure_forces(B);
   if (st) return st;
+  if (!B->tuned && !B->graph[0]) {
+    // launch mappings by the autotuner (MDSC_AUTOTUNE=0: keep the defaults)
+    const char* env = std::getenv("MDSC_AUTOTUNE");
+    if (env && env[0] == '0') {
+      B->tuned = 1;
+    } else {
+      st = autotune(B, 0, 5);
+      if (st) return st;
+    }
+  }
   for (int w = 0; w < 2; ++w)
     if (!B->graph[w]) {
       st = capture_step(B, w);
@@ -1198,6 +1316,53 @@ mdsc_status mdsc_step(mdsc_batch* B, int nsteps, mdsc_observables* obs) {
 }
 
 double mdsc_last_device_ms(const mdsc_batch* B) { return B ? B->last_ms : 0.0; }
+
+mdsc_status mdsc_autotune(mdsc_batch* B, int force) {
+  if (!B) return MDSC_ERR_BAD_ARG;
+  cudaSetDevice(B->device);
+  const mdsc_status st = autotune(B, force, 5);
+  if (st) return st;
+  // the step graphs hold the old mappings: capture them again at the next step
+  for (int w = 0; w < 2; ++w)
+    if (B->graph[w]) {
+      cudaGraphExecDestroy(B->graph[w]);
+      B->graph[w] = nullptr;
+    }
+  return MDSC_OK;
+}
+
+mdsc_status mdsc_set_tuning(mdsc_batch* B, const int* values) {
+  if (!B || !values) return MDSC_ERR_BAD_ARG;
+  const int w = values[0], rt = values[1], wb = values[2], kg = values[3];
+  if (!(w == 1 || w == 2 || w == 4) || !(rt == 128 || rt == 256 || rt == 512) || wb < 1 || wb > (1 << 20) ||
+      !(kg == 0 || kg == 1))
+    return fail(B, MDSC_ERR_BAD_ARG, "mdsc_set_tuning: tiles per block 1/2/4, strip-sum threads 128/256/512, "
+                                     "WCA blocks 1..2^20, gather form 0/1");
+  B->b.tune.rp_warps = w;
+  B->b.tune.rsum_threads = rt;
+  B->b.tune.wca_blocks = wb;
+  B->b.tune.kg_scalar = kg;
+  B->tuned = 1;
+  for (int k = 0; k < 2; ++k)
+    if (B->graph[k]) {
+      cudaGraphExecDestroy(B->graph[k]);
+      B->graph[k] = nullptr;
+    }
+  return MDSC_OK;
+}
+
+mdsc_status mdsc_tuning(const mdsc_batch* B, int* values, char* log, size_t len) {
+  if (!B) return MDSC_ERR_BAD_ARG;
+  if (values) {
+    values[0] = B->b.tune.rp_warps;
+    values[1] = B->b.tune.rsum_threads;
+    values[2] = B->b.tune.wca_blocks;
+    values[3] = B->b.tune.kg_scalar;
+    values[4] = B->tuned;
+  }
+  if (log && len) snprintf(log, len, "%s", B->tune_log.c_str());
+  return MDSC_OK;
+}
 
 mdsc_status mdsc_observe(mdsc_batch* B, mdsc_observables* obs) {
   if (!B) return MDSC_ERR_BAD_ARG;

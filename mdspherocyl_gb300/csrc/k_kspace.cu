@@ -486,9 +486,76 @@ __global__ void __launch_bounds__(kPartBlock / 2) kgather1_kernel(Batch b) {
   }
 }
 
+// The same gather with one particle per thread (128 threads per block):
+// twice the warps of the packed form and no paired instructions.  Every
+// particle goes through the same IEEE operations in the same order as in
+// the packed kernel (explicit _rn intrinsics, no contraction), so the two
+// forms give identical bits and the autotuner may pick either.
+__global__ void __launch_bounds__(kPartBlock) kgather1s_kernel(Batch b) {
+  __shared__ int4 skn[kKBlock];
+  __shared__ float4 skv[kKBlock];
+  __shared__ float2 sks[kKBlock];
+  const int2 bk = b.blk[blockIdx.x];
+  const SysDev& P = b.sys[bk.x];
+  const int t = threadIdx.x;
+  const int i0 = bk.y + t;
+  const bool ok0 = i0 < P.part_off + P.n;
+  const int ND_all = b.ndtot;
+  const int g0 = ok0 ? P.dip_off + (i0 - P.part_off) : 0;
+  const uint32_t ux0 = b.dfx[g0], uy0 = b.dfx[ND_all + g0], uz0 = b.dfx[2 * ND_all + g0];
+  const float mx = ok0 ? b.dm[g0] : 0.f, my = ok0 ? b.dm[ND_all + g0] : 0.f,
+              mz = ok0 ? b.dm[2 * ND_all + g0] : 0.f;
+  float fo[6], fc[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) fo[c] = fc[c] = 0.f;
+  for (int k0 = 0; k0 < P.nk; k0 += kKBlock) {
+    const int nk = min(kKBlock, P.nk - k0);
+    __syncthreads();
+    for (int q = t; q < nk; q += kPartBlock) {
+      skn[q] = b.kn[P.k_off + k0 + q];
+      skv[q] = b.kv[P.k_off + k0 + q];
+      sks[q] = b.kS[P.k_off + k0 + q];
+    }
+    __syncthreads();
+    float ft[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) ft[c] = 0.f;
+#pragma unroll 2
+    for (int q = 0; q < nk; ++q) {
+      const int4 n = skn[q];
+      const float4 kv = skv[q];
+      const float2 vS = sks[q];
+      float c, sn;
+      phase_exp(ux0, uy0, uz0, n, c, sn);
+      const float a = __fmaf_rn(mz, kv.z, __fmaf_rn(my, kv.y, __fmul_rn(mx, kv.x)));
+      const float va = __fmul_rn(kv.w, a);
+      const float Dr = __fmaf_rn(-va, c, vS.x);
+      const float Dn = __fmaf_rn(va, sn, vS.y);
+      const float fF = __fmul_rn(a, __fmaf_rn(c, Dn, __fmul_rn(sn, Dr)));
+      const float fT = __fmaf_rn(sn, Dn, __fmul_rn(-c, Dr));
+      ft[0] = __fmaf_rn(fF, kv.x, ft[0]);
+      ft[1] = __fmaf_rn(fF, kv.y, ft[1]);
+      ft[2] = __fmaf_rn(fF, kv.z, ft[2]);
+      ft[3] = __fmaf_rn(fT, kv.x, ft[3]);
+      ft[4] = __fmaf_rn(fT, kv.y, ft[4]);
+      ft[5] = __fmaf_rn(fT, kv.z, ft[5]);
+    }
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      const float y = __fadd_rn(ft[c], -fc[c]);
+      const float tt = __fadd_rn(fo[c], y);
+      fc[c] = __fadd_rn(__fadd_rn(tt, -fo[c]), -y);
+      fo[c] = tt;
+    }
+  }
+  if (ok0) store_kout(b, g0, fo, fc, mx, my, mz);
+}
+
 template <int ND>
 static void launch_kgather(const Batch& b, cudaStream_t s) {
-  if (ND == 1)
+  if (ND == 1 && b.tune.kg_scalar)
+    kgather1s_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
+  else if (ND == 1)
     kgather1_kernel<<<b.nblk, kPartBlock / 2, 0, s>>>(b);
   else
     kgather_kernel<ND><<<b.nblk, kPartBlock, 0, s>>>(b);

@@ -247,18 +247,28 @@ __device__ __forceinline__ void tile_loop(const PairConst& K, Lane2& s, const ui
 
 }  // namespace
 
-template <bool MULTI>
-__global__ void __launch_bounds__(32) real_pairs_kernel(Batch b) {
-  __shared__ uint4 sj[kTile];    // fixed-point x, y, z and owner of the j-dipoles
-  __shared__ float4 smj[kTile];  // their moments
-  __shared__ float4 sa4[kTile];  // j-side sums: F x, y, z and T x
-  __shared__ float2 sa2[kTile];  // T y, z
+// W warps per block, one tile per warp (tile = W * blockIdx.x + warp): the
+// block size changes how tiles are grouped for scheduling, never what a
+// tile computes, so every W gives the same bits (the autotuner picks W).
+template <bool MULTI, int W>
+__global__ void __launch_bounds__(32 * W) real_pairs_kernel(Batch b) {
+  __shared__ uint4 sj_all[W][kTile];    // fixed-point x, y, z and owner of the j-dipoles
+  __shared__ float4 smj_all[W][kTile];  // their moments
+  __shared__ float4 sa4_all[W][kTile];  // j-side sums: F x, y, z and T x
+  __shared__ float2 sa2_all[W][kTile];  // T y, z
+  const int wid = threadIdx.x >> 5;
+  const int tile = W * blockIdx.x + wid;
+  if (tile >= b.ntiles) return;
+  uint4* sj = sj_all[wid];
+  float4* smj = smj_all[wid];
+  float4* sa4 = sa4_all[wid];
+  float2* sa2 = sa2_all[wid];
 
-  const int4 tl = b.tiles[blockIdx.x];
+  const int4 tl = b.tiles[tile];
   const SysDev& P = b.sys[tl.x];
   const int I = tl.y, J = tl.z;
   const bool diag = (I == J);
-  const int lane = threadIdx.x;
+  const int lane = threadIdx.x & 31;
   const int ndip = P.ndip;
   const int ND = b.ndtot;
 
@@ -377,7 +387,7 @@ __global__ void __launch_bounds__(32) real_pairs_kernel(Batch b) {
   }
   if (lane == 0) {
 #pragma unroll
-    for (int c = 0; c < 10; ++c) b.tileE[(long long)blockIdx.x * 10 + c] = red[c];
+    for (int c = 0; c < 10; ++c) b.tileE[(long long)tile * 10 + c] = red[c];
   }
 }
 
@@ -386,7 +396,7 @@ __global__ void __launch_bounds__(32) real_pairs_kernel(Batch b) {
 // (dipole, component) of a particle block, component-major so that a warp
 // reads 32 consecutive dipoles of one component (coalesced) and the block
 // has six times as many independent load streams as dipoles.
-__global__ void __launch_bounds__(256) real_sum_kernel(Batch b) {
+__global__ void __launch_bounds__(512) real_sum_kernel(Batch b) {
   const int2 bk = b.blk[blockIdx.x];
   const SysDev& P = b.sys[bk.x];
   const int nd = P.nd;
@@ -416,15 +426,23 @@ __global__ void __launch_bounds__(256) real_sum_kernel(Batch b) {
 
 void launch_real_sum(const Batch& b, cudaStream_t s) {
   if (b.ntiles == 0 || b.nblk == 0) return;
-  real_sum_kernel<<<b.nblk, 256, 0, s>>>(b);
+  real_sum_kernel<<<b.nblk, b.tune.rsum_threads, 0, s>>>(b);
 }
 
 void launch_real_pairs(const Batch& b, bool multi, cudaStream_t s) {
   if (b.ntiles == 0) return;
-  if (multi)
-    real_pairs_kernel<true><<<b.ntiles, 32, 0, s>>>(b);
-  else
-    real_pairs_kernel<false><<<b.ntiles, 32, 0, s>>>(b);
+  const int W = b.tune.rp_warps;
+  const int grid = cdiv(b.ntiles, W);
+  if (W == 4) {
+    if (multi) real_pairs_kernel<true, 4><<<grid, 128, 0, s>>>(b);
+    else real_pairs_kernel<false, 4><<<grid, 128, 0, s>>>(b);
+  } else if (W == 2) {
+    if (multi) real_pairs_kernel<true, 2><<<grid, 64, 0, s>>>(b);
+    else real_pairs_kernel<false, 2><<<grid, 64, 0, s>>>(b);
+  } else {
+    if (multi) real_pairs_kernel<true, 1><<<b.ntiles, 32, 0, s>>>(b);
+    else real_pairs_kernel<false, 1><<<b.ntiles, 32, 0, s>>>(b);
+  }
 }
 
 }  // namespace mdsc

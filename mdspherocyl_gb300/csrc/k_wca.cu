@@ -353,14 +353,12 @@ __global__ void __launch_bounds__(kPartBlock) cluster_compress_kernel(Batch b) {
 void launch_list_build(const Batch& b, int force_all, cudaStream_t s) {
   if (b.nblk) list_build_kernel<<<b.nblk, kPartBlock, 0, s>>>(b, force_all);
 }
-// eval grid: enough 128-thread blocks to fill every SM's FP64 unit; each
-// thread loops over the work list
-constexpr int kWcaEvalBlocks = 152 * 8;
 void launch_wca(const Batch& b, cudaStream_t s) {
   if (!b.nblk) return;
   cudaMemsetAsync(b.wlist_n, 0, sizeof(int), s);
   wca_screen_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
-  wca_eval_kernel<<<kWcaEvalBlocks, 128, 0, s>>>(b);
+  // a fixed grid (chosen by the autotuner); each thread loops over the list
+  wca_eval_kernel<<<b.tune.wca_blocks, 128, 0, s>>>(b);
 }
 void launch_cluster_bonds(const Batch& b, cudaStream_t s) {
   if (b.nblk) cluster_bonds_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);

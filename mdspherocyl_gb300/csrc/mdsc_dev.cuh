@@ -104,8 +104,19 @@ struct SysObs {
 };
 
 // One batch, device pointers.
+// Launch mappings the autotuner chooses.  Each one changes only how work
+// is grouped into blocks and grids, never the arithmetic or the order of a
+// sum, so every choice gives the same bits.
+struct Tuning {
+  int rp_warps = 1;          // real-space tiles (warps) per block: 1, 2 or 4
+  int rsum_threads = 256;    // strip-sum block size: 128, 256 or 512
+  int wca_blocks = 152 * 8;  // grid of the FP64 WCA evaluation
+  int kg_scalar = 0;         // k-space gather: 0 two particles per thread, 1 one
+};
+
 struct Batch {
   int nsys, ntot, ndtot, nktot, ntiles, nblk;
+  Tuning tune;
   const SysDev* sys;
   SysState* st;
   SysObs* obs;

@@ -36,6 +36,7 @@ EXPORTS = [
     "mdsc_renorm", "mdsc_neigh_list", "mdsc_check_list", "mdsc_clust_conf", "mdsc_step",
     "mdsc_observe", "mdsc_launches_per_step", "mdsc_stream", "mdsc_profile_steps",
     "mdsc_place_rods", "mdsc_last_device_ms", "mdsc_force_dipR_noalloc", "mdsc_transfer",
+    "mdsc_autotune", "mdsc_tuning", "mdsc_set_tuning",
 ]
 
 
@@ -122,6 +123,9 @@ def load(build: bool = True) -> ctypes.CDLL:
         "mdsc_stream": (c_void_p, [c_void_p]),
         "mdsc_last_device_ms": (c_double, [c_void_p]),
         "mdsc_transfer": (c_int, [c_void_p, c_int, c_void_p, c_int]),
+        "mdsc_autotune": (c_int, [c_void_p, c_int]),
+        "mdsc_tuning": (c_int, [c_void_p, _ip, c_char_p, c_size_t]),
+        "mdsc_set_tuning": (c_int, [c_void_p, _ip]),
         "mdsc_force_dipR_noalloc": (c_int, [c_int, c_void_p, c_void_p, _dp, c_double, c_void_p, c_void_p,
                                             c_void_p, c_void_p]),
         "mdsc_profile_steps": (c_int, [c_void_p, c_int, c_int, c_char_p, c_size_t, _dp, _ip]),
@@ -329,6 +333,24 @@ class Batch:
         obs = (Observables * self.nsys)()
         self._check(self.lib.mdsc_observe(self.h, obs), "mdsc_observe")
         return [o.as_dict() for o in obs]
+
+    def autotune(self, force: bool = False) -> dict:
+        """Choose the launch mappings now (mdsc_autotune) and return them."""
+        self._check(self.lib.mdsc_autotune(self.h, int(force)), "mdsc_autotune")
+        return self.tuning()
+
+    def set_tuning(self, rp_warps: int, rsum_threads: int, wca_blocks: int, kg_scalar: int) -> None:
+        """Pin the launch mappings (mdsc_set_tuning) instead of tuning them."""
+        v = np.array([rp_warps, rsum_threads, wca_blocks, kg_scalar], dtype=np.int32)
+        self._check(self.lib.mdsc_set_tuning(self.h, v.ctypes.data_as(_ip)), "mdsc_set_tuning")
+
+    def tuning(self) -> dict:
+        """The launch mappings in use and the last tuning's timings."""
+        v = np.zeros(5, dtype=np.int32)
+        buf = ctypes.create_string_buffer(4096)
+        self._check(self.lib.mdsc_tuning(self.h, v.ctypes.data_as(_ip), buf, 4096), "mdsc_tuning")
+        return {"rp_warps": int(v[0]), "rsum_threads": int(v[1]), "wca_blocks": int(v[2]),
+                "kg_scalar": int(v[3]), "tuned": bool(v[4]), "log": buf.value.decode()}
 
     def profile(self, nsteps: int):
         nmax, stride = 16, 32
