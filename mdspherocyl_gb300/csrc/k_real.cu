@@ -76,8 +76,8 @@ __device__ __forceinline__ float rsqrt_approx(float y) {
 // minimum-image separation of two fixed-point coordinates: the integer
 // difference times L / 2^32, the scale carried as hi + lo so that its FP32
 // rounding does not bias every separation of the system the same way
-__device__ __forceinline__ f2 fix_diff2(uint32_t a0, uint32_t a1, uint32_t bj, f2 hi, f2 lo) {
-  const f2 k = make_float2((float)(int32_t)(a0 - bj), (float)(int32_t)(a1 - bj));
+__device__ __forceinline__ f2 fix_diff2(uint32_t a0, uint32_t a1, uint32_t b0, uint32_t b1, f2 hi, f2 lo) {
+  const f2 k = make_float2((float)(int32_t)(a0 - b0), (float)(int32_t)(a1 - b1));
   return fma2(k, hi, mul2(k, lo));
 }
 
@@ -105,28 +105,28 @@ struct Lane2 {
   f2 F[3], T[3], pt[9], U, Uc;
 };
 
-// one step of the tile loop: the lane's two i-dipoles against j = lj
-template <bool MASKED, bool MULTI>
-__device__ __forceinline__ void tile_step(const PairConst& K, Lane2& s, const uint4 jp, const float4 jm,
-                                          bool diag, int lane, int lj, int jvalid, float4& ja4, float2& ja2) {
+// j-side results of one step for the two halves (half 0 pairs i-dipole
+// lane with j0, half 1 pairs lane + 32 with j1)
+struct JOut {
+  f2 fx, fy, fz, tx, ty, tz;
+};
+
+// one step of a tile loop: the lane's two i-dipoles against j0 (half 0)
+// and j1 (half 1) -- the same j in off-diagonal tiles.  Pairs masked off
+// (a0, a1 false) contribute exactly zero.
+template <bool MASKED>
+__device__ __forceinline__ void tile_step(const PairConst& K, Lane2& s, const uint4 jp0, const float4 jm0,
+                                          const uint4 jp1, const float4 jm1, bool a0, bool a1, JOut& o) {
   f2 mix = s.mx, miy = s.my, miz = s.mz;
-  bool a0 = true, a1 = true;
   if (MASKED) {
-    const bool jv = lj < jvalid;
-    a0 = s.ok0 && jv && (!diag || lj > lane);
-    a1 = s.ok1 && jv && (!diag || lj > lane + 32);
-    if (MULTI) {
-      a0 = a0 && (s.own0 != (int)jp.w);
-      a1 = a1 && (s.own1 != (int)jp.w);
-    }
     const f2 on = make_float2(a0 ? 1.f : 0.f, a1 ? 1.f : 0.f);
     mix = mul2(mix, on);
     miy = mul2(miy, on);
     miz = mul2(miz, on);
   }
-  const f2 dx = fix_diff2(s.x0, s.x1, jp.x, K.Lhx, K.Llx);
-  const f2 dy = fix_diff2(s.y0, s.y1, jp.y, K.Lhy, K.Lly);
-  const f2 dz = fix_diff2(s.z0, s.z1, jp.z, K.Lhz, K.Llz);
+  const f2 dx = fix_diff2(s.x0, s.x1, jp0.x, jp1.x, K.Lhx, K.Llx);
+  const f2 dy = fix_diff2(s.y0, s.y1, jp0.y, jp1.y, K.Lhy, K.Lly);
+  const f2 dz = fix_diff2(s.z0, s.z1, jp0.z, jp1.z, K.Lhz, K.Llz);
   f2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
   if (MASKED) {
     r2.x = a0 ? r2.x : 1.f;
@@ -178,7 +178,7 @@ __device__ __forceinline__ void tile_step(const PairConst& K, Lane2& s, const ui
   const f2 Cc = fma2(h2, mul2(a2C, add2(a2r2, b2(-1.f))), fma2(nh3, mul2(a2a2rC, add2(a2r2, b2(-3.f))), C));
 
   // dipole-dipole energy, force on i, torques without lever arm
-  const f2 mjx = b2(jm.x), mjy = b2(jm.y), mjz = b2(jm.z);
+  const f2 mjx = make_float2(jm0.x, jm1.x), mjy = make_float2(jm0.y, jm1.y), mjz = make_float2(jm0.z, jm1.z);
   const f2 mimj = fma2(miz, mjz, fma2(miy, mjy, mul2(mix, mjx)));
   const f2 mir = fma2(miz, dz, fma2(miy, dy, mul2(mix, dx)));
   const f2 mjr = fma2(mjz, dz, fma2(mjy, dy, mul2(mjx, dx)));
@@ -206,12 +206,12 @@ __device__ __forceinline__ void tile_step(const PairConst& K, Lane2& s, const ui
   s.T[0] = add2(s.T[0], tix);
   s.T[1] = add2(s.T[1], tiy);
   s.T[2] = add2(s.T[2], tiz);
-  ja4.x -= fx.x + fx.y;
-  ja4.y -= fy.x + fy.y;
-  ja4.z -= fz.x + fz.y;
-  ja4.w += tjx.x + tjx.y;
-  ja2.x += tjy.x + tjy.y;
-  ja2.y += tjz.x + tjz.y;
+  o.fx = fx;
+  o.fy = fy;
+  o.fz = fz;
+  o.tx = tjx;
+  o.ty = tjy;
+  o.tz = tjz;
   // Kahan: U += u
   const f2 yk = sub2(u, s.Uc);
   const f2 tk = add2(s.U, yk);
@@ -228,19 +228,84 @@ __device__ __forceinline__ void tile_step(const PairConst& K, Lane2& s, const ui
   s.pt[8] = fma2(dz, fz, s.pt[8]);
 }
 
+// Off-diagonal tile (strips I < J): 64 steps, at step t lane l pairs both
+// its i-dipoles with j = (l + t) mod 64; the two halves' j-side terms are
+// added into that j's sums.
 template <bool MASKED, bool MULTI>
 __device__ __forceinline__ void tile_loop(const PairConst& K, Lane2& s, const uint4* sj, const float4* smj,
-                                          float4* sa4, float2* sa2, bool diag, int lane, int jvalid) {
+                                          float4* sa4, float2* sa2, int lane, int jvalid) {
 #pragma unroll 1
   for (int t = 0; t < kTile; ++t) {
     const int lj = (lane + t) & (kTile - 1);
     const uint4 jp = sj[lj];
     const float4 jm = smj[lj];
+    bool a0 = true, a1 = true;
+    if (MASKED) {
+      const bool jv = lj < jvalid;
+      a0 = s.ok0 && jv;
+      a1 = s.ok1 && jv;
+      if (MULTI) {
+        a0 = a0 && (s.own0 != (int)jp.w);
+        a1 = a1 && (s.own1 != (int)jp.w);
+      }
+    }
+    JOut o;
+    tile_step<MASKED>(K, s, jp, jm, jp, jm, a0, a1, o);
     float4 ja4 = sa4[lj];
     float2 ja2 = sa2[lj];
-    tile_step<MASKED, MULTI>(K, s, jp, jm, diag, lane, lj, jvalid, ja4, ja2);
+    ja4.x -= o.fx.x + o.fx.y;
+    ja4.y -= o.fy.x + o.fy.y;
+    ja4.z -= o.fz.x + o.fz.y;
+    ja4.w += o.tx.x + o.tx.y;
+    ja2.x += o.ty.x + o.ty.y;
+    ja2.y += o.tz.x + o.tz.y;
     sa4[lj] = ja4;
     sa2[lj] = ja2;
+    __syncwarp();
+  }
+}
+
+// Diagonal tile (strip I with itself): every unordered pair of its 64
+// dipoles once, in 32 steps.  At step t (1..32) i-dipole x = l (half 0) and
+// x = l + 32 (half 1) pair with (x + t) mod 64: each pair at cyclic distance
+// d < 32 is met once from its lower end, d > 32 once from its upper end,
+// and d = 32 from half 0 only.  The 64 j's of a step are distinct.
+template <bool MULTI>
+__device__ __forceinline__ void diag_loop(const PairConst& K, Lane2& s, const uint4* sj, const float4* smj,
+                                          float4* sa4, float2* sa2, int lane, int jvalid) {
+#pragma unroll 1
+  for (int t = 1; t <= kTile / 2; ++t) {
+    const int j0 = (lane + t) & (kTile - 1), j1 = (lane + 32 + t) & (kTile - 1);
+    const uint4 jp0 = sj[j0], jp1 = sj[j1];
+    const float4 jm0 = smj[j0], jm1 = smj[j1];
+    bool a0 = s.ok0 && j0 < jvalid;
+    bool a1 = s.ok1 && j1 < jvalid && t < kTile / 2;
+    if (MULTI) {
+      a0 = a0 && (s.own0 != (int)jp0.w);
+      a1 = a1 && (s.own1 != (int)jp1.w);
+    }
+    JOut o;
+    tile_step<true>(K, s, jp0, jm0, jp1, jm1, a0, a1, o);
+    float4 ja4 = sa4[j0];
+    float2 ja2 = sa2[j0];
+    ja4.x -= o.fx.x;
+    ja4.y -= o.fy.x;
+    ja4.z -= o.fz.x;
+    ja4.w += o.tx.x;
+    ja2.x += o.ty.x;
+    ja2.y += o.tz.x;
+    sa4[j0] = ja4;
+    sa2[j0] = ja2;
+    ja4 = sa4[j1];
+    ja2 = sa2[j1];
+    ja4.x -= o.fx.y;
+    ja4.y -= o.fy.y;
+    ja4.z -= o.fz.y;
+    ja4.w += o.tx.y;
+    ja2.x += o.ty.y;
+    ja2.y += o.tz.y;
+    sa4[j1] = ja4;
+    sa2[j1] = ja2;
     __syncwarp();
   }
 }
@@ -328,10 +393,12 @@ __global__ void __launch_bounds__(32 * W) real_pairs_kernel(Batch b) {
   const int jvalid = min(kTile, ndip - J * kTile);
   // no pair of this tile is skipped: the fast loop without masks
   const bool full = !MULTI && !diag && jvalid == kTile;
-  if (full)
-    tile_loop<false, MULTI>(K, s, sj, smj, sa4, sa2, diag, lane, jvalid);
+  if (diag)
+    diag_loop<MULTI>(K, s, sj, smj, sa4, sa2, lane, jvalid);
+  else if (full)
+    tile_loop<false, MULTI>(K, s, sj, smj, sa4, sa2, lane, jvalid);
   else
-    tile_loop<true, MULTI>(K, s, sj, smj, sa4, sa2, diag, lane, jvalid);
+    tile_loop<true, MULTI>(K, s, sj, smj, sa4, sa2, lane, jvalid);
   __syncwarp();
 
   // partial slots: (strip X, strip Y, component c, local index)
