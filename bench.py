@@ -43,6 +43,11 @@ UNIT = "particle-steps/s"
 # correction 15, three dot products 15, energy 4, force 21, torques 36,
 # pressure tensor 18, accumulation 13 -> ~180, the figure of the survey)
 FLOP_PER_PAIR = 180.0
+# DRAM bytes (read + write) per dipole pair of real_pairs_kernel from one
+# ncu capture: 2.70 MB + 0.02 MB over the 47,281,855 pairs of the 128-replica
+# mix (profiles/real_pairs_replica_mix128.md).  The kernel reads each tile's
+# dipoles once, so its traffic scales with the pairs a launch processes.
+REAL_PAIRS_DRAM_BYTES_PER_PAIR = 2.72e6 / 47_281_855
 
 
 def log(*a):
@@ -346,7 +351,9 @@ def run_ours(args):
                     "d2h_bytes_per_step": bytes_d2h},
             "gpu_launches": launches * args.steps,
             "roofline": {"bound": "fp32", "kernel": "real_pairs", "achieved": achieved, "peak": fp32_peak,
-                         "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
+                         "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+                         "traffic": REAL_PAIRS_DRAM_BYTES_PER_PAIR * pairs,
+                         "traffic_unit": "bytes per launch (ncu dram read+write, scaled by pairs)",
                          "peak_source": (f"nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 FLOP at "
                                          f"{sm_max:.0f} MHz ({src} max SM clock); MEASURED_PEAKS.json has "
                                          f"HBM and bf16 tensor figures only"),
