@@ -61,6 +61,23 @@ def dist_env():
     return ws, rank, local
 
 
+def aggregate_ranks(sums, maxes, device="cpu"):
+    """Whole-job figures over the ranks of the process group: each entry of
+    `sums` added over ranks (particles, work), each entry of `maxes` the
+    maximum over ranks (times).  One rank: returned unchanged."""
+    import torch
+    import torch.distributed as dist
+
+    sums, maxes = [float(x) for x in sums], [float(x) for x in maxes]
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return sums, maxes
+    a = torch.tensor(sums, dtype=torch.float64, device=device)
+    b = torch.tensor(maxes, dtype=torch.float64, device=device)
+    dist.all_reduce(a, op=dist.ReduceOp.SUM)
+    dist.all_reduce(b, op=dist.ReduceOp.MAX)
+    return a.tolist(), b.tolist()
+
+
 def build_mix(seed: int, nsys: int):
     from mdspherocyl_gb300 import systems as S
 
@@ -255,17 +272,16 @@ def run_ours(args):
     torch.cuda.synchronize()
     clocks = clk.stop()
     t_dev = sum(ms) / 1e3
-    if ws > 1:
-        tt = torch.tensor([t_dev], device=f"cuda:{device}")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_dev = float(tt.item())
-    value = ntot * ws * args.steps / t_dev
+    # every rank runs its own mix (different seeds, so different particle
+    # counts): whole-job particles summed, time the slowest rank's
+    (ntot_all,), (t_dev,) = aggregate_ranks([ntot], [t_dev], device=f"cuda:{device}")
+    value = ntot_all * args.steps / t_dev
     obs = bt.observe()
     st_ok = all(o["status"] == 0 for o in obs)
 
     # ---- the plain path: one system per launch sequence, one after another ----
     plain = None
-    if not args.no_plain:
+    if not args.no_plain and ws == 1:  # the batched-vs-plain ratio is a one-GPU figure
         singles = [L.Batch([sp], [st], device=device) for sp, st in zip(specs, sts)]
         for b1 in singles:
             b1.step(2)
@@ -318,11 +334,8 @@ def run_ours(args):
         bt.download_all(h["r"], h["p"], h["O"], h["l"], h["F"], h["T"])
     torch.cuda.synchronize()
     t_e2e = time.perf_counter() - t0
-    if ws > 1:
-        tt = torch.tensor([t_e2e], device=f"cuda:{device}")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_e2e = float(tt.item())
-    e2e = ntot * ws * e2e_steps / t_e2e
+    (_,), (t_e2e,) = aggregate_ranks([0], [t_e2e], device=f"cuda:{device}")
+    e2e = ntot_all * e2e_steps / t_e2e
     launches = bt.launches_per_step + 1  # + the per-call reset of the noise row
     bt.close()
     serving = run_serving(args, device) if (args.jobs > 0 and ws == 1) else None
@@ -342,7 +355,8 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair/k-space arithmetic, f64 state and sums",
             "data": "synthetic",
-            "config": {"workload": "replica_mix", "systems": len(specs), "particles": ntot,
+            "config": {"workload": "replica_mix", "systems": len(specs) * ws, "particles": int(ntot_all),
+                       "particles_rank0": ntot,
                        "N_range": [min(s.n for s in specs), max(s.n for s in specs)], "ksq_max": 36,
                        "alpha": "6/L_box", "real_space": "all minimum-image pairs", "dt": 1e-3,
                        "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{ws}",
