@@ -51,6 +51,7 @@ struct Layout {
   std::vector<SysDev> sys;
   std::vector<int4> tiles, kn, kwork;
   std::vector<float4> kv;
+  std::vector<float4> rtab;  // real-space tables of every system
   std::vector<double> kval, kpre, kvec;
   std::vector<int2> blk, kowner;
   int ntot = 0, ndtot = 0, nktot = 0, maxnd = 0, nchunks = 0;
@@ -99,6 +100,28 @@ std::string check_desc(const mdsc_system_desc& d, int s) {
 // constants of the real-space tiles as float-float pairs: the exponent's
 // alpha sqrt(log2 e) and the fixed-point scale L / 2^32, split on the host so
 // that the tiles do no FP64 work
+// entries 0..n-1 of the reference's table: A, B, C at r = Lh (k + 1), with
+// tabul's own expressions and order of operations (v25/functions.cpp:1680-1697)
+void table_values(double alpha, int n, double* T) {
+  const double extL = 200 * 1.001;
+  const double alsq = alpha * alpha;
+  const double alft = alsq * alsq;
+  const double spi = std::sqrt(M_PI);
+  for (int i = 1; i <= n; i++) {
+    const double r = 0.5 * extL * i / 32768;
+    const double rsq = r * r;
+    const double sr1 = 1.0 / r;
+    const double sr2 = sr1 * sr1;
+    const double sr3 = sr2 * sr1;
+    const double ERFC = std::erfc(alpha * r);
+    const double aer = 2.0 * alpha * std::exp(-alsq * rsq) / spi;
+    const double aa = 2.0 * alsq + 3.0 * sr2;
+    T[3 * (i - 1) + 0] = ERFC * sr3 + aer * sr2;
+    T[3 * (i - 1) + 1] = (3.0 * ERFC * sr3 + aer * aa) * sr2;
+    T[3 * (i - 1) + 2] = 4. * alft * aer;
+  }
+}
+
 void set_pair_consts(SysDev& P) {
   const double xa = P.alpha * 1.2011224087864498;  // sqrt(log2 e)
   P.xh = (float)xa;
@@ -192,6 +215,23 @@ void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
     P.rmax_table = (float)kTableRmax;
     P.sixthLh3 = (float)(kLh * kLh * kLh / 6.0);
     set_pair_consts(P);
+    // the reference's interpolation table (tabul, v25/functions.cpp:1680-1704)
+    // over the distances this box can hold, in FP64 as tabul computes it,
+    // stored as FP32 values and differences to the next entry
+    if (d.nd > 0) {
+      const double hd = 0.5 * std::sqrt(d.box[0] * d.box[0] + d.box[1] * d.box[1] + d.box[2] * d.box[2]);
+      const int n = std::min((int)std::floor(hd / kLh) + 3, 32767);
+      P.rt_off = (int)(Lo.rtab.size() / 2);
+      P.rt_n = n;
+      std::vector<double> T(3 * (size_t)(n + 1));
+      table_values(d.alpha, n + 1, T.data());
+      for (int k = 0; k < n; ++k) {
+        const double* a = &T[3 * (size_t)k];
+        const double* b = &T[3 * (size_t)(k + 1)];
+        Lo.rtab.push_back(make_float4((float)a[0], (float)a[1], (float)a[2], (float)(b[0] - a[0])));
+        Lo.rtab.push_back(make_float4((float)(b[1] - a[1]), (float)(b[2] - a[2]), 0.f, 0.f));
+      }
+    }
     part += d.n;
     dip += P.ndip;
     Lo.maxnd = std::max(Lo.maxnd, d.nd);
@@ -267,6 +307,7 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   b.wrec = A.take<double>(n * kMaxC * 6);
   b.kn = A.take<int4>(nk);
   b.kv = A.take<float4>(nk);
+  b.rtab = A.take<float4>(std::max<size_t>(Lo.rtab.size(), 1));
   b.kval = A.take<double>(nk);
   b.kvec = A.take<double>(3 * nk);
   b.kpre = A.take<double>(nk);
@@ -765,6 +806,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   up(b.blk, lo.blk.data(), sizeof(int2) * lo.blk.size());
   up(b.kn, lo.kn.data(), sizeof(int4) * lo.kn.size());
   up(b.kv, lo.kv.data(), sizeof(float4) * lo.kv.size());
+  up((void*)b.rtab, lo.rtab.data(), sizeof(float4) * lo.rtab.size());
   up(b.kval, lo.kval.data(), sizeof(double) * lo.kval.size());
   up(b.kvec, lo.kvec.data(), sizeof(double) * lo.kvec.size());
   up(b.kpre, lo.kpre.data(), sizeof(double) * lo.kpre.size());

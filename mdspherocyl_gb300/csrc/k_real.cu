@@ -87,6 +87,20 @@ constexpr float kQ0 = 2.820587754e-01f, kQ1 = 2.829789221e-01f, kQ2 = 2.37546384
                 kQ6 = -7.125887275e-01f, kQ7 = 4.623427987e-01f, kQ8 = -1.380545348e-01f,
                 kQ9 = 1.510943193e-02f;
 
+// one 32-byte table entry in a single 256-bit load through the read-only
+// path: the L1 serves a warp's 32 scattered entries in 32 wavefronts, where
+// two 128-bit loads would take 64
+__device__ __forceinline__ void ld_entry(const float4* e, float4& p, float4& q) {
+  asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=f"(p.x), "=f"(p.y), "=f"(p.z), "=f"(p.w), "=f"(q.x), "=f"(q.y), "=f"(q.z), "=f"(q.w)
+               : "l"(e));
+}
+
+// 1/Lh of the reference's table spacing Lh = 0.5*200.2/32768, as hi + lo
+constexpr double kInvLhD = 32768.0 / (0.5 * (200 * 1.001));
+constexpr float kInvLhHi = (float)kInvLhD;
+constexpr float kInvLhLo = (float)(kInvLhD - (double)kInvLhHi);
+
 // per-system constants, the same value in both halves
 struct PairConst {
   f2 xh, xlo;    // alpha sqrt(log2 e) as a float-float pair: 2^(-(x r)^2) = exp(-alpha^2 r^2)
@@ -95,6 +109,9 @@ struct PairConst {
   f2 a2, a4x4;   // 2 alpha^2, 4 alpha^4
   f2 invLh, halfLh2, nsixthLh3;
   f2 Lhx, Lhy, Lhz, Llx, Lly, Llz;  // L / 2^32 per axis as float-float pairs
+  f2 ihh, ihl;                      // 1 / Lh as a float-float pair
+  const float4* tab;                // the system's table entries (TAB kernels)
+  int tn;                           // its number of entries
 };
 
 struct Lane2 {
@@ -114,7 +131,7 @@ struct JOut {
 // one step of a tile loop: the lane's two i-dipoles against j0 (half 0)
 // and j1 (half 1) -- the same j in off-diagonal tiles.  Pairs masked off
 // (a0, a1 false) contribute exactly zero.
-template <bool MASKED>
+template <bool MASKED, bool TAB>
 __device__ __forceinline__ void tile_step(const PairConst& K, Lane2& s, const uint4 jp0, const float4 jm0,
                                           const uint4 jp1, const float4 jm1, bool a0, bool a1, JOut& o) {
   f2 mix = s.mx, miy = s.my, miz = s.mz;
@@ -137,45 +154,63 @@ __device__ __forceinline__ void tile_step(const PairConst& K, Lane2& s, const ui
   const f2 rinv2 = mul2(rinv, rinv);
   const f2 rinv3 = mul2(rinv2, rinv);
 
-  // exp(-x^2) and erfc(x), x = alpha r; the exponent from a once-rounded
-  // product (x up to ~5 puts it near -40, where a biased constant would
-  // shift every far pair's weight alike)
-  const f2 xr = fma2(r, K.xh, mul2(r, K.xlo));
-  const f2 y = mul2(xr, xr);
-  const f2 ex = make_float2(ex2_approx(-y.x), ex2_approx(-y.y));
-  const f2 den = fma2(r, K.ahalf, b2(1.f));
-  const f2 tt = make_float2(rcp_approx(den.x), rcp_approx(den.y));
-  f2 q = fma2(b2(kQ9), tt, b2(kQ8));
-  q = fma2(q, tt, b2(kQ7));
-  q = fma2(q, tt, b2(kQ6));
-  q = fma2(q, tt, b2(kQ5));
-  q = fma2(q, tt, b2(kQ4));
-  q = fma2(q, tt, b2(kQ3));
-  q = fma2(q, tt, b2(kQ2));
-  q = fma2(q, tt, b2(kQ1));
-  q = fma2(q, tt, b2(kQ0));
-  const f2 E = mul2(mul2(ex, tt), q);
-  const f2 G = mul2(ex, K.gpref);
-  const f2 Er3 = mul2(E, rinv3);
-  const f2 A = fma2(G, rinv2, Er3);
-  const f2 B = mul2(fma2(G, fma2(b2(3.f), rinv2, K.a2), mul2(b2(3.f), Er3)), rinv2);
-  const f2 C = mul2(G, K.a4x4);
+  f2 Ac, Bc, Cc;
+  if (TAB) {
+    // the reference's own method: linear interpolation in its table
+    // (v25/functions.cpp:1606-1614), entry ri - 1 and ri for ri = floor(r/Lh);
+    // r/Lh from a float-float 1/Lh, the fraction by one FMA against the
+    // floor so it keeps full precision
+    const f2 uu = fma2(r, K.ihh, mul2(r, K.ihl));
+    const float fl0 = floorf(uu.x), fl1 = floorf(uu.y);
+    const f2 fr = add2(fma2(r, K.ihh, make_float2(-fl0, -fl1)), mul2(r, K.ihl));
+    const int e0 = min(max((int)fl0 - 1, 0), K.tn - 1), e1 = min(max((int)fl1 - 1, 0), K.tn - 1);
+    float4 p0, q0, p1, q1;
+    ld_entry(K.tab + 2 * e0, p0, q0);
+    ld_entry(K.tab + 2 * e1, p1, q1);
+    Ac = fma2(fr, make_float2(p0.w, p1.w), make_float2(p0.x, p1.x));
+    Bc = fma2(fr, make_float2(q0.x, q1.x), make_float2(p0.y, p1.y));
+    Cc = fma2(fr, make_float2(q0.y, q1.y), make_float2(p0.z, p1.z));
+  } else {
+    // exp(-x^2) and erfc(x), x = alpha r; the exponent from a once-rounded
+    // product (x up to ~5 puts it near -40, where a biased constant would
+    // shift every far pair's weight alike)
+    const f2 xr = fma2(r, K.xh, mul2(r, K.xlo));
+    const f2 y = mul2(xr, xr);
+    const f2 ex = make_float2(ex2_approx(-y.x), ex2_approx(-y.y));
+    const f2 den = fma2(r, K.ahalf, b2(1.f));
+    const f2 tt = make_float2(rcp_approx(den.x), rcp_approx(den.y));
+    f2 q = fma2(b2(kQ9), tt, b2(kQ8));
+    q = fma2(q, tt, b2(kQ7));
+    q = fma2(q, tt, b2(kQ6));
+    q = fma2(q, tt, b2(kQ5));
+    q = fma2(q, tt, b2(kQ4));
+    q = fma2(q, tt, b2(kQ3));
+    q = fma2(q, tt, b2(kQ2));
+    q = fma2(q, tt, b2(kQ1));
+    q = fma2(q, tt, b2(kQ0));
+    const f2 E = mul2(mul2(ex, tt), q);
+    const f2 G = mul2(ex, K.gpref);
+    const f2 Er3 = mul2(E, rinv3);
+    const f2 A = fma2(G, rinv2, Er3);
+    const f2 B = mul2(fma2(G, fma2(b2(3.f), rinv2, K.a2), mul2(b2(3.f), Er3)), rinv2);
+    const f2 C = mul2(G, K.a4x4);
 
-  // the table's interpolation error, second and third order
-  const f2 uu = mul2(r, K.invLh);
-  const f2 fr = sub2(uu, make_float2(floorf(uu.x), floorf(uu.y)));
-  const f2 ab = mul2(fr, fma2(fr, b2(-1.f), b2(1.f)));
-  const f2 h2 = mul2(ab, K.halfLh2);
-  const f2 nh3 = mul2(mul2(ab, K.nsixthLh3), fma2(fr, b2(-2.f), b2(1.f)));  // -h3
-  const f2 s5 = fma2(b2(5.f), B, C);
-  const f2 a2C = mul2(K.a2, C);
-  const f2 a2rC = mul2(a2C, r);
-  const f2 a2a2rC = mul2(K.a2, a2rC);
-  const f2 a2r2 = mul2(K.a2, r2);
-  const f2 Ac = fma2(h2, fma2(b2(4.f), B, C), fma2(nh3, fma2(mul2(b2(4.f), s5), rinv, a2rC), A));
-  const f2 Bc = fma2(h2, fma2(mul2(b2(6.f), s5), rinv2, a2C),
-                     fma2(nh3, fma2(mul2(b2(42.f), s5), rinv3, fma2(mul2(b2(6.f), a2C), rinv, a2a2rC)), B));
-  const f2 Cc = fma2(h2, mul2(a2C, add2(a2r2, b2(-1.f))), fma2(nh3, mul2(a2a2rC, add2(a2r2, b2(-3.f))), C));
+    // the table's interpolation error, second and third order
+    const f2 uu = mul2(r, K.invLh);
+    const f2 fr = sub2(uu, make_float2(floorf(uu.x), floorf(uu.y)));
+    const f2 ab = mul2(fr, fma2(fr, b2(-1.f), b2(1.f)));
+    const f2 h2 = mul2(ab, K.halfLh2);
+    const f2 nh3 = mul2(mul2(ab, K.nsixthLh3), fma2(fr, b2(-2.f), b2(1.f)));  // -h3
+    const f2 s5 = fma2(b2(5.f), B, C);
+    const f2 a2C = mul2(K.a2, C);
+    const f2 a2rC = mul2(a2C, r);
+    const f2 a2a2rC = mul2(K.a2, a2rC);
+    const f2 a2r2 = mul2(K.a2, r2);
+    Ac = fma2(h2, fma2(b2(4.f), B, C), fma2(nh3, fma2(mul2(b2(4.f), s5), rinv, a2rC), A));
+    Bc = fma2(h2, fma2(mul2(b2(6.f), s5), rinv2, a2C),
+                       fma2(nh3, fma2(mul2(b2(42.f), s5), rinv3, fma2(mul2(b2(6.f), a2C), rinv, a2a2rC)), B));
+    Cc = fma2(h2, mul2(a2C, add2(a2r2, b2(-1.f))), fma2(nh3, mul2(a2a2rC, add2(a2r2, b2(-3.f))), C));
+  }
 
   // dipole-dipole energy, force on i, torques without lever arm
   const f2 mjx = make_float2(jm0.x, jm1.x), mjy = make_float2(jm0.y, jm1.y), mjz = make_float2(jm0.z, jm1.z);
@@ -231,7 +266,7 @@ __device__ __forceinline__ void tile_step(const PairConst& K, Lane2& s, const ui
 // Off-diagonal tile (strips I < J): 64 steps, at step t lane l pairs both
 // its i-dipoles with j = (l + t) mod 64; the two halves' j-side terms are
 // added into that j's sums.
-template <bool MASKED, bool MULTI>
+template <bool MASKED, bool MULTI, bool TAB>
 __device__ __forceinline__ void tile_loop(const PairConst& K, Lane2& s, const uint4* sj, const float4* smj,
                                           float4* sa4, float2* sa2, int lane, int jvalid) {
 #pragma unroll 1
@@ -250,7 +285,7 @@ __device__ __forceinline__ void tile_loop(const PairConst& K, Lane2& s, const ui
       }
     }
     JOut o;
-    tile_step<MASKED>(K, s, jp, jm, jp, jm, a0, a1, o);
+    tile_step<MASKED, TAB>(K, s, jp, jm, jp, jm, a0, a1, o);
     float4 ja4 = sa4[lj];
     float2 ja2 = sa2[lj];
     ja4.x -= o.fx.x + o.fx.y;
@@ -270,7 +305,7 @@ __device__ __forceinline__ void tile_loop(const PairConst& K, Lane2& s, const ui
 // x = l + 32 (half 1) pair with (x + t) mod 64: each pair at cyclic distance
 // d < 32 is met once from its lower end, d > 32 once from its upper end,
 // and d = 32 from half 0 only.  The 64 j's of a step are distinct.
-template <bool MULTI>
+template <bool MULTI, bool TAB>
 __device__ __forceinline__ void diag_loop(const PairConst& K, Lane2& s, const uint4* sj, const float4* smj,
                                           float4* sa4, float2* sa2, int lane, int jvalid) {
 #pragma unroll 1
@@ -285,7 +320,7 @@ __device__ __forceinline__ void diag_loop(const PairConst& K, Lane2& s, const ui
       a1 = a1 && (s.own1 != (int)jp1.w);
     }
     JOut o;
-    tile_step<true>(K, s, jp0, jm0, jp1, jm1, a0, a1, o);
+    tile_step<true, TAB>(K, s, jp0, jm0, jp1, jm1, a0, a1, o);
     float4 ja4 = sa4[j0];
     float2 ja2 = sa2[j0];
     ja4.x -= o.fx.x;
@@ -315,7 +350,9 @@ __device__ __forceinline__ void diag_loop(const PairConst& K, Lane2& s, const ui
 // W warps per block, one tile per warp (tile = W * blockIdx.x + warp): the
 // block size changes how tiles are grouped for scheduling, never what a
 // tile computes, so every W gives the same bits (the autotuner picks W).
-template <bool MULTI, int W>
+// TAB: interpolate in the reference's table (the batch path); otherwise the
+// analytic terms with the table's error added (callers without the table)
+template <bool MULTI, int W, bool TAB>
 __global__ void __launch_bounds__(32 * W) real_pairs_kernel(Batch b) {
   __shared__ uint4 sj_all[W][kTile];    // fixed-point x, y, z and owner of the j-dipoles
   __shared__ float4 smj_all[W][kTile];  // their moments
@@ -351,6 +388,10 @@ __global__ void __launch_bounds__(32 * W) real_pairs_kernel(Batch b) {
   K.a2 = b2(P.alpha2x2);
   K.a4x4 = b2(P.alpha4x4);
   K.invLh = b2(P.invLh);
+  K.ihh = b2(kInvLhHi);
+  K.ihl = b2(kInvLhLo);
+  K.tab = TAB ? b.rtab + 2 * (long long)P.rt_off : nullptr;
+  K.tn = P.rt_n;
   K.halfLh2 = b2(P.halfLh2);
   K.nsixthLh3 = b2(-P.sixthLh3);
 
@@ -394,11 +435,11 @@ __global__ void __launch_bounds__(32 * W) real_pairs_kernel(Batch b) {
   // no pair of this tile is skipped: the fast loop without masks
   const bool full = !MULTI && !diag && jvalid == kTile;
   if (diag)
-    diag_loop<MULTI>(K, s, sj, smj, sa4, sa2, lane, jvalid);
+    diag_loop<MULTI, TAB>(K, s, sj, smj, sa4, sa2, lane, jvalid);
   else if (full)
-    tile_loop<false, MULTI>(K, s, sj, smj, sa4, sa2, lane, jvalid);
+    tile_loop<false, MULTI, TAB>(K, s, sj, smj, sa4, sa2, lane, jvalid);
   else
-    tile_loop<true, MULTI>(K, s, sj, smj, sa4, sa2, lane, jvalid);
+    tile_loop<true, MULTI, TAB>(K, s, sj, smj, sa4, sa2, lane, jvalid);
   __syncwarp();
 
   // partial slots: (strip X, strip Y, component c, local index)
@@ -500,15 +541,18 @@ void launch_real_pairs(const Batch& b, bool multi, cudaStream_t s) {
   if (b.ntiles == 0) return;
   const int W = b.tune.rp_warps;
   const int grid = cdiv(b.ntiles, W);
-  if (W == 4) {
-    if (multi) real_pairs_kernel<true, 4><<<grid, 128, 0, s>>>(b);
-    else real_pairs_kernel<false, 4><<<grid, 128, 0, s>>>(b);
+  if (b.rtab == nullptr) {  // no table: the analytic form, one tile per block
+    if (multi) real_pairs_kernel<true, 1, false><<<b.ntiles, 32, 0, s>>>(b);
+    else real_pairs_kernel<false, 1, false><<<b.ntiles, 32, 0, s>>>(b);
+  } else if (W == 4) {
+    if (multi) real_pairs_kernel<true, 4, true><<<grid, 128, 0, s>>>(b);
+    else real_pairs_kernel<false, 4, true><<<grid, 128, 0, s>>>(b);
   } else if (W == 2) {
-    if (multi) real_pairs_kernel<true, 2><<<grid, 64, 0, s>>>(b);
-    else real_pairs_kernel<false, 2><<<grid, 64, 0, s>>>(b);
+    if (multi) real_pairs_kernel<true, 2, true><<<grid, 64, 0, s>>>(b);
+    else real_pairs_kernel<false, 2, true><<<grid, 64, 0, s>>>(b);
   } else {
-    if (multi) real_pairs_kernel<true, 1><<<b.ntiles, 32, 0, s>>>(b);
-    else real_pairs_kernel<false, 1><<<b.ntiles, 32, 0, s>>>(b);
+    if (multi) real_pairs_kernel<true, 1, true><<<b.ntiles, 32, 0, s>>>(b);
+    else real_pairs_kernel<false, 1, true><<<b.ntiles, 32, 0, s>>>(b);
   }
 }
 

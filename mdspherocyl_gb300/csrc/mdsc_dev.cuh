@@ -47,6 +47,7 @@ struct SysDev {
   long long pp_off;  // real-space partials: nstrip*nstrip*6*kTile floats
   int tile_off, ntile;  // tile list range
   int k_off, nk;        // k-vector range
+  int rt_off, rt_n;     // real-space table entries (A, B, C of the reference's tabul)
   int kchunk_off, nkchunk;  // structure-factor partial range (chunks of kKChunk particles)
   int gch_off, pad_g;       // first chunk of the system in the G-tensor partials
   int blk_off, nblk;        // per-particle block range
@@ -147,6 +148,7 @@ struct Batch {
   float* dm;     // 3 ndip dipole moment vectors mu*o (SoA blocks)
   // force components
   float* rpart;  // real-space partials
+  const float4* rtab;  // 2 per entry: (A, B, C, dA), (dB, dC, 0, 0); see k_real.cu
   float2* rsum;  // 6 * ndtot: each dipole's real-space force and torque over all strips, float-float, component-major
   float* tileE;  // 10 per tile: U, PT[9]
   int4* tiles;   // (sys, I, J, 0)
