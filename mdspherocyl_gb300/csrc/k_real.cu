@@ -28,8 +28,17 @@
 // reference does not evaluate erfc directly: it interpolates linearly in a
 // 32768-entry FP64 table with spacing Lh = 0.5*200.2/32768
 // (v25/functions.cpp:1563,1606-1614,1680-1697), which differs from the
-// analytic B(r), C(r) by up to ~5e-5 near contact.  The kernel evaluates the
-// analytic terms and adds the table's own interpolation error to second
+// analytic B(r), C(r) by up to ~5e-5 near contact.  Two forms reproduce it:
+//
+// TAB (the batch path): the same interpolation, in the system's own table.
+// The host builds it once per system with tabul's expressions in FP64 over
+// the distances the box can hold and stores each entry as FP32 A, B, C and
+// the differences to the next entry, 32 bytes, read with one 256-bit load
+// (one L1 wavefront per lane per lookup).  The lookups are scattered, so
+// the kernel leans on L2 as well as on the FP32 pipe.
+//
+// Analytic (callers without a table, mdsc_force_dipR_noalloc): the kernel
+// evaluates the analytic terms and adds the table's own interpolation error to second
 // and third order, h2 f''(r) + h3 f'''(r) with a = r - r0, b = r1 - r,
 // h2 = ab/2, h3 = ab(b - a)/6, using the closed forms (A, B, C as the
 // reference's table columns, s = 5B + C)
