@@ -22,6 +22,7 @@ oracle/, all host threads) on a bounded sample of the same workload.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -320,19 +321,26 @@ def run_ours(args):
     h = {k: pin(ntot, 3) for k in ("r", "p", "l", "F", "T")}
     h["O"] = pin(ntot, 3, 3)
     bt.download_all(h["r"], h["p"], h["O"], h["l"], h["F"], h["T"])
+    # every step: the step's input (the whole state of every system) from
+    # pinned host memory, the step, and the step's result (every system's
+    # energies, pressure tensors, thermostat and status) read back
+    obs_buf = (L.Observables * len(specs))()
     bytes_h2d = sum(v.nbytes for v in h.values())
-    bytes_d2h = bytes_h2d
-    for _ in range(2):
+    bytes_d2h = ctypes.sizeof(obs_buf)
+
+    def e2e_step():
         bt.upload_all(h["r"], h["p"], h["O"], h["l"], h["F"], h["T"])
-        bt.lib.mdsc_step(bt.h, 1, None)
-        bt.download_all(h["r"], h["p"], h["O"], h["l"], h["F"], h["T"])
+        code = bt.lib.mdsc_step(bt.h, 1, obs_buf)  # ends with the observables in host memory
+        if code != 0:
+            raise L.MdscError(code, "mdsc_step", bt._err())
+
+    for _ in range(2):
+        e2e_step()
     e2e_steps = max(3, min(args.steps, 20))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        bt.upload_all(h["r"], h["p"], h["O"], h["l"], h["F"], h["T"])
-        bt.lib.mdsc_step(bt.h, 1, None)
-        bt.download_all(h["r"], h["p"], h["O"], h["l"], h["F"], h["T"])
+        e2e_step()
     torch.cuda.synchronize()
     t_e2e = time.perf_counter() - t0
     (_,), (t_e2e,) = aggregate_ranks([0], [t_e2e], device=f"cuda:{device}")

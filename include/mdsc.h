@@ -209,6 +209,31 @@ double mdsc_last_device_ms(const mdsc_batch* b);
 mdsc_status mdsc_profile_steps(mdsc_batch* b, int nsteps, int max_kernels, char* names,
                                size_t name_stride, double* ms_per_launch, int* n_kernels);
 
+/* ---- observables outside the step ----------------------------------------- */
+/* Number of histogram bins of system sys for bar width bar_w:
+   floor(sqrt(3) Lmin / (2 bar_w)), Lmin the shortest box edge, as the
+   reference sizes Hista (v25/main.cpp:251-255); 0 on a bad argument. */
+int mdsc_correlation_bins(const mdsc_batch* b, int sys, double bar_w);
+/* Replaces acc_correl (v25/functions.cpp:2400-2470) for one species per
+   system: adds every unordered pair's terms to the pair-correlation
+   histograms of the current state -- 2, 2 dot, 2 (3 doti dotj - dot) and
+   3 dot^2 - 1 to bin floor(r / bar_w) of 000, 110, 112 and 220.  hist holds,
+   system after system, 4 x nbins doubles (function-major, nbins from
+   mdsc_correlation_bins) and is ADDED TO, as the reference accumulates
+   Hista over a run.  The count is exact and a pair lands in the reference's
+   bin (an FP64 recheck near bin edges); the other three sums carry the
+   FP32 rounding of each pair's term (~1e-7 of the count).  Pairs at a
+   distance past the last bin (the box's corners) are left out, where the
+   reference writes past its matrix. */
+mdsc_status mdsc_correlations(mdsc_batch* b, double bar_w, double* hist);
+/* Replaces oo_params (v25/functions.cpp:2702-2760) per system: G1[sys],
+   G2[sys] (nematic order: the largest |eigenvalue| of
+   Q = sum (3 o o^T - 1) / (2 N), and the polar order |sum o . e| / N along its
+   eigenvector) and M[3 sys ..] = sum over dipoles of mu o (lab frame).  Each
+   argument may be NULL.  The sums are FP64 on the GPU; the reference forms
+   Q in FP32, so G1 and G2 agree with it to ~1e-6. */
+mdsc_status mdsc_order_params(mdsc_batch* b, double* G1, double* G2, double* M);
+
 /* ---- autotuner -------------------------------------------------------- */
 /* Chooses the launch mappings (real-space tiles per block, strip-sum block
    size, grid of the FP64 WCA evaluation, k-space gather form) by timing each

@@ -36,6 +36,9 @@ void launch_cluster_compress(const Batch& b, cudaStream_t s);
 void launch_reset_iter(const Batch& b, cudaStream_t s);
 void launch_kspace_parts(const Batch& b, int maxnd, const int4* kwork, int nkwork, const int2* kowner,
                          double* kE, int part, cudaStream_t s);
+void launch_correlations(const Batch& b, const int2* binfo, double bar_w, int max_bins,
+                         unsigned long long* hist, cudaStream_t s);
+void launch_order_sums(const Batch& b, double* out, cudaStream_t s);
 }  // namespace mdsc
 
 using namespace mdsc;
@@ -715,6 +718,51 @@ void shapes_to_host(const mdsc_batch* B, int s, const mdsc_host_state* h, std::v
   }
 }
 
+// ---- observables outside the step: host helpers ------------------------
+int corr_bins(const SysDev& P, double bar_w) {
+  const double Lmin = std::min(P.L[2], std::min(P.L[1], P.L[0]));
+  return (int)std::floor(std::sqrt(3.) * Lmin / (2. * bar_w));
+}
+
+// eigenvalues d and eigenvectors (columns of V) of a symmetric 3x3 matrix
+// by cyclic Jacobi rotations (Golub & Van Loan, Matrix Computations 8.5)
+void sym3_eigen(const double (&A0)[3][3], double (&d)[3], double (&V)[3][3]) {
+  double A[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      A[i][j] = A0[i][j];
+      V[i][j] = i == j ? 1.0 : 0.0;
+    }
+  for (int sweep = 0; sweep < 64; ++sweep) {
+    const double off = std::fabs(A[0][1]) + std::fabs(A[0][2]) + std::fabs(A[1][2]);
+    const double diag = std::fabs(A[0][0]) + std::fabs(A[1][1]) + std::fabs(A[2][2]);
+    if (off <= 1e-15 * diag + 1e-300) break;
+    for (int p = 0; p < 2; ++p)
+      for (int q = p + 1; q < 3; ++q) {
+        if (A[p][q] == 0.0) continue;
+        const double th = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
+        const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+        for (int k = 0; k < 3; ++k) {
+          const double x = A[k][p], y = A[k][q];
+          A[k][p] = c * x - sn * y;
+          A[k][q] = sn * x + c * y;
+        }
+        for (int k = 0; k < 3; ++k) {
+          const double x = A[p][k], y = A[q][k];
+          A[p][k] = c * x - sn * y;
+          A[q][k] = sn * x + c * y;
+        }
+        for (int k = 0; k < 3; ++k) {
+          const double x = V[k][p], y = V[k][q];
+          V[k][p] = c * x - sn * y;
+          V[k][q] = sn * x + c * y;
+        }
+      }
+  }
+  for (int i = 0; i < 3; ++i) d[i] = A[i][i];
+}
+
 }  // namespace
 
 // ======================================================================
@@ -1226,6 +1274,85 @@ mdsc_status mdsc_clust_conf(mdsc_batch* B, int sys, int* labels, int* n_clusters
   if (st) return st;
   if (labels) std::copy(B->labels[sys].begin(), B->labels[sys].end(), labels);
   if (n_clusters) *n_clusters = B->n_clusters[sys];
+  return MDSC_OK;
+}
+
+// ---- observables outside the step ---------------------------------------
+int mdsc_correlation_bins(const mdsc_batch* B, int sys, double bar_w) {
+  if (!B || sys < 0 || sys >= B->nsys || !(bar_w > 0.0)) return 0;
+  return std::max(0, corr_bins(B->lo.sys[sys], bar_w));
+}
+
+mdsc_status mdsc_correlations(mdsc_batch* B, double bar_w, double* hist) {
+  mdsc_status st = need_state(B);
+  if (st) return st;
+  if (!(bar_w > 0.0) || !hist) return fail(B, MDSC_ERR_BAD_ARG, "mdsc_correlations: bar_w > 0 and hist required");
+  std::vector<int2> binfo(B->nsys);
+  int tot = 0, max_bins = 0;
+  for (int s = 0; s < B->nsys; ++s) {
+    const int nb = std::max(0, corr_bins(B->lo.sys[s], bar_w));
+    binfo[s] = make_int2(nb, tot);
+    tot += 4 * nb;
+    max_bins = std::max(max_bins, nb);
+  }
+  if (tot == 0) return MDSC_OK;
+  char* d = nullptr;
+  const size_t hbytes = sizeof(unsigned long long) * tot;
+  CU(cudaMallocAsync((void**)&d, hbytes + sizeof(int2) * B->nsys, B->st));
+  unsigned long long* dh = reinterpret_cast<unsigned long long*>(d);
+  int2* dinfo = reinterpret_cast<int2*>(d + hbytes);
+  std::vector<unsigned long long> h(tot);
+  CU(cudaMemcpyAsync(dinfo, binfo.data(), sizeof(int2) * B->nsys, cudaMemcpyHostToDevice, B->st));
+  CU(cudaMemsetAsync(dh, 0, hbytes, B->st));
+  launch_derive(B->b, B->st);
+  launch_correlations(B->b, dinfo, bar_w, max_bins, dh, B->st);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(h.data(), dh, hbytes, cudaMemcpyDeviceToHost, B->st));
+  CU(cudaFreeAsync(d, B->st));
+  CU(cudaStreamSynchronize(B->st));
+  // counts are exact integers; the other three are fixed point in 2^-24 units
+  for (int s = 0; s < B->nsys; ++s) {
+    const int nb = binfo[s].x, off = binfo[s].y;
+    for (int k = 0; k < nb; ++k) hist[off + k] += (double)h[off + k];
+    for (int k = nb; k < 4 * nb; ++k) hist[off + k] += std::ldexp((double)(long long)h[off + k], -24);
+  }
+  return MDSC_OK;
+}
+
+mdsc_status mdsc_order_params(mdsc_batch* B, double* G1, double* G2, double* M) {
+  mdsc_status st = need_state(B);
+  if (st) return st;
+  const int nblk = B->b.nblk;
+  std::vector<double> part(12 * (size_t)nblk);
+  double* d = nullptr;
+  CU(cudaMallocAsync((void**)&d, sizeof(double) * part.size(), B->st));
+  launch_derive(B->b, B->st);
+  launch_order_sums(B->b, d, B->st);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(part.data(), d, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, B->st));
+  CU(cudaFreeAsync(d, B->st));
+  CU(cudaStreamSynchronize(B->st));
+  for (int s = 0; s < B->nsys; ++s) {
+    const SysDev& P = B->lo.sys[s];
+    double v[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < P.nblk; ++k)
+      for (int c = 0; c < 12; ++c) v[c] += part[12 * (size_t)(P.blk_off + k) + c];
+    if (M)
+      for (int a = 0; a < 3; ++a) M[3 * s + a] = v[9 + a];
+    // Q = sum (3 o o^T - 1) / (2 N) (Qmat_3d, v25/functions.cpp:3426-3445)
+    const double n = P.n;
+    const int ix[3][3] = {{3, 4, 5}, {4, 6, 7}, {5, 7, 8}};
+    double Q[3][3], ev[3], V[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) Q[i][j] = (3.0 * v[ix[i][j]] - (i == j ? n : 0.0)) / (2.0 * n);
+    sym3_eigen(Q, ev, V);
+    // the reference's choice among equal |eigenvalues| (v25/functions.cpp:2738-2748)
+    const double e1 = std::fabs(ev[0]), e2 = std::fabs(ev[1]), e3 = std::fabs(ev[2]);
+    const int c = (e1 >= e2 && e1 >= e3) ? 0 : (e2 > e1 && e2 >= e3) ? 1 : 2;
+    const double nv = std::sqrt(V[0][c] * V[0][c] + V[1][c] * V[1][c] + V[2][c] * V[2][c]);
+    if (G2) G2[s] = std::fabs(ev[c]);
+    if (G1) G1[s] = std::fabs((V[0][c] * v[0] + V[1][c] * v[1] + V[2][c] * v[2]) / nv) / n;
+  }
   return MDSC_OK;
 }
 

@@ -36,7 +36,8 @@ EXPORTS = [
     "mdsc_renorm", "mdsc_neigh_list", "mdsc_check_list", "mdsc_clust_conf", "mdsc_step",
     "mdsc_observe", "mdsc_launches_per_step", "mdsc_stream", "mdsc_profile_steps",
     "mdsc_place_rods", "mdsc_last_device_ms", "mdsc_force_dipR_noalloc", "mdsc_transfer",
-    "mdsc_autotune", "mdsc_tuning", "mdsc_set_tuning",
+    "mdsc_autotune", "mdsc_tuning", "mdsc_set_tuning", "mdsc_correlation_bins", "mdsc_correlations",
+    "mdsc_order_params",
 ]
 
 
@@ -126,6 +127,9 @@ def load(build: bool = True) -> ctypes.CDLL:
         "mdsc_autotune": (c_int, [c_void_p, c_int]),
         "mdsc_tuning": (c_int, [c_void_p, _ip, c_char_p, c_size_t]),
         "mdsc_set_tuning": (c_int, [c_void_p, _ip]),
+        "mdsc_correlation_bins": (c_int, [c_void_p, c_int, c_double]),
+        "mdsc_correlations": (c_int, [c_void_p, c_double, _dp]),
+        "mdsc_order_params": (c_int, [c_void_p, _dp, _dp, _dp]),
         "mdsc_force_dipR_noalloc": (c_int, [c_int, c_void_p, c_void_p, _dp, c_double, c_void_p, c_void_p,
                                             c_void_p, c_void_p]),
         "mdsc_profile_steps": (c_int, [c_void_p, c_int, c_int, c_char_p, c_size_t, _dp, _ip]),
@@ -319,6 +323,29 @@ class Batch:
                     "mdsc_clust_conf")
         return lab, nc.value
 
+    # -- observables outside the step --
+    def correlation_bins(self, k: int, bar_w: float) -> int:
+        return int(self.lib.mdsc_correlation_bins(self.h, k, float(bar_w)))
+
+    def correlations(self, bar_w: float, hist=None):
+        """acc_correl on the GPU: per system a (4, nbins) array of the 000,
+        110, 112 and 220 pair sums.  hist (a list of such arrays, e.g. the
+        last call's result) is added to, as the reference accumulates."""
+        nb = [self.correlation_bins(k, bar_w) for k in range(self.nsys)]
+        flat = np.zeros(4 * sum(nb))
+        off = np.cumsum([0] + [4 * b for b in nb])
+        if hist is not None:
+            for k in range(self.nsys):
+                flat[off[k]:off[k + 1]] = np.asarray(hist[k], dtype=np.float64).reshape(-1)
+        self._check(self.lib.mdsc_correlations(self.h, float(bar_w), _ptr(flat)), "mdsc_correlations")
+        return [flat[off[k]:off[k + 1]].reshape(4, nb[k]) for k in range(self.nsys)]
+
+    def order_params(self):
+        """oo_params on the GPU: G1 (nsys,), G2 (nsys,), M (nsys, 3)."""
+        G1, G2, M = np.zeros(self.nsys), np.zeros(self.nsys), np.zeros((self.nsys, 3))
+        self._check(self.lib.mdsc_order_params(self.h, _ptr(G1), _ptr(G2), _ptr(M)), "mdsc_order_params")
+        return G1, G2, M
+
     def transfer_from(self, k: int, src: "Batch", ks: int) -> None:
         """Move system ks of src into slot k of this batch, on the GPU."""
         self._check(self.lib.mdsc_transfer(self.h, k, src.h, ks), "mdsc_transfer")
@@ -364,6 +391,25 @@ class Batch:
             nm = names.raw[k * stride:(k + 1) * stride].split(b"\0")[0].decode()
             out[nm] = float(ms[k])
         return out
+
+
+def normalize_correlations(hist, n: int, box, bar_w: float, cor_cont: float = 1.0):
+    """nor_correl (v25/functions.cpp:2472-2540) for one species: the bin
+    centres, the shell volumes and the normalised 000, 110, 112, 220
+    functions (factors 1, 3, 3/2, 5 over norm * cor_cont * n (n - 1)), as
+    arrays instead of the reference's correlation.dat.  cor_cont is the
+    number of accumulated configurations (chrg_correl's counter)."""
+    h = np.asarray(hist, dtype=np.float64).reshape(4, -1)
+    Lmin = float(min(box))
+    pos = (np.arange(h.shape[1]) + 0.5) * bar_w
+    shell = 4.0 * np.pi * pos * pos * (3.0 * Lmin / (2.0 * pos) - 2.0) * bar_w
+    sphere = 4.0 * np.pi * (pos * pos * bar_w + bar_w ** 3 / 12.0)
+    norm = np.where((pos >= Lmin / 2.0) & (pos <= Lmin / np.sqrt(2.0)), shell, sphere)
+    g = np.zeros_like(h)
+    if n > 1:
+        den = norm * cor_cont * n * (n - 1)
+        g = np.array([1.0, 3.0, 1.5, 5.0])[:, None] * h / den
+    return pos, norm, g
 
 
 def place_rods(lengths, dia, box, seed: int, gap: float = 0.0):

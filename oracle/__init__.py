@@ -158,6 +158,8 @@ class Oracle:
         self._rng_u = _bind(lib, "mdsc_or_rng_uniform", c_double, [c_void_p])
         self._rng_free = _bind(lib, "mdsc_or_rng_free", None, [c_void_p])
         self._cl = _bind(lib, "mdsc_or_clust_conf_rng", c_int, [_SP, c_double, c_void_p])
+        self._corr = _bind(lib, "mdsc_or_acc_correl", None, [_SP, c_double, c_int, _dp])
+        self._oo = _bind(lib, "mdsc_or_oo_params", None, [_SP, _dp, _dp, _dp])
         self._tabcache: dict[float, np.ndarray] = {}
 
     def clust_conf(self, sysm: System, min_s: float, seed: int = 1, skip: int = 0):
@@ -173,6 +175,22 @@ class Oracle:
         finally:
             self._rng_free(rng)
         return sysm.clust.copy(), nc, nxt
+
+    def acc_correl(self, sysm: System, bar_w: float, nbins: int, hist=None):
+        """acc_correl (one species): the pair histograms 000, 110, 112, 220
+        of this state, added to hist (4 x nbins)."""
+        h = np.zeros((4, nbins)) if hist is None else hist
+        cs = sysm.cstate()
+        self._corr(ctypes.byref(cs), bar_w, nbins, h.ctypes.data_as(_dp))
+        return h
+
+    def oo_params(self, sysm: System):
+        """oo_params: G1, G2 and the total dipole moment M."""
+        G1, G2 = c_double(0), c_double(0)
+        M = np.zeros(3)
+        cs = sysm.cstate()
+        self._oo(ctypes.byref(cs), ctypes.byref(G1), ctypes.byref(G2), M.ctypes.data_as(_dp))
+        return G1.value, G2.value, M
 
     def set_threads(self, n: int) -> None:
         self._thr(int(n))
@@ -348,6 +366,8 @@ class Ref:
         self._rng_u = _bind(lib, "mdsc_ref_rng_uniform", c_double, [c_void_p])
         self._rng_free = _bind(lib, "mdsc_ref_rng_free", None, [c_void_p])
         self._cl = _bind(lib, "mdsc_ref_clust_conf", None, [_SP, c_double, c_void_p])
+        self._corr = _bind(lib, "mdsc_ref_acc_correl", None, [_SP, c_double, c_int, _dp])
+        self._oo = _bind(lib, "mdsc_ref_oo_params", None, [_SP, _dp, _dp, _dp])
         self._mt = _bind(lib, "mdsc_ref_moveTher", None,
                          [_dp, _dp, c_double, c_double, c_void_p, c_void_p, c_double, c_double, _dp,
                           c_double, c_int])
@@ -358,6 +378,19 @@ class Ref:
         cs = sysm.cstate()
         dsq = self._seg(ctypes.byref(cs), i, j, d.ctypes.data_as(_dp), st.ctypes.data_as(_dp))
         return dsq, d, st
+
+    def acc_correl(self, sysm, bar_w, nbins, hist=None):
+        h = np.zeros((4, nbins)) if hist is None else hist
+        cs = sysm.cstate()
+        self._corr(ctypes.byref(cs), bar_w, nbins, h.ctypes.data_as(_dp))
+        return h
+
+    def oo_params(self, sysm):
+        G1, G2 = c_double(0), c_double(0)
+        M = np.zeros(3)
+        cs = sysm.cstate()
+        self._oo(ctypes.byref(cs), ctypes.byref(G1), ctypes.byref(G2), M.ctypes.data_as(_dp))
+        return G1.value, G2.value, M
 
     def neigh_list(self, sysm, r_list):
         n = sysm.n

@@ -1296,3 +1296,122 @@ void mdsc_or_md_free(mdsc_or_md* md) {
   free(md->saved_r);
   memset(md, 0, sizeof(*md));
 }
+
+/* ------------------------------------------------------------------ */
+/* observables outside the step                                        */
+/* ------------------------------------------------------------------ */
+/* acc_correl (v25/functions.cpp:2400-2470) for one species: the intra
+   histograms, pair by pair (i < j) in the reference's order and arithmetic.
+   hist[f * nbins + bin], f = 000, 110, 112, 220, accumulates.  Pairs whose
+   bin is >= nbins (distance at the very corner of the box) are skipped. */
+void mdsc_or_acc_correl(const mdsc_oracle_state* s, double bar_w, int nbins, double* hist) {
+  const double* L = s->L;
+  for (int f = 0; f < s->n - 1; ++f) {
+    const double* ri = s->r + 3 * f;
+    const double* oi = s->O + 9 * f + 6;
+    for (int g = f + 1; g < s->n; ++g) {
+      const double* rj = s->r + 3 * g;
+      const double* oj = s->O + 9 * g + 6;
+      double XIJ = ri[0] - rj[0];
+      XIJ -= L[0] * floor(XIJ / L[0] + 0.5);
+      double YIJ = ri[1] - rj[1];
+      YIJ -= L[1] * floor(YIJ / L[1] + 0.5);
+      double ZIJ = ri[2] - rj[2];
+      ZIJ -= L[2] * floor(ZIJ / L[2] + 0.5);
+      const double RIJSQ = XIJ * XIJ + YIJ * YIJ + ZIJ * ZIJ;
+      const double RIJ = sqrt(RIJSQ);
+      const double dot = oi[0] * oj[0] + oi[1] * oj[1] + oi[2] * oj[2];
+      const double dotsq = dot * dot;
+      const double doti = (oi[0] * XIJ + oi[1] * YIJ + oi[2] * ZIJ) / RIJ;
+      const double dotj = (oj[0] * XIJ + oj[1] * YIJ + oj[2] * ZIJ) / RIJ;
+      const int bin = (int)floor(RIJ / bar_w);
+      if (bin < 0 || bin >= nbins) continue;
+      hist[0 * nbins + bin] += 2.;
+      hist[1 * nbins + bin] += 2. * dot;
+      hist[2 * nbins + bin] += 2. * (3. * doti * dotj - dot);
+      hist[3 * nbins + bin] += 3. * dotsq - 1.;
+    }
+  }
+}
+
+/* eigenvalues d[3] and eigenvectors (columns of V) of a symmetric 3x3
+   matrix by cyclic Jacobi rotations (Golub & Van Loan, Matrix
+   Computations, 8.5): each rotation zeroes one off-diagonal element. */
+static void sym3_eigen(const double A_in[3][3], double d[3], double V[3][3]) {
+  double A[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      A[i][j] = A_in[i][j];
+      V[i][j] = i == j ? 1.0 : 0.0;
+    }
+  for (int sweep = 0; sweep < 64; ++sweep) {
+    const double off = fabs(A[0][1]) + fabs(A[0][2]) + fabs(A[1][2]);
+    const double scale = fabs(A[0][0]) + fabs(A[1][1]) + fabs(A[2][2]) + 1e-300;
+    if (off <= 1e-15 * scale) break;
+    for (int p = 0; p < 2; ++p)
+      for (int q = p + 1; q < 3; ++q) {
+        if (A[p][q] == 0.0) continue;
+        const double theta = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+        for (int k = 0; k < 3; ++k) {  /* A <- A J */
+          const double akp = A[k][p], akq = A[k][q];
+          A[k][p] = c * akp - sn * akq;
+          A[k][q] = sn * akp + c * akq;
+        }
+        for (int k = 0; k < 3; ++k) {  /* A <- J^T A */
+          const double apk = A[p][k], aqk = A[q][k];
+          A[p][k] = c * apk - sn * aqk;
+          A[q][k] = sn * apk + c * aqk;
+        }
+        for (int k = 0; k < 3; ++k) {  /* V <- V J */
+          const double vkp = V[k][p], vkq = V[k][q];
+          V[k][p] = c * vkp - sn * vkq;
+          V[k][q] = sn * vkp + c * vkq;
+        }
+      }
+  }
+  for (int i = 0; i < 3; ++i) d[i] = A[i][i];
+}
+
+/* oo_params (v25/functions.cpp:2702-2748) with Qmat_3d (:3426-3445): the
+   total dipole moment M = sum mu o (lab frame), the nematic order G2 = the
+   largest |eigenvalue| of Q = sum (3 o o^T - 1) / (2 N) (accumulated in
+   FP32 as Qmat_3d does) and G1 = |sum o . e| / N along its eigenvector.
+   The eigen solver is this file's own (sym3_eigen), not the reference's, so
+   G1 and G2 agree with the reference to FP32 precision, not bit for bit. */
+void mdsc_or_oo_params(const mdsc_oracle_state* s, double* G1, double* G2, double M[3]) {
+  for (int a = 0; a < 3; ++a) M[a] = 0.0;
+  for (int i = 0; i < s->n; ++i)
+    for (int w = 0; w < s->nd; ++w) {
+      double pos[3], ori[3], lev[3], mu;
+      dip_lab(s, i, w, pos, ori, lev, &mu);
+      for (int a = 0; a < 3; ++a) M[a] += mu * ori[a];
+    }
+  float Q[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int k = 0; k < s->n; ++k) {
+    const double* o = s->O + 9 * k + 6;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        Q[i][j] += ((float)(3 * o[i] * o[j]) - (float)(i == j ? 1 : 0)) / (2 * s->n);
+  }
+  double Qd[3][3], d[3], V[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) Qd[i][j] = Q[i][j];
+  sym3_eigen(Qd, d, V);
+  const double e1 = fabs(d[0]), e2 = fabs(d[1]), e3 = fabs(d[2]);
+  int c;
+  if (e1 >= e2 && e1 >= e3) c = 0;
+  else if (e2 > e1 && e2 >= e3) c = 1;
+  else c = 2;
+  *G2 = fabs(d[c]);
+  double Ve[3] = {V[0][c], V[1][c], V[2][c]};
+  const double nv = sqrt(Ve[0] * Ve[0] + Ve[1] * Ve[1] + Ve[2] * Ve[2]);
+  for (int a = 0; a < 3; ++a) Ve[a] /= nv;
+  double g1 = 0.0;
+  for (int k = 0; k < s->n; ++k) {
+    const double* o = s->O + 9 * k + 6;
+    g1 += Ve[0] * o[0] + Ve[1] * o[1] + Ve[2] * o[2];
+  }
+  *G1 = fabs(g1) / s->n;
+}

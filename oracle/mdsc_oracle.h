@@ -140,6 +140,11 @@ void mdsc_or_md_set_thermo(mdsc_or_md* md, const double xi[2], const double strn
 /* number of OpenMP threads the routines may use (1 = serial, bit-exact) */
 void mdsc_or_set_threads(int n);
 
+/* acc_correl, v25/functions.cpp:2400-2470 (one species): hist[4*nbins] += */
+void mdsc_or_acc_correl(const mdsc_oracle_state* s, double bar_w, int nbins, double* hist);
+/* oo_params, v25/functions.cpp:2702-2748: G1, G2 and the total moment M */
+void mdsc_or_oo_params(const mdsc_oracle_state* s, double* G1, double* G2, double M[3]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -14,6 +14,8 @@
 #include "functions.hpp"
 #include <vector>
 #include <deque>
+#include <algorithm>
+#include <cmath>
 
 extern "C" {
 
@@ -313,3 +315,34 @@ void mdsc_ref_moveTher(double* xi, double* strn, double Q, double gamma, void* r
 }
 
 }  // extern "C"
+
+// acc_correl (v25/functions.cpp:2400-2470), one species: the intra
+// histograms of this state added to hist[4*nbins] (000, 110, 112, 220).
+// acc_correl does not check the bin against the matrix, so the matrix here
+// reaches the largest minimum-image distance, half the box diagonal; only
+// the first nbins bins are returned.
+extern "C" void mdsc_ref_acc_correl(mdsc_ref_state* s, double bar_w, int nbins, double* hist) {
+  Dynvec<Dynvec<Spherocyl> > part;
+  part_num NP;
+  build_part(s, part, NP);
+  const double diag = 0.5 * sqrt(s->L[0] * s->L[0] + s->L[1] * s->L[1] + s->L[2] * s->L[2]);
+  const int nfull = std::max(nbins, (int)floor(diag / bar_w) + 2);
+  Dynvec<Matrix<double> > Hista(1), Histe(1);
+  Hista[0].set_size(4, nfull);
+  Hista[0].set_to(0.);
+  acc_correl(part, Hista, Histe, s->L, bar_w, NP, nullptr);
+  for (int f = 0; f < 4; ++f)
+    for (int b = 0; b < nbins; ++b) hist[f * nbins + b] += Hista[0][f][b];
+}
+
+// oo_params (v25/functions.cpp:2702-2748): G1, G2 and the total moment M
+extern "C" void mdsc_ref_oo_params(mdsc_ref_state* s, double* G1, double* G2, double* M) {
+  Dynvec<Dynvec<Spherocyl> > part;
+  part_num NP;
+  build_part(s, part, NP);
+  double g1 = 0, g2 = 0, m[3] = {0, 0, 0};
+  oo_params(part, NP, g1, g2, m);
+  *G1 = g1;
+  *G2 = g2;
+  for (int a = 0; a < 3; ++a) M[a] = m[a];
+}

@@ -96,6 +96,12 @@ def run_case(ref: oracle.Ref, name, st, box, alpha, K_max, ksq):
         d[f"cl{ms}_next"] = nxt
     counts, idx = ref.neigh_list(mk(), 3.5)
     d.update(nl_counts=counts, nl_idx=idx)
+    # observables: pair correlations with ~170 bins, order parameters
+    bar_w = float(min(box)) / 200.0
+    nbins = int(np.floor(np.sqrt(3.0) * float(min(box)) / (2.0 * bar_w)))
+    d.update(corr_bar_w=bar_w, corr_hist=ref.acc_correl(mk(), bar_w, nbins))
+    G1, G2, M = ref.oo_params(mk())
+    d.update(oo_G1=G1, oo_G2=G2, oo_M=M)
     return d
 
 

@@ -6,6 +6,7 @@
   on seeded systems -- runs where the reference sources are present.
 * Restatement vs the golden fixtures made from the reference
   (tests/golden/) -- runs everywhere.
+* Observables outside the step (acc_correl, oo_params) against both.
 """
 import ctypes
 import os
@@ -177,3 +178,30 @@ def test_restatement_matches_golden_fixtures(orc, path):
         assert np.array_equal(lab, g[f"cl{ms}_labels"]) and nxt == g[f"cl{ms}_next"]
     counts, idx = orc.neigh_list(mk(), 3.5)
     assert np.array_equal(counts, g["nl_counts"]) and np.array_equal(idx, g["nl_idx"])
+    _check_observables(orc, mk(), float(g["corr_bar_w"]), g["corr_hist"], g["oo_G1"], g["oo_G2"], g["oo_M"])
+
+
+def _check_observables(orc, s, bar_w, hist, G1, G2, M):
+    """acc_correl: counts exact, the other sums to FP64 rounding (the
+    reference adds them under OpenMP atomics, in thread order); oo_params:
+    M to FP64 rounding, G1 and G2 to 1e-6 (the reference's Q and its eigen
+    solve are FP32, the restatement's solve is FP64)."""
+    h = orc.acc_correl(s, bar_w, hist.shape[1])
+    assert np.array_equal(h[0], hist[0])
+    assert np.abs(h[1:] - hist[1:]).max() <= 1e-12 * max(1.0, hist[0].max())
+    g1, g2, m = orc.oo_params(s)
+    assert abs(g1 - G1) <= 1e-6 and abs(g2 - G2) <= 1e-6
+    assert np.abs(m - M).max() <= 1e-12 * max(1.0, np.abs(M).max())
+
+
+@pytest.mark.parametrize("k", range(3))
+def test_observables_vs_reference(ref, orc, k):
+    st, box, *_ = _systems()[k]
+    bar_w = float(min(box)) / 150.0
+    nbins = int(np.floor(np.sqrt(3.0) * float(min(box)) / (2.0 * bar_w)))
+    hist = ref.acc_correl(_sys(st, box), bar_w, nbins)
+    G1, G2, M = ref.oo_params(_sys(st, box))
+    _check_observables(orc, _sys(st, box), bar_w, hist, G1, G2, M)
+    # accumulation over calls, as Hista accumulates over a run
+    h2 = orc.acc_correl(_sys(st, box), bar_w, nbins, orc.acc_correl(_sys(st, box), bar_w, nbins))
+    assert np.array_equal(h2[0], 2 * hist[0])
