@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define MDSC_ABI_VERSION 1
+#define MDSC_ABI_VERSION 2  /* 2: mdsc_observables gained G1, G2, M */
 #define MDSC_MAX_DIPOLES 4 /* dipoles per particle */
 
 typedef enum {
@@ -109,6 +109,12 @@ typedef struct {
   int n_clusters;   /* clusters found at the last clustering step */
   int list_builds;  /* neighbour-list rebuilds so far */
   int pad;
+  /* oo_params (v25/functions.cpp:2702-2760) of the state after the step, as
+     the driver takes them every step (v25/main.cpp:720-728): nematic order
+     G2, polar order G1 and the total dipole moment M.  Per-particle terms in
+     FP32 (the reference forms Q in FP32 too), float-float sums. */
+  double G1, G2;
+  double M[3];
 } mdsc_observables;
 
 typedef struct mdsc_batch mdsc_batch;

@@ -7,8 +7,10 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <atomic>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -54,7 +56,8 @@ struct Layout {
   std::vector<SysDev> sys;
   std::vector<int4> tiles, kn, kwork;
   std::vector<float4> kv;
-  std::vector<float4> rtab;  // real-space tables of every system
+  std::vector<float4> rtab;  // real-space tables of every system (filled by fill_tables)
+  size_t rtab_n = 0;         // float4 slots the tables take (2 per entry)
   std::vector<double> kval, kpre, kvec;
   std::vector<int2> blk, kowner;
   int ntot = 0, ndtot = 0, nktot = 0, maxnd = 0, nchunks = 0;
@@ -133,6 +136,100 @@ void set_pair_consts(SysDev& P) {
     const double h = P.L[a] / 4294967296.0;
     P.Lhi[a] = (float)h;
     P.Llo[a] = (float)(h - (double)P.Lhi[a]);
+  }
+}
+
+// One system's table as stored on the device: per entry (A, B, C, dA) and
+// (dB, dC, 0, 0), the differences to the next entry.
+std::vector<float4> table_entries(double alpha, int n) {
+  std::vector<double> T(3 * (size_t)(n + 1));
+  table_values(alpha, n + 1, T.data());
+  std::vector<float4> e(2 * (size_t)n);
+  for (int k = 0; k < n; ++k) {
+    const double* a = &T[3 * (size_t)k];
+    const double* b = &T[3 * (size_t)(k + 1)];
+    e[2 * (size_t)k] = make_float4((float)a[0], (float)a[1], (float)a[2], (float)(b[0] - a[0]));
+    e[2 * (size_t)k + 1] = make_float4((float)(b[1] - a[1]), (float)(b[2] - a[2]), 0.f, 0.f);
+  }
+  return e;
+}
+
+// Tables are a pure function of (alpha, entries) and take ~1 ms each to
+// build, so a process keeps the recent ones: a server that rebuilds its
+// batch whenever jobs come and go finds the running systems' tables here.
+// Least recently used tables leave first, above kTableCacheBytes.
+constexpr size_t kTableCacheBytes = size_t(256) << 20;
+struct TableCache {
+  std::mutex mu;
+  std::map<std::pair<uint64_t, int>, std::pair<std::vector<float4>, uint64_t>> m;  // -> (entries, last use)
+  uint64_t clock = 0;
+  size_t bytes = 0;
+};
+TableCache g_tables;
+
+void fill_tables(const mdsc_system_desc* descs, Layout& Lo) {
+  Lo.rtab.assign(Lo.rtab_n, make_float4(0.f, 0.f, 0.f, 0.f));
+  const int nsys = (int)Lo.sys.size();
+  auto key_of = [&](int s) {
+    uint64_t a;
+    memcpy(&a, &descs[s].alpha, 8);
+    return std::make_pair(a, Lo.sys[s].rt_n);
+  };
+  // systems whose table is not cached: build them on all host threads
+  std::vector<int> miss;
+  {
+    std::lock_guard<std::mutex> g(g_tables.mu);
+    std::map<std::pair<uint64_t, int>, int> first;
+    for (int s = 0; s < nsys; ++s) {
+      if (descs[s].nd <= 0) continue;
+      const auto k = key_of(s);
+      auto it = g_tables.m.find(k);
+      if (it != g_tables.m.end()) {
+        it->second.second = ++g_tables.clock;
+        std::copy(it->second.first.begin(), it->second.first.end(), Lo.rtab.begin() + 2 * (size_t)Lo.sys[s].rt_off);
+      } else if (first.emplace(k, s).second) {
+        miss.push_back(s);
+      }
+    }
+  }
+  if (!miss.empty()) {
+    std::vector<std::vector<float4>> built(miss.size());
+    const int nth = (int)std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), (unsigned)miss.size()));
+    std::atomic<int> next{0};
+    auto work = [&] {
+      for (int q; (q = next.fetch_add(1)) < (int)miss.size();)
+        built[q] = table_entries(descs[miss[q]].alpha, Lo.sys[miss[q]].rt_n);
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < nth; ++t) th.emplace_back(work);
+    work();
+    for (auto& t : th) t.join();
+    std::lock_guard<std::mutex> g(g_tables.mu);
+    for (size_t q = 0; q < miss.size(); ++q) {
+      const auto k = key_of(miss[q]);
+      if (g_tables.m.count(k)) continue;
+      g_tables.bytes += sizeof(float4) * built[q].size();
+      g_tables.m[k] = std::make_pair(std::move(built[q]), ++g_tables.clock);
+    }
+    while (g_tables.bytes > kTableCacheBytes && g_tables.m.size() > 1) {
+      auto old = g_tables.m.begin();
+      for (auto it = g_tables.m.begin(); it != g_tables.m.end(); ++it)
+        if (it->second.second < old->second.second) old = it;
+      g_tables.bytes -= sizeof(float4) * old->second.first.size();
+      g_tables.m.erase(old);
+    }
+  }
+  // every system, in order, from the cache or a sibling with the same key
+  std::lock_guard<std::mutex> g(g_tables.mu);
+  for (int s = 0; s < nsys; ++s) {
+    if (descs[s].nd <= 0) continue;
+    auto it = g_tables.m.find(key_of(s));
+    if (it != g_tables.m.end()) {
+      std::copy(it->second.first.begin(), it->second.first.end(), Lo.rtab.begin() + 2 * (size_t)Lo.sys[s].rt_off);
+    } else {  // evicted at once (cache smaller than this batch's tables): build here
+      const std::vector<float4> e = table_entries(descs[s].alpha, Lo.sys[s].rt_n);
+      std::copy(e.begin(), e.end(), Lo.rtab.begin() + 2 * (size_t)Lo.sys[s].rt_off);
+    }
   }
 }
 
@@ -224,16 +321,9 @@ void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
     if (d.nd > 0) {
       const double hd = 0.5 * std::sqrt(d.box[0] * d.box[0] + d.box[1] * d.box[1] + d.box[2] * d.box[2]);
       const int n = std::min((int)std::floor(hd / kLh) + 3, 32767);
-      P.rt_off = (int)(Lo.rtab.size() / 2);
+      P.rt_off = (int)(Lo.rtab_n / 2);
       P.rt_n = n;
-      std::vector<double> T(3 * (size_t)(n + 1));
-      table_values(d.alpha, n + 1, T.data());
-      for (int k = 0; k < n; ++k) {
-        const double* a = &T[3 * (size_t)k];
-        const double* b = &T[3 * (size_t)(k + 1)];
-        Lo.rtab.push_back(make_float4((float)a[0], (float)a[1], (float)a[2], (float)(b[0] - a[0])));
-        Lo.rtab.push_back(make_float4((float)(b[1] - a[1]), (float)(b[2] - a[2]), 0.f, 0.f));
-      }
+      Lo.rtab_n += 2 * (size_t)n;
     }
     part += d.n;
     dip += P.ndip;
@@ -310,7 +400,7 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   b.wrec = A.take<double>(n * kMaxC * 6);
   b.kn = A.take<int4>(nk);
   b.kv = A.take<float4>(nk);
-  b.rtab = A.take<float4>(std::max<size_t>(Lo.rtab.size(), 1));
+  b.rtab = A.take<float4>(std::max<size_t>(Lo.rtab_n, 1));
   b.kval = A.take<double>(nk);
   b.kvec = A.take<double>(3 * nk);
   b.kpre = A.take<double>(nk);
@@ -327,6 +417,7 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   b.kin1 = A.take<double>(2 * nb);
   b.kin2 = A.take<double>(9 * nb);
   b.dmax = A.take<double>(nb);
+  b.osum = A.take<double>(12 * nb);
   b.blk = A.take<int2>(nb);
   b.nb = A.take<int>(n * kMaxNb);
   b.nbc = A.take<int>(n);
@@ -627,6 +718,8 @@ mdsc_status run_clusters(mdsc_batch* B, const std::vector<int>& systems) {
   return MDSC_OK;
 }
 
+void order_params(const double* v, int n, double* G1, double* G2, double* M);
+
 mdsc_status read_obs(mdsc_batch* B, mdsc_observables* out) {
   CU(cudaMemcpyAsync(B->h_obs, B->b.obs, sizeof(SysObs) * B->nsys, cudaMemcpyDeviceToHost, B->st));
   CU(cudaStreamSynchronize(B->st));
@@ -657,6 +750,7 @@ mdsc_status read_obs(mdsc_batch* B, mdsc_observables* out) {
     r.status = status_from_bits(o.status);
     r.n_clusters = B->n_clusters[s];
     r.list_builds = o.list_builds;
+    order_params(o.osum, B->lo.sys[s].n, &r.G1, &r.G2, r.M);
   }
   const mdsc_status st = status_from_bits(bits);
   if (st != MDSC_OK) return fail(B, st, "a system reported an error (see mdsc_observables.status)");
@@ -763,6 +857,31 @@ void sym3_eigen(const double (&A0)[3][3], double (&d)[3], double (&V)[3][3]) {
   for (int i = 0; i < 3; ++i) d[i] = A[i][i];
 }
 
+// oo_params (v25/functions.cpp:2702-2760) from the sums v[12] over n
+// particles: sum o (3), sum o o^T (xx xy xz yy yz zz), sum mu o_dipole (3).
+// Q = sum (3 o o^T - 1) / (2 n) (Qmat_3d, :3426-3445); G2 is its eigenvalue
+// of largest magnitude, chosen among equal magnitudes as the reference
+// chooses (:2738-2748), and G1 = |e . sum o| / n along that eigenvector.
+void order_params(const double* v, int n, double* G1, double* G2, double* M) {
+  if (M)
+    for (int a = 0; a < 3; ++a) M[a] = v[9 + a];
+  if (n <= 0) {
+    if (G1) *G1 = 0.0;
+    if (G2) *G2 = 0.0;
+    return;
+  }
+  const int ix[3][3] = {{3, 4, 5}, {4, 6, 7}, {5, 7, 8}};
+  double Q[3][3], ev[3], V[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) Q[i][j] = (3.0 * v[ix[i][j]] - (i == j ? n : 0.0)) / (2.0 * n);
+  sym3_eigen(Q, ev, V);
+  const double e1 = std::fabs(ev[0]), e2 = std::fabs(ev[1]), e3 = std::fabs(ev[2]);
+  const int c = (e1 >= e2 && e1 >= e3) ? 0 : (e2 > e1 && e2 >= e3) ? 1 : 2;
+  const double nv = std::sqrt(V[0][c] * V[0][c] + V[1][c] * V[1][c] + V[2][c] * V[2][c]);
+  if (G2) *G2 = std::fabs(ev[c]);
+  if (G1) *G1 = std::fabs((V[0][c] * v[0] + V[1][c] * v[1] + V[2][c] * v[2]) / nv) / n;
+}
+
 }  // namespace
 
 // ======================================================================
@@ -806,6 +925,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   B->desc.assign(descs, descs + nsys);
   cudaSetDevice(device);
   make_layout(descs, nsys, B->lo);
+  fill_tables(descs, B->lo);
   const Layout& lo = B->lo;
   Arena A;
   carve(A, lo, nsys, B->b, &B->kwork, &B->kowner, B->noise);
@@ -903,6 +1023,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
     mdsc_destroy(B);
     return MDSC_ERR_CUDA;
   }
+  std::vector<float4>().swap(B->lo.rtab);  // on the device now; the host copy is not read again
   *out = B;
   return MDSC_OK;
 }
@@ -1337,21 +1458,7 @@ mdsc_status mdsc_order_params(mdsc_batch* B, double* G1, double* G2, double* M) 
     double v[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (int k = 0; k < P.nblk; ++k)
       for (int c = 0; c < 12; ++c) v[c] += part[12 * (size_t)(P.blk_off + k) + c];
-    if (M)
-      for (int a = 0; a < 3; ++a) M[3 * s + a] = v[9 + a];
-    // Q = sum (3 o o^T - 1) / (2 N) (Qmat_3d, v25/functions.cpp:3426-3445)
-    const double n = P.n;
-    const int ix[3][3] = {{3, 4, 5}, {4, 6, 7}, {5, 7, 8}};
-    double Q[3][3], ev[3], V[3][3];
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) Q[i][j] = (3.0 * v[ix[i][j]] - (i == j ? n : 0.0)) / (2.0 * n);
-    sym3_eigen(Q, ev, V);
-    // the reference's choice among equal |eigenvalues| (v25/functions.cpp:2738-2748)
-    const double e1 = std::fabs(ev[0]), e2 = std::fabs(ev[1]), e3 = std::fabs(ev[2]);
-    const int c = (e1 >= e2 && e1 >= e3) ? 0 : (e2 > e1 && e2 >= e3) ? 1 : 2;
-    const double nv = std::sqrt(V[0][c] * V[0][c] + V[1][c] * V[1][c] + V[2][c] * V[2][c]);
-    if (G2) G2[s] = std::fabs(ev[c]);
-    if (G1) G1[s] = std::fabs((V[0][c] * v[0] + V[1][c] * v[1] + V[2][c] * v[2]) / nv) / n;
+    order_params(v, P.n, G1 ? &G1[s] : nullptr, G2 ? &G2[s] : nullptr, M ? &M[3 * s] : nullptr);
   }
   return MDSC_OK;
 }

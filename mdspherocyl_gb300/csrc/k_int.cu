@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(kPartBlock) integrate_first_kernel(Batch b) {
 // force assembly (+ ext_field) and optionally moveP(last)
 // ---------------------------------------------------------------------
 __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode) {
-  __shared__ double sh[20 * kPartBlock / 32];
+  __shared__ double sh[32 * kPartBlock / 32];
   const int2 bk = b.blk[blockIdx.x];
   const int s = bk.x;
   const SysDev& P = b.sys[s];
@@ -290,11 +290,36 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
   const int i = bk.y + threadIdx.x;
   const bool ok = i < P.part_off + P.n;
   // block sums: K_t, K_r, PT_kin (6), U_ext, then the WCA terms U, W, PT (9)
-  // of this block's own candidate pairs
-  FF acc[20];
+  // of this block's own candidate pairs, then the order-parameter terms (12)
+  FF acc[32];
 #pragma unroll
-  for (int c = 0; c < 20; ++c) acc[c].hi = acc[c].lo = 0.f;
+  for (int c = 0; c < 32; ++c) acc[c].hi = acc[c].lo = 0.f;
   if (ok) {
+    // oo_params' terms (v25/functions.cpp:2720-2760, Qmat_3d :3426-3445)
+    // from the FP32 working copies of this step's orientation: the rod axis
+    // o, o o^T, and the dipole vectors mu o_dipole
+    const float4 oa = b.pax[i];
+    acc[20] = ff_of(oa.x);
+    acc[21] = ff_of(oa.y);
+    acc[22] = ff_of(oa.z);
+    acc[23] = ff_of(oa.x * oa.x);
+    acc[24] = ff_of(oa.x * oa.y);
+    acc[25] = ff_of(oa.x * oa.z);
+    acc[26] = ff_of(oa.y * oa.y);
+    acc[27] = ff_of(oa.y * oa.z);
+    acc[28] = ff_of(oa.z * oa.z);
+    {
+      const int ND = b.ndtot, g0 = P.dip_off + (i - P.part_off) * P.nd;
+      float m0 = 0.f, m1 = 0.f, m2 = 0.f;
+      for (int w = 0; w < P.nd; ++w) {
+        m0 += b.dm[g0 + w];
+        m1 += b.dm[ND + g0 + w];
+        m2 += b.dm[2 * ND + g0 + w];
+      }
+      acc[29] = ff_of(m0);
+      acc[30] = ff_of(m1);
+      acc[31] = ff_of(m2);
+    }
     double F[3], T[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -448,11 +473,13 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
       b.T[3 * i + a] = T[a];
     }
   }
-  double tot[20];
-  block_sum<20, kPartBlock>(acc, sh, tot);
+  double tot[32];
+  block_sum<32, kPartBlock>(acc, sh, tot);
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int c = 0; c < 9; ++c) b.kin2[9 * blk_slot(P, bk) + c] = tot[c];
+#pragma unroll
+    for (int c = 0; c < 12; ++c) b.osum[12 * blk_slot(P, bk) + c] = tot[20 + c];
     if (mode & kMaskWca) {
 #pragma unroll
       for (int c = 0; c < 11; ++c) b.wcaE[11 * blk_slot(P, bk) + c] = tot[9 + c];
@@ -461,14 +488,14 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
 }
 
 // ---------------------------------------------------------------------
-// per-system sums and the thermostat's last update.  Four blocks per
+// per-system sums and the thermostat's last update.  kRedGroups blocks per
 // system, one per group of sums (real-space tiles, k-vectors, WCA blocks,
-// kinetic terms), each in float-float with a fixed order; the kinetic block
-// also closes the step's thermostat and bookkeeping.
+// kinetic terms, order parameters), each in float-float with a fixed order;
+// the kinetic block also closes the step's thermostat and bookkeeping.
 constexpr int kRedThreads = 128;
 __global__ void __launch_bounds__(kRedThreads) reduce_obs_kernel(Batch b, int mode) {
-  __shared__ double sh[11 * kRedThreads / 32];
-  const int s = blockIdx.x >> 2, grp = blockIdx.x & 3;
+  __shared__ double sh[12 * kRedThreads / 32];
+  const int s = blockIdx.x / kRedGroups, grp = blockIdx.x % kRedGroups;
   const SysDev& P = b.sys[s];
   SysState& S = b.st[s];
   SysObs& ob = b.obs[s];
@@ -513,6 +540,20 @@ __global__ void __launch_bounds__(kRedThreads) reduce_obs_kernel(Batch b, int mo
       ob.W_ss = out[1];
       for (int c = 0; c < 9; ++c) ob.PT_ss[c] = out[2 + c];
     }
+  } else if (grp == 4) {
+    // order-parameter sums per particle block
+    FF w[12];
+#pragma unroll
+    for (int c = 0; c < 12; ++c) w[c].hi = w[c].lo = 0.f;
+    for (int k = threadIdx.x; k < P.nblk; k += kRedThreads) {
+      const double* e = b.osum + (long long)(P.blk_off + k) * 12;
+#pragma unroll
+      for (int c = 0; c < 12; ++c) w[c] = ff_add(w[c], ff_from(e[c]));
+    }
+    double o12[12];
+    block_sum<12, kRedThreads>(w, sh, o12);
+    if (threadIdx.x == 0)
+      for (int c = 0; c < 12; ++c) ob.osum[c] = o12[c];
   } else {
     // kinetic terms and the field energy
     for (int k = threadIdx.x; k < P.nblk; k += kRedThreads) {
@@ -664,7 +705,7 @@ void launch_finalize(const Batch& b, int mode, cudaStream_t s) {
   if (b.nblk) finalize_kernel<<<b.nblk, kPartBlock, 0, s>>>(b, mode);
 }
 void launch_reduce_obs(const Batch& b, int mode, cudaStream_t s) {
-  if (b.nsys) reduce_obs_kernel<<<4 * b.nsys, kRedThreads, 0, s>>>(b, mode);
+  if (b.nsys) reduce_obs_kernel<<<kRedGroups * b.nsys, kRedThreads, 0, s>>>(b, mode);
 }
 void launch_movex(const Batch& b, cudaStream_t s) {
   if (b.nblk) movex_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);

@@ -121,3 +121,22 @@ def test_normalize_correlations():
     k = 12  # pos = 6.25 in [L/2, L/sqrt 2]: the shell cut by the box
     assert norm[k] == pytest.approx(4 * np.pi * pos[k] ** 2 * (3 * 10.0 / (2 * pos[k]) - 2) * bar_w)
     assert g[1, 3] == pytest.approx(3.0 / (norm[3] * 2.0 * 100 * 99))
+
+
+@pytest.mark.gpu
+def test_order_params_every_step(orc):
+    """mdsc_step's G1, G2, M (FP32 terms, taken every step as the driver
+    does) against the FP64 call and the oracle on the state after the step."""
+    systems = _mix()
+    with L.Batch([_spec(st, b) for st, b in systems], [st for st, _ in systems]) as bt:
+        obs = bt.step(2)
+        G1, G2, M = bt.order_params()
+        for k, (st, box) in enumerate(systems):
+            d = bt.download(k)
+            s = oracle.System(d["r"], d["p"], d["O"], d["l"], st.length, st.dia, st.mass, st.dip, box)
+            g1, g2, m = orc.oo_params(s)
+            scale = np.abs(st.dip[:, :, 4]).sum()
+            assert abs(obs[k]["G2"] - G2[k]) <= 1e-6 and abs(G2[k] - g2) <= 1e-5
+            assert abs(obs[k]["G1"] - G1[k]) <= 1e-4 and abs(G1[k] - g1) <= 1e-4
+            assert np.abs(np.array(obs[k]["M"]) - M[k]).max() <= 1e-6 * scale
+            assert np.abs(M[k] - m).max() <= 1e-12 * scale
