@@ -417,7 +417,6 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   b.kin1 = A.take<double>(2 * nb);
   b.kin2 = A.take<double>(9 * nb);
   b.dmax = A.take<double>(nb);
-  b.osum = A.take<double>(12 * nb);
   b.blk = A.take<int2>(nb);
   b.nb = A.take<int>(n * kMaxNb);
   b.nbc = A.take<int>(n);

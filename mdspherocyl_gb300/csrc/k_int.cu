@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(kPartBlock) integrate_first_kernel(Batch b) {
 // force assembly (+ ext_field) and optionally moveP(last)
 // ---------------------------------------------------------------------
 __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode) {
-  __shared__ double sh[32 * kPartBlock / 32];
+  __shared__ double sh[20 * kPartBlock / 32];
   const int2 bk = b.blk[blockIdx.x];
   const int s = bk.x;
   const SysDev& P = b.sys[s];
@@ -290,36 +290,11 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
   const int i = bk.y + threadIdx.x;
   const bool ok = i < P.part_off + P.n;
   // block sums: K_t, K_r, PT_kin (6), U_ext, then the WCA terms U, W, PT (9)
-  // of this block's own candidate pairs, then the order-parameter terms (12)
-  FF acc[32];
+  // of this block's own candidate pairs
+  FF acc[20];
 #pragma unroll
-  for (int c = 0; c < 32; ++c) acc[c].hi = acc[c].lo = 0.f;
+  for (int c = 0; c < 20; ++c) acc[c].hi = acc[c].lo = 0.f;
   if (ok) {
-    // oo_params' terms (v25/functions.cpp:2720-2760, Qmat_3d :3426-3445)
-    // from the FP32 working copies of this step's orientation: the rod axis
-    // o, o o^T, and the dipole vectors mu o_dipole
-    const float4 oa = b.pax[i];
-    acc[20] = ff_of(oa.x);
-    acc[21] = ff_of(oa.y);
-    acc[22] = ff_of(oa.z);
-    acc[23] = ff_of(oa.x * oa.x);
-    acc[24] = ff_of(oa.x * oa.y);
-    acc[25] = ff_of(oa.x * oa.z);
-    acc[26] = ff_of(oa.y * oa.y);
-    acc[27] = ff_of(oa.y * oa.z);
-    acc[28] = ff_of(oa.z * oa.z);
-    {
-      const int ND = b.ndtot, g0 = P.dip_off + (i - P.part_off) * P.nd;
-      float m0 = 0.f, m1 = 0.f, m2 = 0.f;
-      for (int w = 0; w < P.nd; ++w) {
-        m0 += b.dm[g0 + w];
-        m1 += b.dm[ND + g0 + w];
-        m2 += b.dm[2 * ND + g0 + w];
-      }
-      acc[29] = ff_of(m0);
-      acc[30] = ff_of(m1);
-      acc[31] = ff_of(m2);
-    }
     double F[3], T[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -473,13 +448,11 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
       b.T[3 * i + a] = T[a];
     }
   }
-  double tot[32];
-  block_sum<32, kPartBlock>(acc, sh, tot);
+  double tot[20];
+  block_sum<20, kPartBlock>(acc, sh, tot);
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int c = 0; c < 9; ++c) b.kin2[9 * blk_slot(P, bk) + c] = tot[c];
-#pragma unroll
-    for (int c = 0; c < 12; ++c) b.osum[12 * blk_slot(P, bk) + c] = tot[20 + c];
     if (mode & kMaskWca) {
 #pragma unroll
       for (int c = 0; c < 11; ++c) b.wcaE[11 * blk_slot(P, bk) + c] = tot[9 + c];
@@ -541,14 +514,23 @@ __global__ void __launch_bounds__(kRedThreads) reduce_obs_kernel(Batch b, int mo
       for (int c = 0; c < 9; ++c) ob.PT_ss[c] = out[2 + c];
     }
   } else if (grp == 4) {
-    // order-parameter sums per particle block
+    // oo_params' terms (v25/functions.cpp:2720-2760, Qmat_3d :3426-3445)
+    // from the FP32 working copies of the current orientations: the rod
+    // axis o, o o^T and the dipole vectors mu o_dipole, particle by particle
     FF w[12];
 #pragma unroll
     for (int c = 0; c < 12; ++c) w[c].hi = w[c].lo = 0.f;
-    for (int k = threadIdx.x; k < P.nblk; k += kRedThreads) {
-      const double* e = b.osum + (long long)(P.blk_off + k) * 12;
+    const int ND = b.ndtot;
+    for (int i = P.part_off + threadIdx.x; i < P.part_off + P.n; i += kRedThreads) {
+      const float4 o = b.pax[i];
+      const float t[9] = {o.x, o.y, o.z, o.x * o.x, o.x * o.y, o.x * o.z, o.y * o.y, o.y * o.z, o.z * o.z};
 #pragma unroll
-      for (int c = 0; c < 12; ++c) w[c] = ff_add(w[c], ff_from(e[c]));
+      for (int c = 0; c < 9; ++c) w[c] = ff_add(w[c], ff_of(t[c]));
+      const int g0 = P.dip_off + (i - P.part_off) * P.nd;
+      for (int q = 0; q < P.nd; ++q) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) w[9 + a] = ff_add(w[9 + a], ff_of(b.dm[a * ND + g0 + q]));
+      }
     }
     double o12[12];
     block_sum<12, kRedThreads>(w, sh, o12);

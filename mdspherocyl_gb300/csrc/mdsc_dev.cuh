@@ -182,7 +182,6 @@ struct Batch {
   double* kin1;  // 2 per block
   double* kin2;  // 9 per block: K_t, K_r, PTkin xx xy xz yy yz zz, U_ext
   double* dmax;  // 1 per block: largest displacement measure since the last list build
-  double* osum;  // 12 per block: the order-parameter sums of SysObs::osum
   int2* blk;     // (sys, first particle) per block
   // neighbour list
   int* nb;       // n * kMaxNb
