@@ -520,16 +520,33 @@ __global__ void __launch_bounds__(kRedThreads) reduce_obs_kernel(Batch b, int mo
     FF w[12];
 #pragma unroll
     for (int c = 0; c < 12; ++c) w[c].hi = w[c].lo = 0.f;
-    const int ND = b.ndtot;
-    for (int i = P.part_off + threadIdx.x; i < P.part_off + P.n; i += kRedThreads) {
-      const float4 o = b.pax[i];
-      const float t[9] = {o.x, o.y, o.z, o.x * o.x, o.x * o.y, o.x * o.z, o.y * o.y, o.y * o.z, o.z * o.z};
+    // four particles per thread per pass, their loads issued together (the
+    // largest system's block is on the step's critical path)
+    const int ND = b.ndtot, nd = P.nd, end = P.part_off + P.n;
+    for (int i0 = P.part_off + threadIdx.x; i0 < end; i0 += 4 * kRedThreads) {
+      float4 o[4];
+      float m[4][3];
 #pragma unroll
-      for (int c = 0; c < 9; ++c) w[c] = ff_add(w[c], ff_of(t[c]));
-      const int g0 = P.dip_off + (i - P.part_off) * P.nd;
-      for (int q = 0; q < P.nd; ++q) {
+      for (int u = 0; u < 4; ++u) {
+        const int i = i0 + u * kRedThreads;
+        o[u] = i < end ? b.pax[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        m[u][0] = m[u][1] = m[u][2] = 0.f;
+        if (i < end) {
+          const int g0 = P.dip_off + (i - P.part_off) * nd;
+          for (int q = 0; q < nd; ++q) {
 #pragma unroll
-        for (int a = 0; a < 3; ++a) w[9 + a] = ff_add(w[9 + a], ff_of(b.dm[a * ND + g0 + q]));
+            for (int a = 0; a < 3; ++a) m[u][a] += b.dm[a * ND + g0 + q];
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (i0 + u * kRedThreads >= end) break;
+        const float4 q = o[u];
+        const float t[12] = {q.x,       q.y,       q.z,       q.x * q.x, q.x * q.y, q.x * q.z,
+                             q.y * q.y, q.y * q.z, q.z * q.z, m[u][0],   m[u][1],   m[u][2]};
+#pragma unroll
+        for (int c = 0; c < 12; ++c) w[c] = ff_add(w[c], ff_of(t[c]));
       }
     }
     double o12[12];

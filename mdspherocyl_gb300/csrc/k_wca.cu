@@ -52,13 +52,15 @@ __global__ void __launch_bounds__(kPartBlock) list_build_kernel(Batch b, int for
   }
   const float rl = (float)P.r_list;
   const float rl2 = rl * rl;
+  const float Lx = P.Lfix[0], Ly = P.Lfix[1], Lz = P.Lfix[2];
+  const int first = P.part_off, n = P.n;
   int cnt = 0;
   int* out = b.nb + (long long)i * kMaxNb;
-  for (int q0 = 0; q0 < P.n; q0 += kPartBlock) {
-    const int nq = min(kPartBlock, P.n - q0);
+  for (int q0 = 0; q0 < n; q0 += kPartBlock) {
+    const int nq = min(kPartBlock, n - q0);
     __syncthreads();
     if (threadIdx.x < nq) {
-      const int q = P.part_off + q0 + threadIdx.x;
+      const int q = first + q0 + threadIdx.x;
       sx[threadIdx.x] = b.pfx[q];
       sy[threadIdx.x] = b.pfx[N + q];
       sz[threadIdx.x] = b.pfx[2 * N + q];
@@ -66,20 +68,41 @@ __global__ void __launch_bounds__(kPartBlock) list_build_kernel(Batch b, int for
     }
     __syncthreads();
     if (!ok) continue;
-    for (int k = 0; k < nq; ++k) {
-      const int q = P.part_off + q0 + k;
-      if (q == i) continue;
-      const float dx = fix_diff(ux, sx[k], P.Lfix[0]);
-      const float dy = fix_diff(uy, sy[k], P.Lfix[1]);
-      const float dz = fix_diff(uz, sz[k], P.Lfix[2]);
-      const float4 aj = sa[k];
-      const float reach = rl + 0.5f * (ai.w + aj.w);
-      const float r2 = dx * dx + dy * dy + dz * dz;
-      if (r2 >= reach * reach) continue;
-      const float d2 = seg_dist_fast(dx, dy, dz, ai.x, ai.y, ai.z, ai.w, aj.x, aj.y, aj.z, aj.w);
-      if (d2 < rl2) {
-        if (cnt < kMaxNb) out[cnt] = q;
-        ++cnt;
+    // 1. centre distance against the reach of the two rods, branch-free,
+    //    into a mask of the chunk's 128 candidates: nearly every warp has a
+    //    lane with some candidate in reach, so testing the segments inside
+    //    this loop would run the segment routine for every candidate
+    uint32_t m[4];
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+      uint32_t bits = 0u;
+#pragma unroll 8
+      for (int kk = 0; kk < 32; ++kk) {
+        const int k = 32 * w + kk;
+        const float dx = fix_diff(ux, sx[k], Lx);
+        const float dy = fix_diff(uy, sy[k], Ly);
+        const float dz = fix_diff(uz, sz[k], Lz);
+        const float reach = rl + 0.5f * (ai.w + sa[k].w);
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        const bool in = k < nq && r2 < reach * reach && first + q0 + k != i;
+        bits |= (uint32_t)in << kk;
+      }
+      m[w] = bits;
+    }
+    // 2. segment distance of the candidates in reach, in ascending order
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+      for (uint32_t bits = m[w]; bits; bits &= bits - 1u) {
+        const int k = 32 * w + __ffs(bits) - 1;
+        const float dx = fix_diff(ux, sx[k], Lx);
+        const float dy = fix_diff(uy, sy[k], Ly);
+        const float dz = fix_diff(uz, sz[k], Lz);
+        const float4 aj = sa[k];
+        const float d2 = seg_dist_fast(dx, dy, dz, ai.x, ai.y, ai.z, ai.w, aj.x, aj.y, aj.z, aj.w);
+        if (d2 < rl2) {
+          if (cnt < kMaxNb) out[cnt] = first + q0 + k;
+          ++cnt;
+        }
       }
     }
   }
