@@ -98,9 +98,10 @@ constexpr float kQ0 = 2.820587754e-01f, kQ1 = 2.829789221e-01f, kQ2 = 2.37546384
 
 // one 32-byte table entry in a single 256-bit load through the read-only
 // path: the L1 serves a warp's 32 scattered entries in 32 wavefronts, where
-// two 128-bit loads would take 64
+// two 128-bit loads would take 64.  Not volatile: the table is constant
+// during the kernel, so the compiler may hoist the next step's loads.
 __device__ __forceinline__ void ld_entry(const float4* e, float4& p, float4& q) {
-  asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+  asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                : "=f"(p.x), "=f"(p.y), "=f"(p.z), "=f"(p.w), "=f"(q.x), "=f"(q.y), "=f"(q.z), "=f"(q.w)
                : "l"(e));
 }
@@ -278,7 +279,7 @@ __device__ __forceinline__ void tile_step(const PairConst& K, Lane2& s, const ui
 template <bool MASKED, bool MULTI, bool TAB>
 __device__ __forceinline__ void tile_loop(const PairConst& K, Lane2& s, const uint4* sj, const float4* smj,
                                           float4* sa4, float2* sa2, int lane, int jvalid) {
-#pragma unroll 1
+#pragma unroll 2
   for (int t = 0; t < kTile; ++t) {
     const int lj = (lane + t) & (kTile - 1);
     const uint4 jp = sj[lj];
