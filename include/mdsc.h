@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define MDSC_ABI_VERSION 2  /* 2: mdsc_observables gained G1, G2, M */
+#define MDSC_ABI_VERSION 2  /* 2: mdsc_observables gained G1, G2, M, P_tot, L_tot */
 #define MDSC_MAX_DIPOLES 4 /* dipoles per particle */
 
 typedef enum {
@@ -115,6 +115,9 @@ typedef struct {
      FP32 (the reference forms Q in FP32 too), float-float sums. */
   double G1, G2;
   double M[3];
+  /* total momentum and angular momentum after the step (the driver prints
+     their squares, v25/main.cpp:790-800, v25/functions.cpp:2849-2850) */
+  double P_tot[3], L_tot[3];
 } mdsc_observables;
 
 typedef struct mdsc_batch mdsc_batch;
@@ -135,8 +138,9 @@ mdsc_status mdsc_last_error(const mdsc_batch* b, char* buf, size_t len);
 
 /* ---- state transfer (host SoA <-> GPU) -------------------------------- */
 /* Uploads system `sys`.  Shape arrays (len, dia, mass, dip) are read on
-   every upload; F and T may be NULL (then zero).  Rebuilds the
-   neighbour list and the derived single-precision copies. */
+   every upload; F and T may be NULL (then zero); clust, if given, sets the
+   cluster labels (as chrg_conf reads them) until the next clustering step.
+   Rebuilds the neighbour list and the derived single-precision copies. */
 mdsc_status mdsc_upload(mdsc_batch* b, int sys, const mdsc_host_state* s);
 /* Downloads r, p, O, l, F, T and (if non-NULL) clust of system `sys`. */
 mdsc_status mdsc_download(mdsc_batch* b, int sys, mdsc_host_state* s);
@@ -146,6 +150,9 @@ mdsc_status mdsc_upload_all(mdsc_batch* b, const mdsc_host_state* packed);
 mdsc_status mdsc_download_all(mdsc_batch* b, mdsc_host_state* packed);
 /* Thermostat state: xi, stored normal (v25/classes.hpp:147-151). */
 mdsc_status mdsc_set_thermostat(mdsc_batch* b, int sys, const double xi[2], const double strn[2]);
+/* The same, read back (either pointer may be NULL): what print_conf writes
+   after the particles (v25/functions.cpp:1222-1224). */
+mdsc_status mdsc_get_thermostat(mdsc_batch* b, int sys, double xi[2], double strn[2]);
 
 /* ---- the reference's hot-path functions, on every system --------------- */
 /* Zero F and T (v25/main.cpp:582-588). */
@@ -201,6 +208,18 @@ mdsc_status mdsc_transfer(mdsc_batch* dst, int dsys, mdsc_batch* src, int ssys);
 mdsc_status mdsc_step(mdsc_batch* b, int nsteps, mdsc_observables* obs);
 /* Observables of the last step without stepping. */
 mdsc_status mdsc_observe(mdsc_batch* b, mdsc_observables* obs);
+/* mdsc_step that also returns every step's observables: trace holds
+   nsteps x nsys entries, step-major (trace[k * nsys + sys]), as the
+   reference's driver reads them after each step (accumulators, output.dat,
+   v25/main.cpp:618-650,710-800).  n_clusters changes at clustering steps. */
+mdsc_status mdsc_step_trace(mdsc_batch* b, int nsteps, mdsc_observables* trace);
+/* The state of a system's generators: which = 0, 1 the translational and
+   rotational thermostats (Thermostat::m_ran, v25/classes.cpp:344-367), 2 the
+   clustering generator.  MT19937 in GSL's layout: 624 state words and the
+   position of the next one (0..624), so the reference's ran_state files
+   (gsl_rng_fwrite) round-trip through these two calls. */
+mdsc_status mdsc_get_rng(const mdsc_batch* b, int sys, int which, uint32_t mt[624], int* mti);
+mdsc_status mdsc_set_rng(mdsc_batch* b, int sys, int which, const uint32_t mt[624], int mti);
 
 /* ---- instrumentation --------------------------------------------------- */
 /* Number of kernel launches the last mdsc_step issued per step, and the
@@ -220,17 +239,28 @@ mdsc_status mdsc_profile_steps(mdsc_batch* b, int nsteps, int max_kernels, char*
    floor(sqrt(3) Lmin / (2 bar_w)), Lmin the shortest box edge, as the
    reference sizes Hista (v25/main.cpp:251-255); 0 on a bad argument. */
 int mdsc_correlation_bins(const mdsc_batch* b, int sys, double bar_w);
-/* Replaces acc_correl (v25/functions.cpp:2400-2470) for one species per
-   system: adds every unordered pair's terms to the pair-correlation
-   histograms of the current state -- 2, 2 dot, 2 (3 doti dotj - dot) and
-   3 dot^2 - 1 to bin floor(r / bar_w) of 000, 110, 112 and 220.  hist holds,
-   system after system, 4 x nbins doubles (function-major, nbins from
-   mdsc_correlation_bins) and is ADDED TO, as the reference accumulates
-   Hista over a run.  The count is exact and a pair lands in the reference's
-   bin (an FP64 recheck near bin edges); the other three sums carry the
-   FP32 rounding of each pair's term (~1e-7 of the count).  Pairs at a
-   distance past the last bin (the box's corners) are left out, where the
-   reference writes past its matrix. */
+/* Species of system sys: nspecies contiguous blocks of counts[k] particles
+   (the reference's components, numbered as calc_II / rev_II number them,
+   v25/functions.cpp:1158-1179).  Default: one species.  Used by
+   mdsc_correlations only. */
+mdsc_status mdsc_set_species(mdsc_batch* b, int sys, int nspecies, const int* counts);
+/* Doubles mdsc_correlations writes for system sys:
+   (nc + nc (nc - 1) / 2) x 4 x nbins, nc its species. */
+int mdsc_correlation_size(const mdsc_batch* b, int sys, double bar_w);
+/* Replaces acc_correl (v25/functions.cpp:2400-2470): adds every unordered
+   pair's terms to the pair-correlation histograms of the current state, at
+   bin floor(r / bar_w) of the functions 000, 110, 112 and 220 -- for two
+   particles of one species 2, 2 dot, 2 (3 doti dotj - dot), 3 dot^2 - 1 to
+   that species' histogram (Hista), otherwise 1, dot, 3 doti dotj - dot,
+   (3 dot^2 - 1) / 2 to the species pair's (Histe).  hist holds, system after
+   system, its nc species blocks and then its species-pair blocks in the
+   order (0,1), (0,2), ..., (1,2), ..., each 4 x nbins doubles
+   (function-major; mdsc_correlation_size doubles per system), and is ADDED
+   TO, as the reference accumulates over a run.  The counts are exact and a
+   pair lands in the reference's bin (an FP64 recheck near bin edges); the
+   other three sums carry the FP32 rounding of each pair's term (~1e-7 of
+   the count).  Pairs past the last bin (the box's corners) are left out,
+   where the reference writes past its matrix. */
 mdsc_status mdsc_correlations(mdsc_batch* b, double bar_w, double* hist);
 /* Replaces oo_params (v25/functions.cpp:2702-2760) per system: G1[sys],
    G2[sys] (nematic order: the largest |eigenvalue| of

@@ -38,8 +38,8 @@ void launch_cluster_compress(const Batch& b, cudaStream_t s);
 void launch_reset_iter(const Batch& b, cudaStream_t s);
 void launch_kspace_parts(const Batch& b, int maxnd, const int4* kwork, int nkwork, const int2* kowner,
                          double* kE, int part, cudaStream_t s);
-void launch_correlations(const Batch& b, const int2* binfo, double bar_w, int max_bins,
-                         unsigned long long* hist, cudaStream_t s);
+void launch_correlations(const Batch& b, const CorrSys* cs, const unsigned char* species, double bar_w,
+                         int max_bins, unsigned long long* hist, cudaStream_t s);
 void launch_order_sums(const Batch& b, double* out, cudaStream_t s);
 }  // namespace mdsc
 
@@ -446,6 +446,7 @@ struct mdsc_batch {
   double* noise[2] = {nullptr, nullptr};
   double* h_noise = nullptr;  // pinned
   SysObs* h_obs = nullptr;    // pinned
+  SysObs* h_trace = nullptr;  // pinned, kNoiseChunk x nsys: per-step observables of mdsc_step_trace
   char* arena = nullptr;
   size_t arena_bytes = 0;
   std::vector<Mt19937> thermo_rng;  // 2 per system
@@ -454,6 +455,7 @@ struct mdsc_batch {
   std::vector<std::vector<int>> labels;
   std::vector<int> n_clusters;
   std::vector<char> uploaded, built, have_forces;
+  std::vector<std::vector<int>> species;  // per system: particles per species (contiguous blocks)
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   cudaEvent_t t_beg = nullptr, t_end = nullptr;  // device time of the last mdsc_step
   double last_ms = 0.0;
@@ -719,37 +721,43 @@ mdsc_status run_clusters(mdsc_batch* B, const std::vector<int>& systems) {
 
 void order_params(const double* v, int n, double* G1, double* G2, double* M);
 
+// one system's device observables as the ABI struct
+void convert_obs(const SysObs& o, int n, int n_clusters, mdsc_observables& r) {
+  memset(&r, 0, sizeof r);
+  r.K[0] = o.K[0];
+  r.K[1] = o.K[1];
+  r.U_ss = o.U_ss;
+  r.W_ss = o.W_ss;
+  r.U_dipR = o.U_dipR;
+  r.U_dipK = o.U_dipK;
+  r.U_ext = o.U_ext;
+  r.U_self = o.U_self;
+  for (int c = 0; c < 9; ++c) {
+    r.PT_kin[c] = o.PT_kin[c];
+    r.PT_ss[c] = o.PT_ss[c];
+    r.PT_dipR[c] = o.PT_dipR[c];
+    r.PT_dipK[c] = o.PT_dipK[c];
+  }
+  r.xi[0] = o.xi[0];
+  r.xi[1] = o.xi[1];
+  r.step = o.step;
+  r.status = status_from_bits(o.status);
+  r.n_clusters = n_clusters;
+  r.list_builds = o.list_builds;
+  order_params(o.osum, n, &r.G1, &r.G2, r.M);
+  for (int a = 0; a < 3; ++a) {
+    r.P_tot[a] = o.osum[12 + a];
+    r.L_tot[a] = o.osum[15 + a];
+  }
+}
+
 mdsc_status read_obs(mdsc_batch* B, mdsc_observables* out) {
   CU(cudaMemcpyAsync(B->h_obs, B->b.obs, sizeof(SysObs) * B->nsys, cudaMemcpyDeviceToHost, B->st));
   CU(cudaStreamSynchronize(B->st));
   int bits = 0;
   for (int s = 0; s < B->nsys; ++s) {
-    const SysObs& o = B->h_obs[s];
-    bits |= o.status;
-    if (!out) continue;
-    mdsc_observables& r = out[s];
-    memset(&r, 0, sizeof r);
-    r.K[0] = o.K[0];
-    r.K[1] = o.K[1];
-    r.U_ss = o.U_ss;
-    r.W_ss = o.W_ss;
-    r.U_dipR = o.U_dipR;
-    r.U_dipK = o.U_dipK;
-    r.U_ext = o.U_ext;
-    r.U_self = o.U_self;
-    for (int c = 0; c < 9; ++c) {
-      r.PT_kin[c] = o.PT_kin[c];
-      r.PT_ss[c] = o.PT_ss[c];
-      r.PT_dipR[c] = o.PT_dipR[c];
-      r.PT_dipK[c] = o.PT_dipK[c];
-    }
-    r.xi[0] = o.xi[0];
-    r.xi[1] = o.xi[1];
-    r.step = o.step;
-    r.status = status_from_bits(o.status);
-    r.n_clusters = B->n_clusters[s];
-    r.list_builds = o.list_builds;
-    order_params(o.osum, B->lo.sys[s].n, &r.G1, &r.G2, r.M);
+    bits |= B->h_obs[s].status;
+    if (out) convert_obs(B->h_obs[s], B->lo.sys[s].n, B->n_clusters[s], out[s]);
   }
   const mdsc_status st = status_from_bits(bits);
   if (st != MDSC_OK) return fail(B, st, "a system reported an error (see mdsc_observables.status)");
@@ -1017,6 +1025,8 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   B->uploaded.assign(nsys, 0);
   B->built.assign(nsys, 0);
   B->have_forces.assign(nsys, 0);
+  B->species.resize(nsys);
+  for (int s = 0; s < nsys; ++s) B->species[s].assign(1, descs[s].n);
   e = cudaStreamSynchronize(B->st);
   if (e != cudaSuccess) {
     mdsc_destroy(B);
@@ -1036,6 +1046,7 @@ mdsc_status mdsc_destroy(mdsc_batch* B) {
   if (B->arena) cudaFree(B->arena);
   if (B->h_noise) cudaFreeHost(B->h_noise);
   if (B->h_obs) cudaFreeHost(B->h_obs);
+  if (B->h_trace) cudaFreeHost(B->h_trace);
   if (B->ev_fork) cudaEventDestroy(B->ev_fork);
   if (B->ev_j2) cudaEventDestroy(B->ev_j2);
   if (B->ev_j3) cudaEventDestroy(B->ev_j3);
@@ -1068,6 +1079,14 @@ static mdsc_status upload_one(mdsc_batch* B, int s, const mdsc_host_state* h, bo
     return fail(B, MDSC_ERR_BAD_ARG, "the first upload of a system needs len, dia, mass and dip");
   Batch& b = B->b;
   const int i0 = P.part_off;
+  // cluster labels as given (a restart's conf.dat): they stand until the
+  // next clustering step replaces them
+  if (h->clust) {
+    B->labels[s].assign(h->clust, h->clust + n);
+    int mx = -1;
+    for (int i = 0; i < n; ++i) mx = std::max(mx, h->clust[i]);
+    B->n_clusters[s] = mx + 1;
+  }
   auto up = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
     return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, B->st) : cudaSuccess;
   };
@@ -1219,6 +1238,18 @@ mdsc_status mdsc_set_thermostat(mdsc_batch* B, int sys, const double xi[2], cons
     st.strn[1] = strn[1];
   }
   CU(cudaMemcpy(B->b.st + sys, &st, sizeof st, cudaMemcpyHostToDevice));
+  return MDSC_OK;
+}
+
+mdsc_status mdsc_get_thermostat(mdsc_batch* B, int sys, double xi[2], double strn[2]) {
+  if (!B || sys < 0 || sys >= B->nsys) return MDSC_ERR_BAD_ARG;
+  cudaSetDevice(B->device);
+  SysState st;
+  CU(cudaMemcpy(&st, B->b.st + sys, sizeof st, cudaMemcpyDeviceToHost));
+  for (int k = 0; k < 2; ++k) {
+    if (xi) xi[k] = st.xi[k];
+    if (strn) strn[k] = st.strn[k];
+  }
   return MDSC_OK;
 }
 
@@ -1403,38 +1434,67 @@ int mdsc_correlation_bins(const mdsc_batch* B, int sys, double bar_w) {
   return std::max(0, corr_bins(B->lo.sys[sys], bar_w));
 }
 
+mdsc_status mdsc_set_species(mdsc_batch* B, int sys, int nspecies, const int* counts) {
+  if (!B || sys < 0 || sys >= B->nsys || nspecies < 1 || nspecies > 255 || !counts) return MDSC_ERR_BAD_ARG;
+  long long tot = 0;
+  for (int k = 0; k < nspecies; ++k) {
+    if (counts[k] < 1) return fail(B, MDSC_ERR_BAD_ARG, "mdsc_set_species: every species needs a particle");
+    tot += counts[k];
+  }
+  if (tot != B->lo.sys[sys].n) return fail(B, MDSC_ERR_BAD_ARG, "mdsc_set_species: counts do not add up to n");
+  B->species[sys].assign(counts, counts + nspecies);
+  return MDSC_OK;
+}
+
+int mdsc_correlation_size(const mdsc_batch* B, int sys, double bar_w) {
+  if (!B || sys < 0 || sys >= B->nsys || !(bar_w > 0.0)) return 0;
+  const int nc = (int)B->species[sys].size();
+  return (nc + nc * (nc - 1) / 2) * 4 * std::max(0, corr_bins(B->lo.sys[sys], bar_w));
+}
+
 mdsc_status mdsc_correlations(mdsc_batch* B, double bar_w, double* hist) {
   mdsc_status st = need_state(B);
   if (st) return st;
   if (!(bar_w > 0.0) || !hist) return fail(B, MDSC_ERR_BAD_ARG, "mdsc_correlations: bar_w > 0 and hist required");
-  std::vector<int2> binfo(B->nsys);
+  std::vector<CorrSys> cs(B->nsys);
+  std::vector<unsigned char> sp(std::max(B->lo.ntot, 1), 0);
   int tot = 0, max_bins = 0;
   for (int s = 0; s < B->nsys; ++s) {
     const int nb = std::max(0, corr_bins(B->lo.sys[s], bar_w));
-    binfo[s] = make_int2(nb, tot);
-    tot += 4 * nb;
-    max_bins = std::max(max_bins, nb);
+    const int nc = (int)B->species[s].size();
+    const int nblocks = nc + nc * (nc - 1) / 2;
+    cs[s] = CorrSys{nb, tot, nc, 0};
+    tot += nblocks * 4 * nb;
+    max_bins = std::max(max_bins, nblocks * nb);
+    int i = B->lo.sys[s].part_off;
+    for (int k = 0; k < nc; ++k)
+      for (int q = 0; q < B->species[s][k]; ++q) sp[i++] = (unsigned char)k;
   }
   if (tot == 0) return MDSC_OK;
   char* d = nullptr;
-  const size_t hbytes = sizeof(unsigned long long) * tot;
-  CU(cudaMallocAsync((void**)&d, hbytes + sizeof(int2) * B->nsys, B->st));
+  const size_t hbytes = sizeof(unsigned long long) * tot, cbytes = sizeof(CorrSys) * B->nsys;
+  CU(cudaMallocAsync((void**)&d, hbytes + cbytes + sp.size(), B->st));
   unsigned long long* dh = reinterpret_cast<unsigned long long*>(d);
-  int2* dinfo = reinterpret_cast<int2*>(d + hbytes);
+  CorrSys* dcs = reinterpret_cast<CorrSys*>(d + hbytes);
+  unsigned char* dsp = reinterpret_cast<unsigned char*>(d + hbytes + cbytes);
   std::vector<unsigned long long> h(tot);
-  CU(cudaMemcpyAsync(dinfo, binfo.data(), sizeof(int2) * B->nsys, cudaMemcpyHostToDevice, B->st));
+  CU(cudaMemcpyAsync(dcs, cs.data(), cbytes, cudaMemcpyHostToDevice, B->st));
+  CU(cudaMemcpyAsync(dsp, sp.data(), sp.size(), cudaMemcpyHostToDevice, B->st));
   CU(cudaMemsetAsync(dh, 0, hbytes, B->st));
   launch_derive(B->b, B->st);
-  launch_correlations(B->b, dinfo, bar_w, max_bins, dh, B->st);
+  launch_correlations(B->b, dcs, dsp, bar_w, max_bins, dh, B->st);
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(h.data(), dh, hbytes, cudaMemcpyDeviceToHost, B->st));
   CU(cudaFreeAsync(d, B->st));
   CU(cudaStreamSynchronize(B->st));
   // counts are exact integers; the other three are fixed point in 2^-24 units
   for (int s = 0; s < B->nsys; ++s) {
-    const int nb = binfo[s].x, off = binfo[s].y;
-    for (int k = 0; k < nb; ++k) hist[off + k] += (double)h[off + k];
-    for (int k = nb; k < 4 * nb; ++k) hist[off + k] += std::ldexp((double)(long long)h[off + k], -24);
+    const int nb = cs[s].nbins, nc = cs[s].nsp, nblocks = nc + nc * (nc - 1) / 2;
+    for (int q = 0; q < nblocks; ++q) {
+      const int o = cs[s].off + q * 4 * nb;
+      for (int k = 0; k < nb; ++k) hist[o + k] += (double)h[o + k];
+      for (int k = nb; k < 4 * nb; ++k) hist[o + k] += std::ldexp((double)(long long)h[o + k], -24);
+    }
   }
   return MDSC_OK;
 }
@@ -1524,9 +1584,10 @@ mdsc_status mdsc_transfer(mdsc_batch* D, int dsys, mdsc_batch* S, int ssys) {
 }
 
 // ---- the fused step ----------------------------------------------------
-mdsc_status mdsc_step(mdsc_batch* B, int nsteps, mdsc_observables* obs) {
-  if (!B || nsteps < 0) return MDSC_ERR_BAD_ARG;
-  cudaSetDevice(B->device);
+// nsteps steps; trace (nsteps x nsys, may be NULL) gets every step's
+// observables: a copy of the device observables after each graph launch into
+// pinned staging, converted after the chunk
+static mdsc_status run_steps(mdsc_batch* B, int nsteps, mdsc_observables* trace) {
   mdsc_status st = ensure_forces(B);
   if (st) return st;
   if (!B->tuned && !B->graph[0]) {
@@ -1544,6 +1605,7 @@ mdsc_status mdsc_step(mdsc_batch* B, int nsteps, mdsc_observables* obs) {
       st = capture_step(B, w);
       if (st) return st;
     }
+  if (trace && !B->h_trace) CU(cudaMallocHost(&B->h_trace, sizeof(SysObs) * kNoiseChunk * B->nsys));
   int which = 0;
   int done = 0;
   double dev_ms = 0.0;
@@ -1564,7 +1626,12 @@ mdsc_status mdsc_step(mdsc_batch* B, int nsteps, mdsc_observables* obs) {
     CU(cudaMemcpyAsync(B->noise[which], B->h_noise, sizeof(double) * chunk * B->nsys * 4,
                        cudaMemcpyHostToDevice, B->st));
     launch_reset_iter(B->b, B->st);
-    for (int k = 0; k < chunk; ++k) CU(cudaGraphLaunch(B->graph[which], B->st));
+    for (int k = 0; k < chunk; ++k) {
+      CU(cudaGraphLaunch(B->graph[which], B->st));
+      if (trace)
+        CU(cudaMemcpyAsync(B->h_trace + (size_t)k * B->nsys, B->b.obs, sizeof(SysObs) * B->nsys,
+                           cudaMemcpyDeviceToHost, B->st));
+    }
     CU(cudaEventRecord(B->t_end, B->st));
     {
       CU(cudaEventSynchronize(B->t_end));
@@ -1579,15 +1646,56 @@ mdsc_status mdsc_step(mdsc_batch* B, int nsteps, mdsc_observables* obs) {
       if (fr > 0 && last % fr == 0) due.push_back(s);
       B->step_h[s] += chunk;
     }
+    if (trace)  // cluster counts as they stood before this chunk's clustering step
+      for (int k = 0; k < chunk; ++k)
+        for (int s = 0; s < B->nsys; ++s)
+          convert_obs(B->h_trace[(size_t)k * B->nsys + s], B->lo.sys[s].n, B->n_clusters[s],
+                      trace[(size_t)(done + k) * B->nsys + s]);
     if (!due.empty()) {
       st = run_clusters(B, due);
       if (st) return st;
+      if (trace)
+        for (int s : due) trace[(size_t)(done + chunk - 1) * B->nsys + s].n_clusters = B->n_clusters[s];
     }
     done += chunk;
     which ^= 1;
   }
   B->last_ms = dev_ms;
+  return MDSC_OK;
+}
+
+mdsc_status mdsc_step(mdsc_batch* B, int nsteps, mdsc_observables* obs) {
+  if (!B || nsteps < 0) return MDSC_ERR_BAD_ARG;
+  cudaSetDevice(B->device);
+  mdsc_status st = run_steps(B, nsteps, nullptr);
+  if (st) return st;
   return read_obs(B, obs);
+}
+
+mdsc_status mdsc_step_trace(mdsc_batch* B, int nsteps, mdsc_observables* trace) {
+  if (!B || nsteps < 0 || (nsteps > 0 && !trace)) return MDSC_ERR_BAD_ARG;
+  cudaSetDevice(B->device);
+  mdsc_status st = run_steps(B, nsteps, trace);
+  if (st) return st;
+  st = read_obs(B, nullptr);  // a system's error bits persist: they show in its last step
+  if (st) return st;
+  for (size_t k = 0; k < (size_t)nsteps * B->nsys; ++k)
+    if (trace[k].status != MDSC_OK) return fail(B, (mdsc_status)trace[k].status, "a system reported an error");
+  return MDSC_OK;
+}
+
+mdsc_status mdsc_get_rng(const mdsc_batch* B, int sys, int which, uint32_t* mt, int* mti) {
+  if (!B || sys < 0 || sys >= B->nsys || which < 0 || which > 2 || !mt || !mti) return MDSC_ERR_BAD_ARG;
+  const Mt19937& g = which < 2 ? B->thermo_rng[2 * sys + which] : B->clus_rng[sys];
+  g.get_state(mt, mti);
+  return MDSC_OK;
+}
+
+mdsc_status mdsc_set_rng(mdsc_batch* B, int sys, int which, const uint32_t* mt, int mti) {
+  if (!B || sys < 0 || sys >= B->nsys || which < 0 || which > 2 || !mt) return MDSC_ERR_BAD_ARG;
+  Mt19937& g = which < 2 ? B->thermo_rng[2 * sys + which] : B->clus_rng[sys];
+  if (!g.set_state(mt, mti)) return fail(B, MDSC_ERR_BAD_ARG, "mdsc_set_rng: position outside 0..624");
+  return MDSC_OK;
 }
 
 double mdsc_last_device_ms(const mdsc_batch* B) { return B ? B->last_ms : 0.0; }

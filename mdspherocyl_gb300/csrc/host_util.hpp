@@ -15,17 +15,55 @@ namespace mdsc {
 // generator and seeding.
 class Mt19937 {
  public:
+  // MT19937 (Matsumoto & Nishimura, ACM TOMACS 8(1), 1998) with GSL's state
+  // layout and seeding, so that a state read from the reference's generator
+  // files continues the same sequence: 624 words and the position of the
+  // next word; a seed of 0 means 4357 (gsl_rng_set).
+  static constexpr int kN = 624;
   explicit Mt19937(unsigned long seed = 1) { seed_with(seed); }
   void seed_with(unsigned long seed) {
     uint32_t s = (uint32_t)(seed & 0xffffffffUL);
     if (s == 0) s = 4357u;
-    g_.seed(s);
+    mt_[0] = s;
+    for (int i = 1; i < kN; ++i) mt_[i] = 1812433253u * (mt_[i - 1] ^ (mt_[i - 1] >> 30)) + (uint32_t)i;
+    mti_ = kN;
   }
-  double uniform() { return (double)g_() / 4294967296.0; }
-  void discard(unsigned long long n) { g_.discard(n); }
+  uint32_t next() {
+    if (mti_ >= kN) refill();
+    uint32_t y = mt_[mti_++];
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    y ^= y >> 18;
+    return y;
+  }
+  double uniform() { return (double)next() / 4294967296.0; }
+  void discard(unsigned long long n) {
+    for (unsigned long long k = 0; k < n; ++k) next();
+  }
+  void get_state(uint32_t* mt, int* mti) const {
+    for (int i = 0; i < kN; ++i) mt[i] = mt_[i];
+    *mti = mti_;
+  }
+  bool set_state(const uint32_t* mt, int mti) {
+    if (mti < 0 || mti > kN) return false;
+    for (int i = 0; i < kN; ++i) mt_[i] = mt[i];
+    mti_ = mti;
+    return true;
+  }
 
  private:
-  std::mt19937 g_;
+  void refill() {
+    constexpr uint32_t kUpper = 0x80000000u, kLower = 0x7fffffffu, kMatrix = 0x9908b0dfu;
+    constexpr int kM = 397;
+    for (int k = 0; k < kN; ++k) {
+      const uint32_t y = (mt_[k] & kUpper) | (mt_[(k + 1) % kN] & kLower);
+      mt_[k] = mt_[(k + kM) % kN] ^ (y >> 1) ^ ((y & 1u) ? kMatrix : 0u);
+    }
+    mti_ = 0;
+  }
+  uint32_t mt_[kN];
+  int mti_ = kN;
 };
 
 // gauss(1, rnd1, rnd2): Box-Muller as v25/functions.cpp:1149-1156 does it

@@ -467,69 +467,35 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
 // the kinetic block also closes the step's thermostat and bookkeeping.
 constexpr int kRedThreads = 128;
 __global__ void __launch_bounds__(kRedThreads) reduce_obs_kernel(Batch b, int mode) {
-  __shared__ double sh[12 * kRedThreads / 32];
+  __shared__ double sh[18 * kRedThreads / 32];
   const int s = blockIdx.x / kRedGroups, grp = blockIdx.x % kRedGroups;
   const SysDev& P = b.sys[s];
   SysState& S = b.st[s];
   SysObs& ob = b.obs[s];
-  FF v[11];
+  FF v[18];
 #pragma unroll
-  for (int c = 0; c < 11; ++c) v[c].hi = v[c].lo = 0.f;
-  double out[11];
-  if (grp == 0) {
-    // real-space tiles: U, PT (FP32 per tile)
-    for (int t = threadIdx.x; t < P.ntile; t += kRedThreads) {
-      const float* e = b.tileE + (long long)(P.tile_off + t) * 10;
-#pragma unroll
-      for (int c = 0; c < 10; ++c) v[c] = ff_add(v[c], ff_of(e[c]));
-    }
-    block_sum<11, kRedThreads>(v, sh, out);
-    if (threadIdx.x == 0) {
-      ob.U_dipR = out[0];
-      for (int c = 0; c < 9; ++c) ob.PT_dipR[c] = out[1 + c];
-    }
-  } else if (grp == 1) {
-    // k-space: U, PT per k
-    for (int k = threadIdx.x; k < P.nk; k += kRedThreads) {
-      const double* e = b.kE + (long long)(P.k_off + k) * 10;
-#pragma unroll
-      for (int c = 0; c < 10; ++c) v[c] = ff_add(v[c], ff_from(e[c]));
-    }
-    block_sum<11, kRedThreads>(v, sh, out);
-    if (threadIdx.x == 0) {
-      ob.U_dipK = out[0];
-      for (int c = 0; c < 9; ++c) ob.PT_dipK[c] = out[1 + c];
-    }
-  } else if (grp == 2) {
-    // WCA: U, W, PT per particle block (summed by the finalize kernel)
-    for (int k = threadIdx.x; k < P.nblk; k += kRedThreads) {
-      const double* e = b.wcaE + (long long)(P.blk_off + k) * 11;
-#pragma unroll
-      for (int c = 0; c < 11; ++c) v[c] = ff_add(v[c], ff_from(e[c]));
-    }
-    block_sum<11, kRedThreads>(v, sh, out);
-    if (threadIdx.x == 0) {
-      ob.U_ss = out[0];
-      ob.W_ss = out[1];
-      for (int c = 0; c < 9; ++c) ob.PT_ss[c] = out[2 + c];
-    }
-  } else if (grp == 4) {
+  for (int c = 0; c < 18; ++c) v[c].hi = v[c].lo = 0.f;
+  if (grp == 4) {
     // oo_params' terms (v25/functions.cpp:2720-2760, Qmat_3d :3426-3445)
     // from the FP32 working copies of the current orientations: the rod
-    // axis o, o o^T and the dipole vectors mu o_dipole, particle by particle
-    FF w[12];
-#pragma unroll
-    for (int c = 0; c < 12; ++c) w[c].hi = w[c].lo = 0.f;
-    // four particles per thread per pass, their loads issued together (the
-    // largest system's block is on the step's critical path)
+    // axis o, o o^T and the dipole vectors mu o_dipole; then the total
+    // momentum and angular momentum the driver prints (v25/main.cpp:
+    // 790-800) from the FP64 state.  Particle by particle, four per thread
+    // per pass with their loads issued together.
     const int ND = b.ndtot, nd = P.nd, end = P.part_off + P.n;
     for (int i0 = P.part_off + threadIdx.x; i0 < end; i0 += 4 * kRedThreads) {
       float4 o[4];
       float m[4][3];
+      double pl[4][6];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         const int i = i0 + u * kRedThreads;
         o[u] = i < end ? b.pax[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          pl[u][a] = i < end ? b.p[3 * i + a] : 0.0;
+          pl[u][3 + a] = i < end ? b.l[3 * i + a] : 0.0;
+        }
         m[u][0] = m[u][1] = m[u][2] = 0.f;
         if (i < end) {
           const int g0 = P.dip_off + (i - P.part_off) * nd;
@@ -546,47 +512,87 @@ __global__ void __launch_bounds__(kRedThreads) reduce_obs_kernel(Batch b, int mo
         const float t[12] = {q.x,       q.y,       q.z,       q.x * q.x, q.x * q.y, q.x * q.z,
                              q.y * q.y, q.y * q.z, q.z * q.z, m[u][0],   m[u][1],   m[u][2]};
 #pragma unroll
-        for (int c = 0; c < 12; ++c) w[c] = ff_add(w[c], ff_of(t[c]));
-      }
-    }
-    double o12[12];
-    block_sum<12, kRedThreads>(w, sh, o12);
-    if (threadIdx.x == 0)
-      for (int c = 0; c < 12; ++c) ob.osum[c] = o12[c];
-  } else {
-    // kinetic terms and the field energy
-    for (int k = threadIdx.x; k < P.nblk; k += kRedThreads) {
-      const double* e = b.kin2 + (long long)(P.blk_off + k) * 9;
+        for (int c = 0; c < 12; ++c) v[c] = ff_add(v[c], ff_of(t[c]));
 #pragma unroll
-      for (int c = 0; c < 9; ++c) v[c] = ff_add(v[c], ff_from(e[c]));
-    }
-    block_sum<11, kRedThreads>(v, sh, out);
-    if (threadIdx.x == 0) {
-      ob.U_ext = out[8];
-      ob.U_self = P.Uself;
-      if (mode & kRedStep) {
-        ob.K[0] = 0.5 * out[0];
-        ob.K[1] = 0.5 * out[1];
-        const double pt6[6] = {out[2], out[3], out[4], out[5], out[6], out[7]};
-        const int map[9] = {0, 1, 2, 1, 3, 4, 2, 4, 5};
-        for (int c = 0; c < 9; ++c) ob.PT_kin[c] = pt6[map[c]];
-        // moveTher mode 2 (v25/functions.cpp:2207-2213) closes the step
-        const double* nz = b.noise + ((long long)S.iter * b.nsys + s) * 4;
-        S.xi[0] = P.ex1 * S.xi_mid[0] + P.cnoise * nz[1];
-        S.xi[1] = P.ex1 * S.xi_mid[1] + P.cnoise * nz[3];
-        S.strn[0] = nz[1];
-        S.strn[1] = nz[3];
-        S.step += 1;
-        S.iter += 1;
-        if (S.rebuild) S.list_builds += 1;
-        S.force_list = 0;
+        for (int c = 0; c < 6; ++c) v[12 + c] = ff_add(v[12 + c], ff_from(pl[u][c]));
       }
-      ob.xi[0] = S.xi[0];
-      ob.xi[1] = S.xi[1];
-      ob.step = S.step;
-      ob.status = S.status;
-      ob.list_builds = S.list_builds;
     }
+  } else {
+    // the rows of one per-system table, column by column: real-space tiles
+    // (U, PT; FP32), k-vectors (U, PT), WCA blocks (U, W, PT) or kinetic
+    // blocks (K_t, K_r, PT_kin, U_ext).  One code path for the four keeps
+    // the kernel small: its blocks are short, and a larger kernel waited on
+    // instruction fetch.
+    const float* fsrc = nullptr;
+    const double* dsrc = nullptr;
+    int nrow, ncol;
+    if (grp == 0) {
+      fsrc = b.tileE + (long long)P.tile_off * 10;
+      nrow = P.ntile;
+      ncol = 10;
+    } else if (grp == 1) {
+      dsrc = b.kE + (long long)P.k_off * 10;
+      nrow = P.nk;
+      ncol = 10;
+    } else if (grp == 2) {
+      dsrc = b.wcaE + (long long)P.blk_off * 11;
+      nrow = P.nblk;
+      ncol = 11;
+    } else {
+      dsrc = b.kin2 + (long long)P.blk_off * 9;
+      nrow = P.nblk;
+      ncol = 9;
+    }
+    for (int t = threadIdx.x; t < nrow; t += kRedThreads) {
+#pragma unroll
+      for (int c = 0; c < 12; ++c) {
+        if (c < ncol) {
+          const long long e = (long long)t * ncol + c;
+          v[c] = ff_add(v[c], fsrc ? ff_of(fsrc[e]) : ff_from(dsrc[e]));
+        }
+      }
+    }
+  }
+  double out[18];
+  block_sum<18, kRedThreads>(v, sh, out);
+  if (threadIdx.x != 0) return;
+  if (grp == 0) {
+    ob.U_dipR = out[0];
+    for (int c = 0; c < 9; ++c) ob.PT_dipR[c] = out[1 + c];
+  } else if (grp == 1) {
+    ob.U_dipK = out[0];
+    for (int c = 0; c < 9; ++c) ob.PT_dipK[c] = out[1 + c];
+  } else if (grp == 2) {
+    ob.U_ss = out[0];
+    ob.W_ss = out[1];
+    for (int c = 0; c < 9; ++c) ob.PT_ss[c] = out[2 + c];
+  } else if (grp == 4) {
+    for (int c = 0; c < 18; ++c) ob.osum[c] = out[c];
+  } else {
+    ob.U_ext = out[8];
+    ob.U_self = P.Uself;
+    if (mode & kRedStep) {
+      ob.K[0] = 0.5 * out[0];
+      ob.K[1] = 0.5 * out[1];
+      const double pt6[6] = {out[2], out[3], out[4], out[5], out[6], out[7]};
+      const int map[9] = {0, 1, 2, 1, 3, 4, 2, 4, 5};
+      for (int c = 0; c < 9; ++c) ob.PT_kin[c] = pt6[map[c]];
+      // moveTher mode 2 (v25/functions.cpp:2207-2213) closes the step
+      const double* nz = b.noise + ((long long)S.iter * b.nsys + s) * 4;
+      S.xi[0] = P.ex1 * S.xi_mid[0] + P.cnoise * nz[1];
+      S.xi[1] = P.ex1 * S.xi_mid[1] + P.cnoise * nz[3];
+      S.strn[0] = nz[1];
+      S.strn[1] = nz[3];
+      S.step += 1;
+      S.iter += 1;
+      if (S.rebuild) S.list_builds += 1;
+      S.force_list = 0;
+    }
+    ob.xi[0] = S.xi[0];
+    ob.xi[1] = S.xi[1];
+    ob.step = S.step;
+    ob.status = S.status;
+    ob.list_builds = S.list_builds;
   }
 }
 

@@ -2,43 +2,48 @@
 // (v25/functions.cpp:2400-2470) and of the sums behind oo_params
 // (:2702-2748, Qmat_3d :3426-3445).
 //
-// Pair histograms (acc_correl, one species per system): every unordered pair
-// of particles adds 2, 2 dot, 2 (3 doti dotj - dot) and 3 dot^2 - 1 to its
-// distance bin floor(r / bar_w) of the functions 000, 110, 112 and 220.
+// Pair histograms (acc_correl): every unordered pair of particles adds its
+// terms to its distance bin floor(r / bar_w) of the functions 000, 110, 112
+// and 220 -- 2, 2 dot, 2 (3 doti dotj - dot), 3 dot^2 - 1 to its species'
+// histogram when both particles are of one species, and 1, dot,
+// 3 doti dotj - dot, (3 dot^2 - 1) / 2 to the histogram of the species pair
+// otherwise.  Species are contiguous blocks of particles, as the reference
+// numbers them (calc_II / rev_II); a system's histograms are its nc species
+// blocks, then the nc (nc - 1) / 2 pair blocks in the order (0,1), (0,2), ...,
+// (1,2), ..., each 4 x nbins.
 // One block per particle block of 128: each thread holds one particle i and
 // meets every j > i of its system, 128 at a time from shared memory.  The
-// sums are integers -- the count exactly, the three others in fixed point
+// sums are integers -- the counts exactly, the three others in fixed point
 // with 2^24 units -- so they are the same whatever order the atomics land
-// in.  The bins live in shared memory when four of them fit (up to
-// kCorrSmemBins bins), else directly in global memory.
+// in.  The bins live in shared memory when they fit (kCorrSmemBins per
+// block), else directly in global memory.
 //
-// A pair's distance is computed in FP32 from the fixed-point coordinates;
-// when it lies within a few FP32 roundings of a bin edge it is computed again
-// in FP64 from the FP64 positions with the reference's own expressions, so
-// every pair lands in the reference's bin.  Two particles at the same point
-// add to the count only (the reference's doti is 0/0 there).
 #include "mdsc_dev.cuh"
 #include "reduce.cuh"
 
 namespace mdsc {
 
-constexpr int kCorrSmemBins = 1024;  // 4 x 1024 x 8 B = 32 KB of shared memory
+constexpr int kCorrSmemBins = 1024;  // histogram bins (x 4 functions x 8 B = 32 KB) in shared memory
 constexpr float kCorrScale = 16777216.f;  // 2^24: fixed-point unit of the non-count sums
 
 template <bool SMEM>
-__global__ void __launch_bounds__(kPartBlock) corr_kernel(Batch b, const int2* __restrict__ binfo, double bar_w,
+__global__ void __launch_bounds__(kPartBlock) corr_kernel(Batch b, const CorrSys* __restrict__ cs,
+                                                          const unsigned char* __restrict__ species, double bar_w,
                                                           unsigned long long* __restrict__ hist) {
   extern __shared__ unsigned long long shist[];
   __shared__ uint32_t sx[kPartBlock], sy[kPartBlock], sz[kPartBlock];
   __shared__ float4 sa[kPartBlock];
+  __shared__ unsigned char ssp[kPartBlock];
   const int2 bk = b.blk[blockIdx.x];
   const int s = bk.x;
   const SysDev& P = b.sys[s];
-  const int nbins = binfo[s].x;
-  unsigned long long* gh = hist + binfo[s].y;  // 4 x nbins for this system
+  const CorrSys C = cs[s];
+  const int nbins = C.nbins, nc = C.nsp;
+  const int nwords = (nc + nc * (nc - 1) / 2) * 4 * nbins;
+  unsigned long long* gh = hist + C.off;
   unsigned long long* h = SMEM ? shist : gh;
   if (SMEM) {
-    for (int k = threadIdx.x; k < 4 * nbins; k += blockDim.x) shist[k] = 0ull;
+    for (int k = threadIdx.x; k < nwords; k += blockDim.x) shist[k] = 0ull;
     __syncthreads();
   }
   const int N = b.ntot;
@@ -47,11 +52,13 @@ __global__ void __launch_bounds__(kPartBlock) corr_kernel(Batch b, const int2* _
   const bool ok = i < iend;
   uint32_t ux = 0, uy = 0, uz = 0;
   float4 ai = make_float4(0.f, 0.f, 1.f, 0.f);
+  int spi = 0;
   if (ok) {
     ux = b.pfx[i];
     uy = b.pfx[N + i];
     uz = b.pfx[2 * N + i];
     ai = b.pax[i];
+    spi = species[i];
   }
   const float ibw = (float)(1.0 / bar_w);
   // how far the FP32 t = r / bar_w may be from the reference's: ~8 roundings
@@ -67,6 +74,7 @@ __global__ void __launch_bounds__(kPartBlock) corr_kernel(Batch b, const int2* _
       sy[threadIdx.x] = b.pfx[N + q];
       sz[threadIdx.x] = b.pfx[2 * N + q];
       sa[threadIdx.x] = b.pax[q];
+      ssp[threadIdx.x] = species[q];
     }
     __syncthreads();
     if (!ok) continue;
@@ -100,18 +108,25 @@ __global__ void __launch_bounds__(kPartBlock) corr_kernel(Batch b, const int2* _
       const float ir = r > 0.f ? 1.f / r : 0.f;
       const float doti = (ai.x * dx + ai.y * dy + ai.z * dz) * ir;
       const float dotj = (aj.x * dx + aj.y * dy + aj.z * dz) * ir;
-      const int v110 = __float2int_rn(2.f * dot * kCorrScale);
-      const int v112 = __float2int_rn(2.f * (3.f * doti * dotj - dot) * kCorrScale);
-      const int v220 = __float2int_rn((3.f * dot * dot - 1.f) * kCorrScale);
-      atomicAdd(&h[0 * nbins + bin], 2ull);
-      atomicAdd(&h[1 * nbins + bin], (unsigned long long)(long long)v110);
-      atomicAdd(&h[2 * nbins + bin], (unsigned long long)(long long)v112);
-      atomicAdd(&h[3 * nbins + bin], (unsigned long long)(long long)v220);
+      // i < j and species ascend with the index, so spi <= spj
+      const int spj = ssp[k];
+      const bool intra = spi == spj;
+      // pair block (m, n), m < n: after the nc species blocks, in row order
+      const int blkno = intra ? spi : nc + spi * (2 * nc - spi - 1) / 2 + (spj - spi - 1);
+      const float w = intra ? 2.f : 1.f;
+      const int v110 = __float2int_rn(w * dot * kCorrScale);
+      const int v112 = __float2int_rn(w * (3.f * doti * dotj - dot) * kCorrScale);
+      const int v220 = __float2int_rn(0.5f * w * (3.f * dot * dot - 1.f) * kCorrScale);
+      unsigned long long* hb = h + (size_t)blkno * 4 * nbins;
+      atomicAdd(&hb[0 * nbins + bin], intra ? 2ull : 1ull);
+      atomicAdd(&hb[1 * nbins + bin], (unsigned long long)(long long)v110);
+      atomicAdd(&hb[2 * nbins + bin], (unsigned long long)(long long)v112);
+      atomicAdd(&hb[3 * nbins + bin], (unsigned long long)(long long)v220);
     }
   }
   if (SMEM) {
     __syncthreads();
-    for (int k = threadIdx.x; k < 4 * nbins; k += blockDim.x)
+    for (int k = threadIdx.x; k < nwords; k += blockDim.x)
       if (shist[k] != 0ull) atomicAdd(&gh[k], shist[k]);
   }
 }
@@ -156,14 +171,15 @@ __global__ void __launch_bounds__(kPartBlock) order_sums_kernel(Batch b, double*
   }
 }
 
-void launch_correlations(const Batch& b, const int2* binfo, double bar_w, int max_bins,
-                         unsigned long long* hist, cudaStream_t s) {
+// max_bins: the largest (species blocks + pair blocks) x nbins of any system
+void launch_correlations(const Batch& b, const CorrSys* c, const unsigned char* species, double bar_w,
+                         int max_bins, unsigned long long* hist, cudaStream_t s) {
   if (!b.nblk) return;
   if (max_bins <= kCorrSmemBins)
-    corr_kernel<true><<<b.nblk, kPartBlock, 4 * max_bins * sizeof(unsigned long long), s>>>(b, binfo, bar_w,
+    corr_kernel<true><<<b.nblk, kPartBlock, 4 * max_bins * sizeof(unsigned long long), s>>>(b, c, species, bar_w,
                                                                                              hist);
   else
-    corr_kernel<false><<<b.nblk, kPartBlock, 0, s>>>(b, binfo, bar_w, hist);
+    corr_kernel<false><<<b.nblk, kPartBlock, 0, s>>>(b, c, species, bar_w, hist);
 }
 
 void launch_order_sums(const Batch& b, double* out, cudaStream_t s) {

@@ -103,7 +103,7 @@ struct SysObs {
   double xi[2];
   long long step;
   int status, n_clusters, list_builds, pad;
-  double osum[12];  // sum o (3), sum o o^T (xx xy xz yy yz zz), sum mu o_dipole (3)
+  double osum[18];  // sum o (3), sum o o^T (xx xy xz yy yz zz), sum mu o_dipole (3), sum p (3), sum l (3)
 };
 
 // One batch, device pointers.
@@ -194,6 +194,12 @@ struct Batch {
   int* flag;     // 1 changed flag
   // thermostat noise: [iter][sys][4] = g0_t, g1_t, g0_r, g1_r
   const double* noise;
+};
+
+// Per system, for the pair-correlation histograms: bins, first histogram
+// word, number of species.
+struct CorrSys {
+  int nbins, off, nsp, pad;
 };
 
 // ---- small helpers ----------------------------------------------------

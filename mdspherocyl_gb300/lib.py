@@ -37,7 +37,8 @@ EXPORTS = [
     "mdsc_observe", "mdsc_launches_per_step", "mdsc_stream", "mdsc_profile_steps",
     "mdsc_place_rods", "mdsc_last_device_ms", "mdsc_force_dipR_noalloc", "mdsc_transfer",
     "mdsc_autotune", "mdsc_tuning", "mdsc_set_tuning", "mdsc_correlation_bins", "mdsc_correlations",
-    "mdsc_order_params",
+    "mdsc_order_params", "mdsc_step_trace", "mdsc_get_rng", "mdsc_set_rng", "mdsc_set_species",
+    "mdsc_correlation_size", "mdsc_get_thermostat",
 ]
 
 
@@ -65,7 +66,7 @@ class Observables(ctypes.Structure):
         ("PT_kin", c_double * 9), ("PT_ss", c_double * 9), ("PT_dipR", c_double * 9),
         ("PT_dipK", c_double * 9), ("xi", c_double * 2), ("step", c_longlong),
         ("status", c_int), ("n_clusters", c_int), ("list_builds", c_int), ("pad", c_int),
-        ("G1", c_double), ("G2", c_double), ("M", c_double * 3),
+        ("G1", c_double), ("G2", c_double), ("M", c_double * 3), ("P_tot", c_double * 3), ("L_tot", c_double * 3),
     ]
 
     def as_dict(self) -> dict:
@@ -130,7 +131,13 @@ def load(build: bool = True) -> ctypes.CDLL:
         "mdsc_set_tuning": (c_int, [c_void_p, _ip]),
         "mdsc_correlation_bins": (c_int, [c_void_p, c_int, c_double]),
         "mdsc_correlations": (c_int, [c_void_p, c_double, _dp]),
+        "mdsc_set_species": (c_int, [c_void_p, c_int, c_int, _ip]),
+        "mdsc_get_thermostat": (c_int, [c_void_p, c_int, _dp, _dp]),
+        "mdsc_correlation_size": (c_int, [c_void_p, c_int, c_double]),
         "mdsc_order_params": (c_int, [c_void_p, _dp, _dp, _dp]),
+        "mdsc_step_trace": (c_int, [c_void_p, c_int, P(Observables)]),
+        "mdsc_get_rng": (c_int, [c_void_p, c_int, c_int, P(ctypes.c_uint32), _ip]),
+        "mdsc_set_rng": (c_int, [c_void_p, c_int, c_int, P(ctypes.c_uint32), c_int]),
         "mdsc_force_dipR_noalloc": (c_int, [c_int, c_void_p, c_void_p, _dp, c_double, c_void_p, c_void_p,
                                             c_void_p, c_void_p]),
         "mdsc_profile_steps": (c_int, [c_void_p, c_int, c_int, c_char_p, c_size_t, _dp, _ip]),
@@ -238,11 +245,12 @@ class Batch:
         hs.clust = None if clust is None else clust.ctypes.data_as(_ip)
         return hs
 
-    def upload(self, k: int, st: SystemState, F=None, T=None) -> None:
+    def upload(self, k: int, st: SystemState, F=None, T=None, clust=None) -> None:
         c = lambda a: np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
         arrs = dict(r=c(st.r), p=c(st.p), O=c(st.O), l=c(st.l), length=c(st.length), dia=c(st.dia),
                     mass=c(st.mass), dip=c(st.dip), F=None if F is None else c(F),
-                    T=None if T is None else c(T))
+                    T=None if T is None else c(T),
+                    clust=None if clust is None else np.ascontiguousarray(clust, dtype=np.int32))
         hs = self._hoststate(**arrs)
         self._check(self.lib.mdsc_upload(self.h, k, ctypes.byref(hs)), "mdsc_upload")
 
@@ -268,6 +276,12 @@ class Batch:
         self._check(self.lib.mdsc_set_thermostat(self.h, k, _ptr(x), _ptr(s)), "mdsc_set_thermostat")
 
     # -- the reference's functions --
+    def get_thermostat(self, k: int):
+        """(xi[2], stored normal[2]) of system k."""
+        xi, strn = np.zeros(2), np.zeros(2)
+        self._check(self.lib.mdsc_get_thermostat(self.h, k, _ptr(xi), _ptr(strn)), "mdsc_get_thermostat")
+        return xi, strn
+
     def zero_forces(self):
         self._check(self.lib.mdsc_zero_forces(self.h), "mdsc_zero_forces")
 
@@ -328,18 +342,31 @@ class Batch:
     def correlation_bins(self, k: int, bar_w: float) -> int:
         return int(self.lib.mdsc_correlation_bins(self.h, k, float(bar_w)))
 
+    def set_species(self, k: int, counts) -> None:
+        """Species of system k: contiguous blocks of counts[c] particles."""
+        c = np.ascontiguousarray(counts, dtype=np.int32)
+        self._check(self.lib.mdsc_set_species(self.h, k, len(c), c.ctypes.data_as(_ip)), "mdsc_set_species")
+        self._nsp = getattr(self, "_nsp", [1] * self.nsys)
+        self._nsp[k] = len(c)
+
     def correlations(self, bar_w: float, hist=None):
-        """acc_correl on the GPU: per system a (4, nbins) array of the 000,
-        110, 112 and 220 pair sums.  hist (a list of such arrays, e.g. the
-        last call's result) is added to, as the reference accumulates."""
+        """acc_correl on the GPU: per system an array (blocks, 4, nbins) --
+        its species blocks (Hista), then its species-pair blocks (Histe) --
+        of the 000, 110, 112 and 220 pair sums.  hist (a list of such
+        arrays, e.g. the last call's result) is added to, as the reference
+        accumulates."""
+        nsp = getattr(self, "_nsp", [1] * self.nsys)
         nb = [self.correlation_bins(k, bar_w) for k in range(self.nsys)]
-        flat = np.zeros(4 * sum(nb))
-        off = np.cumsum([0] + [4 * b for b in nb])
+        nblk = [c + c * (c - 1) // 2 for c in nsp]
+        size = [self.lib.mdsc_correlation_size(self.h, k, float(bar_w)) for k in range(self.nsys)]
+        assert all(size[k] == nblk[k] * 4 * nb[k] for k in range(self.nsys))
+        off = np.cumsum([0] + size)
+        flat = np.zeros(int(off[-1]))
         if hist is not None:
             for k in range(self.nsys):
                 flat[off[k]:off[k + 1]] = np.asarray(hist[k], dtype=np.float64).reshape(-1)
         self._check(self.lib.mdsc_correlations(self.h, float(bar_w), _ptr(flat)), "mdsc_correlations")
-        return [flat[off[k]:off[k + 1]].reshape(4, nb[k]) for k in range(self.nsys)]
+        return [flat[off[k]:off[k + 1]].reshape(nblk[k], 4, nb[k]) for k in range(self.nsys)]
 
     def order_params(self):
         """oo_params on the GPU: G1 (nsys,), G2 (nsys,), M (nsys, 3)."""
@@ -356,6 +383,25 @@ class Batch:
         obs = (Observables * self.nsys)()
         self._check(self.lib.mdsc_step(self.h, int(nsteps), obs), "mdsc_step")
         return [o.as_dict() for o in obs]
+
+    def step_trace(self, nsteps: int):
+        """nsteps steps; every step's observables, [step][system] dicts."""
+        tr = (Observables * (max(nsteps, 0) * self.nsys))()
+        self._check(self.lib.mdsc_step_trace(self.h, int(nsteps), tr), "mdsc_step_trace")
+        return [[tr[k * self.nsys + s].as_dict() for s in range(self.nsys)] for k in range(nsteps)]
+
+    def get_rng(self, k: int, which: int):
+        """MT19937 state (624 words, position) of generator `which` of system k."""
+        mt = np.zeros(624, dtype=np.uint32)
+        mti = c_int(0)
+        self._check(self.lib.mdsc_get_rng(self.h, k, which, mt.ctypes.data_as(POINTER(ctypes.c_uint32)),
+                                          ctypes.byref(mti)), "mdsc_get_rng")
+        return mt, mti.value
+
+    def set_rng(self, k: int, which: int, mt, mti: int) -> None:
+        a = np.ascontiguousarray(mt, dtype=np.uint32)
+        self._check(self.lib.mdsc_set_rng(self.h, k, which, a.ctypes.data_as(POINTER(ctypes.c_uint32)), int(mti)),
+                    "mdsc_set_rng")
 
     def observe(self):
         obs = (Observables * self.nsys)()
@@ -394,22 +440,33 @@ class Batch:
         return out
 
 
-def normalize_correlations(hist, n: int, box, bar_w: float, cor_cont: float = 1.0):
-    """nor_correl (v25/functions.cpp:2472-2540) for one species: the bin
-    centres, the shell volumes and the normalised 000, 110, 112, 220
-    functions (factors 1, 3, 3/2, 5 over norm * cor_cont * n (n - 1)), as
-    arrays instead of the reference's correlation.dat.  cor_cont is the
-    number of accumulated configurations (chrg_correl's counter)."""
-    h = np.asarray(hist, dtype=np.float64).reshape(4, -1)
+def normalize_correlations(hist, counts, box, bar_w: float, cor_cont: float = 1.0):
+    """nor_correl (v25/functions.cpp:2472-2540): the bin centres, the shell
+    volumes and the normalised 000, 110, 112, 220 functions (factors 1, 3,
+    3/2, 5) of every block of hist (blocks, 4, nbins) as mdsc_correlations
+    lays them out -- a species block over norm * cor_cont * N (N - 1) (zero
+    for a species of one particle), a species-pair block over
+    norm * cor_cont * N_m N_n -- as arrays instead of the reference's
+    correlation.dat.  cor_cont: the accumulated configurations weighted as
+    the driver weights them (1 / V each, v25/main.cpp:716)."""
+    counts = list(counts)
+    nc = len(counts)
+    h = np.asarray(hist, dtype=np.float64).reshape(nc + nc * (nc - 1) // 2, 4, -1)
     Lmin = float(min(box))
-    pos = (np.arange(h.shape[1]) + 0.5) * bar_w
+    pos = (np.arange(h.shape[2]) + 0.5) * bar_w
     shell = 4.0 * np.pi * pos * pos * (3.0 * Lmin / (2.0 * pos) - 2.0) * bar_w
     sphere = 4.0 * np.pi * (pos * pos * bar_w + bar_w ** 3 / 12.0)
     norm = np.where((pos >= Lmin / 2.0) & (pos <= Lmin / np.sqrt(2.0)), shell, sphere)
+    fac = np.array([1.0, 3.0, 1.5, 5.0])[:, None]
     g = np.zeros_like(h)
-    if n > 1:
-        den = norm * cor_cont * n * (n - 1)
-        g = np.array([1.0, 3.0, 1.5, 5.0])[:, None] * h / den
+    for k in range(nc):
+        if counts[k] > 1:
+            g[k] = fac * h[k] / (norm * cor_cont * counts[k] * (counts[k] - 1))
+    q = nc
+    for m in range(nc - 1):
+        for n in range(m + 1, nc):
+            g[q] = fac * h[q] / (norm * cor_cont * counts[n] * counts[m])
+            q += 1
     return pos, norm, g
 
 

@@ -159,6 +159,7 @@ class Oracle:
         self._rng_free = _bind(lib, "mdsc_or_rng_free", None, [c_void_p])
         self._cl = _bind(lib, "mdsc_or_clust_conf_rng", c_int, [_SP, c_double, c_void_p])
         self._corr = _bind(lib, "mdsc_or_acc_correl", None, [_SP, c_double, c_int, _dp])
+        self._corr_sp = _bind(lib, "mdsc_or_acc_correl_species", None, [_SP, c_int, _ip, c_double, c_int, _dp])
         self._oo = _bind(lib, "mdsc_or_oo_params", None, [_SP, _dp, _dp, _dp])
         self._tabcache: dict[float, np.ndarray] = {}
 
@@ -182,6 +183,16 @@ class Oracle:
         h = np.zeros((4, nbins)) if hist is None else hist
         cs = sysm.cstate()
         self._corr(ctypes.byref(cs), bar_w, nbins, h.ctypes.data_as(_dp))
+        return h
+
+    def acc_correl_species(self, sysm: System, counts, bar_w: float, nbins: int, hist=None):
+        """acc_correl with species of counts[k] contiguous particles: the
+        species blocks, then the species-pair blocks, each (4, nbins)."""
+        nsp = len(counts)
+        h = np.zeros((nsp + nsp * (nsp - 1) // 2, 4, nbins)) if hist is None else hist
+        c = np.ascontiguousarray(counts, dtype=np.int32)
+        cs = sysm.cstate()
+        self._corr_sp(ctypes.byref(cs), nsp, c.ctypes.data_as(_ip), bar_w, nbins, h.ctypes.data_as(_dp))
         return h
 
     def oo_params(self, sysm: System):
@@ -367,6 +378,7 @@ class Ref:
         self._rng_free = _bind(lib, "mdsc_ref_rng_free", None, [c_void_p])
         self._cl = _bind(lib, "mdsc_ref_clust_conf", None, [_SP, c_double, c_void_p])
         self._corr = _bind(lib, "mdsc_ref_acc_correl", None, [_SP, c_double, c_int, _dp])
+        self._corr_sp = _bind(lib, "mdsc_ref_acc_correl_species", None, [_SP, c_int, _ip, c_double, c_int, _dp])
         self._oo = _bind(lib, "mdsc_ref_oo_params", None, [_SP, _dp, _dp, _dp])
         self._mt = _bind(lib, "mdsc_ref_moveTher", None,
                          [_dp, _dp, c_double, c_double, c_void_p, c_void_p, c_double, c_double, _dp,
@@ -383,6 +395,14 @@ class Ref:
         h = np.zeros((4, nbins)) if hist is None else hist
         cs = sysm.cstate()
         self._corr(ctypes.byref(cs), bar_w, nbins, h.ctypes.data_as(_dp))
+        return h
+
+    def acc_correl_species(self, sysm, counts, bar_w, nbins, hist=None):
+        nsp = len(counts)
+        h = np.zeros((nsp + nsp * (nsp - 1) // 2, 4, nbins)) if hist is None else hist
+        c = np.ascontiguousarray(counts, dtype=np.int32)
+        cs = sysm.cstate()
+        self._corr_sp(ctypes.byref(cs), nsp, c.ctypes.data_as(_ip), bar_w, nbins, h.ctypes.data_as(_dp))
         return h
 
     def oo_params(self, sysm):

@@ -1334,6 +1334,59 @@ void mdsc_or_acc_correl(const mdsc_oracle_state* s, double bar_w, int nbins, dou
   }
 }
 
+/* acc_correl (v25/functions.cpp:2400-2470) with nsp species, contiguous
+   blocks of counts[k] particles (calc_II / rev_II numbering).  hist: the
+   nsp species blocks (intra: 2, 2 dot, 2 (3 doti dotj - dot), 3 dot^2 - 1),
+   then the species-pair blocks (0,1), (0,2), ..., (1,2), ... (inter: 1, dot,
+   3 doti dotj - dot, (3 dot^2 - 1) / 2), each 4 x nbins; accumulates. */
+void mdsc_or_acc_correl_species(const mdsc_oracle_state* s, int nsp, const int* counts, double bar_w,
+                                int nbins, double* hist) {
+  const double* L = s->L;
+  int* sp = (int*)malloc(sizeof(int) * (s->n > 0 ? s->n : 1));
+  int q = 0;
+  for (int k = 0; k < nsp; ++k)
+    for (int c = 0; c < counts[k]; ++c) sp[q++] = k;
+  for (int f = 0; f < s->n - 1; ++f) {
+    const double* ri = s->r + 3 * f;
+    const double* oi = s->O + 9 * f + 6;
+    for (int g = f + 1; g < s->n; ++g) {
+      const double* rj = s->r + 3 * g;
+      const double* oj = s->O + 9 * g + 6;
+      double XIJ = ri[0] - rj[0];
+      XIJ -= L[0] * floor(XIJ / L[0] + 0.5);
+      double YIJ = ri[1] - rj[1];
+      YIJ -= L[1] * floor(YIJ / L[1] + 0.5);
+      double ZIJ = ri[2] - rj[2];
+      ZIJ -= L[2] * floor(ZIJ / L[2] + 0.5);
+      const double RIJSQ = XIJ * XIJ + YIJ * YIJ + ZIJ * ZIJ;
+      const double RIJ = sqrt(RIJSQ);
+      const double dot = oi[0] * oj[0] + oi[1] * oj[1] + oi[2] * oj[2];
+      const double dotsq = dot * dot;
+      const double doti = (oi[0] * XIJ + oi[1] * YIJ + oi[2] * ZIJ) / RIJ;
+      const double dotj = (oj[0] * XIJ + oj[1] * YIJ + oj[2] * ZIJ) / RIJ;
+      const int bin = (int)floor(RIJ / bar_w);
+      if (bin < 0 || bin >= nbins) continue;
+      const int m = sp[f], n = sp[g];
+      if (m == n) {
+        double* h = hist + (size_t)m * 4 * nbins;
+        h[0 * nbins + bin] += 2.;
+        h[1 * nbins + bin] += 2. * dot;
+        h[2 * nbins + bin] += 2. * (3. * doti * dotj - dot);
+        h[3 * nbins + bin] += 3. * dotsq - 1.;
+      } else {
+        /* the reference's Vc table numbers the pairs m < n row by row */
+        const int cc = m * (2 * nsp - m - 1) / 2 + (n - m - 1);
+        double* h = hist + (size_t)(nsp + cc) * 4 * nbins;
+        h[0 * nbins + bin] += 1.;
+        h[1 * nbins + bin] += dot;
+        h[2 * nbins + bin] += 3. * doti * dotj - dot;
+        h[3 * nbins + bin] += (3. * dotsq - 1.) / 2;
+      }
+    }
+  }
+  free(sp);
+}
+
 /* eigenvalues d[3] and eigenvectors (columns of V) of a symmetric 3x3
    matrix by cyclic Jacobi rotations (Golub & Van Loan, Matrix
    Computations, 8.5): each rotation zeroes one off-diagonal element. */

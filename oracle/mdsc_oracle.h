@@ -142,6 +142,10 @@ void mdsc_or_set_threads(int n);
 
 /* acc_correl, v25/functions.cpp:2400-2470 (one species): hist[4*nbins] += */
 void mdsc_or_acc_correl(const mdsc_oracle_state* s, double bar_w, int nbins, double* hist);
+/* the same with nsp species of counts[k] contiguous particles: the species
+   blocks, then the species-pair blocks, each 4 x nbins (+=) */
+void mdsc_or_acc_correl_species(const mdsc_oracle_state* s, int nsp, const int* counts, double bar_w,
+                                int nbins, double* hist);
 /* oo_params, v25/functions.cpp:2702-2748: G1, G2 and the total moment M */
 void mdsc_or_oo_params(const mdsc_oracle_state* s, double* G1, double* G2, double M[3]);
 

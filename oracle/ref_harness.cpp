@@ -346,3 +346,73 @@ extern "C" void mdsc_ref_oo_params(mdsc_ref_state* s, double* G1, double* G2, do
   *G2 = g2;
   for (int a = 0; a < 3; ++a) M[a] = m[a];
 }
+
+// acc_correl with nsp species of counts[k] contiguous particles: Hista per
+// species, Histe per species pair (the driver's Vc numbering, v25/main.cpp:
+// 118-143); hist gets the species blocks, then the pair blocks, 4 x nbins
+// each (+=).
+extern "C" void mdsc_ref_acc_correl_species(mdsc_ref_state* s, int nsp, const int* counts, double bar_w,
+                                            int nbins, double* hist) {
+  Dynvec<int> np(nsp);
+  for (int k = 0; k < nsp; ++k) np[k] = counts[k];
+  part_num NP;
+  NP.init(nsp, np);
+  Dynvec<Dynvec<Spherocyl> > part(nsp);
+  int i = 0;
+  for (int k = 0; k < nsp; ++k) {
+    part[k].set_size(counts[k]);
+    for (int q = 0; q < counts[k]; ++q, ++i) {
+      Spherocyl& P = part[k][q];
+      double sh[2] = {s->len[i], s->dia[i]};
+      P.set_id(i);
+      P.set_shape(sh);
+      P.set_mass(s->mass[i]);
+      P.set_inertia();
+      P.set_pos(&s->r[3 * i]);
+      Matrix<double> o(3, 3);
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) o[a][b] = s->O[9 * i + 3 * a + b];
+      P.set_omat(o);
+    }
+  }
+  const int ns = nsp * (nsp - 1) / 2;
+  cross* Vc = new cross[nsp];
+  if (nsp > 1) {
+    for (int n = 0; n < nsp; ++n) {
+      Vc[n].C.set_size(nsp - 1);
+      Vc[n].P.set_size(nsp - 1);
+      Vc[n].T.set_size(nsp - 1);
+    }
+    std::vector<int> cct(nsp, 0);
+    int cnt = 0;
+    for (int m = 0; m < nsp - 1; ++m)
+      for (int n = m + 1; n < nsp; ++n) {
+        Vc[m].C[cct[m]] = cnt;
+        Vc[m].P[cct[m]] = n;
+        Vc[m].T[cct[m]] = true;
+        cct[m]++;
+        Vc[n].C[cct[n]] = cnt;
+        Vc[n].P[cct[n]] = m;
+        Vc[n].T[cct[n]] = false;
+        cct[n]++;
+        cnt++;
+      }
+  }
+  const double diag = 0.5 * sqrt(s->L[0] * s->L[0] + s->L[1] * s->L[1] + s->L[2] * s->L[2]);
+  const int nfull = std::max(nbins, (int)floor(diag / bar_w) + 2);
+  Dynvec<Matrix<double> > Hista(nsp), Histe(ns > 0 ? ns : 1);
+  for (int k = 0; k < nsp; ++k) {
+    Hista[k].set_size(4, nfull);
+    Hista[k].set_to(0.);
+  }
+  for (int k = 0; k < (ns > 0 ? ns : 1); ++k) {
+    Histe[k].set_size(4, nfull);
+    Histe[k].set_to(0.);
+  }
+  acc_correl(part, Hista, Histe, s->L, bar_w, NP, Vc);
+  for (int k = 0; k < nsp + ns; ++k)
+    for (int f = 0; f < 4; ++f)
+      for (int b = 0; b < nbins; ++b)
+        hist[((size_t)k * 4 + f) * nbins + b] += k < nsp ? Hista[k][f][b] : Histe[k - nsp][f][b];
+  delete[] Vc;
+}

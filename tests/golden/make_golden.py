@@ -7,6 +7,9 @@ fixtures travel with the repository, so the oracle restatement and the GPU
 path can be checked against the reference where its sources are absent.
 
   python tests/golden/make_golden.py
+
+run_v25/ holds the files the reference's driver writes on its own example
+input, for the file-format and driver tests.
 """
 from __future__ import annotations
 
@@ -132,6 +135,56 @@ def driver_trajectory():
                 fin_clust=fin["clust"], fin_xi=fin["xi"])
 
 
+RUN_FILES = ("input.txt", "conf.dat", "ran_state0F.dat", "ran_state1F.dat", "counters.dat", "correlation.dat",
+             "ptens.dat", "magmom.dat", "output.dat", os.path.join("pos_vel", "pos_vel_0.dat"),
+             os.path.join("pos_vel", "pos_vel_1.dat"))
+
+
+def _edit_input(text, **kv):
+    """v25/input.txt with some lines replaced (label prefix -> new line)."""
+    out = []
+    for ln in text.splitlines():
+        for prefix, new in kv.items():
+            if ln.startswith(prefix):
+                ln = new
+        out.append(ln)
+    return "\n".join(out) + "\n"
+
+
+def run_files():
+    """The reference driver's run files on its own example input
+    (v25/input.txt: two species of 50 rods, two off-axis dipoles each),
+    shortened: a new run of 2 steps with every output every step (init/),
+    then a restart (signal 1) of 3 steps from its files (restart/) and a
+    continuation (signal 2) of 2 steps (continue/)."""
+    import shutil
+    import subprocess
+    import tempfile
+
+    src = open(os.path.join(os.environ.get("MDSC_REFERENCE", "/root/reference"), "v25", "input.txt")).read()
+    common = {"Histogram bar width=": "Histogram bar width=\t0.1", "corr. sum freq.=": "corr. sum freq.=\t1",
+              "DiffCorr. frequency=": "DiffCorr. frequency=    1", "ViscCorr. frequency=": "ViscCorr. frequency=    1",
+              "Steps before average=": "Steps before average=\t0", "clustering frequency=": "clustering frequency=\t2"}
+    drv = os.path.join(oracle.REF_DIR, "DSCmd_v25")
+    stages = (("init", 0, 2), ("restart", 1, 3), ("continue", 2, 2))
+    with tempfile.TemporaryDirectory() as d:
+        for name, sig, steps in stages:
+            text = _edit_input(src, **common, **{"No. of steps=": f"No. of steps=\t\t{steps}",
+                                               "Signal=": f"Signal=\t\t\t{sig}"})
+            open(os.path.join(d, "input.txt"), "w").write(text)
+            if os.path.exists(os.path.join(d, "output.dat")):
+                os.remove(os.path.join(d, "output.dat"))
+            subprocess.run([drv], cwd=d, env=dict(os.environ, OMP_NUM_THREADS="1"), stdout=subprocess.DEVNULL,
+                           timeout=600, check=True)
+            dst = os.path.join(HERE, "run_v25", name)
+            os.makedirs(os.path.join(dst, "pos_vel"), exist_ok=True)
+            for f in RUN_FILES:
+                if os.path.exists(os.path.join(d, f)):
+                    shutil.copy(os.path.join(d, f), os.path.join(dst, f))
+            shutil.rmtree(os.path.join(d, "pos_vel"), ignore_errors=True)
+            print("wrote", dst)
+
+
 def main():
     if not os.path.exists(oracle.REF_SO):
         oracle.build_ref()
@@ -144,6 +197,7 @@ def main():
     path = os.path.join(HERE, "driver_trajectory.npz")
     np.savez_compressed(path, **driver_trajectory())
     print("wrote", path, os.path.getsize(path), "bytes")
+    run_files()
 
 
 if __name__ == "__main__":

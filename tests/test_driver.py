@@ -1,0 +1,117 @@
+"""The run loop (mdspherocyl_gb300/driver.py) on the GPU against the
+reference's own driver: a restart (signal 1) and a continuation (signal 2)
+of the reference's example input (two species, two off-axis dipoles per
+rod), from the files the reference wrote, compared file by file with what
+the reference wrote next (tests/golden/run_v25/).
+
+Tolerances: the GPU's Ewald sums are FP32 (forces ~1e-6 relative), so
+  energies per particle, pressures: 1e-5 relative (+1e-9)
+  positions 1e-9, orientations 1e-8, momenta and angular momenta 1e-7
+  generator states, cluster labels, counters, file layouts: identical
+"""
+import os
+import shutil
+import tempfile
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from mdspherocyl_gb300 import files as F
+from mdspherocyl_gb300.driver import Driver, layout
+
+pytestmark = pytest.mark.gpu
+
+RUN = os.path.join(ROOT, "tests", "golden", "run_v25")
+
+
+def _cmp_numbers(a, b, rel, abs_, what):
+    ta, tb = a.split(), b.split()
+    assert len(ta) == len(tb), (what, a, b)
+    for x, y in zip(ta, tb):
+        try:
+            fx, fy = float(x), float(y)
+        except ValueError:
+            assert x == y, (what, a, b)
+            continue
+        assert abs(fx - fy) <= rel * abs(fy) + abs_, (what, x, y)
+
+
+def _check_stage(d, stage):
+    p = F.read_input(os.path.join(d, "input.txt"))
+    ref = os.path.join(RUN, stage)
+    # output.dat: one line per step (times of the run itself aside), then the report
+    ours = open(os.path.join(d, "output.dat")).read().splitlines()
+    theirs = open(os.path.join(ref, "output.dat")).read().splitlines()
+    assert len(ours) == len(theirs)
+    for a, b in zip(ours, theirs):
+        if " | " in b and b[:1].isdigit() and b.split()[0].endswith("."):
+            assert a.split()[0] == b.split()[0]  # Time
+            _cmp_numbers(a.split(" | ")[1], b.split(" | ")[1], 1e-5, 1e-9, "output.dat")
+        else:
+            ta, tb = a.replace("+/-", " +/- "), b.replace("+/-", " +/- ")
+            if "+/-" in a:  # averages; the fluctuations are differences of nearly equal sums
+                va, vb = ta.split(), tb.split()
+                assert len(va) == len(vb)
+                for k, (x, y) in enumerate(zip(va, vb)):
+                    if k + 1 < len(va) and va[k + 1] == "+/-":
+                        _cmp_numbers(x, y, 1e-5, 1e-9, "report")
+                    elif k > 0 and va[k - 1] == "+/-":
+                        continue
+                    else:
+                        assert x == y
+            else:
+                _cmp_numbers(ta, tb, 1e-5, 1e-9, "report")
+    # conf.dat
+    length, dia, mass, dip, nd, nd_part = layout(p)
+    a = F.read_conf(os.path.join(d, "conf.dat"), p.n_part, nd_part)
+    b = F.read_conf(os.path.join(ref, "conf.dat"), p.n_part, nd_part)
+    assert np.array_equal(a["box"], b["box"])
+    assert np.abs(a["r"] - b["r"]).max() <= 1e-9
+    assert np.abs(a["O"] - b["O"]).max() <= 1e-8
+    assert np.abs(a["p"] - b["p"]).max() <= 1e-7 and np.abs(a["l"] - b["l"]).max() <= 1e-7
+    assert np.array_equal(a["clust"], b["clust"])
+    assert np.abs(a["xi"] - b["xi"]).max() <= 1e-9 and np.array_equal(a["strn"], b["strn"])
+    # the generators drew the same numbers
+    for k in range(2):
+        x = open(os.path.join(d, f"ran_state{k}F.dat"), "rb").read()
+        y = open(os.path.join(ref, f"ran_state{k}F.dat"), "rb").read()
+        assert x[:4996] == y[:4996]
+    # counters.dat: the clock and counters exactly, the sums to the tolerance
+    ca = open(os.path.join(d, "counters.dat")).read().split()
+    cb = open(os.path.join(ref, "counters.dat")).read().split()
+    assert ca[:5] == cb[:5]
+    _cmp_numbers(" ".join(ca[5:]), " ".join(cb[5:]), 1e-5, 1e-9, "counters.dat")
+    # correlation.dat, ptens.dat, magmom.dat
+    for f in ("correlation.dat", "ptens.dat", "magmom.dat"):
+        la, lb = open(os.path.join(d, f)).read().splitlines(), open(os.path.join(ref, f)).read().splitlines()
+        assert len(la) == len(lb), f
+        for x, y in zip(la, lb):
+            _cmp_numbers(x, y, 1e-5, 2e-8, f)
+
+
+def test_restart_and_continue_like_the_reference():
+    with tempfile.TemporaryDirectory() as d:
+        for f in ("conf.dat", "ran_state0F.dat", "ran_state1F.dat", "counters.dat", "correlation.dat"):
+            shutil.copy(os.path.join(RUN, "init", f), d)
+        shutil.copy(os.path.join(RUN, "restart", "input.txt"), d)
+        with open(os.devnull, "w") as devnull:
+            assert Driver(d, out=devnull).run() == 0, open(os.path.join(d, "Error.dat")).read()
+        _check_stage(d, "restart")
+        shutil.copy(os.path.join(RUN, "continue", "input.txt"), d)
+        os.remove(os.path.join(d, "output.dat"))
+        with open(os.devnull, "w") as devnull:
+            assert Driver(d, out=devnull).run() == 0, open(os.path.join(d, "Error.dat")).read()
+        _check_stage(d, "continue")
+
+
+def test_new_run_writes_every_file():
+    """Signal 0: a configuration of its own, then the same files."""
+    with tempfile.TemporaryDirectory() as d:
+        shutil.copy(os.path.join(RUN, "init", "input.txt"), d)
+        with open(os.devnull, "w") as devnull:
+            assert Driver(d, out=devnull).run() == 0, open(os.path.join(d, "Error.dat")).read()
+        for f in ("conf.dat", "ran_state0F.dat", "ran_state1F.dat", "counters.dat", "correlation.dat",
+                  "ptens.dat", "magmom.dat", "output.dat", os.path.join("pos_vel", "pos_vel_0.dat")):
+            assert os.path.getsize(os.path.join(d, f)) > 0, f
+        assert open(os.path.join(d, "Error.dat")).read() == ""

@@ -48,7 +48,8 @@ def test_observables_vs_reference_fixtures(path):
         bar_w = float(g["corr_bar_w"])
         assert bt.correlation_bins(0, bar_w) == g["corr_hist"].shape[1]
         (h,) = bt.correlations(bar_w)
-        _check_hist(h, g["corr_hist"])
+        assert h.shape[0] == 1
+        _check_hist(h[0], g["corr_hist"])
         G1, G2, M = bt.order_params()
         assert abs(G2[0] - g["oo_G2"]) <= 1e-5
         assert abs(G1[0] - g["oo_G1"]) <= 1e-4
@@ -87,7 +88,7 @@ def test_correlations_mix_vs_oracle(orc, bins):
         for k, (st, box) in enumerate(systems):
             assert nb[k] == _nbins(box, bar_w)
             want = orc.acc_correl(_osys(st, box), bar_w, nb[k])
-            _check_hist(hs[k], want)
+            _check_hist(hs[k][0], want)
         # accumulation: a second call adds the same sums
         hs2 = bt.correlations(bar_w, hs)
         for k in range(len(systems)):
@@ -113,14 +114,19 @@ def test_normalize_correlations():
     box = np.array([10.0, 10.0, 10.0])
     bar_w = 0.5
     nb = _nbins(box, bar_w)
-    h = np.ones((4, nb))
-    pos, norm, g = L.normalize_correlations(h, n=100, box=box, bar_w=bar_w, cor_cont=2.0)
+    h = np.ones((1, 4, nb))
+    pos, norm, g = L.normalize_correlations(h, [100], box=box, bar_w=bar_w, cor_cont=2.0)
     assert np.allclose(pos, (np.arange(nb) + 0.5) * bar_w)
     k = 3  # pos = 1.75 < L/2: the full shell
     assert norm[k] == pytest.approx(4 * np.pi * (pos[k] ** 2 * bar_w + bar_w ** 3 / 12))
     k = 12  # pos = 6.25 in [L/2, L/sqrt 2]: the shell cut by the box
     assert norm[k] == pytest.approx(4 * np.pi * pos[k] ** 2 * (3 * 10.0 / (2 * pos[k]) - 2) * bar_w)
-    assert g[1, 3] == pytest.approx(3.0 / (norm[3] * 2.0 * 100 * 99))
+    assert g[0, 1, 3] == pytest.approx(3.0 / (norm[3] * 2.0 * 100 * 99))
+    # two species: the pair block over N_m N_n
+    h2 = np.ones((3, 4, nb))
+    _, _, g2 = L.normalize_correlations(h2, [30, 70], box=box, bar_w=bar_w, cor_cont=2.0)
+    assert g2[2, 3, 5] == pytest.approx(5.0 / (norm[5] * 2.0 * 30 * 70))
+    assert g2[0, 0, 5] == pytest.approx(1.0 / (norm[5] * 2.0 * 30 * 29))
 
 
 @pytest.mark.gpu
@@ -140,3 +146,26 @@ def test_order_params_every_step(orc):
             assert abs(obs[k]["G1"] - G1[k]) <= 1e-4 and abs(G1[k] - g1) <= 1e-4
             assert np.abs(np.array(obs[k]["M"]) - M[k]).max() <= 1e-6 * scale
             assert np.abs(M[k] - m).max() <= 1e-12 * scale
+
+
+@pytest.mark.gpu
+def test_correlations_species_vs_oracle(orc):
+    """Several species per system: intra and inter histograms against the
+    oracle's acc_correl with components (itself equal to the reference's,
+    tests/test_oracle.py), in a batch with a one-species system."""
+    systems = _mix()
+    counts = {0: [1000, 1200, 800], 1: [300, 400]}
+    bar_w = max(float(min(b)) for _, b in systems) / 300.0
+    with L.Batch([_spec(st, b) for st, b in systems], [st for st, _ in systems]) as bt:
+        for k, c in counts.items():
+            bt.set_species(k, c)
+        hs = bt.correlations(bar_w)
+        for k, (st, box) in enumerate(systems):
+            c = counts.get(k, [st.n])
+            want = orc.acc_correl_species(_osys(st, box), c, bar_w, _nbins(box, bar_w))
+            assert hs[k].shape == want.shape
+            for q in range(want.shape[0]):
+                intra = q < len(c)
+                assert np.array_equal(hs[k][q][0], want[q][0])
+                pairs = want[q][0] / (2.0 if intra else 1.0)
+                assert np.all(np.abs(hs[k][q][1:] - want[q][1:]) <= 5e-6 * pairs + 1e-7)

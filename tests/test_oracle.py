@@ -202,6 +202,12 @@ def test_observables_vs_reference(ref, orc, k):
     hist = ref.acc_correl(_sys(st, box), bar_w, nbins)
     G1, G2, M = ref.oo_params(_sys(st, box))
     _check_observables(orc, _sys(st, box), bar_w, hist, G1, G2, M)
+    # components: intra and inter histograms against the reference's own
+    counts = [st.n // 3, st.n // 3, st.n - 2 * (st.n // 3)]
+    hs = ref.acc_correl_species(_sys(st, box), counts, bar_w, nbins)
+    ho = orc.acc_correl_species(_sys(st, box), counts, bar_w, nbins)
+    assert np.array_equal(ho[:, 0], hs[:, 0])
+    assert np.abs(ho - hs).max() <= 1e-12 * max(1.0, hs[:, 0].max())
     # accumulation over calls, as Hista accumulates over a run
     h2 = orc.acc_correl(_sys(st, box), bar_w, nbins, orc.acc_correl(_sys(st, box), bar_w, nbins))
     assert np.array_equal(h2[0], 2 * hist[0])
