@@ -112,7 +112,8 @@ typedef struct {
   /* oo_params (v25/functions.cpp:2702-2760) of the state after the step, as
      the driver takes them every step (v25/main.cpp:720-728): nematic order
      G2, polar order G1 and the total dipole moment M.  Per-particle terms in
-     FP32 (the reference forms Q in FP32 too), float-float sums. */
+     FP32 (the reference forms Q in FP32 too), float-float sums: M carries
+     ~1e-7 of each moment; mdsc_order_params gives it from FP64 terms. */
   double G1, G2;
   double M[3];
   /* total momentum and angular momentum after the step (the driver prints

@@ -247,7 +247,6 @@ class Driver:
                         hist = bt.correlations(p.bar_w, [hist])[0]
                         cor_cont += 1.0 / V
                     var.G1, var.G2 = o["G1"], o["G2"]
-                    M = o["M"]
                     if p.tcfd > 0 and math.fmod(float(np.float32(s)), p.tcfd) == 0:
                         self._pos_vel(bt, np_tc, p, I, mass, Ntcf)
                         Ntcf += 1
@@ -256,6 +255,9 @@ class Driver:
                         HF = np.einsum("ni,nj->ij", d["r"], d["p"])
                         F.append(self.path("ptens.dat"), F.ptens_line(Time, HF, var.PT))
                         Ntcv += 1
+                        # the moment from FP64 sums (the step's own M is summed from
+                        # the FP32 dipole vectors, ~1e-7 of each moment)
+                        M = bt.order_params()[2][0]
                         F.append(self.path("magmom.dat"), F.magmom_line(Time, M))
                         mcont += 1
                     AcT += var
