@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define MDSC_ABI_VERSION 2  /* 2: mdsc_observables gained G1, G2, M, P_tot, L_tot */
+#define MDSC_ABI_VERSION 2  /* 2: mdsc_observables gained G1, G2, M */
 #define MDSC_MAX_DIPOLES 4 /* dipoles per particle */
 
 typedef enum {
@@ -116,9 +116,6 @@ typedef struct {
      ~1e-7 of each moment; mdsc_order_params gives it from FP64 terms. */
   double G1, G2;
   double M[3];
-  /* total momentum and angular momentum after the step (the driver prints
-     their squares, v25/main.cpp:790-800, v25/functions.cpp:2849-2850) */
-  double P_tot[3], L_tot[3];
 } mdsc_observables;
 
 typedef struct mdsc_batch mdsc_batch;

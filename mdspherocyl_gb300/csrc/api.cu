@@ -27,6 +27,7 @@ void launch_derive(const Batch& b, cudaStream_t s);
 void launch_integrate_first(const Batch& b, cudaStream_t s);
 void launch_finalize(const Batch& b, int mode, cudaStream_t s);
 void launch_reduce_obs(const Batch& b, int mode, cudaStream_t s);
+void launch_order_terms(const Batch& b, cudaStream_t s);
 void launch_movex(const Batch& b, cudaStream_t s);
 void launch_renorm(const Batch& b, cudaStream_t s);
 void launch_movep(const Batch& b, const double* xi, int last, cudaStream_t s);
@@ -417,6 +418,7 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   b.kin1 = A.take<double>(2 * nb);
   b.kin2 = A.take<double>(9 * nb);
   b.dmax = A.take<double>(nb);
+  b.obk = A.take<double>(12 * nb);
   b.blk = A.take<int2>(nb);
   b.nb = A.take<int>(n * kMaxNb);
   b.nbc = A.take<int>(n);
@@ -504,6 +506,7 @@ mdsc_status eval_forces(mdsc_batch* B, int force_list) {
   launch_real_sum(b, B->st);
   launch_kspace(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, B->st);
   launch_finalize(b, kMaskAll, B->st);
+  launch_order_terms(b, B->st);
   launch_reduce_obs(b, kRedEnergies, B->st);
   CU(cudaGetLastError());
   for (int s = 0; s < B->nsys; ++s) {
@@ -625,9 +628,10 @@ mdsc_status capture_step(mdsc_batch* B, int which) {
   cudaEventRecord(B->ev_fork, B->st);
   cudaStreamWaitEvent(B->s2, B->ev_fork, 0);
   cudaStreamWaitEvent(B->s3, B->ev_fork, 0);
+  launch_order_terms(b, B->st);
   launch_list_build(b, 0, B->st);
   launch_wca(b, B->st);
-  launches += 3;
+  launches += 4;
   launch_real_pairs(b, B->lo.multi, B->s2);
   launch_real_sum(b, B->s2);
   launches += b.ntiles > 0 ? 2 : 0;
@@ -745,10 +749,6 @@ void convert_obs(const SysObs& o, int n, int n_clusters, mdsc_observables& r) {
   r.n_clusters = n_clusters;
   r.list_builds = o.list_builds;
   order_params(o.osum, n, &r.G1, &r.G2, r.M);
-  for (int a = 0; a < 3; ++a) {
-    r.P_tot[a] = o.osum[12 + a];
-    r.L_tot[a] = o.osum[15 + a];
-  }
 }
 
 mdsc_status read_obs(mdsc_batch* B, mdsc_observables* out) {
@@ -1278,6 +1278,7 @@ mdsc_status mdsc_force_sc(mdsc_batch* B, double* U, double* W, double* PT) {
   launch_list_build(B->b, 0, B->st);
   launch_wca(B->b, B->st);
   launch_finalize(B->b, kMaskWca | kFlagAccum, B->st);
+  launch_order_terms(B->b, B->st);
   launch_reduce_obs(B->b, kRedEnergies, B->st);
   st = read_obs(B, nullptr);
   for (int s = 0; s < B->nsys; ++s) {
@@ -1296,6 +1297,7 @@ mdsc_status mdsc_force_dipR(mdsc_batch* B, double* U, double* PT) {
   launch_real_pairs(B->b, B->lo.multi, B->st);
   launch_real_sum(B->b, B->st);
   launch_finalize(B->b, kMaskReal | kFlagAccum, B->st);
+  launch_order_terms(B->b, B->st);
   launch_reduce_obs(B->b, kRedEnergies, B->st);
   st = read_obs(B, nullptr);
   for (int s = 0; s < B->nsys; ++s) {
@@ -1312,6 +1314,7 @@ mdsc_status mdsc_force_dipK(mdsc_batch* B, double* U, double* PT) {
   launch_derive(B->b, B->st);
   launch_kspace(B->b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, B->b.kE, B->st);
   launch_finalize(B->b, kMaskK | kFlagAccum, B->st);
+  launch_order_terms(B->b, B->st);
   launch_reduce_obs(B->b, kRedEnergies, B->st);
   st = read_obs(B, nullptr);
   for (int s = 0; s < B->nsys; ++s) {
@@ -1327,6 +1330,7 @@ mdsc_status mdsc_ext_field(mdsc_batch* B, double* U) {
   if (st) return st;
   launch_derive(B->b, B->st);
   launch_finalize(B->b, kMaskExt | kFlagAccum, B->st);
+  launch_order_terms(B->b, B->st);
   launch_reduce_obs(B->b, kRedEnergies, B->st);
   st = read_obs(B, nullptr);
   for (int s = 0; s < B->nsys; ++s)
@@ -1761,9 +1765,9 @@ mdsc_status mdsc_profile_steps(mdsc_batch* B, int nsteps, int max_kernels, char*
   cudaSetDevice(B->device);
   mdsc_status st = ensure_forces(B);
   if (st) return st;
-  const char* kn[10] = {"integrate_first", "list_build", "wca", "real_pairs", "real_sum", "kspace_sum",
-                        "kspace_combine", "kspace_gather", "finalize", "reduce_obs"};
-  const int nk = 10;
+  const char* kn[11] = {"integrate_first", "order_terms", "list_build", "wca", "real_pairs", "real_sum",
+                        "kspace_sum", "kspace_combine", "kspace_gather", "finalize", "reduce_obs"};
+  const int nk = 11;
   std::vector<cudaEvent_t> ev(nk + 1);
   for (auto& e : ev) cudaEventCreate(&e);
   std::vector<double> acc(nk, 0.0);
@@ -1775,25 +1779,27 @@ mdsc_status mdsc_profile_steps(mdsc_batch* B, int nsteps, int max_kernels, char*
     cudaEventRecord(ev[0], B->st);
     launch_integrate_first(b, B->st);
     cudaEventRecord(ev[1], B->st);
-    launch_list_build(b, 0, B->st);
+    launch_order_terms(b, B->st);
     cudaEventRecord(ev[2], B->st);
-    launch_wca(b, B->st);
+    launch_list_build(b, 0, B->st);
     cudaEventRecord(ev[3], B->st);
-    launch_real_pairs(b, B->lo.multi, B->st);
+    launch_wca(b, B->st);
     cudaEventRecord(ev[4], B->st);
-    launch_real_sum(b, B->st);
+    launch_real_pairs(b, B->lo.multi, B->st);
     cudaEventRecord(ev[5], B->st);
+    launch_real_sum(b, B->st);
+    cudaEventRecord(ev[6], B->st);
     // the three k-space kernels, timed one by one
     launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 0, B->st);
-    cudaEventRecord(ev[6], B->st);
-    launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 1, B->st);
     cudaEventRecord(ev[7], B->st);
-    launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 2, B->st);
+    launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 1, B->st);
     cudaEventRecord(ev[8], B->st);
-    launch_finalize(b, kMaskAll | kFlagMoveP, B->st);
+    launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 2, B->st);
     cudaEventRecord(ev[9], B->st);
-    launch_reduce_obs(b, kRedStep, B->st);
+    launch_finalize(b, kMaskAll | kFlagMoveP, B->st);
     cudaEventRecord(ev[10], B->st);
+    launch_reduce_obs(b, kRedStep, B->st);
+    cudaEventRecord(ev[11], B->st);
     CU(cudaStreamSynchronize(B->st));
     for (int k = 0; k < nk; ++k) {
       float t = 0;

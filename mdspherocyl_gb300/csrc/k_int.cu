@@ -461,68 +461,59 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
 }
 
 // ---------------------------------------------------------------------
+// oo_params' terms (v25/functions.cpp:2720-2760, Qmat_3d :3426-3445) per
+// particle block, from the FP32 working copies of this step's orientations:
+// the rod axis o, o o^T and the dipole vectors mu o_dipole, float-float
+// block sums.  Its own small kernel, early in the step on the WCA stream:
+// widening finalize's sums cost that kernel occupancy.
+__global__ void __launch_bounds__(kPartBlock) order_terms_kernel(Batch b) {
+  __shared__ double sh[12 * kPartBlock / 32];
+  const int2 bk = b.blk[blockIdx.x];
+  const SysDev& P = b.sys[bk.x];
+  const int i = bk.y + threadIdx.x;
+  FF v[12];
+#pragma unroll
+  for (int c = 0; c < 12; ++c) v[c].hi = v[c].lo = 0.f;
+  if (i < P.part_off + P.n) {
+    const float4 q = b.pax[i];
+    const float t[9] = {q.x, q.y, q.z, q.x * q.x, q.x * q.y, q.x * q.z, q.y * q.y, q.y * q.z, q.z * q.z};
+#pragma unroll
+    for (int c = 0; c < 9; ++c) v[c] = ff_of(t[c]);
+    const int ND = b.ndtot, g0 = P.dip_off + (i - P.part_off) * P.nd;
+    for (int w = 0; w < P.nd; ++w) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) v[9 + a] = ff_add(v[9 + a], ff_of(b.dm[a * ND + g0 + w]));
+    }
+  }
+  double tot[12];
+  block_sum<12, kPartBlock>(v, sh, tot);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int c = 0; c < 12; ++c) b.obk[12 * blk_slot(P, bk) + c] = tot[c];
+  }
+}
+
+// ---------------------------------------------------------------------
 // per-system sums and the thermostat's last update.  kRedGroups blocks per
 // system, one per group of sums (real-space tiles, k-vectors, WCA blocks,
 // kinetic terms, order parameters), each in float-float with a fixed order;
 // the kinetic block also closes the step's thermostat and bookkeeping.
 constexpr int kRedThreads = 128;
 __global__ void __launch_bounds__(kRedThreads) reduce_obs_kernel(Batch b, int mode) {
-  __shared__ double sh[18 * kRedThreads / 32];
+  __shared__ double sh[12 * kRedThreads / 32];
   const int s = blockIdx.x / kRedGroups, grp = blockIdx.x % kRedGroups;
   const SysDev& P = b.sys[s];
   SysState& S = b.st[s];
   SysObs& ob = b.obs[s];
-  FF v[18];
+  FF v[12];
 #pragma unroll
-  for (int c = 0; c < 18; ++c) v[c].hi = v[c].lo = 0.f;
-  if (grp == 4) {
-    // oo_params' terms (v25/functions.cpp:2720-2760, Qmat_3d :3426-3445)
-    // from the FP32 working copies of the current orientations: the rod
-    // axis o, o o^T and the dipole vectors mu o_dipole; then the total
-    // momentum and angular momentum the driver prints (v25/main.cpp:
-    // 790-800) from the FP64 state.  Particle by particle, four per thread
-    // per pass with their loads issued together.
-    const int ND = b.ndtot, nd = P.nd, end = P.part_off + P.n;
-    for (int i0 = P.part_off + threadIdx.x; i0 < end; i0 += 4 * kRedThreads) {
-      float4 o[4];
-      float m[4][3];
-      double pl[4][6];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int i = i0 + u * kRedThreads;
-        o[u] = i < end ? b.pax[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          pl[u][a] = i < end ? b.p[3 * i + a] : 0.0;
-          pl[u][3 + a] = i < end ? b.l[3 * i + a] : 0.0;
-        }
-        m[u][0] = m[u][1] = m[u][2] = 0.f;
-        if (i < end) {
-          const int g0 = P.dip_off + (i - P.part_off) * nd;
-          for (int q = 0; q < nd; ++q) {
-#pragma unroll
-            for (int a = 0; a < 3; ++a) m[u][a] += b.dm[a * ND + g0 + q];
-          }
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        if (i0 + u * kRedThreads >= end) break;
-        const float4 q = o[u];
-        const float t[12] = {q.x,       q.y,       q.z,       q.x * q.x, q.x * q.y, q.x * q.z,
-                             q.y * q.y, q.y * q.z, q.z * q.z, m[u][0],   m[u][1],   m[u][2]};
-#pragma unroll
-        for (int c = 0; c < 12; ++c) v[c] = ff_add(v[c], ff_of(t[c]));
-#pragma unroll
-        for (int c = 0; c < 6; ++c) v[12 + c] = ff_add(v[12 + c], ff_from(pl[u][c]));
-      }
-    }
-  } else {
+  for (int c = 0; c < 12; ++c) v[c].hi = v[c].lo = 0.f;
+  {
     // the rows of one per-system table, column by column: real-space tiles
-    // (U, PT; FP32), k-vectors (U, PT), WCA blocks (U, W, PT) or kinetic
-    // blocks (K_t, K_r, PT_kin, U_ext).  One code path for the four keeps
-    // the kernel small: its blocks are short, and a larger kernel waited on
-    // instruction fetch.
+    // (U, PT; FP32), k-vectors (U, PT), WCA blocks (U, W, PT), kinetic
+    // blocks (K_t, K_r, PT_kin, U_ext) or order-parameter blocks.  One code
+    // path for the five keeps the kernel small: its blocks are short, and a
+    // larger kernel waited on instruction fetch.
     const float* fsrc = nullptr;
     const double* dsrc = nullptr;
     int nrow, ncol;
@@ -538,6 +529,10 @@ __global__ void __launch_bounds__(kRedThreads) reduce_obs_kernel(Batch b, int mo
       dsrc = b.wcaE + (long long)P.blk_off * 11;
       nrow = P.nblk;
       ncol = 11;
+    } else if (grp == 4) {
+      dsrc = b.obk + (long long)P.blk_off * 12;
+      nrow = P.nblk;
+      ncol = 12;
     } else {
       dsrc = b.kin2 + (long long)P.blk_off * 9;
       nrow = P.nblk;
@@ -553,8 +548,8 @@ __global__ void __launch_bounds__(kRedThreads) reduce_obs_kernel(Batch b, int mo
       }
     }
   }
-  double out[18];
-  block_sum<18, kRedThreads>(v, sh, out);
+  double out[12];
+  block_sum<12, kRedThreads>(v, sh, out);
   if (threadIdx.x != 0) return;
   if (grp == 0) {
     ob.U_dipR = out[0];
@@ -567,7 +562,7 @@ __global__ void __launch_bounds__(kRedThreads) reduce_obs_kernel(Batch b, int mo
     ob.W_ss = out[1];
     for (int c = 0; c < 9; ++c) ob.PT_ss[c] = out[2 + c];
   } else if (grp == 4) {
-    for (int c = 0; c < 18; ++c) ob.osum[c] = out[c];
+    for (int c = 0; c < 12; ++c) ob.osum[c] = out[c];
   } else {
     ob.U_ext = out[8];
     ob.U_self = P.Uself;
@@ -708,6 +703,9 @@ void launch_integrate_first(const Batch& b, cudaStream_t s) {
 }
 void launch_finalize(const Batch& b, int mode, cudaStream_t s) {
   if (b.nblk) finalize_kernel<<<b.nblk, kPartBlock, 0, s>>>(b, mode);
+}
+void launch_order_terms(const Batch& b, cudaStream_t s) {
+  if (b.nblk) order_terms_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
 }
 void launch_reduce_obs(const Batch& b, int mode, cudaStream_t s) {
   if (b.nsys) reduce_obs_kernel<<<kRedGroups * b.nsys, kRedThreads, 0, s>>>(b, mode);

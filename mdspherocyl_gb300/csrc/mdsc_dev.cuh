@@ -103,7 +103,7 @@ struct SysObs {
   double xi[2];
   long long step;
   int status, n_clusters, list_builds, pad;
-  double osum[18];  // sum o (3), sum o o^T (xx xy xz yy yz zz), sum mu o_dipole (3), sum p (3), sum l (3)
+  double osum[12];  // sum o (3), sum o o^T (xx xy xz yy yz zz), sum mu o_dipole (3)
 };
 
 // One batch, device pointers.
@@ -182,6 +182,7 @@ struct Batch {
   double* kin1;  // 2 per block
   double* kin2;  // 9 per block: K_t, K_r, PTkin xx xy xz yy yz zz, U_ext
   double* dmax;  // 1 per block: largest displacement measure since the last list build
+  double* obk;   // 12 per block: the order-parameter terms of SysObs::osum
   int2* blk;     // (sys, first particle) per block
   // neighbour list
   int* nb;       // n * kMaxNb

@@ -264,11 +264,12 @@ class Driver:
                     AcTsq += var * var
                     cont += 1
                 if math.fmod(float(s), p.iprint) == 0:
-                    self._print_conf(bt, box, dip)
+                    d = self._print_conf(bt, box, dip)
                     F.write_counters(self.path("counters.dat"), Time, cont, Ntcf, Ntcv, mcont, AcT, AcTsq)
                     if s >= p.pre_steps and p.corrf > 0 and math.fmod(float(np.float32(s)), p.corrf) == 0:
                         F.write_correlation(self.path("correlation.dat"), hist, p.n_part, Lmin, p.bar_w, cor_cont)
-                    Mom = list(o["P_tot"]) + list(o["L_tot"])
+                    # total momentum and angular momentum (v25/main.cpp:788-800)
+                    Mom = list(d["p"].sum(axis=0)) + list(d["l"].sum(axis=0))
                     t_wall, t_cpu = time.perf_counter(), time.process_time()
                     # microseconds as integers, divided as the reference divides them
                     te = (int((t_wall - t_wall0) * 1e6) // p.iprint) * 1e-6
@@ -319,6 +320,7 @@ class Driver:
         for k in range(2):
             mt, mti = bt.get_rng(0, k)
             F.write_mt_state(self.path(f"ran_state{k}F.dat"), mt, mti)
+        return d
 
     def _pos_vel(self, bt, np_tc, p, I, mass, num) -> None:
         """pos_vel/pos_vel_<num>.dat (v25/functions.cpp:2602-2643): centre,

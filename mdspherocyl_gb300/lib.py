@@ -66,7 +66,7 @@ class Observables(ctypes.Structure):
         ("PT_kin", c_double * 9), ("PT_ss", c_double * 9), ("PT_dipR", c_double * 9),
         ("PT_dipK", c_double * 9), ("xi", c_double * 2), ("step", c_longlong),
         ("status", c_int), ("n_clusters", c_int), ("list_builds", c_int), ("pad", c_int),
-        ("G1", c_double), ("G2", c_double), ("M", c_double * 3), ("P_tot", c_double * 3), ("L_tot", c_double * 3),
+        ("G1", c_double), ("G2", c_double), ("M", c_double * 3),
     ]
 
     def as_dict(self) -> dict:
