@@ -268,6 +268,27 @@ mdsc_status mdsc_correlations(mdsc_batch* b, double bar_w, double* hist);
    Q in FP32, so G1 and G2 agree with it to ~1e-6. */
 mdsc_status mdsc_order_params(mdsc_batch* b, double* G1, double* G2, double* M);
 
+/* ---- picture ----------------------------------------------------------- */
+/* What mdsc_render draws and from where: the reference viewer's controls
+   (v25/graphic.cpp:24-41), with its defaults in brackets. */
+typedef struct {
+  int width, height;         /* pixels [480 x 480] */
+  double theta, phi, dist;   /* camera direction and distance [0.1, 0, 15] */
+  double ref[3];             /* the point looked at [0 0 0] */
+  double shift[3];           /* added to every position, the viewer's d [0 0 0] */
+  int dipoles;               /* draw the dipoles [1] */
+  int images;                /* and the 26 periodic images [0] */
+  int box;                   /* the box edges [1] */
+  int cluster;               /* only the particles with this cluster label; -1 all [-1] */
+} mdsc_view;
+/* Replaces the SDL/OpenGL viewer (v25/graphic.cpp) without a display: a
+   ray-cast picture of system sys in its current state on the GPU -- rods
+   grey by species with a blue +axis tip and red/green meridians on the body
+   x/y axes, dipoles as blue/red segments, the box edges, on white, from the
+   viewer's camera and light -- written to rgb (height x width x 3 bytes,
+   rows from the top). */
+mdsc_status mdsc_render(mdsc_batch* b, int sys, const mdsc_view* view, unsigned char* rgb);
+
 /* ---- autotuner -------------------------------------------------------- */
 /* Chooses the launch mappings (real-space tiles per block, strip-sum block
    size, grid of the FP64 WCA evaluation, k-space gather form) by timing each

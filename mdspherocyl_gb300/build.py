@@ -18,7 +18,8 @@ INCLUDE = os.path.join(ROOT, "include")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libmdsc.so")
 
-SOURCES = ["k_real.cu", "k_kspace.cu", "k_int.cu", "k_wca.cu", "k_obs.cu", "api.cu", "gen.cpp", "noalloc.cu"]
+SOURCES = ["k_real.cu", "k_kspace.cu", "k_int.cu", "k_wca.cu", "k_obs.cu", "k_render.cu", "api.cu", "gen.cpp",
+           "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
            "--expt-relaxed-constexpr", "-I", CSRC, "-I", INCLUDE]

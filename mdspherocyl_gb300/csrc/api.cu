@@ -42,6 +42,11 @@ void launch_kspace_parts(const Batch& b, int maxnd, const int4* kwork, int nkwor
 void launch_correlations(const Batch& b, const CorrSys* cs, const unsigned char* species, double bar_w,
                          int max_bins, unsigned long long* hist, cudaStream_t s);
 void launch_order_sums(const Batch& b, double* out, cudaStream_t s);
+size_t render_scratch_bytes(int n, int nd, int images);
+void launch_render(const Batch& b, int sys, int n, const unsigned char* species, const int* keep, int images,
+                   int dipoles, int draw_box, float seg_rad, float box_rad, const float* eye, const float* fwd,
+                   const float* right, const float* up, const float* light, float tan_half, int width,
+                   int height, void* scratch, unsigned char* rgb, cudaStream_t s);
 }  // namespace mdsc
 
 using namespace mdsc;
@@ -1523,6 +1528,81 @@ mdsc_status mdsc_order_params(mdsc_batch* B, double* G1, double* G2, double* M) 
       for (int c = 0; c < 12; ++c) v[c] += part[12 * (size_t)(P.blk_off + k) + c];
     order_params(v, P.n, G1 ? &G1[s] : nullptr, G2 ? &G2[s] : nullptr, M ? &M[3 * s] : nullptr);
   }
+  return MDSC_OK;
+}
+
+// ---- picture ---------------------------------------------------------------
+mdsc_status mdsc_render(mdsc_batch* B, int sys, const mdsc_view* v, unsigned char* rgb) {
+  mdsc_status st = need_state(B);
+  if (st) return st;
+  if (sys < 0 || sys >= B->nsys || !v || !rgb || v->width <= 0 || v->height <= 0 || v->width > 16384 ||
+      v->height > 16384)
+    return fail(B, MDSC_ERR_BAD_ARG, "mdsc_render: bad system, view or buffer");
+  const SysDev& P = B->lo.sys[sys];
+  // the viewer's camera (v25/graphic.cpp:680-692,405-415): gluLookAt from usr
+  // to ref, then the scene pushed back |usr| along the view
+  const double usr[3] = {v->dist * std::sin(v->theta) * std::cos(v->phi),
+                         v->dist * std::sin(v->theta) * std::sin(v->phi), v->dist * std::cos(v->theta)};
+  double ref[3], view[3];
+  for (int a = 0; a < 3; ++a) ref[a] = v->ref[a];
+  for (int a = 0; a < 3; ++a) view[a] = usr[a] - ref[a];
+  const double vn = std::sqrt(view[0] * view[0] + view[1] * view[1] + view[2] * view[2]);
+  const double un = std::sqrt(usr[0] * usr[0] + usr[1] * usr[1] + usr[2] * usr[2]);
+  if (!(vn > 0.0)) return fail(B, MDSC_ERR_BAD_ARG, "mdsc_render: the camera sits on the point it looks at");
+  double eye[3], fwd[3], right[3], up[3];
+  for (int a = 0; a < 3; ++a) {
+    eye[a] = usr[a] + un * view[a] / vn - v->shift[a];  // shifting the scene = shifting the camera back
+    fwd[a] = -view[a] / vn;
+  }
+  const double zup[3] = {0.0, 0.0, 1.0}, yup[3] = {0.0, 1.0, 0.0};
+  const double* wu = std::fabs(fwd[2]) > 0.999999 ? yup : zup;
+  right[0] = fwd[1] * wu[2] - fwd[2] * wu[1];
+  right[1] = fwd[2] * wu[0] - fwd[0] * wu[2];
+  right[2] = fwd[0] * wu[1] - fwd[1] * wu[0];
+  const double rn = std::sqrt(right[0] * right[0] + right[1] * right[1] + right[2] * right[2]);
+  for (int a = 0; a < 3; ++a) right[a] /= rn;
+  up[0] = right[1] * fwd[2] - right[2] * fwd[1];
+  up[1] = right[2] * fwd[0] - right[0] * fwd[2];
+  up[2] = right[0] * fwd[1] - right[1] * fwd[0];
+  const double tan_half = std::tan(M_PI / 6.0);
+  // a pixel at the distance looked at: the viewer's 2-pixel dipole lines and 1-pixel box edges
+  const double pix = 2.0 * (vn + un) * tan_half / v->height;
+  float e[3], f[3], r[3], u[3], l[3];
+  for (int a = 0; a < 3; ++a) {
+    e[a] = (float)eye[a];
+    f[a] = (float)fwd[a];
+    r[a] = (float)right[a];
+    u[a] = (float)up[a];
+    l[a] = un > 0.0 ? (float)(usr[a] / un) : (a == 2 ? 1.f : 0.f);
+  }
+  // species and the cluster filter, per particle
+  std::vector<unsigned char> sp(std::max(P.n, 1), 0);
+  {
+    int i = 0;
+    for (size_t k = 0; k < B->species[sys].size(); ++k)
+      for (int q = 0; q < B->species[sys][k]; ++q) sp[i++] = (unsigned char)k;
+  }
+  std::vector<int> keep;
+  if (v->cluster >= 0) {
+    keep.assign(std::max(P.n, 1), 0);
+    for (int i = 0; i < P.n; ++i) keep[i] = B->labels[sys][i] == v->cluster ? 1 : 0;
+  }
+  const size_t img = (size_t)v->width * v->height * 3;
+  const size_t scratch = render_scratch_bytes(P.n, P.nd, v->images);
+  char* d = nullptr;
+  const size_t spb = (sp.size() + 255) / 256 * 256, kb = (keep.size() * sizeof(int) + 255) / 256 * 256;
+  CU(cudaMallocAsync((void**)&d, scratch + spb + kb + img, B->st));
+  unsigned char* dsp = reinterpret_cast<unsigned char*>(d + scratch);
+  int* dkeep = keep.empty() ? nullptr : reinterpret_cast<int*>(d + scratch + spb);
+  unsigned char* dimg = reinterpret_cast<unsigned char*>(d + scratch + spb + kb);
+  CU(cudaMemcpyAsync(dsp, sp.data(), sp.size(), cudaMemcpyHostToDevice, B->st));
+  if (dkeep) CU(cudaMemcpyAsync(dkeep, keep.data(), sizeof(int) * keep.size(), cudaMemcpyHostToDevice, B->st));
+  launch_render(B->b, sys, P.n, dsp, dkeep, v->images, v->dipoles, v->box, (float)pix, (float)(0.5 * pix), e, f, r,
+                u, l, (float)tan_half, v->width, v->height, d, dimg, B->st);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(rgb, dimg, img, cudaMemcpyDeviceToHost, B->st));
+  CU(cudaFreeAsync(d, B->st));
+  CU(cudaStreamSynchronize(B->st));
   return MDSC_OK;
 }
 

@@ -38,7 +38,7 @@ EXPORTS = [
     "mdsc_place_rods", "mdsc_last_device_ms", "mdsc_force_dipR_noalloc", "mdsc_transfer",
     "mdsc_autotune", "mdsc_tuning", "mdsc_set_tuning", "mdsc_correlation_bins", "mdsc_correlations",
     "mdsc_order_params", "mdsc_step_trace", "mdsc_get_rng", "mdsc_set_rng", "mdsc_set_species",
-    "mdsc_correlation_size", "mdsc_get_thermostat",
+    "mdsc_correlation_size", "mdsc_get_thermostat", "mdsc_render",
 ]
 
 
@@ -75,6 +75,44 @@ class Observables(ctypes.Structure):
             v = getattr(self, name)
             d[name] = list(v) if hasattr(v, "__len__") else v
         return d
+
+
+class View(ctypes.Structure):
+    """mdsc_view: what mdsc_render draws and from where (the reference
+    viewer's controls and defaults, v25/graphic.cpp:24-41)."""
+
+    _fields_ = [
+        ("width", c_int), ("height", c_int), ("theta", c_double), ("phi", c_double), ("dist", c_double),
+        ("ref", c_double * 3), ("shift", c_double * 3), ("dipoles", c_int), ("images", c_int), ("box", c_int),
+        ("cluster", c_int),
+    ]
+
+    @classmethod
+    def make(cls, width=480, height=480, theta=0.1, phi=0.0, dist=15.0, ref=(0, 0, 0), shift=(0, 0, 0),
+             dipoles=True, images=False, box=True, cluster=-1) -> "View":
+        v = cls()
+        v.width, v.height, v.theta, v.phi, v.dist = int(width), int(height), float(theta), float(phi), float(dist)
+        for a in range(3):
+            v.ref[a], v.shift[a] = float(ref[a]), float(shift[a])
+        v.dipoles, v.images, v.box, v.cluster = int(bool(dipoles)), int(bool(images)), int(bool(box)), int(cluster)
+        return v
+
+
+def write_ppm(path: str, rgb) -> None:
+    """A binary PPM (P6) of an (height, width, 3) uint8 image."""
+    a = np.ascontiguousarray(rgb, dtype=np.uint8)
+    with open(path, "wb") as f:
+        f.write(b"P6\n%d %d\n255\n" % (a.shape[1], a.shape[0]))
+        f.write(a.tobytes())
+
+
+def read_ppm(path: str):
+    """The (height, width, 3) uint8 image of a binary PPM written by write_ppm."""
+    data = open(path, "rb").read()
+    parts = data.split(b"\n", 3)
+    assert parts[0] == b"P6" and parts[2] == b"255"
+    w, h = (int(x) for x in parts[1].split())
+    return np.frombuffer(parts[3], dtype=np.uint8, count=w * h * 3).reshape(h, w, 3)
 
 
 class MdscError(RuntimeError):
@@ -133,6 +171,7 @@ def load(build: bool = True) -> ctypes.CDLL:
         "mdsc_correlations": (c_int, [c_void_p, c_double, _dp]),
         "mdsc_set_species": (c_int, [c_void_p, c_int, c_int, _ip]),
         "mdsc_get_thermostat": (c_int, [c_void_p, c_int, _dp, _dp]),
+        "mdsc_render": (c_int, [c_void_p, c_int, P(View), c_void_p]),
         "mdsc_correlation_size": (c_int, [c_void_p, c_int, c_double]),
         "mdsc_order_params": (c_int, [c_void_p, _dp, _dp, _dp]),
         "mdsc_step_trace": (c_int, [c_void_p, c_int, P(Observables)]),
@@ -373,6 +412,13 @@ class Batch:
         G1, G2, M = np.zeros(self.nsys), np.zeros(self.nsys), np.zeros((self.nsys, 3))
         self._check(self.lib.mdsc_order_params(self.h, _ptr(G1), _ptr(G2), _ptr(M)), "mdsc_order_params")
         return G1, G2, M
+
+    def render(self, k: int, view: "View | None" = None, **kw):
+        """A picture of system k (mdsc_render): (height, width, 3) uint8."""
+        v = view if view is not None else View.make(**kw)
+        img = np.zeros((v.height, v.width, 3), dtype=np.uint8)
+        self._check(self.lib.mdsc_render(self.h, k, ctypes.byref(v), img.ctypes.data_as(c_void_p)), "mdsc_render")
+        return img
 
     def transfer_from(self, k: int, src: "Batch", ks: int) -> None:
         """Move system ks of src into slot k of this batch, on the GPU."""
