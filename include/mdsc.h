@@ -268,6 +268,22 @@ mdsc_status mdsc_correlations(mdsc_batch* b, double bar_w, double* hist);
    Q in FP32, so G1 and G2 agree with it to ~1e-6. */
 mdsc_status mdsc_order_params(mdsc_batch* b, double* G1, double* G2, double* M);
 
+/* ---- a new configuration ----------------------------------------------- */
+/* ini_pos (v25/functions.cpp:491-675) on the GPU: system sys (shapes
+   uploaded) put on the reference's lattice, species by species (nspecies
+   contiguous blocks of counts[k] rods, shapes from their first rod), every
+   rod along z, sites that come closer than the mean diameter to an earlier
+   species skipped, the sites reused from the first when they run out.
+   *n_overlaps: the overlapping pairs ini_pos's closing test finds (it reports
+   them and the run stops at its first force evaluation).  Momenta are left
+   as they are; the reference's 1000 cluster moves (GCAmix) are not made. */
+mdsc_status mdsc_lattice(mdsc_batch* b, int sys, int nspecies, const int* counts, int* n_overlaps);
+/* Momenta and angular momenta of system sys from the Maxwell-Boltzmann
+   distribution at temperature temp, zero total momentum, from a counter-
+   based generator seeded by seed (the reference's ini_mom draws differently,
+   v25/functions.cpp:677-1147). */
+mdsc_status mdsc_thermalize(mdsc_batch* b, int sys, double temp, unsigned long long seed);
+
 /* ---- picture ----------------------------------------------------------- */
 /* What mdsc_render draws and from where: the reference viewer's controls
    (v25/graphic.cpp:24-41), with its defaults in brackets. */

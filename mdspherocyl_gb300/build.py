@@ -18,8 +18,10 @@ INCLUDE = os.path.join(ROOT, "include")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libmdsc.so")
 
-SOURCES = ["k_real.cu", "k_kspace.cu", "k_int.cu", "k_wca.cu", "k_obs.cu", "k_render.cu", "api.cu", "gen.cpp",
-           "noalloc.cu"]
+SOURCES = ["k_real.cu", "k_kspace.cu", "k_int.cu", "k_wca.cu", "k_obs.cu", "k_render.cu", "k_init.cu", "api.cu",
+           "gen.cpp", "noalloc.cu"]
+# files that repeat the reference's FP64 arithmetic operation by operation
+NO_FMA = ("k_wca.cu", "k_init.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
            "--expt-relaxed-constexpr", "-I", CSRC, "-I", INCLUDE]
@@ -61,7 +63,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
     def one(src):
         obj = os.path.join(objdir, os.path.splitext(src)[0] + ".o")
         cmd = [cc] + ARCH + flags + ["-c", os.path.join(CSRC, src), "-o", obj]
-        if src == "k_wca.cu":
+        if src in NO_FMA:
             # the exact FP64 pair path keeps the reference's rounding: no FMA contraction
             cmd.insert(1, "-fmad=false")
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -43,6 +43,10 @@ void launch_correlations(const Batch& b, const CorrSys* cs, const unsigned char*
                          int max_bins, unsigned long long* hist, cudaStream_t s);
 void launch_order_sums(const Batch& b, double* out, cudaStream_t s);
 size_t render_scratch_bytes(int n, int nd, int images);
+void launch_lattice_sites(const Batch& b, int sys, double len, double dia, int num1, int num2, int nsites,
+                          int prev_first, int prev_n, double* site_r, int* ok, cudaStream_t s);
+void launch_overlap_count(const Batch& b, int sys, int n, int* count, cudaStream_t s);
+void launch_thermalize(const Batch& b, int sys, int n, double temp, unsigned long long seed, cudaStream_t s);
 void launch_render(const Batch& b, int sys, int n, const unsigned char* species, const int* keep, int images,
                    int dipoles, int draw_box, float seg_rad, float box_rad, const float* eye, const float* fwd,
                    const float* right, const float* up, const float* light, float tan_half, int width,
@@ -1528,6 +1532,89 @@ mdsc_status mdsc_order_params(mdsc_batch* B, double* G1, double* G2, double* M) 
       for (int c = 0; c < 12; ++c) v[c] += part[12 * (size_t)(P.blk_off + k) + c];
     order_params(v, P.n, G1 ? &G1[s] : nullptr, G2 ? &G2[s] : nullptr, M ? &M[3 * s] : nullptr);
   }
+  return MDSC_OK;
+}
+
+// ---- a new configuration ----------------------------------------------------
+mdsc_status mdsc_lattice(mdsc_batch* B, int sys, int nspecies, const int* counts, int* n_overlaps) {
+  mdsc_status st = need_state(B);
+  if (st) return st;
+  if (sys < 0 || sys >= B->nsys || nspecies < 1 || !counts) return MDSC_ERR_BAD_ARG;
+  const SysDev& P = B->lo.sys[sys];
+  long long tot = 0;
+  for (int k = 0; k < nspecies; ++k) {
+    if (counts[k] < 1) return fail(B, MDSC_ERR_BAD_ARG, "mdsc_lattice: every species needs a particle");
+    tot += counts[k];
+  }
+  if (tot != P.n) return fail(B, MDSC_ERR_BAD_ARG, "mdsc_lattice: counts do not add up to n");
+  Batch& b = B->b;
+  std::vector<double> len(P.n), dia(P.n);
+  CU(cudaMemcpyAsync(len.data(), b.len + P.part_off, sizeof(double) * P.n, cudaMemcpyDeviceToHost, B->st));
+  CU(cudaMemcpyAsync(dia.data(), b.dia + P.part_off, sizeof(double) * P.n, cudaMemcpyDeviceToHost, B->st));
+  CU(cudaStreamSynchronize(B->st));
+  const double sq = std::sqrt(3.) / 2., sqtt = std::sqrt(6.) / 3;
+  int first = 0;
+  for (int k = 0; k < nspecies; ++k) {
+    const double L0 = len[first], D0 = dia[first];
+    // sites per row, rows per layer, layers (v25/functions.cpp:507-509)
+    const int num1 = (int)std::max(std::floor(P.L[0] / D0), 1.);
+    const int num2 = (int)std::max(std::floor(P.L[1] / (D0 * sq)), 1.);
+    const int num3 = (int)std::max(std::floor(P.L[2] / (D0 * sqtt + L0)), 1.);
+    const long long ns = (long long)num1 * num2 * num3;
+    if (ns > (1 << 28)) return fail(B, MDSC_ERR_TOO_LARGE, "mdsc_lattice: too many lattice sites");
+    double* d_r = nullptr;
+    int* d_ok = nullptr;
+    CU(cudaMallocAsync((void**)&d_r, sizeof(double) * 3 * ns, B->st));
+    CU(cudaMallocAsync((void**)&d_ok, sizeof(int) * ns, B->st));
+    launch_lattice_sites(b, sys, L0, D0, num1, num2, (int)ns, P.part_off, first, d_r, d_ok, B->st);
+    CU(cudaGetLastError());
+    std::vector<double> hr(3 * ns);
+    std::vector<int> ok(ns);
+    CU(cudaMemcpyAsync(hr.data(), d_r, sizeof(double) * 3 * ns, cudaMemcpyDeviceToHost, B->st));
+    CU(cudaMemcpyAsync(ok.data(), d_ok, sizeof(int) * ns, cudaMemcpyDeviceToHost, B->st));
+    CU(cudaFreeAsync(d_r, B->st));
+    CU(cudaFreeAsync(d_ok, B->st));
+    CU(cudaStreamSynchronize(B->st));
+    std::vector<long long> acc;
+    for (long long q = 0; q < ns; ++q)
+      if (ok[q]) acc.push_back(q);
+    if (acc.empty()) return fail(B, MDSC_ERR_OVERLAP, "mdsc_lattice: no free lattice site for a species");
+    // the accepted sites in order, from the first again when they run out
+    std::vector<double> r(3 * counts[k]), O(9 * counts[k], 0.0);
+    for (int q = 0; q < counts[k]; ++q) {
+      const long long site = acc[q % acc.size()];
+      for (int a = 0; a < 3; ++a) r[3 * q + a] = hr[3 * site + a];
+      O[9 * q + 0] = O[9 * q + 4] = O[9 * q + 8] = 1.0;
+    }
+    CU(cudaMemcpyAsync(b.r + 3 * (P.part_off + first), r.data(), sizeof(double) * r.size(), cudaMemcpyHostToDevice,
+                       B->st));
+    CU(cudaMemcpyAsync(b.O + 9 * (P.part_off + first), O.data(), sizeof(double) * O.size(), cudaMemcpyHostToDevice,
+                       B->st));
+    first += counts[k];
+  }
+  int* d_cnt = nullptr;
+  int cnt = 0;
+  CU(cudaMallocAsync((void**)&d_cnt, sizeof(int), B->st));
+  CU(cudaMemsetAsync(d_cnt, 0, sizeof(int), B->st));
+  launch_overlap_count(b, sys, P.n, d_cnt, B->st);
+  CU(cudaMemcpyAsync(&cnt, d_cnt, sizeof(int), cudaMemcpyDeviceToHost, B->st));
+  CU(cudaFreeAsync(d_cnt, B->st));
+  const int one = 1;
+  CU(cudaMemcpyAsync((char*)(b.st + sys) + offsetof(SysState, force_list), &one, sizeof(int), cudaMemcpyHostToDevice,
+                     B->st));
+  CU(cudaStreamSynchronize(B->st));
+  B->have_forces[sys] = 0;
+  if (n_overlaps) *n_overlaps = cnt;
+  return MDSC_OK;
+}
+
+mdsc_status mdsc_thermalize(mdsc_batch* B, int sys, double temp, unsigned long long seed) {
+  mdsc_status st = need_state(B);
+  if (st) return st;
+  if (sys < 0 || sys >= B->nsys || !(temp >= 0.0)) return MDSC_ERR_BAD_ARG;
+  launch_thermalize(B->b, sys, B->lo.sys[sys].n, temp, seed, B->st);
+  CU(cudaGetLastError());
+  CU(cudaStreamSynchronize(B->st));
   return MDSC_OK;
 }
 

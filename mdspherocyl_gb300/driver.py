@@ -10,11 +10,14 @@ step taken on the GPU by mdsc_step_trace.
   signal 1  restart from conf.dat and the thermostats' generator states
             (ran_state0F.dat, ran_state1F.dat); averages start afresh
   signal 2  the same, continuing counters.dat and correlation.dat
-  signal 0  a new configuration.  The reference builds a lattice and
-            shuffles it with 1000 cluster moves (v25/functions.cpp:491-675,
-            3328-3409); here the rods are placed at random without overlap
-            (mdsc_place_rods) with Maxwell-Boltzmann momenta of zero sum, so
-            a signal-0 run starts from a different (equally valid) state.
+  signal 0  a new configuration: the reference's lattice on the GPU
+            (mdsc_lattice, ini_pos of v25/functions.cpp:491-675, written to
+            iniPos.dat as the reference writes it) with Maxwell-Boltzmann
+            momenta of zero sum (mdsc_thermalize).  The reference then
+            shuffles the lattice with 1000 cluster moves (GCAmix,
+            :3328-3409) and draws its momenta with ini_mom from its run
+            generator; neither is restated, so a signal-0 run starts from
+            the reference's lattice with other momenta.
 
 Per step (v25/main.cpp:520-818): the thermodynamic values of the step
 (energies per particle, pressures, pressure tensors), then past the
@@ -81,21 +84,10 @@ def check_input(p: F.RunInput) -> None:
                 raise RunError(f"dipole {i} of species {n} is ouside the core!")
 
 
-def new_configuration(p: F.RunInput, length, dia, mass, seed: int = 1):
-    """Signal 0: the box from the density and aspect ratios
-    (v25/main.cpp:216-219), rods placed at random without overlap, momenta
-    and angular momenta from the Maxwell-Boltzmann distribution at temp with
-    zero total momentum."""
+def new_box(p: F.RunInput):
+    """Signal 0: the box from the density and aspect ratios (v25/main.cpp:216-219)."""
     Lz = (p.n_total / (p.ArLx * p.ArLy * p.dens)) ** (1.0 / 3)
-    box = np.array([p.ArLx * Lz, p.ArLy * Lz, Lz])
-    r, O = L.place_rods(length, dia, box, seed=seed)
-    rng = np.random.default_rng(seed)
-    I = inertia(length, dia, mass)
-    pm = rng.normal(size=(len(mass), 3)) * np.sqrt(mass * p.temp)[:, None]
-    pm -= pm.mean(axis=0, keepdims=True)
-    lb = rng.normal(size=(len(mass), 3)) * np.sqrt(I * p.temp)
-    l = np.einsum("nab,na->nb", O, lb)
-    return box, r, pm, O, l
+    return np.array([p.ArLx * Lz, p.ArLy * Lz, Lz])
 
 
 class Driver:
@@ -134,7 +126,10 @@ class Driver:
         clust = np.zeros(n, dtype=np.int32)
         hist = None
         if p.signal == 0:
-            box, r, pm, O, l = new_configuration(p, length, dia, mass)
+            # positions and momenta are made on the GPU once the batch exists
+            box = new_box(p)
+            r, pm, l = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros((n, 3))
+            O = np.tile(np.eye(3), (n, 1, 1))
         elif p.signal in (1, 2):
             if p.signal == 2:
                 if not os.path.exists(self.path("counters.dat")):
@@ -193,6 +188,13 @@ class Driver:
               Ntcf, Ntcv, mcont, AcT, AcTsq, length, dia, mass, dip, nd_part) -> int:
         n = p.n_total
         bt.upload(0, st, clust=clust)
+        if p.signal == 0:
+            nov = bt.lattice(0, p.n_part)
+            d0 = bt.download(0)
+            F.write_ini_pos(self.path("iniPos.dat"), d0["r"], box)
+            if nov:
+                self.error("initial conf. overlap")
+            bt.thermalize(0, p.temp, seed=1)
         bt.set_thermostat(0, xi, strn)
         for k in range(2):
             if rng_state[k] is not None:

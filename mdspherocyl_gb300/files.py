@@ -16,6 +16,7 @@ restart point:
   ptens.dat, magmom.dat  print_ptens / print_magmom v25/functions.cpp:2645-2700
   pos_vel/pos_vel_N.dat  pos_vel    v25/functions.cpp:2602-2643
   compConf.dat       savec_list     v25/functions.cpp:1336-1354
+  iniPos.dat         ini_pos        v25/functions.cpp:584-597
 """
 from __future__ import annotations
 
@@ -287,6 +288,18 @@ def read_conf(path: str, n_part, nd_part):
     xi = np.array([float(toks[k]), float(toks[k + 2])])
     strn = np.array([float(toks[k + 1]), float(toks[k + 3])])
     return dict(box=box, r=r, p=p, O=O, l=l, mass=mass, clust=clust, xi=xi, strn=strn)
+
+
+def write_ini_pos(path: str, r, box) -> None:
+    """iniPos.dat as ini_pos writes it (v25/functions.cpp:584-597): per rod
+    its position, zero momentum, the identity orientation and zero angular
+    momentum with a trailing 1, then the box -- iostream's default format."""
+    out = []
+    for v in np.asarray(r, dtype=np.float64).reshape(-1, 3):
+        out.append(f"{g6(v[0])} {g6(v[1])} {g6(v[2])} 0 0 0 1 0 0 0 1 0 0 0 1  0 0 0 1\n")
+    out.append(f"{g6(box[0])} {g6(box[1])} {g6(box[2])}\n")
+    with open(path, "w") as f:
+        f.write("".join(out))
 
 
 def write_comp_conf(path: str, r) -> None:

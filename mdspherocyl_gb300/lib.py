@@ -38,7 +38,7 @@ EXPORTS = [
     "mdsc_place_rods", "mdsc_last_device_ms", "mdsc_force_dipR_noalloc", "mdsc_transfer",
     "mdsc_autotune", "mdsc_tuning", "mdsc_set_tuning", "mdsc_correlation_bins", "mdsc_correlations",
     "mdsc_order_params", "mdsc_step_trace", "mdsc_get_rng", "mdsc_set_rng", "mdsc_set_species",
-    "mdsc_correlation_size", "mdsc_get_thermostat", "mdsc_render",
+    "mdsc_correlation_size", "mdsc_get_thermostat", "mdsc_render", "mdsc_lattice", "mdsc_thermalize",
 ]
 
 
@@ -172,6 +172,8 @@ def load(build: bool = True) -> ctypes.CDLL:
         "mdsc_set_species": (c_int, [c_void_p, c_int, c_int, _ip]),
         "mdsc_get_thermostat": (c_int, [c_void_p, c_int, _dp, _dp]),
         "mdsc_render": (c_int, [c_void_p, c_int, P(View), c_void_p]),
+        "mdsc_lattice": (c_int, [c_void_p, c_int, c_int, _ip, _ip]),
+        "mdsc_thermalize": (c_int, [c_void_p, c_int, c_double, ctypes.c_ulonglong]),
         "mdsc_correlation_size": (c_int, [c_void_p, c_int, c_double]),
         "mdsc_order_params": (c_int, [c_void_p, _dp, _dp, _dp]),
         "mdsc_step_trace": (c_int, [c_void_p, c_int, P(Observables)]),
@@ -412,6 +414,18 @@ class Batch:
         G1, G2, M = np.zeros(self.nsys), np.zeros(self.nsys), np.zeros((self.nsys, 3))
         self._check(self.lib.mdsc_order_params(self.h, _ptr(G1), _ptr(G2), _ptr(M)), "mdsc_order_params")
         return G1, G2, M
+
+    def lattice(self, k: int, counts) -> int:
+        """The reference's lattice for system k (mdsc_lattice); returns the
+        overlapping pairs its closing test finds."""
+        c = np.ascontiguousarray(counts, dtype=np.int32)
+        nov = c_int(0)
+        self._check(self.lib.mdsc_lattice(self.h, k, len(c), c.ctypes.data_as(_ip), ctypes.byref(nov)),
+                    "mdsc_lattice")
+        return nov.value
+
+    def thermalize(self, k: int, temp: float, seed: int = 1) -> None:
+        self._check(self.lib.mdsc_thermalize(self.h, k, float(temp), int(seed)), "mdsc_thermalize")
 
     def render(self, k: int, view: "View | None" = None, **kw):
         """A picture of system k (mdsc_render): (height, width, 3) uint8."""

@@ -135,7 +135,8 @@ def driver_trajectory():
                 fin_clust=fin["clust"], fin_xi=fin["xi"])
 
 
-RUN_FILES = ("input.txt", "conf.dat", "ran_state0F.dat", "ran_state1F.dat", "counters.dat", "correlation.dat",
+RUN_FILES = ("input.txt", "iniPos.dat", "conf.dat", "ran_state0F.dat", "ran_state1F.dat", "counters.dat",
+             "correlation.dat",
              "ptens.dat", "magmom.dat", "output.dat", os.path.join("pos_vel", "pos_vel_0.dat"),
              os.path.join("pos_vel", "pos_vel_1.dat"))
 
@@ -179,7 +180,7 @@ def run_files():
             dst = os.path.join(HERE, "run_v25", name)
             os.makedirs(os.path.join(dst, "pos_vel"), exist_ok=True)
             for f in RUN_FILES:
-                if os.path.exists(os.path.join(d, f)):
+                if os.path.exists(os.path.join(d, f)) and (f != "iniPos.dat" or sig == 0):
                     shutil.copy(os.path.join(d, f), os.path.join(dst, f))
             shutil.rmtree(os.path.join(d, "pos_vel"), ignore_errors=True)
             print("wrote", dst)

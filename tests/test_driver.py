@@ -115,3 +115,39 @@ def test_new_run_writes_every_file():
                   "ptens.dat", "magmom.dat", "output.dat", os.path.join("pos_vel", "pos_vel_0.dat")):
             assert os.path.getsize(os.path.join(d, f)) > 0, f
         assert open(os.path.join(d, "Error.dat")).read() == ""
+
+
+def test_new_run_lattice_is_the_references():
+    """Signal 0: the lattice on the GPU is ini_pos's -- iniPos.dat byte for
+    byte what the reference wrote for its own example (two species on one
+    lattice: the second species takes the sites the first left free)."""
+    with tempfile.TemporaryDirectory() as d:
+        shutil.copy(os.path.join(RUN, "init", "input.txt"), d)
+        with open(os.devnull, "w") as devnull:
+            assert Driver(d, out=devnull).run() == 0, open(os.path.join(d, "Error.dat")).read()
+        assert open(os.path.join(d, "iniPos.dat")).read() == open(os.path.join(RUN, "init", "iniPos.dat")).read()
+
+
+def test_thermalize_momenta():
+    """mdsc_thermalize: zero total momentum, the equipartition temperature
+    within the sampling error, the same draws for the same seed."""
+    from mdspherocyl_gb300 import lib as L
+    from mdspherocyl_gb300 import systems as S
+
+    rng = np.random.default_rng(3)
+    st, box = S.make_system(n=3000, phi=0.1, lengths=rng.uniform(1, 3, 3000), mu=np.ones(3000), seed=3,
+                            mass=rng.uniform(0.5, 2.0, 3000))
+    spec = S.SystemSpec(n=3000, box=box, alpha=5.0 / box[0], K_max=4, ksq_max=0)
+    with L.Batch([spec], [st]) as bt:
+        bt.thermalize(0, 1.7, seed=11)
+        a = bt.download(0)
+        bt.thermalize(0, 1.7, seed=11)
+        b = bt.download(0)
+    assert np.array_equal(a["p"], b["p"]) and np.array_equal(a["l"], b["l"])
+    assert np.abs(a["p"].sum(axis=0)).max() < 1e-10
+    Kt = 0.5 * np.sum(a["p"] ** 2 / st.mass[:, None])
+    assert abs(2 * Kt / (3 * 3000) - 1.7) < 0.05 * 1.7
+    I = S.inertia(st.length, st.dia, st.mass)
+    lb = np.einsum("nab,nb->na", st.O, a["l"])  # body frame
+    Kr = 0.5 * np.sum(lb ** 2 / I)
+    assert abs(2 * Kr / (3 * 3000) - 1.7) < 0.05 * 1.7
