@@ -407,6 +407,8 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   b.wcaE = A.take<double>(11 * nb);
   b.wcand = A.take<int>(n * kMaxC);
   b.wcnt = A.take<int>(n);
+  b.win = A.take<int>(n * kMaxC);
+  b.wincnt = A.take<int>(n);
   b.wrec = A.take<double>(n * kMaxC * 6);
   b.kn = A.take<int4>(nk);
   b.kv = A.take<float4>(nk);
@@ -1012,6 +1014,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   cudaMemsetAsync(b.usave, 0, sizeof(float) * 3 * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.nbc, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.wcnt, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
+  cudaMemsetAsync(b.wincnt, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.kgcnt, 0, sizeof(int) * std::max(nsys, 1), B->st);
   cudaMemsetAsync(b.icnt, 0, sizeof(int) * std::max(nsys, 1), B->st);
   cudaMemsetAsync(b.F, 0, sizeof(double) * 3 * std::max(lo.ntot, 1), B->st);

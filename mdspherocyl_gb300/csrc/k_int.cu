@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(kPartBlock) integrate_first_kernel(Batch b) {
 // ---------------------------------------------------------------------
 // force assembly (+ ext_field) and optionally moveP(last)
 // ---------------------------------------------------------------------
-__global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode) {
+__global__ void __launch_bounds__(kPartBlock, 6) finalize_kernel(Batch b, int mode) {
   __shared__ double sh[20 * kPartBlock / 32];
   const int2 bk = b.blk[blockIdx.x];
   const int s = bk.x;
@@ -319,22 +319,26 @@ __global__ void __launch_bounds__(kPartBlock) finalize_kernel(Batch b, int mode)
         }
       }
       // shares of the pairs this particle forms with lower-index partners,
-      // left by the WCA kernel in the partner's records (ascending partner)
-      const int nl = b.nbc[i];
-      const int* lst = b.nb + (long long)i * kMaxNb;
-      for (int k = 0; k < nl; ++k) {
-        const int q = lst[k];
-        if (q >= i) break;
-        const int nc = b.wcnt[q];
-        const int* cq = b.wcand + (long long)q * kMaxC;
-        for (int c = 0; c < nc; ++c) {
-          if (cq[c] != i) continue;
-          const double* rec = b.wrec + ((long long)q * kMaxC + c) * 6;
+      // left by the WCA kernel in the partner's records.  The screen listed
+      // their slots here in arrival order; sorted, the slots ascend with the
+      // partner (slot = partner * kMaxC + c), the order force_sc adds them.
+      const int nin = min(b.wincnt[i], kMaxC);
+      int sl[kMaxC];
+      for (int k = 0; k < nin; ++k) {
+        const int v = b.win[(long long)i * kMaxC + k];
+        int m = k;
+        while (m > 0 && sl[m - 1] > v) {
+          sl[m] = sl[m - 1];
+          --m;
+        }
+        sl[m] = v;
+      }
+      for (int k = 0; k < nin; ++k) {
+        const double* rec = b.wrec + (long long)sl[k] * 6;
 #pragma unroll
-          for (int a = 0; a < 3; ++a) {
-            F[a] += rec[a];
-            T[a] += rec[3 + a];
-          }
+        for (int a = 0; a < 3; ++a) {
+          F[a] += rec[a];
+          T[a] += rec[3 + a];
         }
       }
     }

@@ -240,7 +240,15 @@ __global__ void __launch_bounds__(kPartBlock) wca_screen_kernel(Batch b) {
       const float d2 = seg_dist_fast(dx, dy, dz, ai.x, ai.y, ai.z, ai.w, aj.x, aj.y, aj.z, aj.w);
       // 2^(1/3) sigma^2, with a margin for the FP32 screen
       if (d2 >= 1.2599211f * sg * sg * 1.002f) continue;
-      if (nc < kMaxC) b.wcand[(long long)i * kMaxC + nc] = q;
+      if (nc < kMaxC) {
+        b.wcand[(long long)i * kMaxC + nc] = q;
+        // the partner learns where its share of this pair will be
+        const int k = atomicAdd(&b.wincnt[q], 1);
+        if (k < kMaxC)
+          b.win[(long long)q * kMaxC + k] = i * kMaxC + nc;
+        else
+          err |= kErrListOverflow;
+      }
       ++nc;
     }
     if (nc > kMaxC) {
@@ -379,6 +387,7 @@ void launch_list_build(const Batch& b, int force_all, cudaStream_t s) {
 void launch_wca(const Batch& b, cudaStream_t s) {
   if (!b.nblk) return;
   cudaMemsetAsync(b.wlist_n, 0, sizeof(int), s);
+  cudaMemsetAsync(b.wincnt, 0, sizeof(int) * b.ntot, s);
   wca_screen_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
   // a fixed grid (chosen by the autotuner); each thread loops over the list
   wca_eval_kernel<<<b.tune.wca_blocks, 128, 0, s>>>(b);

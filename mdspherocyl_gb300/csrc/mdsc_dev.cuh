@@ -161,6 +161,8 @@ struct Batch {
   double* wcaE;  // per particle block: U, W, PT (11) of its own candidates
   int* wcand;    // n * kMaxC contact candidates (higher index) of each particle
   int* wcnt;     // n
+  int* win;      // n * kMaxC: the candidate slots in which a lower-index particle holds this one
+  int* wincnt;   // n: their number (zeroed before each screen)
   double* wrec;  // n * kMaxC * 6: the partner's force and torque of each candidate
   // k-space
   int4* kn;      // (nx, ny, nz, 0) per k
