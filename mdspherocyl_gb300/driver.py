@@ -188,10 +188,12 @@ class Driver:
               Ntcf, Ntcv, mcont, AcT, AcTsq, length, dia, mass, dip, nd_part) -> int:
         n = p.n_total
         bt.upload(0, st, clust=clust)
+        r_start = st.r
         if p.signal == 0:
             nov = bt.lattice(0, p.n_part)
             d0 = bt.download(0)
             F.write_ini_pos(self.path("iniPos.dat"), d0["r"], box)
+            r_start = d0["r"]
             if nov:
                 self.error("initial conf. overlap")
             bt.thermalize(0, p.temp, seed=1)
@@ -203,7 +205,7 @@ class Driver:
             bt.set_species(0, p.n_part)
         if p.signal == 0:
             self._print_conf(bt, box, dip)
-        F.write_comp_conf(self.path("compConf.dat"), st.r)
+        F.write_comp_conf(self.path("compConf.dat"), r_start)
         # the initial forces: force_sc's overlap check before the loop
         try:
             obs0 = bt.observe()[0]
