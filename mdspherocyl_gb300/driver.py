@@ -1,6 +1,6 @@
 """mdSpherocyl's run loop (v25/main.cpp) on the GB300 library.
 
-    python -m mdspherocyl_gb300.driver [workdir] [--device N]
+    python -m mdspherocyl_gb300.driver [workdir] [--device N] [--variant v25|v251]
 
 Reads input.txt in workdir and runs it as the reference's executable does:
 the same restart modes, the same per-step bookkeeping and the same files,
@@ -28,6 +28,12 @@ generator states, counters.dat, correlation.dat and a line of output.dat;
 at the end the averages block of output.dat and time.dat.  The reference's
 neighbour-list bookkeeping file compConf.dat is written once, at the start:
 this library keeps its own list state on the GPU.
+
+--variant v251 runs the reference's later driver (v25/v251/main.cpp): the
+thermostats start at xi = 1 (v25/v251/classes.hpp:154), each clustering adds
+to the degree-of-polymerisation counters (clusterings; particles in clusters
+of two or more, v25/v251/functions.cpp:3249-3256), which counters.dat
+carries and the closing report divides.
 """
 from __future__ import annotations
 
@@ -91,10 +97,13 @@ def new_box(p: F.RunInput):
 
 
 class Driver:
-    def __init__(self, workdir: str = ".", device: int = 0, out=sys.stdout):
+    def __init__(self, workdir: str = ".", device: int = 0, out=sys.stdout, variant: str = "v25"):
+        if variant not in ("v25", "v251"):
+            raise ValueError(f"unknown driver variant {variant}")
         self.d = workdir
         self.device = device
         self.out = out
+        self.v251 = variant == "v251"
 
     def path(self, name: str) -> str:
         return os.path.join(self.d, name)
@@ -121,7 +130,9 @@ class Driver:
         Time, cont, Ntcf, Ntcv, mcont = 0.0, 0, 0, 0, 0
         AcT, AcTsq = F.Accumulator(), F.Accumulator()
         cor_cont = 0.0
-        xi, strn = np.zeros(2), np.zeros(2)
+        # the thermostats' starting xi: 0 in v25, 1 in v251 (Thermostat())
+        xi, strn = (np.ones(2) if self.v251 else np.zeros(2)), np.zeros(2)
+        self._npc = [0, 0]
         rng_state = [None, None]
         clust = np.zeros(n, dtype=np.int32)
         hist = None
@@ -134,7 +145,10 @@ class Driver:
             if p.signal == 2:
                 if not os.path.exists(self.path("counters.dat")):
                     raise RunError("problem opening counters.dat for reading")
-                Time, cont, Ntcf, Ntcv, mcont, AcT, AcTsq = F.read_counters(self.path("counters.dat"))
+                got = F.read_counters(self.path("counters.dat"), npc=self.v251)
+                Time, cont, Ntcf, Ntcv, mcont, AcT, AcTsq = got[:7]
+                if self.v251:
+                    self._npc = list(got[7])
             if not os.path.exists(self.path("conf.dat")):
                 raise RunError("problem opening conf.dat for reading")
             c = F.read_conf(self.path("conf.dat"), p.n_part, nd_part)
@@ -246,6 +260,12 @@ class Driver:
                 print(F.g6(Time), file=self.out)
                 self._set_var(var, o, n, V, p.dens, Uself)
                 Time += p.Dt
+                if self.v251 and p.cl_fr > 0 and math.fmod(float(s), p.cl_fr) == 0:
+                    # this step clustered (the last of its chunk): the degree of polymerisation
+                    lab = bt.download(0)["clust"]
+                    sizes = np.bincount(lab[lab >= 0])
+                    self._npc[0] += 1
+                    self._npc[1] += int(sizes[sizes > 1].sum())
                 if s >= p.pre_steps:
                     if p.corrf > 0 and math.fmod(float(np.float32(s)), p.corrf) == 0:
                         hist = bt.correlations(p.bar_w, [hist])[0]
@@ -269,7 +289,8 @@ class Driver:
                     cont += 1
                 if math.fmod(float(s), p.iprint) == 0:
                     d = self._print_conf(bt, box, dip)
-                    F.write_counters(self.path("counters.dat"), Time, cont, Ntcf, Ntcv, mcont, AcT, AcTsq)
+                    F.write_counters(self.path("counters.dat"), Time, cont, Ntcf, Ntcv, mcont, AcT, AcTsq,
+                                     npc=self._npc if self.v251 else None)
                     if s >= p.pre_steps and p.corrf > 0 and math.fmod(float(np.float32(s)), p.corrf) == 0:
                         F.write_correlation(self.path("correlation.dat"), hist, p.n_part, Lmin, p.bar_w, cor_cont)
                     # total momentum and angular momentum (v25/main.cpp:788-800)
@@ -284,12 +305,18 @@ class Driver:
         with open(self.path("time.dat"), "w") as f:
             f.write(f"GB300 step time. elap: {F.g6((time.perf_counter() - t_start) / max(total, 1))}\n")
         if cont > 0:
-            F.append(self.path("output.dat"), F.final_report(Time, AcT, AcTsq, cont, p, box))
+            pol = None
+            if self.v251:
+                num, den = float(self._npc[1]), float(n * self._npc[0])
+                pol = num / den if den != 0 else (float("nan") if num == 0 else float("inf"))
+            F.append(self.path("output.dat"), F.final_report(Time, AcT, AcTsq, cont, p, box, pol_deg=pol))
         return 0
 
     def _event(self, p, s: int) -> bool:
         """A step after which the loop needs more than the step's observables."""
         if math.fmod(float(s), p.iprint) == 0:
+            return True
+        if self.v251 and p.cl_fr > 0 and math.fmod(float(s), p.cl_fr) == 0:
             return True
         if s >= p.pre_steps:
             for fr in (p.corrf, p.tcfd, p.tcfv):
@@ -348,8 +375,9 @@ def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("workdir", nargs="?", default=".")
     ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--variant", choices=("v25", "v251"), default="v25")
     a = ap.parse_args(argv)
-    return Driver(a.workdir, a.device).run()
+    return Driver(a.workdir, a.device, variant=a.variant).run()
 
 
 if __name__ == "__main__":

@@ -383,10 +383,12 @@ class Accumulator:
 
 
 def write_counters(path: str, Time: float, cont: int, Ntcf: int, Ntcv: int, mcont: int, AcT: Accumulator,
-                   AcTsq: Accumulator) -> None:
+                   AcTsq: Accumulator, npc=None) -> None:
     """counters.dat (save_cont): the run's clock and counters, then each
     accumulated value next to its accumulated square, the tensors row by
-    row, all fixed to 12 decimals."""
+    row, all fixed to 12 decimals.  npc: the later driver's two
+    polymerisation counters (clusterings, particles in clusters of two or
+    more; v25/v251/functions.cpp:2294), written last."""
     v = [f12(Time), str(int(cont)), str(int(Ntcf)), str(int(Ntcv)), str(int(mcont))]
     for k in SCALARS:
         v += [f12(getattr(AcT, k)), f12(getattr(AcTsq, k))]
@@ -394,13 +396,20 @@ def write_counters(path: str, Time: float, cont: int, Ntcf: int, Ntcv: int, mcon
         v += [f12(x) for x in getattr(AcT, k).ravel()]
         v += [f12(x) for x in getattr(AcTsq, k).ravel()]
     v += [f12(AcT.G1), f12(AcTsq.G1), f12(AcT.G2), f12(AcTsq.G2)]
+    if npc is not None:
+        v += [str(int(npc[0])), str(int(npc[1]))]
     with open(path, "w") as f:
         f.write(" ".join(v) + " \n")
 
 
-def read_counters(path: str):
-    """counters.dat (chrg_cont): (Time, cont, Ntcf, Ntcv, mcont, AcT, AcTsq)."""
+def read_counters(path: str, npc: bool = False):
+    """counters.dat (chrg_cont): (Time, cont, Ntcf, Ntcv, mcont, AcT, AcTsq),
+    and the two polymerisation counters last when npc (the later driver)."""
     t = open(path).read().split()
+    extra = None
+    if npc:
+        extra = [int(t[-2]), int(t[-1])]
+        t = t[:-2]
     Time, cont, Ntcf, Ntcv, mcont = float(t[0]), int(t[1]), int(t[2]), int(t[3]), int(t[4])
     vals = [float(x) for x in t[5:]]
     AcT, AcTsq = Accumulator(), Accumulator()
@@ -414,6 +423,8 @@ def read_counters(path: str):
         setattr(AcTsq, name, np.array(vals[k + 9:k + 18]).reshape(3, 3))
         k += 18
     AcT.G1, AcTsq.G1, AcT.G2, AcTsq.G2 = vals[k:k + 4]
+    if npc:
+        return Time, cont, Ntcf, Ntcv, mcont, AcT, AcTsq, extra
     return Time, cont, Ntcf, Ntcv, mcont, AcT, AcTsq
 
 
@@ -512,10 +523,11 @@ def read_correlation(path: str, counts, nbins: int):
     return cor_cont, hist
 
 
-def final_report(Time, AcT: Accumulator, AcTsq: Accumulator, cont: int, p: RunInput, box) -> str:
+def final_report(Time, AcT: Accumulator, AcTsq: Accumulator, cont: int, p: RunInput, box, pol_deg=None) -> str:
     """The closing block print_final appends to output.dat: run parameters,
     then each average with its fluctuation sqrt(<x^2> - <x>^2), in
-    iostream's default format."""
+    iostream's default format; the later driver adds the degree of
+    polymerisation (v25/v251/functions.cpp:2876)."""
     def av(x, xsq):
         a = x / cont
         return a, math.sqrt(xsq / cont - a * a) if xsq / cont - a * a >= 0 else float("nan")
@@ -566,6 +578,8 @@ def final_report(Time, AcT: Accumulator, AcTsq: Accumulator, cont: int, p: RunIn
     o.append(f"{g6(g1)} +/- {g6(fg1)}\n")
     o.append("Average G2(S) mayer-saupe parameter:\n")
     o.append(f"{g6(g2)} +/- {g6(fg2)}\n")
+    if pol_deg is not None:
+        o.append(f"Polymerization degree: {g6(pol_deg)}\n")
     return "".join(o)
 
 

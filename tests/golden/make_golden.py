@@ -8,8 +8,8 @@ path can be checked against the reference where its sources are absent.
 
   python tests/golden/make_golden.py
 
-run_v25/ holds the files the reference's driver writes on its own example
-input, for the file-format and driver tests.
+run_v25/ and run_v251/ hold the files the reference's two drivers write on
+their own example inputs, for the file-format and driver tests.
 """
 from __future__ import annotations
 
@@ -152,21 +152,15 @@ def _edit_input(text, **kv):
     return "\n".join(out) + "\n"
 
 
-def run_files():
-    """The reference driver's run files on its own example input
-    (v25/input.txt: two species of 50 rods, two off-axis dipoles each),
-    shortened: a new run of 2 steps with every output every step (init/),
-    then a restart (signal 1) of 3 steps from its files (restart/) and a
-    continuation (signal 2) of 2 steps (continue/)."""
+def _run_stages(src, common, binary, outdir):
+    """init (signal 0, 2 steps), restart (signal 1, 3 steps) and continue
+    (signal 2, 2 steps) of one input in one directory, each stage's files
+    copied to outdir/<stage>."""
     import shutil
     import subprocess
     import tempfile
 
-    src = open(os.path.join(os.environ.get("MDSC_REFERENCE", "/root/reference"), "v25", "input.txt")).read()
-    common = {"Histogram bar width=": "Histogram bar width=\t0.1", "corr. sum freq.=": "corr. sum freq.=\t1",
-              "DiffCorr. frequency=": "DiffCorr. frequency=    1", "ViscCorr. frequency=": "ViscCorr. frequency=    1",
-              "Steps before average=": "Steps before average=\t0", "clustering frequency=": "clustering frequency=\t2"}
-    drv = os.path.join(oracle.REF_DIR, "DSCmd_v25")
+    drv = os.path.join(oracle.REF_DIR, binary)
     stages = (("init", 0, 2), ("restart", 1, 3), ("continue", 2, 2))
     with tempfile.TemporaryDirectory() as d:
         for name, sig, steps in stages:
@@ -176,14 +170,42 @@ def run_files():
             if os.path.exists(os.path.join(d, "output.dat")):
                 os.remove(os.path.join(d, "output.dat"))
             subprocess.run([drv], cwd=d, env=dict(os.environ, OMP_NUM_THREADS="1"), stdout=subprocess.DEVNULL,
-                           timeout=600, check=True)
-            dst = os.path.join(HERE, "run_v25", name)
+                           timeout=1200, check=True)
+            dst = os.path.join(HERE, outdir, name)
             os.makedirs(os.path.join(dst, "pos_vel"), exist_ok=True)
             for f in RUN_FILES:
                 if os.path.exists(os.path.join(d, f)) and (f != "iniPos.dat" or sig == 0):
                     shutil.copy(os.path.join(d, f), os.path.join(dst, f))
             shutil.rmtree(os.path.join(d, "pos_vel"), ignore_errors=True)
             print("wrote", dst)
+
+
+def run_files():
+    """The reference driver's run files on its own example input
+    (v25/input.txt: two species of 50 rods, two off-axis dipoles each),
+    shortened: a new run of 2 steps with every output every step (init/),
+    then a restart (signal 1) of 3 steps from its files (restart/) and a
+    continuation (signal 2) of 2 steps (continue/)."""
+    ref = os.environ.get("MDSC_REFERENCE", "/root/reference")
+    src = open(os.path.join(ref, "v25", "input.txt")).read()
+    common = {"Histogram bar width=": "Histogram bar width=\t0.1", "corr. sum freq.=": "corr. sum freq.=\t1",
+              "DiffCorr. frequency=": "DiffCorr. frequency=    1", "ViscCorr. frequency=": "ViscCorr. frequency=    1",
+              "Steps before average=": "Steps before average=\t0", "clustering frequency=": "clustering frequency=\t2"}
+    _run_stages(src, common, "DSCmd_v25", "run_v25")
+
+
+def run_files_v251():
+    """The same three stages with the later driver (v25/v251) on its own
+    example (v25/v251/run1/input.txt: rods of length 9 with an axial dipole
+    in a field), at 200 rods and the same density, clustering every step."""
+    ref = os.environ.get("MDSC_REFERENCE", "/root/reference")
+    src = open(os.path.join(ref, "v25", "v251", "run1", "input.txt")).read()
+    common = {"Histogram bar width=": "Histogram bar width=\t0.5", "corr. sum freq.=": "corr. sum freq.=\t1",
+              "DiffCorr. frequency=": "DiffCorr. frequency=    1", "ViscCorr. frequency=": "ViscCorr. frequency=    1",
+              "Steps before average=": "Steps before average=\t0", "clustering frequency=": "clustering frequency=\t1",
+              "Printing frequency=": "Printing frequency=\t1", "No. of Particles=": "No. of Particles=\t200",
+              "proximity dist.=": "proximity dist.=\t1.5"}
+    _run_stages(src, common, "DSCmd_v251", "run_v251")
 
 
 def main():
@@ -199,6 +221,7 @@ def main():
     np.savez_compressed(path, **driver_trajectory())
     print("wrote", path, os.path.getsize(path), "bytes")
     run_files()
+    run_files_v251()
 
 
 if __name__ == "__main__":

@@ -22,7 +22,8 @@ from mdspherocyl_gb300.driver import Driver, layout
 
 pytestmark = pytest.mark.gpu
 
-RUN = os.path.join(ROOT, "tests", "golden", "run_v25")
+GOLD = os.path.join(ROOT, "tests", "golden")
+RUN = os.path.join(GOLD, "run_v25")
 
 
 def _cmp_numbers(a, b, rel, abs_, what):
@@ -37,9 +38,9 @@ def _cmp_numbers(a, b, rel, abs_, what):
         assert abs(fx - fy) <= rel * abs(fy) + abs_, (what, x, y)
 
 
-def _check_stage(d, stage):
+def _check_stage(d, stage, run=RUN):
     p = F.read_input(os.path.join(d, "input.txt"))
-    ref = os.path.join(RUN, stage)
+    ref = os.path.join(run, stage)
     # output.dat: one line per step (times of the run itself aside), then the report
     ours = open(os.path.join(d, "output.dat")).read().splitlines()
     theirs = open(os.path.join(ref, "output.dat")).read().splitlines()
@@ -90,19 +91,24 @@ def _check_stage(d, stage):
             _cmp_numbers(x, y, 1e-5, 2e-8, f)
 
 
-def test_restart_and_continue_like_the_reference():
+@pytest.mark.parametrize("variant", ["v25", "v251"])
+def test_restart_and_continue_like_the_reference(variant):
+    """v25: two species, off-axis dipoles; v251 (the later driver): rods of
+    length 9 with an axial dipole in a field, clustering every step, the
+    degree-of-polymerisation counters."""
+    run = os.path.join(GOLD, f"run_{variant}")
     with tempfile.TemporaryDirectory() as d:
         for f in ("conf.dat", "ran_state0F.dat", "ran_state1F.dat", "counters.dat", "correlation.dat"):
-            shutil.copy(os.path.join(RUN, "init", f), d)
-        shutil.copy(os.path.join(RUN, "restart", "input.txt"), d)
+            shutil.copy(os.path.join(run, "init", f), d)
+        shutil.copy(os.path.join(run, "restart", "input.txt"), d)
         with open(os.devnull, "w") as devnull:
-            assert Driver(d, out=devnull).run() == 0, open(os.path.join(d, "Error.dat")).read()
-        _check_stage(d, "restart")
-        shutil.copy(os.path.join(RUN, "continue", "input.txt"), d)
+            assert Driver(d, out=devnull, variant=variant).run() == 0, open(os.path.join(d, "Error.dat")).read()
+        _check_stage(d, "restart", run)
+        shutil.copy(os.path.join(run, "continue", "input.txt"), d)
         os.remove(os.path.join(d, "output.dat"))
         with open(os.devnull, "w") as devnull:
-            assert Driver(d, out=devnull).run() == 0, open(os.path.join(d, "Error.dat")).read()
-        _check_stage(d, "continue")
+            assert Driver(d, out=devnull, variant=variant).run() == 0, open(os.path.join(d, "Error.dat")).read()
+        _check_stage(d, "continue", run)
 
 
 def test_new_run_writes_every_file():

@@ -12,8 +12,18 @@ from conftest import ROOT
 from mdspherocyl_gb300 import files as F
 from mdspherocyl_gb300.driver import layout
 
-RUN = os.path.join(ROOT, "tests", "golden", "run_v25")
-STAGES = ("init", "restart", "continue")
+GOLD = os.path.join(ROOT, "tests", "golden")
+RUN = os.path.join(GOLD, "run_v25")
+# both drivers' runs: v25 (two species, off-axis dipoles) and v251 (one species, field, clusters every step)
+STAGES = tuple(f"{r}/{s}" for r in ("run_v25", "run_v251") for s in ("init", "restart", "continue"))
+
+
+def _v251(stage):
+    return stage.startswith("run_v251")
+
+
+def _init(stage):
+    return os.path.join(GOLD, stage.split("/")[0], "init")
 
 
 def _nums(tokens):
@@ -49,11 +59,11 @@ def test_conf_round_trip(stage):
     """conf.dat read and written again: every token equal, except the lab
     dipole coordinates, which follow from r and O as printed (12 decimals)
     and so may differ by one unit in the last place."""
-    p = F.read_input(os.path.join(RUN, stage, "input.txt"))
+    p = F.read_input(os.path.join(GOLD, stage, "input.txt"))
     length, dia, mass, dip, nd, nd_part = layout(p)
-    src = os.path.join(RUN, stage, "conf.dat")
+    src = os.path.join(GOLD, stage, "conf.dat")
     c = F.read_conf(src, p.n_part, nd_part)
-    assert c["r"].shape == (100, 3) and np.all(c["mass"] == 1.0)
+    assert c["r"].shape == (p.n_total, 3) and np.all(c["mass"] == 1.0)
     with tempfile.TemporaryDirectory() as d:
         out = os.path.join(d, "conf.dat")
         F.write_conf(out, c["box"], c["r"], c["p"], c["O"], c["l"], mass, dip, c["clust"], c["xi"], c["strn"])
@@ -75,7 +85,7 @@ def test_conf_round_trip(stage):
 def test_generator_state_and_counters_round_trip(stage):
     with tempfile.TemporaryDirectory() as d:
         for k in range(2):
-            src = os.path.join(RUN, stage, f"ran_state{k}F.dat")
+            src = os.path.join(GOLD, stage, f"ran_state{k}F.dat")
             mt, mti = F.read_mt_state(src)
             assert mt.shape == (624,) and 0 <= mti <= 624
             F.write_mt_state(os.path.join(d, "s.dat"), mt, mti)
@@ -83,8 +93,9 @@ def test_generator_state_and_counters_round_trip(stage):
             # reference's memory held; everything before them is equal
             a, w = open(src, "rb").read(), open(os.path.join(d, "s.dat"), "rb").read()
             assert len(a) == len(w) == 5000 and a[:4996] == w[:4996]
-        src = os.path.join(RUN, stage, "counters.dat")
-        F.write_counters(os.path.join(d, "c.dat"), *F.read_counters(src))
+        src = os.path.join(GOLD, stage, "counters.dat")
+        got = F.read_counters(src, npc=_v251(stage))
+        F.write_counters(os.path.join(d, "c.dat"), *got[:7], npc=got[7] if _v251(stage) else None)
         assert open(src).read() == open(os.path.join(d, "c.dat")).read()
 
 
@@ -110,8 +121,8 @@ def test_output_lines_and_report(stage):
     """output.dat: every step line printed again from its own values is the
     same line; the closing report rebuilt from counters.dat has the same
     text and, within the rounding counters.dat imposes, the same averages."""
-    p = F.read_input(os.path.join(RUN, stage, "input.txt"))
-    lines = open(os.path.join(RUN, stage, "output.dat")).read().splitlines()
+    p = F.read_input(os.path.join(GOLD, stage, "input.txt"))
+    lines = open(os.path.join(GOLD, stage, "output.dat")).read().splitlines()
     steps = [ln for ln in lines if " | " in ln and ln[:1].isdigit() and ln.split()[0].endswith(".")]
     assert len(steps) == p.Nsteps
     for ln in steps:
@@ -125,13 +136,15 @@ def test_output_lines_and_report(stage):
         ta, tb = ln.split(), again.split()
         assert ta[:-2] == tb[:-2]  # the momentum squares pass through a square root here
         assert abs(float(ta[-1]) - float(tb[-1])) <= 1e-12 and abs(float(ta[-2]) - float(tb[-2])) <= 1e-12
-    Time, cont, Ntcf, Ntcv, mcont, AcT, AcTsq = F.read_counters(os.path.join(RUN, stage, "counters.dat"))
+    got = F.read_counters(os.path.join(GOLD, stage, "counters.dat"), npc=_v251(stage))
+    Time, cont, Ntcf, Ntcv, mcont, AcT, AcTsq = got[:7]
+    pol = got[7][1] / (p.n_total * got[7][0]) if _v251(stage) else None
     if p.signal == 0:
         Lz = (p.n_total / (p.ArLx * p.ArLy * p.dens)) ** (1.0 / 3)
         box = (p.ArLx * Lz, p.ArLy * Lz, Lz)
     else:
-        box = tuple(float(x) for x in open(os.path.join(RUN, "init", "conf.dat")).readline().split())
-    rep = F.final_report(Time, AcT, AcTsq, cont, p, box).splitlines()
+        box = tuple(float(x) for x in open(os.path.join(_init(stage), "conf.dat")).readline().split())
+    rep = F.final_report(Time, AcT, AcTsq, cont, p, box, pol_deg=pol).splitlines()
     tail = lines[-len(rep):]
     assert tail[0] == "NVT ensemble"
     for a, b in zip(tail, rep):
@@ -151,19 +164,20 @@ def test_correlation_file(stage):
     """correlation.dat read back into histograms and normalised again: the
     bin columns are the same text and the functions agree to the
     precision the file keeps."""
-    p = F.read_input(os.path.join(RUN, stage, "input.txt"))
-    src = os.path.join(RUN, stage, "correlation.dat")
-    box = [float(x) for x in open(os.path.join(RUN, stage, "conf.dat")).readline().split()]
+    p = F.read_input(os.path.join(GOLD, stage, "input.txt"))
+    src = os.path.join(GOLD, stage, "correlation.dat")
+    box = [float(x) for x in open(os.path.join(GOLD, stage, "conf.dat")).readline().split()]
     if p.signal == 0:
         Lz = (p.n_total / (p.ArLx * p.ArLy * p.dens)) ** (1.0 / 3)
         box = [p.ArLx * Lz, p.ArLy * Lz, Lz]
     Lmin = min(box)
     nbins = int(math.floor(math.sqrt(3.0) * Lmin / (2.0 * p.bar_w)))
     cor_cont, hist = F.read_correlation(src, p.n_part, nbins)
-    assert hist.shape == (3, 4, nbins) and cor_cont > 0
-    # intra counts: even integers; inter counts: integers; all pairs inside the sphere
-    assert np.allclose(hist[:2, 0], np.round(hist[:2, 0] / 2) * 2, atol=1e-3)
-    assert np.allclose(hist[2, 0], np.round(hist[2, 0]), atol=1e-3)
+    nc = p.n_comp
+    assert hist.shape == (nc + nc * (nc - 1) // 2, 4, nbins) and cor_cont > 0
+    # intra counts: even integers; inter counts: integers
+    assert np.allclose(hist[:nc, 0], np.round(hist[:nc, 0] / 2) * 2, atol=1e-3)
+    assert np.allclose(hist[nc:, 0], np.round(hist[nc:, 0]), atol=1e-3)
     with tempfile.TemporaryDirectory() as d:
         out = os.path.join(d, "c.dat")
         F.write_correlation(out, hist, p.n_part, Lmin, p.bar_w, cor_cont)
@@ -182,20 +196,21 @@ def test_correlation_file(stage):
 @pytest.mark.parametrize("stage", STAGES)
 def test_ptens_magmom_pos_vel_lines(stage):
     with tempfile.TemporaryDirectory() as d:
-        for ln in open(os.path.join(RUN, stage, "ptens.dat")).read().splitlines():
+        for ln in open(os.path.join(GOLD, stage, "ptens.dat")).read().splitlines():
             t = ln.split()
             v = [float(x) for x in t]
             assert F.ptens_line(v[0], np.array(v[1:10]), np.array(v[10:19])).rstrip("\n") == ln
-        for ln in open(os.path.join(RUN, stage, "magmom.dat")).read().splitlines():
+        for ln in open(os.path.join(GOLD, stage, "magmom.dat")).read().splitlines():
             v = [float(x) for x in ln.split()]
             assert F.magmom_line(v[0], v[1:4]).rstrip("\n") == ln
-        pv = os.path.join(RUN, "init", "pos_vel", "pos_vel_0.dat")
+        pv = os.path.join(_init(stage), "pos_vel", "pos_vel_0.dat")
         lines = open(pv).read().splitlines()
         rows = []
         for ln in lines[:-1]:
             a, b = ln.split(" | ")
             x, y = [float(v) for v in a.split()], [float(v) for v in b.split()]
             rows.append((x[:3], x[3:], y[:3], y[3:]))
-        assert len(rows) == 50  # 25 of each species
+        p = F.read_input(os.path.join(_init(stage), "input.txt"))
+        assert len(rows) == sum(min(25, k) for k in p.n_part)  # up to 25 of each species
         F.write_pos_vel(os.path.join(d, "pv.dat"), rows, float(lines[-1]))
         assert open(os.path.join(d, "pv.dat")).read() == open(pv).read()
