@@ -190,6 +190,8 @@ class Driver:
                           min_s=p.min_s, cl_fr=p.cl_fr)
         st = SystemState(r, pm, O, l, length, dia, mass, dip)
         self._mass = mass
+        # each particle's own dipoles (its species'): print_conf writes no padding
+        self._ndip = np.repeat(np.asarray(nd_part, dtype=np.int64), p.n_part)
         bt = L.Batch([spec], None, device=self.device, descs=[L.desc_from_spec(spec, nd)])
         try:
             return self._loop(p, bt, st, clust, xi, strn, rng_state, box, V, Lmin, nbins, hist, cor_cont, Time,
@@ -347,7 +349,7 @@ class Driver:
         d = bt.download(0)
         xi, strn = bt.get_thermostat(0)
         F.write_conf(self.path("conf.dat"), box, d["r"], d["p"], d["O"], d["l"], self._mass, dip, d["clust"], xi,
-                     strn)
+                     strn, ndip=self._ndip)
         for k in range(2):
             mt, mti = bt.get_rng(0, k)
             F.write_mt_state(self.path(f"ran_state{k}F.dat"), mt, mti)

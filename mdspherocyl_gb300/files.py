@@ -232,27 +232,41 @@ def dipoles_lab(r, O, dip):
     return out
 
 
-def write_conf(path: str, box, r, p, O, l, mass, dip, clust, xi, strn) -> None:
+def write_conf(path: str, box, r, p, O, l, mass, dip, clust, xi, strn, ndip=None) -> None:
     """conf.dat as print_conf writes it: the box line in iostream's default
     format, then per particle r, p, O (row-major), l, ' | ', the mass, per
     dipole its lab position, direction and moment with ' . ', and the
     cluster label, all fixed to 12 decimals; then 'xi stored-normal' of the
-    two thermostats.  dip: per particle (nd_i, 5) body-frame rows."""
+    two thermostats.  dip: per particle (nd, 5) body-frame rows; ndip: how
+    many of them each particle has (its species' count; default all).  The
+    lab dipoles are computed for all particles at once with the operations
+    of dipoles_lab, in its order."""
     r = np.asarray(r, dtype=np.float64).reshape(-1, 3)
-    p = np.asarray(p, dtype=np.float64).reshape(-1, 3)
-    O = np.asarray(O, dtype=np.float64).reshape(-1, 3, 3)
-    l = np.asarray(l, dtype=np.float64).reshape(-1, 3)
-    mass = np.asarray(mass, dtype=np.float64).reshape(-1)
-    clust = np.asarray(clust).reshape(-1)
-    out = [f"{g6(box[0])} {g6(box[1])} {g6(box[2])}\n"]
-    for i in range(len(r)):
-        fields = [f12(v) for v in r[i]] + [f12(v) for v in p[i]] + [f12(v) for v in O[i].ravel()] + \
-                 [f12(v) for v in l[i]]
-        line = " ".join(fields) + "  | " + f12(mass[i]) + " "
-        for pos, ori, mu in dipoles_lab(r[i], O[i], dip[i]):
-            line += " ".join(f12(v) for v in pos) + " " + " ".join(f12(v) for v in ori) + " " + f12(mu) + " . "
-        line += str(int(clust[i])) + "\n"
-        out.append(line)
+    n = len(r)
+    p = np.asarray(p, dtype=np.float64).reshape(n, 3)
+    O = np.asarray(O, dtype=np.float64).reshape(n, 3, 3)
+    l = np.asarray(l, dtype=np.float64).reshape(n, 3)
+    mass = np.asarray(mass, dtype=np.float64).reshape(n)
+    clust = np.asarray(clust).reshape(n)
+    dip = np.asarray(dip, dtype=np.float64).reshape(n, -1, 5) if n else np.zeros((0, 0, 5))
+    ndip = np.full(n, dip.shape[1], dtype=np.int64) if ndip is None else np.asarray(ndip).reshape(n)
+    lines = [None] * n
+    for k in np.unique(ndip):
+        idx = np.nonzero(ndip == k)[0]
+        cols = [r[idx], p[idx], O[idx].reshape(-1, 9), l[idx], mass[idx, None]]
+        for w in range(int(k)):
+            d = dip[idx, w]
+            pos = r[idx] + d[:, 0:1] * O[idx, 2, :]
+            ori = np.zeros((len(idx), 3))
+            ori = ori + O[idx, 0, :] * d[:, 1:2]
+            ori = ori + O[idx, 1, :] * d[:, 2:3]
+            ori = ori + O[idx, 2, :] * d[:, 3:4]
+            cols += [pos, ori, d[:, 4:5]]
+        vals = np.concatenate(cols, axis=1)
+        fmt = " ".join(["%.12f"] * 18) + "  | %.12f " + "%.12f %.12f %.12f %.12f %.12f %.12f %.12f . " * int(k)
+        for q, i in enumerate(idx):
+            lines[i] = fmt % tuple(vals[q]) + str(int(clust[i])) + "\n"
+    out = [f"{g6(box[0])} {g6(box[1])} {g6(box[2])}\n"] + lines
     for k in range(2):
         out.append(f"{f12(xi[k])} {f12(strn[k])}\n")
     with open(path, "w") as f:

@@ -66,7 +66,8 @@ def test_conf_round_trip(stage):
     assert c["r"].shape == (p.n_total, 3) and np.all(c["mass"] == 1.0)
     with tempfile.TemporaryDirectory() as d:
         out = os.path.join(d, "conf.dat")
-        F.write_conf(out, c["box"], c["r"], c["p"], c["O"], c["l"], mass, dip, c["clust"], c["xi"], c["strn"])
+        F.write_conf(out, c["box"], c["r"], c["p"], c["O"], c["l"], mass, dip, c["clust"], c["xi"], c["strn"],
+                     ndip=np.repeat(nd_part, p.n_part))
         a, b = open(src).read().splitlines(), open(out).read().splitlines()
     assert len(a) == len(b) and a[0] == b[0] and a[-2:] == b[-2:]
     for la, lb in zip(a[1:-2], b[1:-2]):
