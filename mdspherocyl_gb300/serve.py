@@ -11,7 +11,9 @@ mdsc_estimate_bytes of the would-be batch must fit it.
 
 A job's result is independent of the jobs it shares the GPU with: every
 kernel works per system and sums in a fixed order, so a system gives the
-same bits alone and in any mix (tests/test_serve.py).
+same bits alone and in any mix (tests/test_serve.py).  A system that reports
+an error (the reference's overlap abort, a NaN, a full list) fails its own
+job, which leaves at the next tick; the others run on undisturbed.
 """
 from __future__ import annotations
 
@@ -38,6 +40,7 @@ class Job:
     done: int = 0
     result: dict | None = None
     obs: dict | None = None
+    error: str | None = None  # the status of a system that failed (overlap, NaN, ...)
 
     @property
     def n(self) -> int:
@@ -107,8 +110,8 @@ class Server:
     def tick_once(self) -> bool:
         """Retire, admit, advance.  Returns False when nothing is running."""
         now = self.clock()
-        finished = [j for j in self.running if j.done >= j.steps]
-        keep = [j for j in self.running if j.done < j.steps]
+        finished = [j for j in self.running if j.done >= j.steps or j.error]
+        keep = [j for j in self.running if j.done < j.steps and not j.error]
         for j in finished:
             k = self.running.index(j)
             if self.keep_results:
@@ -133,7 +136,16 @@ class Server:
         if not self.running:
             return False
         steps = min(self.tick, min(j.steps - j.done for j in self.running))
-        obs = self.batch.step(steps)
+        arr = (L.Observables * len(self.running))()
+        code = self.batch.lib.mdsc_step(self.batch.h, steps, arr)
+        obs = [o.as_dict() for o in arr]
+        if code != 0:
+            # a system's own error fails its job only; anything else is the server's
+            bad = [k for k, o in enumerate(obs) if o["status"] != 0]
+            if not bad:
+                raise L.MdscError(code, "mdsc_step", self.batch._err())
+            for k in bad:
+                self.running[k].error = L.STATUS.get(obs[k]["status"], str(obs[k]["status"]))
         self.stats.gpu_ms += self.batch.lib.mdsc_last_device_ms(self.batch.h)
         for j, o in zip(self.running, obs):
             j.done += steps
@@ -174,6 +186,7 @@ def summarize(stats: ServerStats, wall_s: float) -> dict:
     lat = stats.latencies()
     return {
         "jobs": len(stats.completed),
+        "failed": sum(1 for j in stats.completed if j.error),
         "p50_latency_s": float(np.percentile(lat, 50)) if len(lat) else None,
         "p99_latency_s": float(np.percentile(lat, 99)) if len(lat) else None,
         "mean_latency_s": float(lat.mean()) if len(lat) else None,

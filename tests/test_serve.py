@@ -50,3 +50,33 @@ def test_budget_admission_serialises_jobs():
     assert len(stats.completed) == 3 and stats.max_running == 1
     lat = stats.latencies()
     assert np.all(lat > 0)
+
+
+def test_a_failing_job_leaves_alone():
+    """One job starts with two rods on top of each other: the reference's
+    overlap abort fails that job (status MDSC_ERR_OVERLAP); every other job
+    finishes with the bits it has alone."""
+    jobs = _jobs()
+    bad = jobs[2]
+    bad.state = bad.state.copy()
+    bad.state.r[1] = bad.state.r[0] + np.array([0.05, 0.0, 0.0])
+    bad.state.O[1] = bad.state.O[0]
+    alone = {}
+    for j in _jobs():
+        if j.jid == bad.jid:
+            continue
+        with L.Batch([j.spec], [j.state]) as bt:
+            bt.step(j.steps)
+            alone[j.jid] = bt.download(0)
+    srv = serve.Server(tick_steps=9, keep_results=True)
+    stats = srv.run(jobs)
+    assert len(stats.completed) == 6
+    failed = [j for j in stats.completed if j.error]
+    assert [j.jid for j in failed] == [bad.jid] and failed[0].error == "MDSC_ERR_OVERLAP"
+    for j in stats.completed:
+        if j.jid == bad.jid:
+            continue
+        assert j.done == j.steps and j.error is None
+        for f in ("r", "p", "O", "l", "F", "T", "clust"):
+            assert np.array_equal(j.result[f], alone[j.jid][f]), (j.jid, f)
+    assert serve.summarize(stats, 1.0)["failed"] == 1
