@@ -215,3 +215,34 @@ def test_ptens_magmom_pos_vel_lines(stage):
         assert len(rows) == sum(min(25, k) for k in p.n_part)  # up to 25 of each species
         F.write_pos_vel(os.path.join(d, "pv.dat"), rows, float(lines[-1]))
         assert open(os.path.join(d, "pv.dat")).read() == open(pv).read()
+
+
+@pytest.mark.parametrize("run", ["run1", "run2"])
+def test_shipped_restart_states(run):
+    """The restart states the reference ships (v25/run1: 64-bit generator
+    files of 5000 bytes; v25/run2: a 32-bit build's, 2500 bytes): input,
+    configuration, counters and generator states read, the configuration
+    written back token for token.  Runs where the reference is present."""
+    from conftest import REFERENCE
+
+    d = os.path.join(REFERENCE, "v25", run)
+    if not os.path.isdir(d):
+        pytest.skip("reference run directories not present")
+    p = F.read_input(os.path.join(d, "input.txt"))
+    length, dia, mass, dip, nd, nd_part = layout(p)
+    c = F.read_conf(os.path.join(d, "conf.dat"), p.n_part, nd_part)
+    assert c["r"].shape == (p.n_total, 3)
+    assert np.allclose(np.einsum("nab,ncb->nac", c["O"], c["O"]), np.eye(3), atol=1e-8)  # orthonormal frames
+    for k in range(2):
+        mt, mti = F.read_mt_state(os.path.join(d, f"ran_state{k}F.dat"))
+        assert 0 <= mti <= 624 and mt.dtype == np.uint32
+    F.read_counters(os.path.join(d, "counters.dat"))
+    with tempfile.TemporaryDirectory() as t:
+        out = os.path.join(t, "conf.dat")
+        F.write_conf(out, c["box"], c["r"], c["p"], c["O"], c["l"], mass, dip, c["clust"], c["xi"], c["strn"],
+                     ndip=np.repeat(nd_part, p.n_part))
+        a, b = open(os.path.join(d, "conf.dat")).read().split(), open(out).read().split()
+    assert len(a) == len(b)
+    diff = [(x, y) for x, y in zip(a, b) if x != y]
+    # only lab dipole coordinates may differ, in the last printed place
+    assert all(abs(float(x) - float(y)) <= 2.5e-12 for x, y in diff)
