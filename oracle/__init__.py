@@ -28,6 +28,8 @@ BUILD = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(BUILD, "libmdsc_oracle.so")
 REF_SO = os.path.join(REF_DIR, "libmdsc_ref.so")
+# the same sources without OpenMP, for systems below 16 particles per thread
+REF_SERIAL_SO = os.path.join(REF_DIR, "libmdsc_ref_serial.so")
 
 _dp = POINTER(c_double)
 _ip = POINTER(c_int)

@@ -4,6 +4,13 @@
 #
 #   oracle/_ref/libmdsc_ref.so  function-level harness (oracle/ref_harness.cpp)
 #                               + v25/classes.cpp v25/functions.cpp v25/jacobi.c
+#   oracle/_ref/libmdsc_ref_serial.so
+#                               the same, without -fopenmp: the reference's
+#                               loops use schedule(dynamic, floor(N/(16 threads)))
+#                               (v25/functions.cpp:1411-1414 and the like), a
+#                               chunk of 0 below 16 particles per thread, on
+#                               which libgomp never advances; this build runs
+#                               the same loops serially for small systems
 #   oracle/_ref/DSCmd_v25       the reference driver, v25/main.cpp
 #   oracle/_ref/DSCmd_v251      the later variant, v25/v251/main.cpp
 #
@@ -27,6 +34,8 @@ V251="$REF/v25/v251"
 
 "$CXX" "${FLAGS[@]}" -fPIC -shared -I"$V25" -o "$OUT/libmdsc_ref.so" \
   "$HERE/ref_harness.cpp" "$V25/classes.cpp" "$V25/functions.cpp" "$V25/jacobi.c" &
+"$CXX" -O2 -ffp-contract=off -w -I"$HERE" -fPIC -shared -I"$V25" -o "$OUT/libmdsc_ref_serial.so" \
+  "$HERE/ref_harness.cpp" "$V25/classes.cpp" "$V25/functions.cpp" "$V25/jacobi.c" -lgomp &
 "$CXX" "${FLAGS[@]}" -I"$V25" -o "$OUT/DSCmd_v25" \
   "$V25/main.cpp" "$V25/classes.cpp" "$V25/functions.cpp" "$V25/jacobi.c" &
 # v25/v251/functions.cpp calls getcwd without including <unistd.h>

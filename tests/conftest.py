@@ -35,6 +35,19 @@ def ref():
     return oracle.Ref()
 
 
+@pytest.fixture(scope="session")
+def ref_serial():
+    """The reference built without OpenMP: its loops' dynamic schedule takes
+    a chunk of 0 below 16 particles per thread and never ends there."""
+    import oracle
+
+    if not os.path.isdir(os.path.join(REFERENCE, "v25")):
+        pytest.skip("reference sources not present")
+    if not os.path.exists(oracle.REF_SERIAL_SO):
+        oracle.build_ref()
+    return oracle.Ref(oracle.REF_SERIAL_SO)
+
+
 def rms_rel(a, b):
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
