@@ -188,6 +188,17 @@ mdsc_status mdsc_check_list(mdsc_batch* b, int* rebuild);
    labels of system `sys` with the reference's numbering, drawing from the
    system's cluster generator.  labels: n ints (may be NULL). */
 mdsc_status mdsc_clust_conf(mdsc_batch* b, int sys, int* labels, int* n_clusters);
+/* The bond test of system sys's clusterings (mdsc_clust_conf and the
+   clustering every cl_fr steps of mdsc_step).  u_bond_kT = 0: the reference's
+   geometric test (the default).  u_bond_kT > 0: an energy criterion, an
+   extension the reference does not have: i and j are bonded when
+     U_pair = U_WCA (force_sc's pair energy) + sum over their dipole pairs of
+              mu_a mu_b (o_a.o_b - 3 (o_a.r)(o_b.r) / r^2) / r^3
+   (bare dipole-dipole energy at the minimum image of the dipole sites) is
+   below -u_bond_kT * T, T the system's temperature.  Labels are then
+   numbered as clust_conf numbers them.  MDSC_ERR_LIST_OVERFLOW from the
+   clustering if a particle has more than 16 such bonds to higher indices. */
+mdsc_status mdsc_set_cluster_energy(mdsc_batch* b, int sys, double u_bond_kT);
 
 /* Moves system ssys of batch src into slot dsys of batch dst (same device,
    same n and nd) without leaving the GPU: particle state, forces, shapes,

@@ -34,6 +34,7 @@ void launch_movep(const Batch& b, const double* xi, int last, cudaStream_t s);
 void launch_list_build(const Batch& b, int force_all, cudaStream_t s);
 void launch_wca(const Batch& b, cudaStream_t s);
 void launch_cluster_bonds(const Batch& b, cudaStream_t s);
+void launch_ebond(const Batch& b, cudaStream_t s);
 void launch_cluster_hook(const Batch& b, cudaStream_t s);
 void launch_cluster_compress(const Batch& b, cudaStream_t s);
 void launch_reset_iter(const Batch& b, cudaStream_t s);
@@ -438,6 +439,9 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   b.comp = A.take<int>(n);
   b.eflag = A.take<unsigned char>(n * kMaxNb);
   b.flag = A.take<int>(1);
+  b.ebond = A.take<int>(n * kMaxC);
+  b.ebcnt = A.take<int>(n);
+  b.eovf = A.take<int>(std::max(nsys, 1));
   *kwork = A.take<int4>(std::max<size_t>(Lo.kwork.size(), 1));
   *kowner = A.take<int2>(nk);
   noise2[0] = A.take<double>((size_t)kNoiseChunk * nsys * 4);
@@ -689,6 +693,20 @@ void draw_noise(mdsc_batch* B, int steps) {
 mdsc_status run_clusters(mdsc_batch* B, const std::vector<int>& systems) {
   Batch b = B->b;
   launch_cluster_bonds(b, B->st);
+  bool energy = false;
+  for (int s = 0; s < B->nsys; ++s) energy |= B->lo.sys[s].cl_mode == 1;
+  if (energy) {
+    CU(cudaMemsetAsync(b.eovf, 0, sizeof(int) * B->nsys, B->st));
+    launch_ebond(b, B->st);
+    std::vector<int> ovf(B->nsys);
+    CU(cudaMemcpyAsync(ovf.data(), b.eovf, sizeof(int) * B->nsys, cudaMemcpyDeviceToHost, B->st));
+    CU(cudaStreamSynchronize(B->st));
+    for (int s : systems)
+      if (ovf[s])
+        return fail(B, MDSC_ERR_LIST_OVERFLOW,
+                    "system " + std::to_string(s) + ": a particle has more than " + std::to_string(kMaxC) +
+                        " energy bonds to higher indices");
+  }
   for (int it = 0; it < 64; ++it) {
     CU(cudaMemsetAsync(b.flag, 0, sizeof(int), B->st));
     launch_cluster_hook(b, B->st);
@@ -1444,6 +1462,17 @@ mdsc_status mdsc_clust_conf(mdsc_batch* B, int sys, int* labels, int* n_clusters
   return MDSC_OK;
 }
 
+mdsc_status mdsc_set_cluster_energy(mdsc_batch* B, int sys, double u_bond_kT) {
+  if (!B || sys < 0 || sys >= B->nsys || !(u_bond_kT >= 0.0)) return MDSC_ERR_BAD_ARG;
+  cudaSetDevice(B->device);
+  SysDev& P = B->lo.sys[sys];
+  P.cl_mode = u_bond_kT > 0.0 ? 1 : 0;
+  P.cl_ubond = u_bond_kT * B->desc[sys].temp;
+  CU(cudaMemcpyAsync((void*)(B->b.sys + sys), &P, sizeof(SysDev), cudaMemcpyHostToDevice, B->st));
+  CU(cudaStreamSynchronize(B->st));
+  return MDSC_OK;
+}
+
 // ---- observables outside the step ---------------------------------------
 int mdsc_correlation_bins(const mdsc_batch* B, int sys, double bar_w) {
   if (!B || sys < 0 || sys >= B->nsys || !(bar_w > 0.0)) return 0;
@@ -1737,6 +1766,8 @@ mdsc_status mdsc_transfer(mdsc_batch* D, int dsys, mdsc_batch* S, int ssys) {
   Pd.skin = Ps.skin;
   Pd.r_list = Ps.r_list;
   Pd.Uself = Ps.Uself;
+  Pd.cl_mode = Ps.cl_mode;
+  Pd.cl_ubond = Ps.cl_ubond;
   CU(cudaMemcpyAsync((void*)(b.sys + dsys), &Pd, sizeof(SysDev), cudaMemcpyHostToDevice, D->st));
   SysState st;
   CU(cudaMemcpy(&st, a.st + ssys, sizeof st, cudaMemcpyDeviceToHost));

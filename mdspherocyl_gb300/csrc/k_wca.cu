@@ -1,6 +1,7 @@
 // Verlet list, WCA core forces and cluster bonds -- the GPU form of
 // neigh_list / check_list (v25/functions.cpp:1298-1394), force_sc
-// (:1397-1553) and the cluster criterion of clust_conf (:2987-3016).
+// (:1397-1553) and the cluster criterion of clust_conf (:2987-3016), plus
+// an energy criterion for clusters (pair energy below a threshold).
 //
 // List: each particle keeps every partner (both directions, ascending
 // index) whose segment distance is below r_list = max(2^(1/6) sigma_max,
@@ -313,10 +314,11 @@ __global__ void __launch_bounds__(kPartBlock) cluster_bonds_kernel(Batch b) {
   const SysDev& P = b.sys[bk.x];
   const int i = bk.y + threadIdx.x;
   if (i >= P.part_off + P.n) return;
+  b.comp[i] = i;
+  if (P.cl_mode) return;  // energy criterion: ebond_kernel
   const int nc = b.nbc[i];
   const int* lst = b.nb + (long long)i * kMaxNb;
   unsigned char* fl = b.eflag + (long long)i * kMaxNb;
-  b.comp[i] = i;
   RodD ri;
   load_rod(b, i, ri);
   for (int k = 0; k < nc; ++k) {
@@ -339,6 +341,141 @@ __global__ void __launch_bounds__(kPartBlock) cluster_bonds_kernel(Batch b) {
   }
 }
 
+// ---- energy criterion (an extension; the reference's test is geometric) --
+// U_pair = the WCA pair energy of force_sc (v25/functions.cpp:1436-1483) +
+// the bare dipole-dipole energy of every dipole pair of the two rods at the
+// minimum image of the sites, mu_a mu_b (o_a.o_b - 3 (o_a.r)(o_b.r)/r^2)/r^3,
+// in FP64 with the operations in the oracle's order (A < B; this file is
+// compiled without FMA contraction, and sqrt and division round correctly).
+__device__ void dip_lab_ref(const Batch& b, const SysDev& P, int i, int w, double pos[3], double ori[3],
+                            double* mu) {
+  const int g = P.dip_off + (i - P.part_off) * P.nd + w;
+  const double* O = b.O + 9 * (long long)i;
+  const double d0 = b.dpc[g];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) pos[a] = b.r[3 * i + a] + d0 * O[6 + a];
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {  // transpose(O) times the body direction, summed from 0
+    double acc = 0.;
+    acc += O[m] * b.dob[3 * g];
+    acc += O[3 + m] * b.dob[3 * g + 1];
+    acc += O[6 + m] * b.dob[3 * g + 2];
+    ori[m] = acc;
+  }
+  *mu = b.dmu[g];
+}
+
+__device__ double pair_energy_ref(const Batch& b, const SysDev& P, int A, int B) {
+  RodD ra, rb;
+  load_rod(b, A, ra);
+  load_rod(b, B, rb);
+  double rij[3], dij[3], st[2];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    rij[a] = ra.r[a] - rb.r[a];
+    rij[a] -= P.L[a] * floor(rij[a] / P.L[a] + 0.5);
+  }
+  const double dsq = seg_dist_ref<true>(ra, rb, P.L, rij, dij, st);
+  const double sigma = (b.dia[A] + b.dia[B]) / 2;
+  const double sig_sq = sigma * sigma;
+  const double srt = 1.122462048309373;  // 2^(1/6)
+  double U = 0.;
+  if (dsq < srt * srt * sig_sq) {
+    const double SR2s = sig_sq / dsq;
+    const double SR6s = SR2s * SR2s * SR2s;
+    U = 4 * SR6s * (SR6s - 1.) + 1.;
+  }
+  for (int a = 0; a < P.nd; ++a) {
+    double pa[3], oa[3], ma;
+    dip_lab_ref(b, P, A, a, pa, oa, &ma);
+    if (ma == 0.) continue;
+    for (int c = 0; c < P.nd; ++c) {
+      double pb[3], ob[3], mb;
+      dip_lab_ref(b, P, B, c, pb, ob, &mb);
+      if (mb == 0.) continue;
+      double r[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) r[k] = dmimg(pa[k] - pb[k], P.L[k]);
+      const double r2 = ddot(r, r);
+      const double ir = 1. / sqrt(r2);
+      const double ir3 = ir * ir * ir;
+      const double dd = ddot(oa, ob), da = ddot(oa, r), db = ddot(ob, r);
+      U += ma * mb * (dd - 3. * da * db / r2) * ir3;
+    }
+  }
+  return U;
+}
+
+// bonds U_pair < -cl_ubond to every higher index of the system.  An FP32
+// screen on the centres (fixed-point minimum image) keeps the pairs that
+// can bond: |U_dd| <= 2 M_i M_j / (r - e_i - e_j)^3, with M the sum of a
+// rod's moments and e its largest dipole offset, and U_WCA >= 0; those are
+// evaluated exactly.
+__global__ void __launch_bounds__(kPartBlock) ebond_kernel(Batch b) {
+  __shared__ uint32_t sx[kPartBlock], sy[kPartBlock], sz[kPartBlock];
+  __shared__ float2 sme[kPartBlock];
+  const int2 bk = b.blk[blockIdx.x];
+  const int s = bk.x;
+  const SysDev& P = b.sys[s];
+  if (P.cl_mode != 1) return;  // the same for the whole block
+  const int first = P.part_off, n = P.n, N = b.ntot;
+  const int i = bk.y + threadIdx.x;
+  const bool ok = i < first + n;
+  auto bound = [&](int q) {
+    float m = 0.f, e = 0.f;
+    for (int w = 0; w < P.nd; ++w) {
+      const int g = P.dip_off + (q - first) * P.nd + w;
+      const float ob = (float)sqrt(b.dob[3 * g] * b.dob[3 * g] + b.dob[3 * g + 1] * b.dob[3 * g + 1] +
+                                   b.dob[3 * g + 2] * b.dob[3 * g + 2]);
+      m += fabsf((float)b.dmu[g]) * ob;
+      e = fmaxf(e, fabsf((float)b.dpc[g]));
+    }
+    return make_float2(m * 1.0001f, e * 1.0001f);
+  };
+  uint32_t ux = 0, uy = 0, uz = 0;
+  float2 mi = make_float2(0.f, 0.f);
+  if (ok) {
+    ux = b.pfx[i];
+    uy = b.pfx[N + i];
+    uz = b.pfx[2 * N + i];
+    mi = bound(i);
+  }
+  const float Lx = P.Lfix[0], Ly = P.Lfix[1], Lz = P.Lfix[2];
+  const float thr = (float)P.cl_ubond * 0.999f;
+  int* out = b.ebond + (long long)i * kMaxC;
+  int cnt = 0;
+  for (int q0 = (bk.y - first) / kPartBlock * kPartBlock; q0 < n; q0 += kPartBlock) {
+    __syncthreads();
+    if (q0 + (int)threadIdx.x < n) {
+      const int q = first + q0 + threadIdx.x;
+      sx[threadIdx.x] = b.pfx[q];
+      sy[threadIdx.x] = b.pfx[N + q];
+      sz[threadIdx.x] = b.pfx[2 * N + q];
+      sme[threadIdx.x] = bound(q);
+    }
+    __syncthreads();
+    if (!ok || mi.x == 0.f) continue;
+    const int nq = min(kPartBlock, n - q0);
+    for (int t = 0; t < nq; ++t) {
+      const int j = first + q0 + t;
+      if (j <= i) continue;
+      const float2 mj = sme[t];
+      if (mj.x == 0.f) continue;
+      const float dx = fix_diff(ux, sx[t], Lx), dy = fix_diff(uy, sy[t], Ly), dz = fix_diff(uz, sz[t], Lz);
+      const float gap = sqrtf(dx * dx + dy * dy + dz * dz) * 0.9999f - mi.y - mj.y;
+      if (gap > 0.f && 2.f * mi.x * mj.x < thr * gap * gap * gap) continue;
+      if (pair_energy_ref(b, P, i, j) < -P.cl_ubond) {
+        if (cnt < kMaxC) out[cnt] = j;
+        ++cnt;
+      }
+    }
+  }
+  if (ok) {
+    b.ebcnt[i] = min(cnt, kMaxC);
+    if (cnt > kMaxC) atomicOr(&b.eovf[s], 1);
+  }
+}
+
 __device__ __forceinline__ int find_root(const int* comp, int x) {
   int p = comp[x];
   while (p != x) {
@@ -354,11 +491,12 @@ __global__ void __launch_bounds__(kPartBlock) cluster_hook_kernel(Batch b) {
   const SysDev& P = b.sys[bk.x];
   const int i = bk.y + threadIdx.x;
   if (i >= P.part_off + P.n) return;
-  const int nc = b.nbc[i];
-  const int* lst = b.nb + (long long)i * kMaxNb;
-  const unsigned char* fl = b.eflag + (long long)i * kMaxNb;
+  const bool en = P.cl_mode == 1;
+  const int nc = en ? b.ebcnt[i] : b.nbc[i];
+  const int* lst = en ? b.ebond + (long long)i * kMaxC : b.nb + (long long)i * kMaxNb;
+  const unsigned char* fl = en ? nullptr : b.eflag + (long long)i * kMaxNb;
   for (int k = 0; k < nc; ++k) {
-    if (!fl[k]) continue;
+    if (fl && !fl[k]) continue;
     int ra = find_root(b.comp, i), rb = find_root(b.comp, lst[k]);
     while (ra != rb) {
       const int hi = max(ra, rb), lo = min(ra, rb);
@@ -394,6 +532,9 @@ void launch_wca(const Batch& b, cudaStream_t s) {
 }
 void launch_cluster_bonds(const Batch& b, cudaStream_t s) {
   if (b.nblk) cluster_bonds_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
+}
+void launch_ebond(const Batch& b, cudaStream_t s) {
+  if (b.nblk) ebond_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
 }
 void launch_cluster_hook(const Batch& b, cudaStream_t s) {
   if (b.nblk) cluster_hook_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);

@@ -53,6 +53,8 @@ struct SysDev {
   int gch_off, pad_g;       // first chunk of the system in the G-tensor partials
   int blk_off, nblk;        // per-particle block range
   int cl_fr;
+  int cl_mode;     // cluster bonds: 0 the reference's geometric test, 1 pair energy
+  double cl_ubond; // mode 1: a bond is U_pair < -cl_ubond (the threshold times T)
   double L[3];
   double invL[3];
   double invL32[3];  // 2^32 / L: coordinate to fixed-point box fraction
@@ -195,6 +197,9 @@ struct Batch {
   int* comp;     // n component representative
   unsigned char* eflag;  // n * kMaxNb: list entry is a cluster bond
   int* flag;     // 1 changed flag
+  int* ebond;    // n * kMaxC: energy-criterion bonds to higher indices
+  int* ebcnt;    // n: their number
+  int* eovf;     // nsys: a particle had more than kMaxC energy bonds
   // thermostat noise: [iter][sys][4] = g0_t, g1_t, g0_r, g1_r
   const double* noise;
 };

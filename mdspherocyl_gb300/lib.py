@@ -33,7 +33,8 @@ EXPORTS = [
     "mdsc_last_error", "mdsc_upload", "mdsc_download", "mdsc_upload_all", "mdsc_download_all",
     "mdsc_set_thermostat", "mdsc_zero_forces", "mdsc_force_sc", "mdsc_force_dipR",
     "mdsc_force_dipK", "mdsc_ext_field", "mdsc_self_ener", "mdsc_moveX", "mdsc_moveP",
-    "mdsc_renorm", "mdsc_neigh_list", "mdsc_check_list", "mdsc_clust_conf", "mdsc_step",
+    "mdsc_renorm", "mdsc_neigh_list", "mdsc_check_list", "mdsc_clust_conf", "mdsc_set_cluster_energy",
+    "mdsc_step",
     "mdsc_observe", "mdsc_launches_per_step", "mdsc_stream", "mdsc_profile_steps",
     "mdsc_place_rods", "mdsc_last_device_ms", "mdsc_force_dipR_noalloc", "mdsc_transfer",
     "mdsc_autotune", "mdsc_tuning", "mdsc_set_tuning", "mdsc_correlation_bins", "mdsc_correlations",
@@ -158,6 +159,7 @@ def load(build: bool = True) -> ctypes.CDLL:
         "mdsc_neigh_list": (c_int, [c_void_p]),
         "mdsc_check_list": (c_int, [c_void_p, _ip]),
         "mdsc_clust_conf": (c_int, [c_void_p, c_int, _ip, _ip]),
+        "mdsc_set_cluster_energy": (c_int, [c_void_p, c_int, c_double]),
         "mdsc_step": (c_int, [c_void_p, c_int, P(Observables)]),
         "mdsc_observe": (c_int, [c_void_p, P(Observables)]),
         "mdsc_launches_per_step": (c_int, [c_void_p]),
@@ -378,6 +380,11 @@ class Batch:
         self._check(self.lib.mdsc_clust_conf(self.h, k, lab.ctypes.data_as(_ip), ctypes.byref(nc)),
                     "mdsc_clust_conf")
         return lab, nc.value
+
+    def set_cluster_energy(self, k: int, u_bond_kT: float) -> None:
+        """System k's cluster bonds: U_pair < -u_bond_kT * T (pair energy =
+        WCA + bare dipole-dipole), or the reference's geometric test for 0."""
+        self._check(self.lib.mdsc_set_cluster_energy(self.h, k, float(u_bond_kT)), "mdsc_set_cluster_energy")
 
     # -- observables outside the step --
     def correlation_bins(self, k: int, bar_w: float) -> int:

@@ -160,6 +160,8 @@ class Oracle:
         self._rng_u = _bind(lib, "mdsc_or_rng_uniform", c_double, [c_void_p])
         self._rng_free = _bind(lib, "mdsc_or_rng_free", None, [c_void_p])
         self._cl = _bind(lib, "mdsc_or_clust_conf_rng", c_int, [_SP, c_double, c_void_p])
+        self._cle = _bind(lib, "mdsc_or_clust_energy_rng", c_int, [_SP, c_double, c_void_p])
+        self._pe = _bind(lib, "mdsc_or_pair_energy", c_double, [_SP, c_int, c_int])
         self._corr = _bind(lib, "mdsc_or_acc_correl", None, [_SP, c_double, c_int, _dp])
         self._corr_sp = _bind(lib, "mdsc_or_acc_correl_species", None, [_SP, c_int, _ip, c_double, c_int, _dp])
         self._oo = _bind(lib, "mdsc_or_oo_params", None, [_SP, _dp, _dp, _dp])
@@ -174,6 +176,26 @@ class Oracle:
                 self._rng_u(rng)
             cs = sysm.cstate()
             nc = self._cl(ctypes.byref(cs), min_s, rng)
+            nxt = self._rng_u(rng)
+        finally:
+            self._rng_free(rng)
+        return sysm.clust.copy(), nc, nxt
+
+    def pair_energy(self, sysm: System, a: int, b: int) -> float:
+        """The energy criterion's pair energy (WCA + bare dipole-dipole) of
+        particles a < b."""
+        cs = sysm.cstate()
+        return self._pe(ctypes.byref(cs), int(a), int(b))
+
+    def clust_energy(self, sysm: System, u_bond: float, seed: int = 1, skip: int = 0):
+        """clust_conf's labelling over the energy criterion: bonds where the
+        pair energy is below -u_bond; returns (labels, clusters, next draw)."""
+        rng = self._rng_new(seed)
+        try:
+            for _ in range(skip):
+                self._rng_u(rng)
+            cs = sysm.cstate()
+            nc = self._cle(ctypes.byref(cs), u_bond, rng)
             nxt = self._rng_u(rng)
         finally:
             self._rng_free(rng)

@@ -1081,7 +1081,64 @@ static int dist_test(const mdsc_oracle_state* s, int A, int B, double min_s) {
   return dsq < sig_sq;
 }
 
-int mdsc_or_clust_conf(mdsc_oracle_state* s, double min_s, mdsc_mt19937* ran) {
+/* The pair energy of the energy criterion for clusters -- an extension: the
+   reference's own criterion is the geometric one above.  U_pair = the WCA
+   pair energy of force_sc (v25/functions.cpp:1436-1483, 2^(1/6) sigma range,
+   shifted by 1) + the bare dipole-dipole energy of every dipole pair of the
+   two rods, at the minimum image of the dipole sites:
+     mu_a mu_b (o_a.o_b - 3 (o_a.r)(o_b.r) / r^2) / r^3.
+   A is the lower index.  Zero-moment dipoles are skipped. */
+double mdsc_or_pair_energy(const mdsc_oracle_state* s, int A, int B) {
+  const double* ri = &s->r[3 * A];
+  const double* rj = &s->r[3 * B];
+  double rij[3], dij[3], st[2];
+  for (int a = 0; a < 3; ++a) {
+    rij[a] = ri[a] - rj[a];
+    rij[a] -= s->L[a] * floor(rij[a] / s->L[a] + 0.5);
+  }
+  const double dsq = mdsc_or_seg_dist(s, A, B, rij, dij, st);
+  const double sigma = (s->dia[A] + s->dia[B]) / 2;
+  const double sig_sq = sigma * sigma;
+  const double srt = 1.122462048309373; /* 2^(1/6) */
+  double U = 0.;
+  if (dsq < srt * srt * sig_sq) {
+    const double SR2s = sig_sq / dsq;
+    const double SR6s = SR2s * SR2s * SR2s;
+    U = 4 * SR6s * (SR6s - 1.) + 1.;
+  }
+  for (int a = 0; a < s->nd; ++a) {
+    double pa[3], oa[3], la[3], ma;
+    dip_lab(s, A, a, pa, oa, la, &ma);
+    if (ma == 0.) continue;
+    for (int b = 0; b < s->nd; ++b) {
+      double pb[3], ob[3], lb[3], mb;
+      dip_lab(s, B, b, pb, ob, lb, &mb);
+      if (mb == 0.) continue;
+      double r[3];
+      for (int k = 0; k < 3; ++k) r[k] = mimg(pa[k] - pb[k], s->L[k]);
+      const double r2 = dot3(r, r);
+      const double ir = 1. / sqrt(r2);
+      const double ir3 = ir * ir * ir;
+      const double dd = dot3(oa, ob), da = dot3(oa, r), db = dot3(ob, r);
+      U += ma * mb * (dd - 3. * da * db / r2) * ir3;
+    }
+  }
+  return U;
+}
+
+/* the bond test of a labelling: geometric (dist_test, min_s) or energy
+   (U_pair < -u_bond, lower index first) */
+typedef struct {
+  int energy;
+  double v;
+} bond_rule;
+
+static int bonded(const mdsc_oracle_state* s, int A, int B, const bond_rule* br) {
+  if (!br->energy) return dist_test(s, A, B, br->v);
+  return (A < B ? mdsc_or_pair_energy(s, A, B) : mdsc_or_pair_energy(s, B, A)) < -br->v;
+}
+
+static int clust_bfs(mdsc_oracle_state* s, const bond_rule* br, mdsc_mt19937* ran) {
   const int TP = s->n;
   int* NI = (int*)malloc(sizeof(int) * (TP > 0 ? TP : 1)); /* remaining, ascending */
   int nrem = TP;
@@ -1108,7 +1165,7 @@ int mdsc_or_clust_conf(mdsc_oracle_state* s, double min_s, mdsc_mt19937* ran) {
       int ii = queue[qh];
       for (int j = 0; j < TP; ++j) {
         if (locadd[j]) continue;
-        if (dist_test(s, ii, j, min_s)) {
+        if (bonded(s, ii, j, br)) {
           if (!added[j]) {
             queue[qt++] = j;
             int loc = 0;
@@ -1137,6 +1194,17 @@ int mdsc_or_clust_conf(mdsc_oracle_state* s, double min_s, mdsc_mt19937* ran) {
   return n_clust;
 }
 
+int mdsc_or_clust_conf(mdsc_oracle_state* s, double min_s, mdsc_mt19937* ran) {
+  const bond_rule br = {0, min_s};
+  return clust_bfs(s, &br, ran);
+}
+
+/* clust_conf's labelling over the energy criterion: bonds U_pair < -u_bond */
+int mdsc_or_clust_energy(mdsc_oracle_state* s, double u_bond, mdsc_mt19937* ran) {
+  const bond_rule br = {1, u_bond};
+  return clust_bfs(s, &br, ran);
+}
+
 void* mdsc_or_rng_new(unsigned long seed) {
   mdsc_mt19937* g = (mdsc_mt19937*)malloc(sizeof(mdsc_mt19937));
   mdsc_mt_seed(g, seed);
@@ -1146,6 +1214,9 @@ double mdsc_or_rng_uniform(void* g) { return mdsc_mt_uniform((mdsc_mt19937*)g); 
 void mdsc_or_rng_free(void* g) { free(g); }
 int mdsc_or_clust_conf_rng(mdsc_oracle_state* s, double min_s, void* g) {
   return mdsc_or_clust_conf(s, min_s, (mdsc_mt19937*)g);
+}
+int mdsc_or_clust_energy_rng(mdsc_oracle_state* s, double u_bond, void* g) {
+  return mdsc_or_clust_energy(s, u_bond, (mdsc_mt19937*)g);
 }
 
 /* ------------------------------------------------------------------ */

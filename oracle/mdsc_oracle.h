@@ -97,12 +97,17 @@ void mdsc_or_moveTher(mdsc_or_thermo* th, double temp, double dt, const double K
 /* clust_conf with p_check = false, v25/functions.cpp:2950-3148,3282-3324:
    labels into s->clust, draws from ran.  Returns the number of clusters. */
 int mdsc_or_clust_conf(mdsc_oracle_state* s, double min_s, mdsc_mt19937* ran);
+/* energy criterion (an extension): pair energy, lower index A; labelling over
+   bonds U_pair < -u_bond */
+double mdsc_or_pair_energy(const mdsc_oracle_state* s, int A, int B);
+int mdsc_or_clust_energy(mdsc_oracle_state* s, double u_bond, mdsc_mt19937* ran);
 
 /* heap generator handles for callers without the struct layout */
 void* mdsc_or_rng_new(unsigned long seed);
 double mdsc_or_rng_uniform(void* g);
 void mdsc_or_rng_free(void* g);
 int mdsc_or_clust_conf_rng(mdsc_oracle_state* s, double min_s, void* g);
+int mdsc_or_clust_energy_rng(mdsc_oracle_state* s, double u_bond, void* g);
 
 /* One MD step of the reference driver's loop body, v25/main.cpp:520-708
    (no file output).  The context keeps what the driver keeps between
