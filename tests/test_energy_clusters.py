@@ -157,16 +157,21 @@ def test_gpu_energy_labels_equal_oracle(orc):
 
 @pytest.mark.gpu
 def test_gpu_energy_clusters_inside_the_step(orc):
-    """cl_fr = 5: the step's own clustering uses the system's criterion; the
-    labels after 5 steps are the oracle's on the state after those steps."""
+    """cl_fr = 5: the step's own clustering uses the system's criterion, on
+    the reference's schedule (step index % cl_fr == 0: after the 1st and the
+    6th step); labels equal the oracle's on the state after those steps, the
+    generator going on from one labelling to the next."""
     from mdspherocyl_gb300 import lib as L
 
     st, box, u = _cases()[0]
     spec = S.SystemSpec(n=len(st.length), box=box, alpha=6.0 / box[0], K_max=5, ksq_max=0, temp=1.0, cl_fr=5)
+    drawn = 0
     with L.Batch([spec], [st]) as bt:
         bt.set_cluster_energy(0, u)
-        bt.step(5)
-        d = bt.download(0)
-    after = S.SystemState(d["r"], d["p"], d["O"], d["l"], st.length, st.dia, st.mass, st.dip)
-    want, ncw, _ = orc.clust_energy(_osys(after, box), u, seed=1, skip=0)
-    assert np.array_equal(d["clust"], want)
+        for steps in (1, 5):
+            bt.step(steps)
+            d = bt.download(0)
+            after = S.SystemState(d["r"], d["p"], d["O"], d["l"], st.length, st.dia, st.mass, st.dip)
+            want, ncw, _ = orc.clust_energy(_osys(after, box), u, seed=1, skip=drawn)
+            assert np.array_equal(d["clust"], want), steps
+            drawn += ncw
