@@ -15,6 +15,11 @@ the packed state (r, p, O, l, F, T) from pinned memory, steps once and
 downloads it again.
 
   python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+                  [--workload replica_mix|c0|c1|c2]
+
+--workload c0/c1/c2 runs one system of the single-system configurations
+instead (N = 256, 4096, 32768; c2 clusters every 100 steps by pair energy,
+timed beside the steps).
 
 --impl reference times the reference's CPU routines (the C restatement in
 oracle/, all host threads) on a bounded sample of the same workload.
@@ -85,6 +90,29 @@ def build_mix(seed: int, nsys: int):
 
     ds = S.replica_mix_specs(n_systems=nsys, seed=seed)
     return [S.replica_system(d) for d in ds], ds
+
+
+# the single-system configurations: builder, description, energy-criterion
+# cluster threshold (kT) or None
+SINGLE = {
+    "c0": ("plain_c0", "N=256, phi=0.10, L ~ N(3, 0.3), mu^2=2 axial, alpha=5.6/L_box, |n|^2<=27", None),
+    "c1": ("plain_c1", "N=4096, phi=0.20, L ~ U[2, 5], mu ~ volume with <mu^2>=3, alpha=7/L_box, |n|^2<=64", None),
+    "c2": ("plain_c2", "N=32768, phi=0.15, mu^2=5, field mu B/kT=2 along z, L ~ N(3, 0.5), alpha=6/L_box, "
+                       "|n|^2<=100, clusters every 100 steps by pair energy < -1.5 kT", 1.5),
+}
+
+
+def build_workload(args, rank: int = 0):
+    """[(spec, state)] of the workload and its config entries."""
+    if args.workload == "replica_mix":
+        states, _ = build_mix(args.seed + 1000 * rank, args.systems)
+        return states, {"workload": "replica_mix", "ksq_max": 36, "alpha": "6/L_box"}
+    from mdspherocyl_gb300 import systems as S
+
+    fn, desc, _ = SINGLE[args.workload]
+    spec, st = getattr(S, fn)(seed=args.seed + 1000 * rank)
+    return [(spec, st)], {"workload": f"plain_{args.workload}", "description": desc, "ksq_max": spec.ksq_max,
+                          "alpha": float(spec.alpha), "box": float(spec.box[0])}
 
 
 class ClockSampler:
@@ -180,24 +208,29 @@ def run_reference(args):
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    states, _ = build_mix(args.seed, args.systems)
+    states, cfg = build_workload(args)
+    single = args.workload != "replica_mix"
     vals = []
     used, tt = [], 0.0
-    for it in range(args.warmup + args.steps):
-        v, used, tt = cpu_sample(states, threads, budget_s=args.cpu_budget / max(args.steps, 1))
-        if it >= args.warmup:
+    runs = (0, 1) if single else (args.warmup, args.steps)  # one full-size step is the bounded sample
+    for it in range(runs[0] + runs[1]):
+        v, used, tt = cpu_sample(states, threads, budget_s=args.cpu_budget / max(runs[1], 1),
+                                 stride=1 if single else 16)
+        if it >= runs[0]:
             vals.append(v)
     value = statistics.median(vals)
     sample = (f"oracle MD step (reference routines restated in C, OpenMP) on {len(used)} of "
               f"{len(states)} systems (every 16th, N={min(used)}..{max(used)}, {sum(used)} particles), "
-              f"one step each per timed step")
+              f"one step each per timed step") if not single else \
+        (f"oracle MD step (reference routines restated in C, OpenMP) on the whole system (N={used[0]}), "
+         f"one step")
+    cfg.update({"systems": len(states), "particles": int(sum(s.n for s, _ in states)),
+                "real_space": "all minimum-image pairs"})
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * tt, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "replica_mix", "systems": len(states),
-                   "particles": int(sum(s.n for s, _ in states)), "ksq_max": 36,
-                   "real_space": "all minimum-image pairs"},
+        "config": cfg,
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -246,12 +279,16 @@ def run_ours(args):
     from mdspherocyl_gb300 import lib as L
 
     t0 = time.time()
-    states, _ = build_mix(args.seed + 1000 * rank, args.systems)
+    states, cfg = build_workload(args, rank)
+    single = args.workload != "replica_mix"
     specs = [s for s, _ in states]
     sts = [st for _, st in states]
     ntot = int(sum(s.n for s in specs))
     log(f"[rank {rank}] workload built in {time.time() - t0:.1f}s: {len(specs)} systems, {ntot} particles")
     bt = L.Batch(specs, sts, device=device)
+    u_bond = SINGLE[args.workload][2] if single else None
+    if u_bond:
+        bt.set_cluster_energy(0, u_bond)
     stream = torch.cuda.ExternalStream(bt.lib.mdsc_stream(bt.h), device=device)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{device}")
 
@@ -280,10 +317,27 @@ def run_ours(args):
     value = ntot_all * args.steps / t_dev
     obs = bt.observe()
     st_ok = all(o["status"] == 0 for o in obs)
+    clustering = None
+    if single and specs[0].cl_fr > 0:
+        # the clusterings the step runs every cl_fr steps are outside the
+        # device-timed graph launches: timed here, host clock around a
+        # synchronous mdsc_clust_conf (bonds, union-find, label replay)
+        bt.clust_conf(0)
+        tc = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            _, ncl = bt.clust_conf(0)
+            tc.append(time.perf_counter() - t0)
+        c_ms = 1e3 * statistics.median(tc)
+        per_step = c_ms / specs[0].cl_fr
+        clustering = {"every": specs[0].cl_fr, "criterion": f"pair energy < -{u_bond} kT" if u_bond else "geometric",
+                      "ms_per_clustering": c_ms, "clusters": ncl,
+                      "value_with_clustering": ntot * args.steps / (t_dev + args.steps * per_step / 1e3)}
 
     # ---- the plain path: one system per launch sequence, one after another ----
     plain = None
-    if not args.no_plain and ws == 1:  # the batched-vs-plain ratio is a one-GPU figure
+    if not args.no_plain and ws == 1 and not single:  # the batched-vs-plain ratio: a one-GPU, mix figure
         singles = [L.Batch([sp], [st], device=device) for sp, st in zip(specs, sts)]
         for b1 in singles:
             b1.step(2)
@@ -347,27 +401,29 @@ def run_ours(args):
     e2e = ntot_all * e2e_steps / t_e2e
     launches = bt.launches_per_step + 1  # + the per-call reset of the noise row
     bt.close()
-    serving = run_serving(args, device) if (args.jobs > 0 and ws == 1) else None
+    serving = run_serving(args, device) if (args.jobs > 0 and ws == 1 and not single) else None
 
     out = None
     if rank == 0:
         cpu = None
         if not args.no_cpu and ws == 1:
             threads = os.cpu_count() or 1
-            v, used, tt = cpu_sample(states, threads, budget_s=args.cpu_budget)
+            v, used, tt = cpu_sample(states, threads, budget_s=args.cpu_budget, stride=1 if single else 16)
             cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": (f"oracle MD step (reference routines restated in C, OpenMP, {threads} threads) "
                               f"on every 16th system of the mix ({len(used)} systems, N={min(used)}..{max(used)}, "
-                              f"{sum(used)} particles), one step each, {tt:.1f}s")}
+                              f"{sum(used)} particles), one step each, {tt:.1f}s") if not single else
+                             (f"oracle MD step (reference routines restated in C, OpenMP, {threads} threads) "
+                              f"on the whole system (N={used[0]}), one step, {tt:.1f}s")}
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair/k-space arithmetic, f64 state and sums",
             "data": "synthetic",
-            "config": {"workload": "replica_mix", "systems": len(specs) * ws, "particles": int(ntot_all),
+            "config": {**cfg, "systems": len(specs) * ws, "particles": int(ntot_all),
                        "particles_rank0": ntot,
-                       "N_range": [min(s.n for s in specs), max(s.n for s in specs)], "ksq_max": 36,
-                       "alpha": "6/L_box", "real_space": "all minimum-image pairs", "dt": 1e-3,
+                       "N_range": [min(s.n for s in specs), max(s.n for s in specs)],
+                       "real_space": "all minimum-image pairs", "dt": 1e-3,
                        "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{ws}",
                        "graph": "one CUDA graph per step", "launch_mappings": tuning},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": bytes_h2d,
@@ -385,6 +441,7 @@ def run_ours(args):
             "kernel_ms": prof,
             "plain_gpu": plain,
             "serving": serving,
+            "clustering": clustering,
             "clocks": clocks,
             "status_ok": st_ok,
         }
@@ -404,6 +461,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--systems", type=int, default=256)
+    ap.add_argument("--workload", default="replica_mix", choices=["replica_mix", *SINGLE],
+                    help="replica_mix: the 256-system mix (the headline); c0/c1/c2: one system of that config")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")

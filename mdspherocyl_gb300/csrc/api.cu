@@ -71,7 +71,8 @@ struct Layout {
   size_t rtab_n = 0;         // float4 slots the tables take (2 per entry)
   std::vector<double> kval, kpre, kvec;
   std::vector<int2> blk, kowner;
-  int ntot = 0, ndtot = 0, nktot = 0, maxnd = 0, nchunks = 0;
+  std::vector<int2> bstrips;  // strips of the systems whose tile energies are summed per strip
+  int ntot = 0, ndtot = 0, nktot = 0, maxnd = 0, nchunks = 0, nstrips = 0;
   long long rpart = 0, kpart = 0;
   bool multi = false;
 };
@@ -258,12 +259,16 @@ void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
     P.part_off = part;
     P.dip_off = dip;
     P.nstrip = cdiv(P.ndip, kTile);
+    P.strip_off = Lo.nstrips;
+    Lo.nstrips += P.nstrip;
     P.pp_off = pp;
     pp += (long long)P.nstrip * P.nstrip * 6 * kTile;
     P.tile_off = (int)Lo.tiles.size();
     for (int I = 0; I < P.nstrip; ++I)
       for (int J = I; J < P.nstrip; ++J) Lo.tiles.push_back(make_int4(s, I, J, 0));
     P.ntile = (int)Lo.tiles.size() - P.tile_off;
+    if (P.nstrip > kStripRows)
+      for (int X = 0; X < P.nstrip; ++X) Lo.bstrips.push_back(make_int2(s, X));
     // k-vectors and their prefactors (wave_v, v25/functions.cpp:1963-1990)
     P.k_off = (int)Lo.kn.size();
     std::vector<int4> kn;
@@ -400,6 +405,8 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   b.rpart = A.take<float>(std::max<long long>(Lo.rpart, 1));
   b.rsum = A.take<float2>(6 * (size_t)std::max(Lo.ndtot, 1));
   b.tileE = A.take<float>(10 * nt);
+  b.stripE = A.take<double>(10 * (size_t)std::max(Lo.nstrips, 1));
+  b.bstrips = A.take<int2>(std::max<size_t>(Lo.bstrips.size(), 1));
   b.tiles = A.take<int4>(nt);
   b.wlist = A.take<int2>(n * kMaxC);
   b.wlist_n = A.take<int>(1);
@@ -649,7 +656,7 @@ mdsc_status capture_step(mdsc_batch* B, int which) {
   launches += 4;
   launch_real_pairs(b, B->lo.multi, B->s2);
   launch_real_sum(b, B->s2);
-  launches += b.ntiles > 0 ? 2 : 0;
+  launches += b.ntiles > 0 ? 2 + (b.nbstrips > 0 ? 1 : 0) : 0;
   launch_kspace(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, B->s3);
   launches += b.nktot > 0 ? 3 : 0;
   cudaEventRecord(B->ev_j2, B->s2);
@@ -980,6 +987,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   b.ndtot = lo.ndtot;
   b.nktot = lo.nktot;
   b.ntiles = (int)lo.tiles.size();
+  b.nbstrips = (int)lo.bstrips.size();
   b.nblk = (int)lo.blk.size();
   b.noise = B->noise[0];
   // The step graph forks the real-space tiles (stream s2) from the WCA and
@@ -1007,6 +1015,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   };
   up((void*)b.sys, lo.sys.data(), sizeof(SysDev) * nsys);
   up(b.tiles, lo.tiles.data(), sizeof(int4) * lo.tiles.size());
+  if (!lo.bstrips.empty()) up(b.bstrips, lo.bstrips.data(), sizeof(int2) * lo.bstrips.size());
   up(b.blk, lo.blk.data(), sizeof(int2) * lo.blk.size());
   up(b.kn, lo.kn.data(), sizeof(int4) * lo.kn.size());
   up(b.kv, lo.kv.data(), sizeof(float4) * lo.kv.size());
@@ -1033,6 +1042,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   cudaMemsetAsync(b.nbc, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.wcnt, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.wincnt, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
+  cudaMemsetAsync(b.stripE, 0, sizeof(double) * 10 * std::max(lo.nstrips, 1), B->st);
   cudaMemsetAsync(b.kgcnt, 0, sizeof(int) * std::max(nsys, 1), B->st);
   cudaMemsetAsync(b.icnt, 0, sizeof(int) * std::max(nsys, 1), B->st);
   cudaMemsetAsync(b.F, 0, sizeof(double) * 3 * std::max(lo.ntot, 1), B->st);

@@ -514,14 +514,19 @@ __global__ void __launch_bounds__(kRedThreads) reduce_obs_kernel(Batch b, int mo
   for (int c = 0; c < 12; ++c) v[c].hi = v[c].lo = 0.f;
   {
     // the rows of one per-system table, column by column: real-space tiles
-    // (U, PT; FP32), k-vectors (U, PT), WCA blocks (U, W, PT), kinetic
+    // (U, PT; FP32) or, in large systems, strips (each strip's tiles summed
+    // in float-float by strip_energy), k-vectors (U, PT), WCA blocks (U, W, PT), kinetic
     // blocks (K_t, K_r, PT_kin, U_ext) or order-parameter blocks.  One code
     // path for the five keeps the kernel small: its blocks are short, and a
     // larger kernel waited on instruction fetch.
     const float* fsrc = nullptr;
     const double* dsrc = nullptr;
     int nrow, ncol;
-    if (grp == 0) {
+    if (grp == 0 && P.nstrip > kStripRows) {  // the strips' sums of their tiles (strip_energy)
+      dsrc = b.stripE + (long long)P.strip_off * 10;
+      nrow = P.nstrip;
+      ncol = 10;
+    } else if (grp == 0) {  // the tiles themselves
       fsrc = b.tileE + (long long)P.tile_off * 10;
       nrow = P.ntile;
       ncol = 10;

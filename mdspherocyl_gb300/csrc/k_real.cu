@@ -54,6 +54,7 @@
 // x = 9.35 exp(-x^2) is below the FP32 range and both terms are 0, as the
 // reference's table is there to FP32 precision.
 #include "mdsc_dev.cuh"
+#include "reduce.cuh"
 
 namespace mdsc {
 
@@ -542,9 +543,39 @@ __global__ void __launch_bounds__(512) real_sum_kernel(Batch b) {
   }
 }
 
+// Energy rows of the strips of large systems (more than kStripRows strips):
+// a warp per strip X sums the tile energies (U, PT) of the tiles (X, J >= X),
+// lanes over J (J = X + lane, + 32, ...), float-float, then a shuffle tree
+// -- lane 0's sums are in a fixed order.  The per-system sum then adds one
+// row per strip instead of one per tile.
+__global__ void __launch_bounds__(128) strip_energy_kernel(Batch b) {
+  const int w = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (w >= b.nbstrips) return;
+  const int2 sx = b.bstrips[w];
+  const SysDev& P = b.sys[sx.x];
+  const int X = sx.y, ns = P.nstrip;
+  const long long t0 = P.tile_off + (long long)X * ns - (long long)X * (X - 1) / 2;
+  FF acc[10];
+#pragma unroll
+  for (int c = 0; c < 10; ++c) acc[c] = ff_of(0.f);
+  for (int J = X + lane; J < ns; J += 32) {
+    const float* e = b.tileE + (t0 + (J - X)) * 10;
+#pragma unroll
+    for (int c = 0; c < 10; ++c) acc[c] = ff_add(acc[c], ff_of(e[c]));
+  }
+#pragma unroll
+  for (int c = 0; c < 10; ++c) acc[c] = ff_warp_sum(acc[c]);
+  if (lane == 0) {  // hi + lo in FP64 keeps the float-float value; the per-system sum splits it back
+    double* out = b.stripE + (long long)(P.strip_off + X) * 10;
+#pragma unroll
+    for (int c = 0; c < 10; ++c) out[c] = soft_f2d(acc[c].hi) + soft_f2d(acc[c].lo);
+  }
+}
+
 void launch_real_sum(const Batch& b, cudaStream_t s) {
   if (b.ntiles == 0 || b.nblk == 0) return;
   real_sum_kernel<<<b.nblk, b.tune.rsum_threads, 0, s>>>(b);
+  if (b.nbstrips) strip_energy_kernel<<<cdiv(b.nbstrips, 4), 128, 0, s>>>(b);
 }
 
 void launch_real_pairs(const Batch& b, bool multi, cudaStream_t s) {

@@ -15,6 +15,9 @@ constexpr int kMaxD = 4;         // dipoles per particle (MDSC_MAX_DIPOLES)
 constexpr int kPartBlock = 128;  // threads per block of the per-particle kernels
 constexpr int kKBlock = 128;     // k-vectors per block of the k-space kernels
 constexpr int kKChunk = 256;     // particles per block of the structure-factor kernel
+// systems of more strips than this sum their real-space tile energies per
+// strip first (real_sum); smaller ones are summed tile by tile
+constexpr int kStripRows = 32;
 constexpr int kMaxC = 16;        // WCA contact candidates of higher index per particle
 
 // status bits (OR-ed per system; mapped to mdsc_status on the host)
@@ -45,6 +48,7 @@ struct SysDev {
   int part_off;   // first particle of the system in the batch arrays
   int dip_off;    // first dipole
   int nstrip;     // ceil(ndip / kTile)
+  int strip_off;  // first strip of the system in the per-strip energy rows
   long long pp_off;  // real-space partials: nstrip*nstrip*6*kTile floats
   int tile_off, ntile;  // tile list range
   int k_off, nk;        // k-vector range
@@ -155,6 +159,9 @@ struct Batch {
   const float4* rtab;  // 2 per entry: (A, B, C, dA), (dB, dC, 0, 0); see k_real.cu
   float2* rsum;  // 6 * ndtot: each dipole's real-space force and torque over all strips, float-float, component-major
   float* tileE;  // 10 per tile: U, PT[9]
+  double* stripE; // 10 per strip: U, PT[9] of the strip's tiles (I, J >= I) (a float-float sum, hi + lo in FP64)
+  int2* bstrips;  // (system, strip) of every strip of the systems of more than kStripRows strips
+  int nbstrips;
   int4* tiles;   // (sys, I, J, 0)
   int2* wlist;   // WCA work list: (candidate slot, system), n * kMaxC at most
   int* wlist_n;  // its length this step
