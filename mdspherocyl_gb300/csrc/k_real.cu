@@ -362,9 +362,12 @@ __device__ __forceinline__ void diag_loop(const PairConst& K, Lane2& s, const ui
 // block size changes how tiles are grouped for scheduling, never what a
 // tile computes, so every W gives the same bits (the autotuner picks W).
 // TAB: interpolate in the reference's table (the batch path); otherwise the
-// analytic terms with the table's error added (callers without the table)
+// analytic terms with the table's error added (callers without the table).
+// 20 warps per SM hold the kernel to 96 registers (16 B of spills) from
+// 126: the table lookups' latency is hidden by warps, and 21 warps instead
+// of 16 made the table form 3% faster on the 256-replica mix.
 template <bool MULTI, int W, bool TAB>
-__global__ void __launch_bounds__(32 * W) real_pairs_kernel(Batch b) {
+__global__ void __launch_bounds__(32 * W, 20 / W) real_pairs_kernel(Batch b) {
   __shared__ uint4 sj_all[W][kTile];    // fixed-point x, y, z and owner of the j-dipoles
   __shared__ float4 smj_all[W][kTile];  // their moments
   __shared__ float4 sa4_all[W][kTile];  // j-side sums: F x, y, z and T x
