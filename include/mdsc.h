@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define MDSC_ABI_VERSION 2  /* 2: mdsc_observables gained G1, G2, M */
+#define MDSC_ABI_VERSION 3  /* 2: mdsc_observables gained G1, G2, M; 3: mdsc_system_desc.rc_real */
 #define MDSC_MAX_DIPOLES 4 /* dipoles per particle */
 
 typedef enum {
@@ -78,6 +78,13 @@ typedef struct {
   unsigned long thermo_seed[2]; /* MT19937 seeds of the two thermostats (1, 2 in the driver) */
   unsigned long cluster_seed;   /* MT19937 seed of the cluster generator (1 in the driver) */
   unsigned long cluster_skip;   /* draws already taken from it (e.g. by initialisation) */
+  /* Real-space cutoff.  0: every minimum-image dipole pair, as the reference
+     sums (v25/functions.cpp:1570-1672).  > 0: the reference's force_dipR
+     with its table zeroed beyond rc_real -- entries k with Lh (k + 1) >
+     rc_real set to 0 (Lh = 0.5*200.2/32768, v25/functions.cpp:1563,1681),
+     so pairs beyond rc_real + Lh contribute nothing -- summed over a
+     neighbour list of the system's rods instead of all pairs. */
+  double rc_real;
 } mdsc_system_desc;
 
 /* Host-side structure-of-arrays view of one system (FP64).  Shapes:
@@ -131,6 +138,10 @@ int mdsc_num_systems(const mdsc_batch* b);
 size_t mdsc_device_bytes(const mdsc_batch* b);
 /* GPU memory a batch of these systems would need, without creating it */
 size_t mdsc_estimate_bytes(const mdsc_system_desc* descs, int nsys);
+/* sizeof of the ABI's structures as this library was built (for bindings
+   that lay them out by hand): mdsc_system_desc, mdsc_host_state,
+   mdsc_observables, mdsc_view.  Any pointer may be NULL. */
+void mdsc_abi_sizes(size_t* desc, size_t* host_state, size_t* observables, size_t* view);
 /* human-readable detail of the last error on this handle */
 mdsc_status mdsc_last_error(const mdsc_batch* b, char* buf, size_t len);
 

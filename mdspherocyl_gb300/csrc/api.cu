@@ -21,6 +21,7 @@
 namespace mdsc {
 void launch_real_pairs(const Batch& b, bool multi, cudaStream_t s);
 void launch_real_sum(const Batch& b, cudaStream_t s);
+void launch_real_cut(const Batch& b, cudaStream_t s);
 void launch_kspace(const Batch& b, int maxnd, const int4* kwork, int nkwork, const int2* kowner,
                    double* kE, cudaStream_t s);
 void launch_derive(const Batch& b, cudaStream_t s);
@@ -73,6 +74,7 @@ struct Layout {
   std::vector<int2> blk, kowner;
   std::vector<int2> bstrips;  // strips of the systems whose tile energies are summed per strip
   int ntot = 0, ndtot = 0, nktot = 0, maxnd = 0, nchunks = 0, nstrips = 0;
+  bool any_rc = false;  // some system sums its real space over a neighbour list
   long long rpart = 0, kpart = 0;
   bool multi = false;
 };
@@ -103,6 +105,10 @@ std::string check_desc(const mdsc_system_desc& d, int s) {
     }
   if (d.K_max < 1 || d.alpha <= 0 || d.dt <= 0 || d.Q <= 0) {
     snprintf(buf, sizeof buf, "system %d: K_max, alpha, dt and Q must be positive", s);
+    return buf;
+  }
+  if (!(d.rc_real >= 0.0)) {
+    snprintf(buf, sizeof buf, "system %d: rc_real must be 0 (all pairs) or positive", s);
     return buf;
   }
   const double hd = 0.5 * std::sqrt(d.box[0] * d.box[0] + d.box[1] * d.box[1] + d.box[2] * d.box[2]);
@@ -152,10 +158,15 @@ void set_pair_consts(SysDev& P) {
 }
 
 // One system's table as stored on the device: per entry (A, B, C, dA) and
-// (dB, dC, 0, 0), the differences to the next entry.
-std::vector<float4> table_entries(double alpha, int n) {
+// (dB, dC, 0, 0), the differences to the next entry.  rc > 0: the entries
+// beyond the real-space cutoff zeroed (Lh (k + 1) > rc), before the
+// differences are taken.
+std::vector<float4> table_entries(double alpha, int n, double rc) {
   std::vector<double> T(3 * (size_t)(n + 1));
   table_values(alpha, n + 1, T.data());
+  if (rc > 0)
+    for (int k = 0; k <= n; ++k)
+      if (0.5 * (200 * 1.001) * (k + 1) / 32768 > rc) T[3 * (size_t)k] = T[3 * (size_t)k + 1] = T[3 * (size_t)k + 2] = 0.0;
   std::vector<float4> e(2 * (size_t)n);
   for (int k = 0; k < n; ++k) {
     const double* a = &T[3 * (size_t)k];
@@ -173,7 +184,7 @@ std::vector<float4> table_entries(double alpha, int n) {
 constexpr size_t kTableCacheBytes = size_t(256) << 20;
 struct TableCache {
   std::mutex mu;
-  std::map<std::pair<uint64_t, int>, std::pair<std::vector<float4>, uint64_t>> m;  // -> (entries, last use)
+  std::map<std::tuple<uint64_t, uint64_t, int>, std::pair<std::vector<float4>, uint64_t>> m;  // -> (entries, last use)
   uint64_t clock = 0;
   size_t bytes = 0;
 };
@@ -183,15 +194,16 @@ void fill_tables(const mdsc_system_desc* descs, Layout& Lo) {
   Lo.rtab.assign(Lo.rtab_n, make_float4(0.f, 0.f, 0.f, 0.f));
   const int nsys = (int)Lo.sys.size();
   auto key_of = [&](int s) {
-    uint64_t a;
+    uint64_t a, c;
     memcpy(&a, &descs[s].alpha, 8);
-    return std::make_pair(a, Lo.sys[s].rt_n);
+    memcpy(&c, &descs[s].rc_real, 8);
+    return std::make_tuple(a, c, Lo.sys[s].rt_n);
   };
   // systems whose table is not cached: build them on all host threads
   std::vector<int> miss;
   {
     std::lock_guard<std::mutex> g(g_tables.mu);
-    std::map<std::pair<uint64_t, int>, int> first;
+    std::map<std::tuple<uint64_t, uint64_t, int>, int> first;
     for (int s = 0; s < nsys; ++s) {
       if (descs[s].nd <= 0) continue;
       const auto k = key_of(s);
@@ -210,7 +222,7 @@ void fill_tables(const mdsc_system_desc* descs, Layout& Lo) {
     std::atomic<int> next{0};
     auto work = [&] {
       for (int q; (q = next.fetch_add(1)) < (int)miss.size();)
-        built[q] = table_entries(descs[miss[q]].alpha, Lo.sys[miss[q]].rt_n);
+        built[q] = table_entries(descs[miss[q]].alpha, Lo.sys[miss[q]].rt_n, descs[miss[q]].rc_real);
     };
     std::vector<std::thread> th;
     for (int t = 1; t < nth; ++t) th.emplace_back(work);
@@ -239,7 +251,7 @@ void fill_tables(const mdsc_system_desc* descs, Layout& Lo) {
     if (it != g_tables.m.end()) {
       std::copy(it->second.first.begin(), it->second.first.end(), Lo.rtab.begin() + 2 * (size_t)Lo.sys[s].rt_off);
     } else {  // evicted at once (cache smaller than this batch's tables): build here
-      const std::vector<float4> e = table_entries(descs[s].alpha, Lo.sys[s].rt_n);
+      const std::vector<float4> e = table_entries(descs[s].alpha, Lo.sys[s].rt_n, descs[s].rc_real);
       std::copy(e.begin(), e.end(), Lo.rtab.begin() + 2 * (size_t)Lo.sys[s].rt_off);
     }
   }
@@ -258,7 +270,10 @@ void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
     P.ndip = d.n * d.nd;
     P.part_off = part;
     P.dip_off = dip;
-    P.nstrip = cdiv(P.ndip, kTile);
+    // the all-pairs tiles (rc_real = 0) or the neighbour-list pass (rc_real > 0)
+    P.rc_real = d.rc_real;
+    if (d.rc_real > 0) Lo.any_rc = true;
+    P.nstrip = d.rc_real > 0 ? 0 : cdiv(P.ndip, kTile);
     P.strip_off = Lo.nstrips;
     Lo.nstrips += P.nstrip;
     P.pp_off = pp;
@@ -407,6 +422,9 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   b.tileE = A.take<float>(10 * nt);
   b.stripE = A.take<double>(10 * (size_t)std::max(Lo.nstrips, 1));
   b.bstrips = A.take<int2>(std::max<size_t>(Lo.bstrips.size(), 1));
+  b.rnb = A.take<int>(Lo.any_rc ? n * kMaxR : 1);
+  b.rnbc = A.take<int>(n);
+  b.rlE = A.take<double>(10 * nb);
   b.tiles = A.take<int4>(nt);
   b.wlist = A.take<int2>(n * kMaxC);
   b.wlist_n = A.take<int>(1);
@@ -523,6 +541,7 @@ mdsc_status eval_forces(mdsc_batch* B, int force_list) {
   Batch b = batch_with_noise(B, 0);
   launch_derive(b, B->st);
   launch_list_build(b, force_list, B->st);
+  launch_real_cut(b, B->st);
   launch_wca(b, B->st);
   launch_real_pairs(b, B->lo.multi, B->st);
   launch_real_sum(b, B->st);
@@ -652,13 +671,14 @@ mdsc_status capture_step(mdsc_batch* B, int which) {
   cudaStreamWaitEvent(B->s3, B->ev_fork, 0);
   launch_order_terms(b, B->st);
   launch_list_build(b, 0, B->st);
+  launch_real_cut(b, B->st);  // systems with a real-space cutoff: after their list
   launch_wca(b, B->st);
-  launches += 4;
+  launches += 4 + (b.any_rc ? 1 : 0);
   launch_real_pairs(b, B->lo.multi, B->s2);
   launch_real_sum(b, B->s2);
   launches += b.ntiles > 0 ? 2 + (b.nbstrips > 0 ? 1 : 0) : 0;
   launch_kspace(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, B->s3);
-  launches += b.nktot > 0 ? 3 : 0;
+  launches += b.nktot > 0 ? (B->lo.maxnd > 1 ? 5 : 3) : 0;  // multi-dipole batches: both ksum and kgather forms
   cudaEventRecord(B->ev_j2, B->s2);
   cudaEventRecord(B->ev_j3, B->s3);
   cudaStreamWaitEvent(B->st, B->ev_j2, 0);
@@ -988,6 +1008,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   b.nktot = lo.nktot;
   b.ntiles = (int)lo.tiles.size();
   b.nbstrips = (int)lo.bstrips.size();
+  b.any_rc = lo.any_rc ? 1 : 0;
   b.nblk = (int)lo.blk.size();
   b.noise = B->noise[0];
   // The step graph forks the real-space tiles (stream s2) from the WCA and
@@ -1043,6 +1064,8 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   cudaMemsetAsync(b.wcnt, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.wincnt, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.stripE, 0, sizeof(double) * 10 * std::max(lo.nstrips, 1), B->st);
+  cudaMemsetAsync(b.rnbc, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
+  cudaMemsetAsync(b.rlE, 0, sizeof(double) * 10 * std::max<size_t>(lo.blk.size(), 1), B->st);
   cudaMemsetAsync(b.kgcnt, 0, sizeof(int) * std::max(nsys, 1), B->st);
   cudaMemsetAsync(b.icnt, 0, sizeof(int) * std::max(nsys, 1), B->st);
   cudaMemsetAsync(b.F, 0, sizeof(double) * 3 * std::max(lo.ntot, 1), B->st);
@@ -1166,6 +1189,15 @@ static mdsc_status upload_one(mdsc_batch* B, int s, const mdsc_host_state* h, bo
     Pm.sig_max = dmax;
     Pm.skin = 0.9 * dmin;
     Pm.r_list = std::max(1.122462048309373 * dmax, dmax + B->desc[s].min_s) + Pm.skin;
+    if (Pm.rc_real > 0) {
+      // real-space neighbours: rods whose centres are within rc + Lh (the
+      // last table interval) + the dipoles' offsets + the skin, with room
+      // for the FP32 centre distance
+      double e = 0;
+      for (int g = 0; g < nd; ++g) e = std::max(e, std::fabs(dpc[g]));
+      const double rr = (Pm.rc_real + kLh + 2 * e + Pm.skin) * 1.0001 + 1e-4;
+      Pm.rl_r2 = (float)(rr * rr);
+    }
     Pm.Uself = Uself;
     CU(up((void*)(b.sys + s), &Pm, sizeof(SysDev)));
     if (B->uploaded[s]) {
@@ -1334,6 +1366,8 @@ mdsc_status mdsc_force_dipR(mdsc_batch* B, double* U, double* PT) {
   mdsc_status st = need_state(B);
   if (st) return st;
   launch_derive(B->b, B->st);
+  if (B->b.any_rc) launch_list_build(B->b, 0, B->st);
+  launch_real_cut(B->b, B->st);
   launch_real_pairs(B->b, B->lo.multi, B->st);
   launch_real_sum(B->b, B->st);
   launch_finalize(B->b, kMaskReal | kFlagAccum, B->st);
@@ -1481,6 +1515,13 @@ mdsc_status mdsc_set_cluster_energy(mdsc_batch* B, int sys, double u_bond_kT) {
   CU(cudaMemcpyAsync((void*)(B->b.sys + sys), &P, sizeof(SysDev), cudaMemcpyHostToDevice, B->st));
   CU(cudaStreamSynchronize(B->st));
   return MDSC_OK;
+}
+
+void mdsc_abi_sizes(size_t* desc, size_t* host_state, size_t* observables, size_t* view) {
+  if (desc) *desc = sizeof(mdsc_system_desc);
+  if (host_state) *host_state = sizeof(mdsc_host_state);
+  if (observables) *observables = sizeof(mdsc_observables);
+  if (view) *view = sizeof(mdsc_view);
 }
 
 // ---- observables outside the step ---------------------------------------
@@ -1777,6 +1818,7 @@ mdsc_status mdsc_transfer(mdsc_batch* D, int dsys, mdsc_batch* S, int ssys) {
   Pd.r_list = Ps.r_list;
   Pd.Uself = Ps.Uself;
   Pd.cl_mode = Ps.cl_mode;
+  Pd.rl_r2 = Ps.rl_r2;
   Pd.cl_ubond = Ps.cl_ubond;
   CU(cudaMemcpyAsync((void*)(b.sys + dsys), &Pd, sizeof(SysDev), cudaMemcpyHostToDevice, D->st));
   SysState st;
@@ -1976,9 +2018,9 @@ mdsc_status mdsc_profile_steps(mdsc_batch* B, int nsteps, int max_kernels, char*
   cudaSetDevice(B->device);
   mdsc_status st = ensure_forces(B);
   if (st) return st;
-  const char* kn[11] = {"integrate_first", "order_terms", "list_build", "wca", "real_pairs", "real_sum",
-                        "kspace_sum", "kspace_combine", "kspace_gather", "finalize", "reduce_obs"};
-  const int nk = 11;
+  const char* kn[12] = {"integrate_first", "order_terms", "list_build", "wca", "real_pairs", "real_sum",
+                        "real_cut", "kspace_sum", "kspace_combine", "kspace_gather", "finalize", "reduce_obs"};
+  const int nk = 12;
   std::vector<cudaEvent_t> ev(nk + 1);
   for (auto& e : ev) cudaEventCreate(&e);
   std::vector<double> acc(nk, 0.0);
@@ -2000,17 +2042,19 @@ mdsc_status mdsc_profile_steps(mdsc_batch* B, int nsteps, int max_kernels, char*
     cudaEventRecord(ev[5], B->st);
     launch_real_sum(b, B->st);
     cudaEventRecord(ev[6], B->st);
+    launch_real_cut(b, B->st);
+    cudaEventRecord(ev[7], B->st);
     // the three k-space kernels, timed one by one
     launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 0, B->st);
-    cudaEventRecord(ev[7], B->st);
-    launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 1, B->st);
     cudaEventRecord(ev[8], B->st);
-    launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 2, B->st);
+    launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 1, B->st);
     cudaEventRecord(ev[9], B->st);
-    launch_finalize(b, kMaskAll | kFlagMoveP, B->st);
+    launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 2, B->st);
     cudaEventRecord(ev[10], B->st);
-    launch_reduce_obs(b, kRedStep, B->st);
+    launch_finalize(b, kMaskAll | kFlagMoveP, B->st);
     cudaEventRecord(ev[11], B->st);
+    launch_reduce_obs(b, kRedStep, B->st);
+    cudaEventRecord(ev[12], B->st);
     CU(cudaStreamSynchronize(B->st));
     for (int k = 0; k < nk; ++k) {
       float t = 0;

@@ -522,7 +522,11 @@ __global__ void __launch_bounds__(kRedThreads) reduce_obs_kernel(Batch b, int mo
     const float* fsrc = nullptr;
     const double* dsrc = nullptr;
     int nrow, ncol;
-    if (grp == 0 && P.nstrip > kStripRows) {  // the strips' sums of their tiles (strip_energy)
+    if (grp == 0 && P.rc_real > 0.0) {  // the neighbour pass's block sums (real_cut)
+      dsrc = b.rlE + (long long)P.blk_off * 10;
+      nrow = P.nblk;
+      ncol = 10;
+    } else if (grp == 0 && P.nstrip > kStripRows) {  // the strips' sums of their tiles (strip_energy)
       dsrc = b.stripE + (long long)P.strip_off * 10;
       nrow = P.nstrip;
       ncol = 10;

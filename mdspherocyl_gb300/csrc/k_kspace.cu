@@ -47,6 +47,7 @@ __global__ void __launch_bounds__(kKBlock) ksum_kernel(Batch b, const int4* __re
   __shared__ double shG[6 * kKBlock / 32];
   const int4 w = kwork[blockIdx.x];
   const SysDev& P = b.sys[w.x];
+  if (ND > 1 && P.nd <= 1) return;  // single-dipole systems: ksum1_kernel
   const int chunk = w.y;
   const int kl = w.z * kKBlock + threadIdx.x;
   const int ND_all = b.ndtot;
@@ -137,6 +138,7 @@ __global__ void __launch_bounds__(kKBlock / 2) ksum1_kernel(Batch b, const int4*
   __shared__ double shG[6 * (kKBlock / 2) / 32];
   const int4 w = kwork[blockIdx.x];
   const SysDev& P = b.sys[w.x];
+  if (P.nd != 1) return;  // other systems: ksum_kernel<ND>
   const int chunk = w.y;
   const int t = threadIdx.x;
   const int kl0 = w.z * kKBlock + t, kl1 = kl0 + kKBlock / 2;
@@ -212,10 +214,10 @@ __global__ void __launch_bounds__(kKBlock / 2) ksum1_kernel(Batch b, const int4*
 
 template <int ND>
 static void launch_ksum(const Batch& b, const int4* kwork, int nkwork, cudaStream_t s) {
-  if (ND == 1)
-    ksum1_kernel<<<nkwork, kKBlock / 2, 0, s>>>(b, kwork);
-  else
-    ksum_kernel<ND><<<nkwork, kKBlock, 0, s>>>(b, kwork);
+  // every single-dipole system through the single-dipole kernel, in any
+  // batch, so that it gives the same bits alone and beside multi-dipole ones
+  ksum1_kernel<<<nkwork, kKBlock / 2, 0, s>>>(b, kwork);
+  if (ND > 1) ksum_kernel<ND><<<nkwork, kKBlock, 0, s>>>(b, kwork);
 }
 
 // one thread per k over the whole batch: chunk sums in FP64, S(k), and the
@@ -227,7 +229,10 @@ __global__ void kcombine_kernel(Batch b, const int2* __restrict__ kowner, double
   const int2 ow = kowner[k];  // (system, k index within the system)
   const SysDev& P = b.sys[ow.x];
   const int kl = ow.y;
-  const int nv = ND == 1 ? 6 : 10;
+  // single-dipole systems (all of them when ND = 1): 6 sums per chunk and
+  // the self terms from the moment tensor, as ksum1_kernel leaves them
+  const bool one = ND == 1 || P.nd == 1;
+  const int nv = one ? 6 : 10;
   // chunk sums in float-float (FP32 instructions; ~48 bits), then FP64
   FF sf[10];
 #pragma unroll
@@ -247,7 +252,7 @@ __global__ void kcombine_kernel(Batch b, const int2* __restrict__ kowner, double
 #pragma unroll
   for (int c = 0; c < 10; ++c) s[c] = c < nv ? soft_f2d(sf[c].hi) + soft_f2d(sf[c].lo) : 0.0;
   const double kx = b.kvec[3 * k], ky = b.kvec[3 * k + 1], kz = b.kvec[3 * k + 2];
-  if (ND == 1) {
+  if (one) {
     const double* G = b.kGs + 6 * ow.x;
     const double gx = G[0] * kx + G[1] * ky + G[2] * kz;
     const double gy = G[1] * kx + G[3] * ky + G[4] * kz;
@@ -304,6 +309,7 @@ __global__ void __launch_bounds__(kPartBlock) kgather_kernel(Batch b) {
   __shared__ float2 sks[kKBlock];
   const int2 bk = b.blk[blockIdx.x];
   const SysDev& P = b.sys[bk.x];
+  if (ND > 1 && P.nd <= 1) return;  // single-dipole systems: kgather1 / kgather1s
   const int i = bk.y + threadIdx.x;  // batch particle index
   const bool ok = i < P.part_off + P.n;
   const int nd = P.nd;
@@ -412,6 +418,7 @@ __global__ void __launch_bounds__(kPartBlock / 2) kgather1_kernel(Batch b) {
   __shared__ float2 sks[kKBlock];
   const int2 bk = b.blk[blockIdx.x];
   const SysDev& P = b.sys[bk.x];
+  if (P.nd != 1) return;  // other systems: kgather_kernel<ND>
   const int t = threadIdx.x;
   const int i0 = bk.y + t, i1 = i0 + kPartBlock / 2;
   const int iend = P.part_off + P.n;
@@ -497,6 +504,7 @@ __global__ void __launch_bounds__(kPartBlock) kgather1s_kernel(Batch b) {
   __shared__ float2 sks[kKBlock];
   const int2 bk = b.blk[blockIdx.x];
   const SysDev& P = b.sys[bk.x];
+  if (P.nd != 1) return;  // other systems: kgather_kernel<ND>
   const int t = threadIdx.x;
   const int i0 = bk.y + t;
   const bool ok0 = i0 < P.part_off + P.n;
@@ -553,12 +561,11 @@ __global__ void __launch_bounds__(kPartBlock) kgather1s_kernel(Batch b) {
 
 template <int ND>
 static void launch_kgather(const Batch& b, cudaStream_t s) {
-  if (ND == 1 && b.tune.kg_scalar)
+  if (b.tune.kg_scalar)
     kgather1s_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
-  else if (ND == 1)
-    kgather1_kernel<<<b.nblk, kPartBlock / 2, 0, s>>>(b);
   else
-    kgather_kernel<ND><<<b.nblk, kPartBlock, 0, s>>>(b);
+    kgather1_kernel<<<b.nblk, kPartBlock / 2, 0, s>>>(b);
+  if (ND > 1) kgather_kernel<ND><<<b.nblk, kPartBlock, 0, s>>>(b);
 }
 
 template <int ND>

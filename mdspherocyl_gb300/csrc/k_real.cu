@@ -513,6 +513,107 @@ __global__ void __launch_bounds__(32 * W, 20 / W) real_pairs_kernel(Batch b) {
   }
 }
 
+// Real space over a neighbour list, for systems with a real-space cutoff:
+// the reference's force_dipR with its table zeroed beyond rc_real, where
+// pairs beyond rc_real + Lh add nothing, so only the rods the list holds
+// (centres within rc_real + Lh + the dipoles' offsets + the skin) are
+// visited.  One thread per dipole i takes its partner dipoles -- the listed
+// rods' dipoles, rods in ascending order -- two at a time through the
+// tiles' pair step (both halves holding dipole i) and keeps i's own force
+// and torque; every pair is met from both ends, so the energy and pressure
+// tensor take half of each meeting.  Per-dipole sums in list order: no
+// atomics, the same bits alone and in any batch.  Writes each dipole's
+// force and torque where real_sum writes them, and its block's energy and
+// pressure tensor (float-float block sums) for the per-system sum.
+__global__ void __launch_bounds__(kPartBlock) real_cut_kernel(Batch b) {
+  __shared__ double sh[10 * kPartBlock / 32];
+  const int2 bk = b.blk[blockIdx.x];
+  const SysDev& P = b.sys[bk.x];
+  if (P.rc_real <= 0.0) return;  // the same for the whole block
+  const int nd = P.nd;
+  const int p0 = bk.y - P.part_off;
+  const int np = min(kPartBlock, P.n - p0);
+  const int ND = b.ndtot;
+  PairConst K;
+  K.xh = b2(P.xh);
+  K.xlo = b2(P.xlo);
+  K.Lhx = b2(P.Lhi[0]);
+  K.Llx = b2(P.Llo[0]);
+  K.Lhy = b2(P.Lhi[1]);
+  K.Lly = b2(P.Llo[1]);
+  K.Lhz = b2(P.Lhi[2]);
+  K.Llz = b2(P.Llo[2]);
+  K.ahalf = b2(0.5f * P.alphaf);
+  K.gpref = b2(P.gpref);
+  K.a2 = b2(P.alpha2x2);
+  K.a4x4 = b2(P.alpha4x4);
+  K.invLh = b2(P.invLh);
+  K.ihh = b2(kInvLhHi);
+  K.ihl = b2(kInvLhLo);
+  K.tab = b.rtab + 2 * (long long)P.rt_off;
+  K.tn = P.rt_n;
+  K.halfLh2 = b2(P.halfLh2);
+  K.nsixthLh3 = b2(-P.sixthLh3);
+  FF e[10];
+#pragma unroll
+  for (int c = 0; c < 10; ++c) e[c] = ff_of(0.f);
+  for (int loc = threadIdx.x; loc < np * nd; loc += kPartBlock) {
+    const int il = p0 * nd + loc;  // dipole within the system
+    const int g = P.dip_off + il;
+    const int ip = P.part_off + il / nd;
+    Lane2 s;
+    s.x0 = s.x1 = b.dfx[g];
+    s.y0 = s.y1 = b.dfx[ND + g];
+    s.z0 = s.z1 = b.dfx[2 * ND + g];
+    s.mx = b2(b.dm[g]);
+    s.my = b2(b.dm[ND + g]);
+    s.mz = b2(b.dm[2 * ND + g]);
+    s.own0 = s.own1 = ip;
+    s.ok0 = s.ok1 = true;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) s.F[c] = s.T[c] = b2(0.f);
+#pragma unroll
+    for (int c = 0; c < 9; ++c) s.pt[c] = b2(0.f);
+    s.U = s.Uc = b2(0.f);
+    const int* lst = b.rnb + (long long)ip * kMaxR;
+    const int nj = b.rnbc[ip] * nd;
+    for (int k = 0; k < nj; k += 2) {
+      const bool two = k + 1 < nj;
+      const int k1 = two ? k + 1 : k;
+      const int ga = P.dip_off + (lst[k / nd] - P.part_off) * nd + k % nd;
+      const int gb = P.dip_off + (lst[k1 / nd] - P.part_off) * nd + k1 % nd;
+      const uint4 jpa = make_uint4(b.dfx[ga], b.dfx[ND + ga], b.dfx[2 * ND + ga], 0u);
+      const uint4 jpb = make_uint4(b.dfx[gb], b.dfx[ND + gb], b.dfx[2 * ND + gb], 0u);
+      const float4 jma = make_float4(b.dm[ga], b.dm[ND + ga], b.dm[2 * ND + ga], 0.f);
+      const float4 jmb = make_float4(b.dm[gb], b.dm[ND + gb], b.dm[2 * ND + gb], 0.f);
+      JOut o;
+      tile_step<true, true>(K, s, jpa, jma, jpb, jmb, true, two, o);
+    }
+    float fv[6];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      fv[c] = s.F[c].x + s.F[c].y;
+      fv[3 + c] = s.T[c].x + s.T[c].y;
+    }
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {  // as (hi, lo) the way real_sum stores its sums
+      const float hx = c < 3 ? s.F[c].x : s.T[c - 3].x, hy = c < 3 ? s.F[c].y : s.T[c - 3].y;
+      const float bb = fv[c] - hx;
+      b.rsum[(long long)c * ND + g] = make_float2(fv[c], (hx - (fv[c] - bb)) + (hy - bb));
+    }
+    e[0] = ff_add(e[0], ff_of(0.5f * ((s.U.x + (-s.Uc.x)) + (s.U.y + (-s.Uc.y)))));
+#pragma unroll
+    for (int c = 0; c < 9; ++c) e[1 + c] = ff_add(e[1 + c], ff_of(0.5f * (s.pt[c].x + s.pt[c].y)));
+  }
+  double out[10];
+  block_sum<10, kPartBlock>(e, sh, out);
+  if (threadIdx.x == 0) {
+    double* dst = b.rlE + (long long)blk_slot(P, bk) * 10;
+#pragma unroll
+    for (int c = 0; c < 10; ++c) dst[c] = out[c];
+  }
+}
+
 // Each dipole's real-space force and torque: the sum of its tile partials
 // over all partner strips, in strip order, in float-float.  One thread per
 // (dipole, component) of a particle block, component-major so that a warp
@@ -521,6 +622,7 @@ __global__ void __launch_bounds__(32 * W, 20 / W) real_pairs_kernel(Batch b) {
 __global__ void __launch_bounds__(512) real_sum_kernel(Batch b) {
   const int2 bk = b.blk[blockIdx.x];
   const SysDev& P = b.sys[bk.x];
+  if (P.rc_real > 0.0) return;  // summed by the neighbour pass (real_cut)
   const int nd = P.nd;
   const int p0 = bk.y - P.part_off;
   const int np = min(kPartBlock, P.n - p0);
@@ -573,6 +675,10 @@ __global__ void __launch_bounds__(128) strip_energy_kernel(Batch b) {
 #pragma unroll
     for (int c = 0; c < 10; ++c) out[c] = soft_f2d(acc[c].hi) + soft_f2d(acc[c].lo);
   }
+}
+
+void launch_real_cut(const Batch& b, cudaStream_t s) {
+  if (b.any_rc && b.nblk) real_cut_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
 }
 
 void launch_real_sum(const Batch& b, cudaStream_t s) {

@@ -57,6 +57,11 @@ __global__ void __launch_bounds__(kPartBlock) list_build_kernel(Batch b, int for
   const int first = P.part_off, n = P.n;
   int cnt = 0;
   int* out = b.nb + (long long)i * kMaxNb;
+  // real-space neighbours (systems with a real-space cutoff): every rod whose
+  // centre is within rl_r2, in ascending order, both directions
+  const bool rcut = P.rc_real > 0.0;
+  int rcnt = 0;
+  int* rout = b.rnb + (long long)i * kMaxR;
   for (int q0 = 0; q0 < n; q0 += kPartBlock) {
     const int nq = min(kPartBlock, n - q0);
     __syncthreads();
@@ -69,6 +74,17 @@ __global__ void __launch_bounds__(kPartBlock) list_build_kernel(Batch b, int for
     }
     __syncthreads();
     if (!ok) continue;
+    if (rcut) {
+      for (int k = 0; k < nq; ++k) {
+        const float dx = fix_diff(ux, sx[k], Lx);
+        const float dy = fix_diff(uy, sy[k], Ly);
+        const float dz = fix_diff(uz, sz[k], Lz);
+        if (dx * dx + dy * dy + dz * dz < P.rl_r2 && first + q0 + k != i) {
+          if (rcnt < kMaxR) rout[rcnt] = first + q0 + k;
+          ++rcnt;
+        }
+      }
+    }
     // 1. centre distance against the reach of the two rods, branch-free,
     //    into a mask of the chunk's 128 candidates: nearly every warp has a
     //    lane with some candidate in reach, so testing the segments inside
@@ -108,8 +124,9 @@ __global__ void __launch_bounds__(kPartBlock) list_build_kernel(Batch b, int for
     }
   }
   if (!ok) return;
-  if (cnt > kMaxNb) atomicOr(&S.status, kErrListOverflow);
+  if (cnt > kMaxNb || rcnt > kMaxR) atomicOr(&S.status, kErrListOverflow);
   b.nbc[i] = min(cnt, kMaxNb);
+  if (rcut) b.rnbc[i] = min(rcnt, kMaxR);
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     b.fsave[3 * i + a] = b.pfx[a * N + i];

@@ -18,6 +18,7 @@ constexpr int kKChunk = 256;     // particles per block of the structure-factor 
 // systems of more strips than this sum their real-space tile energies per
 // strip first (real_sum); smaller ones are summed tile by tile
 constexpr int kStripRows = 32;
+constexpr int kMaxR = 256;       // real-space neighbours per rod (systems with a real-space cutoff)
 constexpr int kMaxC = 16;        // WCA contact candidates of higher index per particle
 
 // status bits (OR-ed per system; mapped to mdsc_status on the host)
@@ -58,6 +59,8 @@ struct SysDev {
   int blk_off, nblk;        // per-particle block range
   int cl_fr;
   int cl_mode;     // cluster bonds: 0 the reference's geometric test, 1 pair energy
+  float rl_r2;     // rc_real > 0: squared centre-distance radius of the real-space neighbour list
+  double rc_real;  // real-space cutoff (0: all minimum-image pairs, the tiles)
   double cl_ubond; // mode 1: a bond is U_pair < -cl_ubond (the threshold times T)
   double L[3];
   double invL[3];
@@ -162,6 +165,10 @@ struct Batch {
   double* stripE; // 10 per strip: U, PT[9] of the strip's tiles (I, J >= I) (a float-float sum, hi + lo in FP64)
   int2* bstrips;  // (system, strip) of every strip of the systems of more than kStripRows strips
   int nbstrips;
+  int any_rc;     // some system has a real-space cutoff
+  int* rnb;       // n * kMaxR: real-space neighbour rods (both directions, ascending) of rc_real systems
+  int* rnbc;      // n: their number
+  double* rlE;    // 10 per particle block: U, PT of the block's real-space neighbour pairs (rc_real systems)
   int4* tiles;   // (sys, I, J, 0)
   int2* wlist;   // WCA work list: (candidate slot, system), n * kMaxC at most
   int* wlist_n;  // its length this step

@@ -34,6 +34,7 @@ EXPORTS = [
     "mdsc_set_thermostat", "mdsc_zero_forces", "mdsc_force_sc", "mdsc_force_dipR",
     "mdsc_force_dipK", "mdsc_ext_field", "mdsc_self_ener", "mdsc_moveX", "mdsc_moveP",
     "mdsc_renorm", "mdsc_neigh_list", "mdsc_check_list", "mdsc_clust_conf", "mdsc_set_cluster_energy",
+    "mdsc_abi_sizes",
     "mdsc_step",
     "mdsc_observe", "mdsc_launches_per_step", "mdsc_stream", "mdsc_profile_steps",
     "mdsc_place_rods", "mdsc_last_device_ms", "mdsc_force_dipR_noalloc", "mdsc_transfer",
@@ -50,6 +51,7 @@ class SystemDesc(ctypes.Structure):
         ("temp", c_double), ("Q", c_double), ("gamma", c_double), ("xi0", c_double),
         ("B", c_double * 3), ("min_s", c_double), ("cl_fr", c_int),
         ("thermo_seed", c_ulong * 2), ("cluster_seed", c_ulong), ("cluster_skip", c_ulong),
+        ("rc_real", c_double),
     ]
 
 
@@ -160,6 +162,7 @@ def load(build: bool = True) -> ctypes.CDLL:
         "mdsc_check_list": (c_int, [c_void_p, _ip]),
         "mdsc_clust_conf": (c_int, [c_void_p, c_int, _ip, _ip]),
         "mdsc_set_cluster_energy": (c_int, [c_void_p, c_int, c_double]),
+        "mdsc_abi_sizes": (None, [P(c_size_t), P(c_size_t), P(c_size_t), P(c_size_t)]),
         "mdsc_step": (c_int, [c_void_p, c_int, P(Observables)]),
         "mdsc_observe": (c_int, [c_void_p, P(Observables)]),
         "mdsc_launches_per_step": (c_int, [c_void_p]),
@@ -209,6 +212,7 @@ def desc_from_spec(spec: SystemSpec, nd: int) -> SystemDesc:
     d.cl_fr = int(spec.cl_fr)
     d.thermo_seed[0], d.thermo_seed[1] = 1, 2
     d.cluster_seed, d.cluster_skip = 1, 0
+    d.rc_real = float(getattr(spec, "rc_real", 0.0))
     return d
 
 

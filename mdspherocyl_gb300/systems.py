@@ -158,6 +158,7 @@ class SystemSpec:
     cl_fr: int = 0
     steps: int = 1000
     label: str = ""
+    rc_real: float = 0.0  # real-space cutoff: 0 = all minimum-image pairs (the reference)
 
 
 @dataclass

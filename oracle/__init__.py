@@ -147,6 +147,7 @@ class Oracle:
         self._sc = _bind(lib, "mdsc_or_force_sc", c_int, [_SP, c_double, c_double, _dp, _dp, _dp])
         self._tab = _bind(lib, "mdsc_or_tabul", None, [c_double, _dp])
         self._dipR = _bind(lib, "mdsc_or_force_dipR", None, [_SP, _dp, _dp, _dp])
+        self._mask = _bind(lib, "mdsc_or_mask_table", None, [_dp, c_double])
         self._wave = _bind(lib, "mdsc_or_wave_v", None, [_dp, _dp, c_double, c_int, c_int])
         self._dipK = _bind(lib, "mdsc_or_force_dipK", None, [_SP, c_int, c_double, _dp, _dp, _dp])
         self._ext = _bind(lib, "mdsc_or_ext_field", None, [_SP, _dp, _dp])
@@ -274,8 +275,14 @@ class Oracle:
             self._tabcache[key] = tab
         return self._tabcache[key]
 
-    def force_dipR(self, sysm: System, alpha: float):
+    def force_dipR(self, sysm: System, alpha: float, rc: float = 0.0):
+        """force_dipR; rc > 0: with tabul's table zeroed beyond rc (entry k
+        holds r = 0.5 * 200.2 * (k + 1) / 32768), the real-space cutoff of
+        the library's rc_real."""
         tab = self.tabul(alpha)
+        if rc > 0:
+            tab = tab.copy()
+            self._mask(tab.ctypes.data_as(_dp), rc)
         U = c_double(0)
         PT = np.zeros(9)
         cs = sysm.cstate()
@@ -333,7 +340,7 @@ class MDOracle:
         pass
 
     def __init__(self, oracle: Oracle, sysm: System, *, dt, temp, Q, gamma, xi0, sr_cut, K_max,
-                 ksq_max, alpha, B, cl_fr=0, min_s=0.1):
+                 ksq_max, alpha, B, cl_fr=0, min_s=0.1, rc_real=0.0):
         lib = oracle.lib
         self.lib = lib
         self.sys = sysm
@@ -351,6 +358,9 @@ class MDOracle:
         ok = init(self._buf, ctypes.byref(self._cs), dt, temp, Q, gamma, xi0, sr_cut, K_max,
                   ksq_max, alpha, Bc.ctypes.data_as(_dp), cl_fr, min_s)
         if not ok:
+            raise RuntimeError("initial overlap")
+        if rc_real > 0 and not _bind(lib, "mdsc_or_md_mask_table", c_int, [c_void_p, _SP, c_double])(
+                self._buf, ctypes.byref(self._cs), rc_real):
             raise RuntimeError("initial overlap")
 
     def step(self) -> bool:
@@ -391,6 +401,7 @@ class Ref:
         self._sc = _bind(lib, "mdsc_ref_force_sc", c_int, [_SP, c_double, c_double, _dp, _dp, _dp])
         self._tab = _bind(lib, "mdsc_ref_tabul", None, [c_double, _dp])
         self._dipR = _bind(lib, "mdsc_ref_force_dipR", None, [_SP, c_double, _dp, _dp])
+        self._dipRc = _bind(lib, "mdsc_ref_force_dipR_cut", None, [_SP, c_double, c_double, _dp, _dp])
         self._dipK = _bind(lib, "mdsc_ref_force_dipK", None, [_SP, c_int, c_double, c_int, _dp, _dp])
         self._ext = _bind(lib, "mdsc_ref_ext_field", None, [_SP, _dp, _dp])
         self._self = _bind(lib, "mdsc_ref_self_ener", c_double, [_SP])
@@ -460,11 +471,14 @@ class Ref:
         self._tab(alpha, tab.ctypes.data_as(_dp))
         return tab
 
-    def force_dipR(self, sysm, alpha):
+    def force_dipR(self, sysm, alpha, rc=0.0):
         U = c_double(0)
         PT = np.zeros(9)
         cs = sysm.cstate()
-        self._dipR(ctypes.byref(cs), alpha, ctypes.byref(U), PT.ctypes.data_as(_dp))
+        if rc > 0:
+            self._dipRc(ctypes.byref(cs), alpha, rc, ctypes.byref(U), PT.ctypes.data_as(_dp))
+        else:
+            self._dipR(ctypes.byref(cs), alpha, ctypes.byref(U), PT.ctypes.data_as(_dp))
         return U.value, PT.reshape(3, 3)
 
     def force_dipK(self, sysm, K_max, alpha, ksq_max=0):

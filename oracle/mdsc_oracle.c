@@ -424,6 +424,15 @@ int mdsc_or_force_sc(mdsc_oracle_state* s, double r_cut, double r_list, double* 
   return ok;
 }
 
+/* The real-space cutoff of this library's rc_real: tabul's table with the
+   entries beyond rc zeroed (entry i-1 holds r = 0.5 * extL * i / 32768). */
+void mdsc_or_mask_table(double* tab, double rc) {
+  if (!(rc > 0)) return;
+  double extL = 200 * 1.001;
+  for (int i = 1; i < 32769; i++)
+    if (0.5 * extL * i / 32768 > rc) tab[3 * (i - 1)] = tab[3 * (i - 1) + 1] = tab[3 * (i - 1) + 2] = 0.;
+}
+
 /* ------------------------------------------------------------------ */
 /* tabul, v25/functions.cpp:1680-1704                                  */
 /* ------------------------------------------------------------------ */
@@ -1357,6 +1366,13 @@ void mdsc_or_md_set_thermo(mdsc_or_md* md, const double xi[2], const double strn
   md->thermo.xi[1] = xi[1];
   md->thermo.strn[0] = strn[0];
   md->thermo.strn[1] = strn[1];
+}
+
+/* the step's real-space table with entries beyond rc zeroed, and the
+   forces of the current state again with it (as mdsc_or_md_init left them) */
+int mdsc_or_md_mask_table(mdsc_or_md* md, mdsc_oracle_state* s, double rc) {
+  mdsc_or_mask_table(md->tab, rc);
+  return md_forces(md, s);
 }
 
 void mdsc_or_md_free(mdsc_or_md* md) {

@@ -57,6 +57,8 @@ int mdsc_or_force_sc_list(mdsc_oracle_state* s, double r_cut, const int* start, 
                           double* U, double* W, double PT[9]);
 /* tabul, v25/functions.cpp:1680-1704 (32768 x 3) */
 void mdsc_or_tabul(double alpha, double* tab);
+/* tabul's table with the entries beyond a real-space cutoff rc zeroed */
+void mdsc_or_mask_table(double* tab, double rc);
 /* force_dipR, v25/functions.cpp:1555-1678 */
 void mdsc_or_force_dipR(mdsc_oracle_state* s, const double* tab, double* U, double PT[9]);
 /* wave_v, v25/functions.cpp:1963-1990, into kvec[(nx*(K+1)+ny)*(K+1)+nz];
@@ -134,6 +136,7 @@ typedef struct {
 int mdsc_or_md_init(mdsc_or_md* md, mdsc_oracle_state* s, double dt, double temp, double Q,
                     double gamma, double xi0, double sr_cut, int K_max, int ksq_max, double alpha,
                     const double B[3], int cl_fr, double min_s);
+int mdsc_or_md_mask_table(mdsc_or_md* md, mdsc_oracle_state* s, double rc);
 int mdsc_or_md_step(mdsc_or_md* md, mdsc_oracle_state* s);
 void mdsc_or_md_free(mdsc_or_md* md);
 /* observables of the last step: K_t, K_r, Uss, Wss, UdipR, UdipK, Uext,

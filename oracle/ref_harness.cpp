@@ -176,6 +176,25 @@ void mdsc_ref_force_dipR(mdsc_ref_state* s, double alpha, double* U, double* PT)
   write_back(s, part);
 }
 
+// force_dipR with tabul's table zeroed beyond rc (entry i-1 holds
+// r = 0.5 * 200.2 * i / 32768): the real-space cutoff of this library's
+// rc_real, through the reference's own routine
+void mdsc_ref_force_dipR_cut(mdsc_ref_state* s, double alpha, double rc, double* U, double* PT) {
+  Dynvec<Dynvec<Spherocyl> > part;
+  part_num NP;
+  build_part(s, part, NP);
+  tabul(g_tab, alpha);
+  const double extL = 200 * 1.001;
+  for (int i = 1; i < 32769; i++)
+    if (0.5 * extL * i / 32768 > rc) g_tab[i - 1][0] = g_tab[i - 1][1] = g_tab[i - 1][2] = 0.;
+  double pt[3][3];
+  double u = 0;
+  force_dipR(part, NP, s->L, g_tab, u, pt);
+  *U = u;
+  copy_pt(pt, PT);
+  write_back(s, part);
+}
+
 // force_dipK (v25/functions.cpp:1706-1961) with Kvec from wave_v
 // (v25/functions.cpp:1963-1990).  ksq_max > 0 zeroes Kvec outside
 // nx^2+ny^2+nz^2 <= ksq_max, giving a spherical k-set.

@@ -34,6 +34,16 @@ def test_library_exports_every_declared_symbol():
     assert set(names) == set(L.EXPORTS)
 
 
+def test_ctypes_structures_match_the_library():
+    """The Python layouts of mdsc_system_desc, mdsc_host_state,
+    mdsc_observables and mdsc_view have the library's sizes."""
+    lib = ctypes.CDLL(B.build())
+    lib.mdsc_abi_sizes.restype = None
+    sz = [ctypes.c_size_t(0) for _ in range(4)]
+    lib.mdsc_abi_sizes(*[ctypes.byref(x) for x in sz])
+    assert [x.value for x in sz] == [ctypes.sizeof(t) for t in (L.SystemDesc, L.HostState, L.Observables, L.View)]
+
+
 def test_estimate_bytes_without_gpu():
     spec, st = S.plain_c0(seed=0, n=64)
     d = L.desc_from_spec(spec, 1)
