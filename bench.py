@@ -111,8 +111,17 @@ def build_workload(args, rank: int = 0):
 
     fn, desc, _ = SINGLE[args.workload]
     spec, st = getattr(S, fn)(seed=args.seed + 1000 * rank)
+    spec.rc_real = 0.5 * float(min(spec.box)) if args.real_cutoff == "half" else float(args.real_cutoff)
+    args.rc_value = spec.rc_real
     return [(spec, st)], {"workload": f"plain_{args.workload}", "description": desc, "ksq_max": spec.ksq_max,
                           "alpha": float(spec.alpha), "box": float(spec.box[0])}
+
+
+def real_space(args) -> str:
+    rc = getattr(args, "rc_value", 0.0)
+    if args.workload != "replica_mix" and rc > 0:
+        return f"cutoff {rc:.4g}: the reference's table zeroed beyond it, over a neighbour list (rc_real)"
+    return "all minimum-image pairs"
 
 
 class ClockSampler:
@@ -191,7 +200,8 @@ def cpu_sample(states, threads: int, budget_s: float = 20.0, stride: int = 16):
         spec, st = states[k]
         o = oracle.System(st.r, st.p, st.O, st.l, st.length, st.dia, st.mass, st.dip, spec.box)
         md = oracle.MDOracle(orc, o, dt=spec.dt, temp=spec.temp, Q=spec.Q, gamma=spec.gamma, xi0=spec.xi0,
-                             sr_cut=3.0, K_max=spec.K_max, ksq_max=spec.ksq_max, alpha=spec.alpha, B=spec.B)
+                             sr_cut=3.0, K_max=spec.K_max, ksq_max=spec.ksq_max, alpha=spec.alpha, B=spec.B,
+                             rc_real=spec.rc_real)
         t0 = time.perf_counter()
         md.step()
         t_tot += time.perf_counter() - t0
@@ -225,7 +235,7 @@ def run_reference(args):
         (f"oracle MD step (reference routines restated in C, OpenMP) on the whole system (N={used[0]}), "
          f"one step")
     cfg.update({"systems": len(states), "particles": int(sum(s.n for s, _ in states)),
-                "real_space": "all minimum-image pairs"})
+                "real_space": real_space(args)})
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * tt, "higher_is_better": True, "scaling": "weak",
@@ -363,8 +373,11 @@ def run_ours(args):
     tuning["chosen_by"] = "autotuner (mdsc_autotune)" if tun["tuned"] else "defaults"
     prof = bt.profile(max(2, min(5, args.steps)))
     pairs = sum(s.n * (s.n - 1) // 2 for s in specs)
+    # with a real-space cutoff the tiles do not run (real_cut does, over the
+    # neighbour list): no all-pairs roofline
+    cutoff = single and getattr(args, "rc_value", 0.0) > 0
     rp_ms = prof.get("real_pairs", float("nan"))
-    achieved = FLOP_PER_PAIR * pairs / (rp_ms * 1e-3) / 1e12
+    achieved = FLOP_PER_PAIR * pairs / (rp_ms * 1e-3) / 1e12 if not cutoff else float("nan")
     peaks, src = measured_peaks()
     sm_max = float(peaks.get("sm_max_mhz", 2070.0))
     fp32_peak = 2 * 128 * 152 * sm_max * 1e6 / 1e12
@@ -423,21 +436,22 @@ def run_ours(args):
             "config": {**cfg, "systems": len(specs) * ws, "particles": int(ntot_all),
                        "particles_rank0": ntot,
                        "N_range": [min(s.n for s in specs), max(s.n for s in specs)],
-                       "real_space": "all minimum-image pairs", "dt": 1e-3,
+                       "real_space": real_space(args), "dt": 1e-3,
                        "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{ws}",
                        "graph": "one CUDA graph per step", "launch_mappings": tuning},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": bytes_h2d,
                     "d2h_bytes_per_step": bytes_d2h},
             "gpu_launches": launches * args.steps,
-            "roofline": {"bound": "fp32", "kernel": "real_pairs", "achieved": achieved, "peak": fp32_peak,
-                         "unit": "TFLOP/s", "frac": achieved / fp32_peak,
-                         "traffic": REAL_PAIRS_DRAM_BYTES_PER_PAIR * pairs,
-                         "traffic_unit": "bytes per launch (ncu dram read+write, scaled by pairs)",
-                         "peak_source": (f"nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 FLOP at "
-                                         f"{sm_max:.0f} MHz ({src} max SM clock); MEASURED_PEAKS.json has "
-                                         f"HBM and bf16 tensor figures only"),
-                         "flop_per_pair": FLOP_PER_PAIR, "pairs_per_launch": pairs,
-                         "kernel_ms": rp_ms},
+            "roofline": None if cutoff else {
+                "bound": "fp32", "kernel": "real_pairs", "achieved": achieved, "peak": fp32_peak,
+                "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+                "traffic": REAL_PAIRS_DRAM_BYTES_PER_PAIR * pairs,
+                "traffic_unit": "bytes per launch (ncu dram read+write, scaled by pairs)",
+                "peak_source": (f"nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 FLOP at "
+                                f"{sm_max:.0f} MHz ({src} max SM clock); MEASURED_PEAKS.json has "
+                                f"HBM and bf16 tensor figures only"),
+                "flop_per_pair": FLOP_PER_PAIR, "pairs_per_launch": pairs,
+                "kernel_ms": rp_ms},
             "kernel_ms": prof,
             "plain_gpu": plain,
             "serving": serving,
@@ -463,6 +477,9 @@ def main():
     ap.add_argument("--systems", type=int, default=256)
     ap.add_argument("--workload", default="replica_mix", choices=["replica_mix", *SINGLE],
                     help="replica_mix: the 256-system mix (the headline); c0/c1/c2: one system of that config")
+    ap.add_argument("--real-cutoff", default="0",
+                    help="c0/c1/c2: real-space cutoff, a length or 'half' (L_box/2); 0 = all pairs, the "
+                         "reference (config 0 states L_box/2, config 1 3.5)")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
