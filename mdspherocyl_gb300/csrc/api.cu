@@ -732,7 +732,7 @@ mdsc_status run_clusters(mdsc_batch* B, const std::vector<int>& systems) {
       if (ovf[s])
         return fail(B, MDSC_ERR_LIST_OVERFLOW,
                     "system " + std::to_string(s) + ": a particle has more than " + std::to_string(kMaxC) +
-                        " energy bonds to higher indices");
+                        " energy bonds (or " + std::to_string(kMaxE) + " candidates) to higher indices");
   }
   for (int it = 0; it < 64; ++it) {
     CU(cudaMemsetAsync(b.flag, 0, sizeof(int), B->st));
@@ -1107,6 +1107,8 @@ mdsc_status mdsc_destroy(mdsc_batch* B) {
   for (auto& g : B->graph)
     if (g) cudaGraphExecDestroy(g);
   if (B->arena) cudaFree(B->arena);
+  if (B->b.ecand) cudaFree(B->b.ecand);
+  if (B->b.ecnt) cudaFree(B->b.ecnt);
   if (B->h_noise) cudaFreeHost(B->h_noise);
   if (B->h_obs) cudaFreeHost(B->h_obs);
   if (B->h_trace) cudaFreeHost(B->h_trace);
@@ -1506,9 +1508,24 @@ mdsc_status mdsc_clust_conf(mdsc_batch* B, int sys, int* labels, int* n_clusters
   return MDSC_OK;
 }
 
+// the candidate lists of the energy screen, for every particle of the batch,
+// allocated when a system of it first takes the energy criterion
+static mdsc_status ensure_energy_lists(mdsc_batch* B) {
+  if (B->b.ecand) return MDSC_OK;
+  const size_t n = (size_t)std::max(B->lo.ntot, 1);
+  CU(cudaMalloc(&B->b.ecand, sizeof(int) * n * kMaxE));
+  CU(cudaMalloc(&B->b.ecnt, sizeof(int) * n));
+  CU(cudaMemsetAsync(B->b.ecnt, 0, sizeof(int) * n, B->st));
+  return MDSC_OK;
+}
+
 mdsc_status mdsc_set_cluster_energy(mdsc_batch* B, int sys, double u_bond_kT) {
   if (!B || sys < 0 || sys >= B->nsys || !(u_bond_kT >= 0.0)) return MDSC_ERR_BAD_ARG;
   cudaSetDevice(B->device);
+  if (u_bond_kT > 0.0) {
+    const mdsc_status st = ensure_energy_lists(B);
+    if (st) return st;
+  }
   SysDev& P = B->lo.sys[sys];
   P.cl_mode = u_bond_kT > 0.0 ? 1 : 0;
   P.cl_ubond = u_bond_kT * B->desc[sys].temp;
@@ -1819,6 +1836,10 @@ mdsc_status mdsc_transfer(mdsc_batch* D, int dsys, mdsc_batch* S, int ssys) {
   Pd.Uself = Ps.Uself;
   Pd.cl_mode = Ps.cl_mode;
   Pd.rl_r2 = Ps.rl_r2;
+  if (Pd.cl_mode == 1) {
+    const mdsc_status est = ensure_energy_lists(D);
+    if (est) return est;
+  }
   Pd.cl_ubond = Ps.cl_ubond;
   CU(cudaMemcpyAsync((void*)(b.sys + dsys), &Pd, sizeof(SysDev), cudaMemcpyHostToDevice, D->st));
   SysState st;

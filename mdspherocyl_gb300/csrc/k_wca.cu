@@ -423,12 +423,12 @@ __device__ double pair_energy_ref(const Batch& b, const SysDev& P, int A, int B)
   return U;
 }
 
-// bonds U_pair < -cl_ubond to every higher index of the system.  An FP32
-// screen on the centres (fixed-point minimum image) keeps the pairs that
-// can bond: |U_dd| <= 2 M_i M_j / (r - e_i - e_j)^3, with M the sum of a
-// rod's moments and e its largest dipole offset, and U_WCA >= 0; those are
-// evaluated exactly.
-__global__ void __launch_bounds__(kPartBlock) ebond_kernel(Batch b) {
+// Candidates for bonds U_pair < -cl_ubond among the higher indices of the
+// system: an FP32 screen on the centres (fixed-point minimum image) keeps
+// the pairs that can bond, |U_dd| <= 2 M_i M_j / (r - e_i - e_j)^3 with M
+// the sum of a rod's moments and e its largest dipole offset, U_WCA >= 0.
+// Ascending order; ebond_eval_kernel evaluates them exactly.
+__global__ void __launch_bounds__(kPartBlock) ebond_screen_kernel(Batch b) {
   __shared__ uint32_t sx[kPartBlock], sy[kPartBlock], sz[kPartBlock];
   __shared__ float2 sme[kPartBlock];
   const int2 bk = b.blk[blockIdx.x];
@@ -459,7 +459,7 @@ __global__ void __launch_bounds__(kPartBlock) ebond_kernel(Batch b) {
   }
   const float Lx = P.Lfix[0], Ly = P.Lfix[1], Lz = P.Lfix[2];
   const float thr = (float)P.cl_ubond * 0.999f;
-  int* out = b.ebond + (long long)i * kMaxC;
+  int* out = b.ecand + (long long)i * kMaxE;
   int cnt = 0;
   for (int q0 = (bk.y - first) / kPartBlock * kPartBlock; q0 < n; q0 += kPartBlock) {
     __syncthreads();
@@ -475,22 +475,44 @@ __global__ void __launch_bounds__(kPartBlock) ebond_kernel(Batch b) {
     const int nq = min(kPartBlock, n - q0);
     for (int t = 0; t < nq; ++t) {
       const int j = first + q0 + t;
-      if (j <= i) continue;
       const float2 mj = sme[t];
-      if (mj.x == 0.f) continue;
       const float dx = fix_diff(ux, sx[t], Lx), dy = fix_diff(uy, sy[t], Ly), dz = fix_diff(uz, sz[t], Lz);
       const float gap = sqrtf(dx * dx + dy * dy + dz * dz) * 0.9999f - mi.y - mj.y;
-      if (gap > 0.f && 2.f * mi.x * mj.x < thr * gap * gap * gap) continue;
-      if (pair_energy_ref(b, P, i, j) < -P.cl_ubond) {
-        if (cnt < kMaxC) out[cnt] = j;
+      const bool cand = j > i && mj.x != 0.f && (gap <= 0.f || 2.f * mi.x * mj.x >= thr * gap * gap * gap);
+      if (cand) {
+        if (cnt < kMaxE) out[cnt] = j;
         ++cnt;
       }
     }
   }
   if (ok) {
-    b.ebcnt[i] = min(cnt, kMaxC);
-    if (cnt > kMaxC) atomicOr(&b.eovf[s], 1);
+    b.ecnt[i] = min(cnt, kMaxE);
+    if (cnt > kMaxE) atomicOr(&b.eovf[s], 1);
   }
+}
+
+// the screened candidates of each rod, exactly: a bond where the FP64 pair
+// energy (pair_energy_ref, lower index first) is below -cl_ubond
+__global__ void __launch_bounds__(kPartBlock) ebond_eval_kernel(Batch b) {
+  const int2 bk = b.blk[blockIdx.x];
+  const int s = bk.x;
+  const SysDev& P = b.sys[s];
+  if (P.cl_mode != 1) return;
+  const int i = bk.y + threadIdx.x;
+  if (i >= P.part_off + P.n) return;
+  const int nc = b.ecnt[i];
+  const int* cand = b.ecand + (long long)i * kMaxE;
+  int* out = b.ebond + (long long)i * kMaxC;
+  int cnt = 0;
+  for (int k = 0; k < nc; ++k) {
+    const int j = cand[k];
+    if (pair_energy_ref(b, P, i, j) < -P.cl_ubond) {
+      if (cnt < kMaxC) out[cnt] = j;
+      ++cnt;
+    }
+  }
+  b.ebcnt[i] = min(cnt, kMaxC);
+  if (cnt > kMaxC) atomicOr(&b.eovf[s], 1);
 }
 
 __device__ __forceinline__ int find_root(const int* comp, int x) {
@@ -551,7 +573,9 @@ void launch_cluster_bonds(const Batch& b, cudaStream_t s) {
   if (b.nblk) cluster_bonds_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
 }
 void launch_ebond(const Batch& b, cudaStream_t s) {
-  if (b.nblk) ebond_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
+  if (!b.nblk || !b.ecand) return;
+  ebond_screen_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
+  ebond_eval_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
 }
 void launch_cluster_hook(const Batch& b, cudaStream_t s) {
   if (b.nblk) cluster_hook_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);

@@ -19,6 +19,7 @@ constexpr int kKChunk = 256;     // particles per block of the structure-factor 
 // strip first (real_sum); smaller ones are summed tile by tile
 constexpr int kStripRows = 32;
 constexpr int kMaxR = 256;       // real-space neighbours per rod (systems with a real-space cutoff)
+constexpr int kMaxE = 64;        // energy-criterion candidates (higher index) per rod
 constexpr int kMaxC = 16;        // WCA contact candidates of higher index per particle
 
 // status bits (OR-ed per system; mapped to mdsc_status on the host)
@@ -213,7 +214,9 @@ struct Batch {
   int* flag;     // 1 changed flag
   int* ebond;    // n * kMaxC: energy-criterion bonds to higher indices
   int* ebcnt;    // n: their number
-  int* eovf;     // nsys: a particle had more than kMaxC energy bonds
+  int* eovf;     // nsys: a particle had more than kMaxC energy bonds (or kMaxE candidates)
+  int* ecand;    // n * kMaxE: energy-criterion candidates of higher index (allocated on first use)
+  int* ecnt;     // n: their number
   // thermostat noise: [iter][sys][4] = g0_t, g1_t, g0_r, g1_r
   const double* noise;
 };
