@@ -73,6 +73,8 @@ struct Layout {
   std::vector<double> kval, kpre, kvec;
   std::vector<int2> blk, kowner;
   std::vector<int2> bstrips;  // strips of the systems whose tile energies are summed per strip
+  std::vector<int2> kgwork;   // (particle block, part) of the k-space gather
+  long long kgsets = 0;       // partial sets of the split gathers
   int ntot = 0, ndtot = 0, nktot = 0, maxnd = 0, nchunks = 0, nstrips = 0;
   bool any_rc = false;  // some system sums its real space over a neighbour list
   long long rpart = 0, kpart = 0;
@@ -317,6 +319,13 @@ void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
     P.blk_off = blk;
     P.nblk = cdiv(d.n, kPartBlock);
     for (int k = 0; k < P.nblk; ++k) Lo.blk.push_back(make_int2(s, part + k * kPartBlock));
+    // the k-space gather of a large single-dipole system runs its k tiles in
+    // parts on separate blocks (a function of the system only, so the same
+    // bits alone and in any batch); smaller systems fill the GPU as they are
+    const int ktiles = cdiv(P.nk, kKBlock);
+    P.kgs = (d.nd == 1 && d.n >= 4096 && ktiles > 1) ? std::min(8, ktiles) : 1;
+    P.kgp_off = (int)Lo.kgsets;
+    if (P.kgs > 1) Lo.kgsets += (long long)P.nblk * P.kgs;
     blk += P.nblk;
     P.cl_fr = d.cl_fr;
     for (int a = 0; a < 3; ++a) {
@@ -368,6 +377,10 @@ void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
   // order.
   std::stable_sort(Lo.blk.begin(), Lo.blk.end(),
                    [&](const int2& u, const int2& v) { return descs[u.x].n > descs[v.x].n; });
+  // the k-space gather's blocks: every part of every particle block, in the
+  // launch order above (entries index the sorted block list)
+  for (int g = 0; g < (int)Lo.blk.size(); ++g)
+    for (int q = 0; q < Lo.sys[Lo.blk[g].x].kgs; ++q) Lo.kgwork.push_back(make_int2(g, q));
   Lo.ntot = part;
   Lo.ndtot = dip;
   Lo.nktot = (int)Lo.kn.size();
@@ -422,6 +435,9 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   b.tileE = A.take<float>(10 * nt);
   b.stripE = A.take<double>(10 * (size_t)std::max(Lo.nstrips, 1));
   b.bstrips = A.take<int2>(std::max<size_t>(Lo.bstrips.size(), 1));
+  b.kgwork = A.take<int2>(std::max<size_t>(Lo.kgwork.size(), 1));
+  b.kgpart = A.take<float>(std::max<long long>(Lo.kgsets, 1) * kPartBlock * 12);
+  b.kgdone = A.take<int>(nb);
   b.rnb = A.take<int>(Lo.any_rc ? n * kMaxR : 1);
   b.rnbc = A.take<int>(n);
   b.rlE = A.take<double>(10 * nb);
@@ -1009,6 +1025,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   b.ntiles = (int)lo.tiles.size();
   b.nbstrips = (int)lo.bstrips.size();
   b.any_rc = lo.any_rc ? 1 : 0;
+  b.nkgwork = (int)lo.kgwork.size();
   b.nblk = (int)lo.blk.size();
   b.noise = B->noise[0];
   // The step graph forks the real-space tiles (stream s2) from the WCA and
@@ -1037,6 +1054,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   up((void*)b.sys, lo.sys.data(), sizeof(SysDev) * nsys);
   up(b.tiles, lo.tiles.data(), sizeof(int4) * lo.tiles.size());
   if (!lo.bstrips.empty()) up(b.bstrips, lo.bstrips.data(), sizeof(int2) * lo.bstrips.size());
+  if (!lo.kgwork.empty()) up(b.kgwork, lo.kgwork.data(), sizeof(int2) * lo.kgwork.size());
   up(b.blk, lo.blk.data(), sizeof(int2) * lo.blk.size());
   up(b.kn, lo.kn.data(), sizeof(int4) * lo.kn.size());
   up(b.kv, lo.kv.data(), sizeof(float4) * lo.kv.size());
@@ -1065,6 +1083,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   cudaMemsetAsync(b.wincnt, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.stripE, 0, sizeof(double) * 10 * std::max(lo.nstrips, 1), B->st);
   cudaMemsetAsync(b.rnbc, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
+  cudaMemsetAsync(b.kgdone, 0, sizeof(int) * std::max<size_t>(lo.blk.size(), 1), B->st);
   cudaMemsetAsync(b.rlE, 0, sizeof(double) * 10 * std::max<size_t>(lo.blk.size(), 1), B->st);
   cudaMemsetAsync(b.kgcnt, 0, sizeof(int) * std::max(nsys, 1), B->st);
   cudaMemsetAsync(b.icnt, 0, sizeof(int) * std::max(nsys, 1), B->st);

@@ -400,6 +400,41 @@ __global__ void __launch_bounds__(kPartBlock) kgather_kernel(Batch b) {
     if (d < nd) store_kout(b, gd0 + d, fo[d], fc[d], mx[d], my[d], mz[d]);
 }
 
+// Split gathers (large single-dipole systems, SysDev::kgs > 1): block part
+// ks of a particle block takes the k tiles [ks tpk, (ks + 1) tpk), tpk =
+// ceil(tiles / kgs), and leaves its Kahan sums (fo, fc per component) in
+// its partial set; the block that finishes last adds the parts in part
+// order (Kahan over the sums, the compensations apart) and stores the
+// result, so the order of the sums does not depend on which block ends last.
+__device__ __forceinline__ void kpart_range(const SysDev& P, int ks, int& k0, int& k1) {
+  const int tpk = cdiv(cdiv(P.nk, kKBlock), P.kgs) * kKBlock;
+  k0 = min(P.nk, ks * tpk);
+  k1 = min(P.nk, (ks + 1) * tpk);
+}
+__device__ __forceinline__ float* kpart_set(const Batch& b, const SysDev& P, int slot, int ks) {
+  return b.kgpart + ((long long)P.kgp_off + (long long)(slot - P.blk_off) * P.kgs + ks) * kPartBlock * 12;
+}
+// the parts of local particle p of a particle block, added in part order
+__device__ __forceinline__ void kpart_combine(const Batch& b, const SysDev& P, int slot, int p, float* fo,
+                                              float* fc) {
+  float cs[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) fo[c] = fc[c] = cs[c] = 0.f;
+  for (int q = 0; q < P.kgs; ++q) {
+    const float* part = kpart_set(b, P, slot, q) + p * 12;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      const float y = __fadd_rn(__ldcg(part + c), -fc[c]);
+      const float tt = __fadd_rn(fo[c], y);
+      fc[c] = __fadd_rn(__fadd_rn(tt, -fo[c]), -y);
+      fo[c] = tt;
+      cs[c] = __fadd_rn(cs[c], __ldcg(part + 6 + c));
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 6; ++c) fc[c] = __fadd_rn(fc[c], cs[c]);
+}
+
 // Single-dipole systems: a thread takes two particles, i and i + 64 of its
 // block, and runs them side by side in the halves of float2 values with
 // the paired FP32 instructions, so every k read from shared memory serves
@@ -416,9 +451,13 @@ __global__ void __launch_bounds__(kPartBlock / 2) kgather1_kernel(Batch b) {
   __shared__ int4 skn[kKBlock];
   __shared__ float4 skv[kKBlock];
   __shared__ float2 sks[kKBlock];
-  const int2 bk = b.blk[blockIdx.x];
+  __shared__ int last;
+  const int2 wk = b.kgwork[blockIdx.x];  // (particle block, part)
+  const int2 bk = b.blk[wk.x];
   const SysDev& P = b.sys[bk.x];
   if (P.nd != 1) return;  // other systems: kgather_kernel<ND>
+  int kb, ke;
+  kpart_range(P, wk.y, kb, ke);
   const int t = threadIdx.x;
   const int i0 = bk.y + t, i1 = i0 + kPartBlock / 2;
   const int iend = P.part_off + P.n;
@@ -437,8 +476,8 @@ __global__ void __launch_bounds__(kPartBlock / 2) kgather1_kernel(Batch b) {
 #pragma unroll
   for (int c = 0; c < 6; ++c) fo[c] = fc[c] = bc(0.f);
 
-  for (int k0 = 0; k0 < P.nk; k0 += kKBlock) {
-    const int nk = min(kKBlock, P.nk - k0);
+  for (int k0 = kb; k0 < ke; k0 += kKBlock) {
+    const int nk = min(kKBlock, ke - k0);
     __syncthreads();
     for (int q = t; q < nk; q += kPartBlock / 2) {
       skn[q] = b.kn[P.k_off + k0 + q];
@@ -479,18 +518,36 @@ __global__ void __launch_bounds__(kPartBlock / 2) kgather1_kernel(Batch b) {
       fo[c] = tt;
     }
   }
-  if (ok0 || ok1) {
-    float a0[6], c0[6], a1[6], c1[6];
+  float a0[6], c0[6], a1[6], c1[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    a0[c] = fo[c].x;
+    c0[c] = fc[c].x;
+    a1[c] = fo[c].y;
+    c1[c] = fc[c].y;
+  }
+  if (P.kgs > 1) {  // a part: leave the sums, the last part combines
+    const int slot = blk_slot(P, bk);
+    float* mine = kpart_set(b, P, slot, wk.y);
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
-      a0[c] = fo[c].x;
-      c0[c] = fc[c].x;
-      a1[c] = fo[c].y;
-      c1[c] = fc[c].y;
+      mine[t * 12 + c] = a0[c];
+      mine[t * 12 + 6 + c] = c0[c];
+      mine[(t + kPartBlock / 2) * 12 + c] = a1[c];
+      mine[(t + kPartBlock / 2) * 12 + 6 + c] = c1[c];
     }
-    if (ok0) store_kout(b, g0, a0, c0, mx.x, my.x, mz.x);
-    if (ok1) store_kout(b, g1, a1, c1, mx.y, my.y, mz.y);
+    __threadfence();
+    __syncthreads();
+    if (t == 0) last = atomicAdd(&b.kgdone[slot], 1) == P.kgs - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    kpart_combine(b, P, slot, t, a0, c0);
+    kpart_combine(b, P, slot, t + kPartBlock / 2, a1, c1);
+    if (t == 0) b.kgdone[slot] = 0;
   }
+  if (ok0) store_kout(b, g0, a0, c0, mx.x, my.x, mz.x);
+  if (ok1) store_kout(b, g1, a1, c1, mx.y, my.y, mz.y);
 }
 
 // The same gather with one particle per thread (128 threads per block):
@@ -502,9 +559,13 @@ __global__ void __launch_bounds__(kPartBlock) kgather1s_kernel(Batch b) {
   __shared__ int4 skn[kKBlock];
   __shared__ float4 skv[kKBlock];
   __shared__ float2 sks[kKBlock];
-  const int2 bk = b.blk[blockIdx.x];
+  __shared__ int last;
+  const int2 wk = b.kgwork[blockIdx.x];  // (particle block, part)
+  const int2 bk = b.blk[wk.x];
   const SysDev& P = b.sys[bk.x];
   if (P.nd != 1) return;  // other systems: kgather_kernel<ND>
+  int kb, ke;
+  kpart_range(P, wk.y, kb, ke);
   const int t = threadIdx.x;
   const int i0 = bk.y + t;
   const bool ok0 = i0 < P.part_off + P.n;
@@ -516,8 +577,8 @@ __global__ void __launch_bounds__(kPartBlock) kgather1s_kernel(Batch b) {
   float fo[6], fc[6];
 #pragma unroll
   for (int c = 0; c < 6; ++c) fo[c] = fc[c] = 0.f;
-  for (int k0 = 0; k0 < P.nk; k0 += kKBlock) {
-    const int nk = min(kKBlock, P.nk - k0);
+  for (int k0 = kb; k0 < ke; k0 += kKBlock) {
+    const int nk = min(kKBlock, ke - k0);
     __syncthreads();
     for (int q = t; q < nk; q += kPartBlock) {
       skn[q] = b.kn[P.k_off + k0 + q];
@@ -556,15 +617,32 @@ __global__ void __launch_bounds__(kPartBlock) kgather1s_kernel(Batch b) {
       fo[c] = tt;
     }
   }
+  if (P.kgs > 1) {  // a part: leave the sums, the last part combines
+    const int slot = blk_slot(P, bk);
+    float* mine = kpart_set(b, P, slot, wk.y) + t * 12;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      mine[c] = fo[c];
+      mine[6 + c] = fc[c];
+    }
+    __threadfence();
+    __syncthreads();
+    if (t == 0) last = atomicAdd(&b.kgdone[slot], 1) == P.kgs - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    kpart_combine(b, P, slot, t, fo, fc);
+    if (t == 0) b.kgdone[slot] = 0;
+  }
   if (ok0) store_kout(b, g0, fo, fc, mx, my, mz);
 }
 
 template <int ND>
 static void launch_kgather(const Batch& b, cudaStream_t s) {
   if (b.tune.kg_scalar)
-    kgather1s_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
+    kgather1s_kernel<<<b.nkgwork, kPartBlock, 0, s>>>(b);
   else
-    kgather1_kernel<<<b.nblk, kPartBlock / 2, 0, s>>>(b);
+    kgather1_kernel<<<b.nkgwork, kPartBlock / 2, 0, s>>>(b);
   if (ND > 1) kgather_kernel<ND><<<b.nblk, kPartBlock, 0, s>>>(b);
 }
 

@@ -56,6 +56,8 @@ struct SysDev {
   int k_off, nk;        // k-vector range
   int rt_off, rt_n;     // real-space table entries (A, B, C of the reference's tabul)
   int kchunk_off, nkchunk;  // structure-factor partial range (chunks of kKChunk particles)
+  int kgs;                  // k-space gather parts: the k tiles split over kgs blocks per particle block
+  int kgp_off;              // first partial set of the system (kgs > 1)
   int gch_off, pad_g;       // first chunk of the system in the G-tensor partials
   int blk_off, nblk;        // per-particle block range
   int cl_fr;
@@ -195,6 +197,10 @@ struct Batch {
   double* kGs;   // 6 per system: the chunk sums added in chunk order
   int* kgcnt;    // per system: chunks done this step (the last one adds them)
   int* icnt;     // per system: first-half blocks done this step (the last one sets xi_mid)
+  int2* kgwork;  // (particle block, part) of every k-space gather block
+  int nkgwork;
+  float* kgpart; // partial gather sums of split systems: per (particle block, part) kPartBlock x 12
+  int* kgdone;   // per particle block: parts done this launch (the last one combines them)
   float2* Fk;    // 3 ndip: k-space force on each dipole, float-float (hi, lo)
   float2* Tk;    // 3 ndip: k-space torque m x G, float-float
   // integrator partials, per block

@@ -210,6 +210,41 @@ def test_batch_results_equal_alone():
                 assert np.array_equal(np.asarray(obs[k][key]), np.asarray(alone[k][0][key])), (k, key)
 
 
+def test_split_kspace_gather_alone_equals_in_batch():
+    """A system of 4096 rods runs its k-space gather in parts on separate
+    blocks (a function of the system alone): it has the same bits alone and
+    beside small systems, in both gather forms (one or two rods a thread),
+    and its forces stay on the oracle's."""
+    rs = np.random.default_rng(78)
+    n = 4096
+    st, box = S.make_system(n=n, phi=0.2, lengths=rs.uniform(2, 4, n), mu=np.full(n, 1.3), seed=120)
+    big = S.SystemSpec(n=n, box=box, alpha=6.0 / box[0], K_max=5, ksq_max=0)
+    small = []
+    for k, m in enumerate((90, 200)):
+        s2, b2 = S.make_system(n=m, phi=0.1, lengths=rs.uniform(2, 4, m), mu=np.full(m, 1.1), seed=130 + k)
+        small.append((S.SystemSpec(n=m, box=b2, alpha=6.0 / b2[0], K_max=5, ksq_max=0), s2))
+    results = []
+    for kg in (0, 1):
+        with L.Batch([big], [st]) as bt:
+            bt.set_tuning(1, 256, 152 * 8, kg)
+            bt.step(6)
+            results.append(bt.download(0))
+    with L.Batch([small[0][0], big, small[1][0]], [small[0][1], st, small[1][1]]) as bt:
+        bt.step(6)
+        results.append(bt.download(1))
+    for f in ("r", "p", "O", "l", "F", "T"):
+        assert np.array_equal(results[0][f], results[1][f]), ("forms", f)
+        assert np.array_equal(results[0][f], results[2][f]), ("batch", f)
+    with L.Batch([big], [st]) as bt:
+        bt.zero_forces()
+        bt.force_dipK()
+        d = bt.download(0)
+    o = oracle.System(st.r, st.p, st.O, st.l, st.length, st.dia, st.mass, st.dip, box)
+    orc = oracle.Oracle()
+    orc.force_dipK(o, big.K_max, big.alpha, big.ksq_max)
+    assert rms_rel(d["F"], o.F) < TOL_F and rms_rel(d["T"], o.T) < TOL_F
+
+
 def test_noncubic_box_and_field_vs_oracle():
     rng = np.random.default_rng(31)
     n = 120
