@@ -241,6 +241,9 @@ class Batch:
         self.h = h
         self.n = [d.n for d in descs]
         self.nd = [d.nd for d in descs]
+        for k, spec in enumerate(self.specs):
+            if spec is not None and getattr(spec, "cl_energy", 0.0) > 0:
+                self.set_cluster_energy(k, spec.cl_energy)
         if states is not None:
             for k, st in enumerate(states):
                 self.upload(k, st)

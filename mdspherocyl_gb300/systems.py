@@ -159,6 +159,7 @@ class SystemSpec:
     steps: int = 1000
     label: str = ""
     rc_real: float = 0.0  # real-space cutoff: 0 = all minimum-image pairs (the reference)
+    cl_energy: float = 0.0  # cluster bonds by pair energy below -cl_energy kT; 0 = the reference's test
 
 
 @dataclass

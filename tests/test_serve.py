@@ -80,3 +80,29 @@ def test_a_failing_job_leaves_alone():
         for f in ("r", "p", "O", "l", "F", "T", "clust"):
             assert np.array_equal(j.result[f], alone[j.jid][f]), (j.jid, f)
     assert serve.summarize(stats, 1.0)["failed"] == 1
+
+
+def test_cutoff_and_energy_cluster_jobs_as_alone():
+    """Jobs with a real-space cutoff and jobs clustered by pair energy, beside
+    plain ones, moved between batches as the server repacks: each ends with
+    the bits (and the cluster labels) it has alone."""
+    rs = np.random.default_rng(9)
+    jobs = []
+    for k, (n, steps, rc, ce, fr) in enumerate(((300, 31, 4.0, 1.2, 5), (200, 40, 0.0, 0.0, 0), (260, 27, 0.0, 1.5, 7),
+                                                (150, 35, 3.0, 0.0, 0), (120, 22, 0.0, 0.0, 4))):
+        st, box = S.make_system(n=n, phi=float(rs.uniform(0.1, 0.25)), lengths=rs.uniform(2, 3.5, n),
+                                mu=np.full(n, float(rs.uniform(1.5, 2.5))), seed=300 + k, temp=1.0)
+        spec = S.SystemSpec(n=n, box=box, alpha=7.0 / box[0], K_max=6, ksq_max=0, rc_real=rc, cl_energy=ce, cl_fr=fr)
+        jobs.append(serve.Job(k, spec, st, steps, arrival=0.01 * k))
+    alone = {}
+    for j in jobs:
+        with L.Batch([j.spec], [j.state]) as bt:
+            bt.step(j.steps)
+            alone[j.jid] = bt.download(0)
+    srv = serve.Server(tick_steps=9, keep_results=True)
+    stats = srv.run(jobs)
+    assert len(stats.completed) == 5 and stats.repacks >= 3
+    for j in stats.completed:
+        assert j.done == j.steps and j.error is None
+        for f in ("r", "p", "O", "l", "F", "T", "clust"):
+            assert np.array_equal(j.result[f], alone[j.jid][f]), (j.jid, f)
