@@ -936,11 +936,66 @@ void sym3_eigen(const double (&A0)[3][3], double (&d)[3], double (&V)[3][3]) {
   for (int i = 0; i < 3; ++i) d[i] = A[i][i];
 }
 
+// The eigenvalue of largest magnitude of a symmetric 3x3 matrix and its unit
+// eigenvector in closed form: the eigenvalues by the trigonometric solution
+// of the characteristic cubic (O. K. Smith, Commun. ACM 4 (1961) 168), the
+// eigenvector as the longest cross product of two rows of A - lambda I.
+// false when that eigenvalue is within 1e-6 of another (the eigenvector is
+// then ill-determined in closed form; the Jacobi sweeps decide it).
+bool sym3_dominant(const double (&A)[3][3], double& lam, double (&e)[3]) {
+  const double p1 = A[0][1] * A[0][1] + A[0][2] * A[0][2] + A[1][2] * A[1][2];
+  const double q = (A[0][0] + A[1][1] + A[2][2]) / 3.0;
+  const double p2 = (A[0][0] - q) * (A[0][0] - q) + (A[1][1] - q) * (A[1][1] - q) +
+                    (A[2][2] - q) * (A[2][2] - q) + 2.0 * p1;
+  const double p = std::sqrt(p2 / 6.0);
+  if (!(p > 0)) return false;
+  double B[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) B[i][j] = (A[i][j] - (i == j ? q : 0.0)) / p;
+  const double det = B[0][0] * (B[1][1] * B[2][2] - B[1][2] * B[2][1]) -
+                     B[0][1] * (B[1][0] * B[2][2] - B[1][2] * B[2][0]) +
+                     B[0][2] * (B[1][0] * B[2][1] - B[1][1] * B[2][0]);
+  const double r = std::fmin(1.0, std::fmax(-1.0, det / 2.0));
+  const double phi = std::acos(r) / 3.0;
+  const double l1 = q + 2.0 * p * std::cos(phi), l3 = q + 2.0 * p * std::cos(phi + 2.0 * M_PI / 3.0);
+  const double ls[3] = {l1, 3.0 * q - l1 - l3, l3};
+  int c = 0;
+  for (int k = 1; k < 3; ++k)
+    if (std::fabs(ls[k]) > std::fabs(ls[c])) c = k;
+  lam = ls[c];
+  double gap = 1e300;
+  for (int k = 0; k < 3; ++k)
+    if (k != c) gap = std::fmin(gap, std::fabs(ls[k] - lam));
+  if (gap < 1e-6 * (std::fabs(l1) + std::fabs(l3))) return false;
+  double R[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) R[i][j] = A[i][j] - (i == j ? lam : 0.0);
+  double best = -1.0, v[3] = {0.0, 0.0, 0.0};
+  for (int a = 0; a < 2; ++a)
+    for (int b2 = a + 1; b2 < 3; ++b2) {
+      const double x[3] = {R[a][1] * R[b2][2] - R[a][2] * R[b2][1], R[a][2] * R[b2][0] - R[a][0] * R[b2][2],
+                           R[a][0] * R[b2][1] - R[a][1] * R[b2][0]};
+      const double n2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
+      if (n2 > best) {
+        best = n2;
+        v[0] = x[0];
+        v[1] = x[1];
+        v[2] = x[2];
+      }
+    }
+  const double nv = std::sqrt(best);
+  if (!(nv > 0)) return false;
+  for (int k = 0; k < 3; ++k) e[k] = v[k] / nv;
+  return true;
+}
+
 // oo_params (v25/functions.cpp:2702-2760) from the sums v[12] over n
 // particles: sum o (3), sum o o^T (xx xy xz yy yz zz), sum mu o_dipole (3).
 // Q = sum (3 o o^T - 1) / (2 n) (Qmat_3d, :3426-3445); G2 is its eigenvalue
 // of largest magnitude, chosen among equal magnitudes as the reference
 // chooses (:2738-2748), and G1 = |e . sum o| / n along that eigenvector.
+// Closed form when that eigenvalue is distinct (every step of every system
+// converts these, so its cost shows), the Jacobi sweeps otherwise.
 void order_params(const double* v, int n, double* G1, double* G2, double* M) {
   if (M)
     for (int a = 0; a < 3; ++a) M[a] = v[9 + a];
@@ -953,6 +1008,12 @@ void order_params(const double* v, int n, double* G1, double* G2, double* M) {
   double Q[3][3], ev[3], V[3][3];
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) Q[i][j] = (3.0 * v[ix[i][j]] - (i == j ? n : 0.0)) / (2.0 * n);
+  double lam, e[3];
+  if (sym3_dominant(Q, lam, e)) {  // the common case, in closed form
+    if (G2) *G2 = std::fabs(lam);
+    if (G1) *G1 = std::fabs(e[0] * v[0] + e[1] * v[1] + e[2] * v[2]) / n;
+    return;
+  }
   sym3_eigen(Q, ev, V);
   const double e1 = std::fabs(ev[0]), e2 = std::fabs(ev[1]), e3 = std::fabs(ev[2]);
   const int c = (e1 >= e2 && e1 >= e3) ? 0 : (e2 > e1 && e2 >= e3) ? 1 : 2;
