@@ -517,16 +517,18 @@ __global__ void __launch_bounds__(32 * W, 20 / W) real_pairs_kernel(Batch b) {
 // the reference's force_dipR with its table zeroed beyond rc_real, where
 // pairs beyond rc_real + Lh add nothing, so only the rods the list holds
 // (centres within rc_real + Lh + the dipoles' offsets + the skin) are
-// visited.  One thread per dipole i takes its partner dipoles -- the listed
-// rods' dipoles, rods in ascending order -- two at a time through the
-// tiles' pair step (both halves holding dipole i) and keeps i's own force
-// and torque; every pair is met from both ends, so the energy and pressure
-// tensor take half of each meeting.  Per-dipole sums in list order: no
-// atomics, the same bits alone and in any batch.  Writes each dipole's
-// force and torque where real_sum writes them, and its block's energy and
-// pressure tensor (float-float block sums) for the per-system sum.
-__global__ void __launch_bounds__(kPartBlock) real_cut_kernel(Batch b) {
-  __shared__ double sh[10 * kPartBlock / 32];
+// visited.  A group of kCutLanes lanes per dipole i takes its partner
+// dipoles -- the listed rods' dipoles, rods in ascending order -- two at a
+// time through the tiles' pair step (both halves holding dipole i), lane j
+// the pair steps j, j + kCutLanes, ...; a fixed shuffle tree adds the
+// lanes' sums.  Only i's own force and torque are kept, so every pair is met
+// from both ends and the energy and pressure tensor take half of each
+// meeting.  No atomics: the same bits alone and in any batch.  Writes each
+// dipole's force and torque where real_sum writes them, and its block's
+// energy and pressure tensor (float-float block sums) for the per-system sum.
+constexpr int kCutLanes = 4;
+__global__ void __launch_bounds__(kPartBlock * kCutLanes) real_cut_kernel(Batch b) {
+  __shared__ double sh[10 * kPartBlock * kCutLanes / 32];
   const int2 bk = b.blk[blockIdx.x];
   const SysDev& P = b.sys[bk.x];
   if (P.rc_real <= 0.0) return;  // the same for the whole block
@@ -534,6 +536,7 @@ __global__ void __launch_bounds__(kPartBlock) real_cut_kernel(Batch b) {
   const int p0 = bk.y - P.part_off;
   const int np = min(kPartBlock, P.n - p0);
   const int ND = b.ndtot;
+  const int lane = threadIdx.x % kCutLanes;
   PairConst K;
   K.xh = b2(P.xh);
   K.xlo = b2(P.xlo);
@@ -557,7 +560,13 @@ __global__ void __launch_bounds__(kPartBlock) real_cut_kernel(Batch b) {
   FF e[10];
 #pragma unroll
   for (int c = 0; c < 10; ++c) e[c] = ff_of(0.f);
-  for (int loc = threadIdx.x; loc < np * nd; loc += kPartBlock) {
+  // a warp holds 32 / kCutLanes groups; every lane of a warp takes the same
+  // trips (the shuffles need the whole warp), groups past the block's
+  // dipoles with no partners
+  const int wg = (threadIdx.x % 32) / kCutLanes;
+  for (int base = (threadIdx.x / 32) * (32 / kCutLanes); base < np * nd; base += kPartBlock) {
+    const bool act = base + wg < np * nd;
+    const int loc = act ? base + wg : base;
     const int il = p0 * nd + loc;  // dipole within the system
     const int g = P.dip_off + il;
     const int ip = P.part_off + il / nd;
@@ -576,8 +585,8 @@ __global__ void __launch_bounds__(kPartBlock) real_cut_kernel(Batch b) {
     for (int c = 0; c < 9; ++c) s.pt[c] = b2(0.f);
     s.U = s.Uc = b2(0.f);
     const int* lst = b.rnb + (long long)ip * kMaxR;
-    const int nj = b.rnbc[ip] * nd;
-    for (int k = 0; k < nj; k += 2) {
+    const int nj = act ? b.rnbc[ip] * nd : 0;
+    for (int k = 2 * lane; k < nj; k += 2 * kCutLanes) {
       const bool two = k + 1 < nj;
       const int k1 = two ? k + 1 : k;
       const int ga = P.dip_off + (lst[k / nd] - P.part_off) * nd + k % nd;
@@ -589,24 +598,48 @@ __global__ void __launch_bounds__(kPartBlock) real_cut_kernel(Batch b) {
       JOut o;
       tile_step<true, true>(K, s, jpa, jma, jpb, jmb, true, two, o);
     }
-    float fv[6];
+    // a lane's sums, then the group's (xor tree over the kCutLanes lanes)
+    float v[17];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      fv[c] = s.F[c].x + s.F[c].y;
-      fv[3 + c] = s.T[c].x + s.T[c].y;
+      v[c] = s.F[c].x + s.F[c].y;
+      v[3 + c] = s.T[c].x + s.T[c].y;
     }
+    v[6] = (s.U.x + (-s.Uc.x)) + (s.U.y + (-s.Uc.y));
 #pragma unroll
-    for (int c = 0; c < 6; ++c) {  // as (hi, lo) the way real_sum stores its sums
-      const float hx = c < 3 ? s.F[c].x : s.T[c - 3].x, hy = c < 3 ? s.F[c].y : s.T[c - 3].y;
-      const float bb = fv[c] - hx;
-      b.rsum[(long long)c * ND + g] = make_float2(fv[c], (hx - (fv[c] - bb)) + (hy - bb));
+    for (int c = 0; c < 9; ++c) v[7 + c] = s.pt[c].x + s.pt[c].y;
+    float lo[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) lo[c] = 0.f;
+#pragma unroll
+    for (int off = kCutLanes / 2; off > 0; off >>= 1) {
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        const float w = __shfl_xor_sync(0xffffffffu, v[c], off);
+        if (c < 6) {  // forces and torques in float-float (TwoSum)
+          const float wl = __shfl_xor_sync(0xffffffffu, lo[c], off);
+          const float sum = v[c] + w;
+          const float bb = sum - v[c];
+          lo[c] += wl + ((v[c] - (sum - bb)) + (w - bb));
+          v[c] = sum;
+        } else {
+          v[c] += w;
+        }
+      }
     }
-    e[0] = ff_add(e[0], ff_of(0.5f * ((s.U.x + (-s.Uc.x)) + (s.U.y + (-s.Uc.y)))));
+    if (act && lane == 0) {
 #pragma unroll
-    for (int c = 0; c < 9; ++c) e[1 + c] = ff_add(e[1 + c], ff_of(0.5f * (s.pt[c].x + s.pt[c].y)));
+      for (int c = 0; c < 6; ++c) {
+        const float r = v[c] + lo[c];
+        b.rsum[(long long)c * ND + g] = make_float2(r, lo[c] - (r - v[c]));
+      }
+      e[0] = ff_add(e[0], ff_of(0.5f * v[6]));
+#pragma unroll
+      for (int c = 0; c < 9; ++c) e[1 + c] = ff_add(e[1 + c], ff_of(0.5f * v[7 + c]));
+    }
   }
   double out[10];
-  block_sum<10, kPartBlock>(e, sh, out);
+  block_sum<10, kPartBlock * kCutLanes>(e, sh, out);
   if (threadIdx.x == 0) {
     double* dst = b.rlE + (long long)blk_slot(P, bk) * 10;
 #pragma unroll
@@ -678,7 +711,7 @@ __global__ void __launch_bounds__(128) strip_energy_kernel(Batch b) {
 }
 
 void launch_real_cut(const Batch& b, cudaStream_t s) {
-  if (b.any_rc && b.nblk) real_cut_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
+  if (b.any_rc && b.nblk) real_cut_kernel<<<b.nblk, kPartBlock * kCutLanes, 0, s>>>(b);
 }
 
 void launch_real_sum(const Batch& b, cudaStream_t s) {
