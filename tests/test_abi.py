@@ -52,6 +52,25 @@ def test_estimate_bytes_without_gpu():
     assert L.estimate_bytes([d, d]) > nb
 
 
+def test_estimate_bytes_counts_the_cutoff_lists_and_gather_parts():
+    """The HBM a batch needs (what the server admits against) includes the
+    real-space neighbour lists of a cutoff system (256 ints per rod) and the
+    partial sums of a split k-space gather (N >= 4096, one dipole)."""
+    spec, st = S.plain_c0(seed=0, n=512)
+    d0 = L.desc_from_spec(spec, 1)
+    spec.rc_real = 3.0
+    d1 = L.desc_from_spec(spec, 1)
+    b0, b1 = L.estimate_bytes([d0]), L.estimate_bytes([d1])
+    # the lists (512 x 256 ints) less the all-pairs tiles' partials it drops (8 x 8 tiles x 6 x 64 floats)
+    assert b1 - b0 >= 512 * 256 * 4 - 8 * 8 * 6 * 64 * 4 - 64 * 1024
+    big, _ = S.plain_c1(seed=0, n=4096)
+    d2 = L.desc_from_spec(big, 1)
+    d3 = L.desc_from_spec(big, 1)
+    d3.n = 4095  # below the split: one part per particle block
+    # 32 particle blocks, at least 2 parts each, kPartBlock x 12 floats a part
+    assert L.estimate_bytes([d2]) - L.estimate_bytes([d3]) >= 32 * 2 * 128 * 12 * 4
+
+
 @pytest.mark.skipif(os.path.exists("/dev/nvidia0"), reason="a GPU is visible")
 def test_create_without_gpu_fails_cleanly():
     spec, st = S.plain_c0(seed=0, n=32)
