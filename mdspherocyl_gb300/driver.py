@@ -25,7 +25,8 @@ equilibration steps the correlation histograms every corrf steps, the order
 parameters, the pos_vel dumps every tcfd steps, ptens.dat and magmom.dat
 every tcfv steps and the running sums; every iprint steps conf.dat, the
 generator states, counters.dat, correlation.dat and a line of output.dat;
-at the end the averages block of output.dat and time.dat.  The reference's
+at the end the averages block of output.dat and time.dat (the reference's
+per-function lines, from the GPU kernels' times).  The reference's
 neighbour-list bookkeeping file compConf.dat is written once, at the start:
 this library keeps its own list state on the GPU.
 
@@ -97,13 +98,20 @@ def new_box(p: F.RunInput):
 
 
 class Driver:
-    def __init__(self, workdir: str = ".", device: int = 0, out=sys.stdout, variant: str = "v25"):
+    def __init__(self, workdir: str = ".", device: int = 0, out=sys.stdout, variant: str = "v25",
+                 rc_real: float = 0.0, ksq_max: int = 0, cl_energy: float = 0.0):
+        """rc_real, ksq_max and cl_energy are this library's knobs, not
+        input.txt's (which keeps the reference's layout): a real-space
+        cutoff, a spherical k-set |n|^2 <= ksq_max, clusters by pair energy
+        below -cl_energy kT.  Their defaults are the reference's behaviour."""
         if variant not in ("v25", "v251"):
             raise ValueError(f"unknown driver variant {variant}")
         self.d = workdir
         self.device = device
         self.out = out
         self.v251 = variant == "v251"
+        self.rc_real, self.ksq_max, self.cl_energy = float(rc_real), int(ksq_max), float(cl_energy)
+        self._cor_s = 0.0  # host seconds in the correlation calls
 
     def path(self, name: str) -> str:
         return os.path.join(self.d, name)
@@ -185,9 +193,9 @@ class Driver:
         if Lmin > 200:
             raise RunError(f"Tab is not large enough. Lmin={F.g6(Lmin)} > 200")
 
-        spec = SystemSpec(n=n, box=box, alpha=p.alpha, K_max=p.K_max, ksq_max=0, temp=p.temp, Q=p.Q,
+        spec = SystemSpec(n=n, box=box, alpha=p.alpha, K_max=p.K_max, ksq_max=self.ksq_max, temp=p.temp, Q=p.Q,
                           gamma=p.gamma, dt=p.Dt, B=np.asarray(p.B, dtype=np.float64), sr_cut=sr_cut, xi0=0.0,
-                          min_s=p.min_s, cl_fr=p.cl_fr)
+                          min_s=p.min_s, cl_fr=p.cl_fr, rc_real=self.rc_real, cl_energy=self.cl_energy)
         st = SystemState(r, pm, O, l, length, dia, mass, dip)
         self._mass = mass
         # each particle's own dipoles (its species'): print_conf writes no padding
@@ -235,7 +243,6 @@ class Driver:
         I = inertia(length, dia, mass)
         total = p.pre_steps + p.Nsteps
         t_wall0, t_cpu0 = time.perf_counter(), time.process_time()
-        t_start = t_wall0
         step = 0
         while step < total:
             # steps up to the next one that needs more than its observables
@@ -270,7 +277,9 @@ class Driver:
                     self._npc[1] += int(sizes[sizes > 1].sum())
                 if s >= p.pre_steps:
                     if p.corrf > 0 and math.fmod(float(np.float32(s)), p.corrf) == 0:
+                        t_c = time.perf_counter()
                         hist = bt.correlations(p.bar_w, [hist])[0]
+                        self._cor_s += time.perf_counter() - t_c
                         cor_cont += 1.0 / V
                     var.G1, var.G2 = o["G1"], o["G2"]
                     if p.tcfd > 0 and math.fmod(float(np.float32(s)), p.tcfd) == 0:
@@ -304,8 +313,7 @@ class Driver:
                     F.append(self.path("output.dat"), F.output_line(Time, te, tc, var, Mom))
                     t_wall0, t_cpu0 = t_wall, t_cpu
             step = nxt + 1
-        with open(self.path("time.dat"), "w") as f:
-            f.write(f"GB300 step time. elap: {F.g6((time.perf_counter() - t_start) / max(total, 1))}\n")
+        self._write_time(bt, p, V, cor_cont)
         if cont > 0:
             pol = None
             if self.v251:
@@ -313,6 +321,33 @@ class Driver:
                 pol = num / den if den != 0 else (float("nan") if num == 0 else float("inf"))
             F.append(self.path("output.dat"), F.final_report(Time, AcT, AcTsq, cont, p, box, pol_deg=pol))
         return 0
+
+    def _write_time(self, bt, p, V: float, cor_cont: float) -> None:
+        """time.dat in the reference's layout (v25/main.cpp:825-838; the later
+        driver adds the two Ewald lines, v25/v251/main.cpp:826-840): seconds
+        per step of each function's GPU kernels, timed with CUDA events on a
+        copy of the final state (the run's own state is not advanced), and
+        the correlation calls' host time divided as the reference divides
+        it.  The cpu column is the host's share, which the GPU work leaves at
+        about zero."""
+        ms = {}
+        try:
+            with L.Batch([None], None, device=self.device, descs=[bt._descs[0]]) as sc:
+                sc.transfer_from(0, bt, 0)
+                ms = sc.profile(5)
+        except L.MdscError:
+            pass
+        t = lambda *names: sum(ms.get(x, 0.0) for x in names) * 1e-3  # noqa: E731
+        rows = [("X move time", t("integrate_first")), ("Force_ss time", t("list_build", "wca"))]
+        if self.v251:
+            rows += [("Force_dipR time", t("real_pairs", "real_sum", "real_cut")),
+                     ("Force_dipK time", t("kspace_sum", "kspace_combine", "kspace_gather"))]
+        rows.append(("P move time", t("finalize", "reduce_obs")))
+        cor = self._cor_s / (V * cor_cont) if cor_cont > 0 else 0.0
+        rows.append(("correl. time", cor))
+        with open(self.path("time.dat"), "w") as f:
+            for name, sec in rows:
+                f.write(f"{name}. elap: {F.g6(sec)} cpu: 0\n")
 
     def _event(self, p, s: int) -> bool:
         """A step after which the loop needs more than the step's observables."""
@@ -378,8 +413,14 @@ def main(argv=None) -> int:
     ap.add_argument("workdir", nargs="?", default=".")
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--variant", choices=("v25", "v251"), default="v25")
+    ap.add_argument("--real-cutoff", type=float, default=0.0,
+                    help="real-space cutoff (the reference's table zeroed beyond it); 0: all pairs")
+    ap.add_argument("--ksq-max", type=int, default=0, help="keep |n|^2 <= this of the k cube; 0: the whole cube")
+    ap.add_argument("--cluster-energy", type=float, default=0.0,
+                    help="clusters by pair energy below -this kT; 0: the reference's geometric test")
     a = ap.parse_args(argv)
-    return Driver(a.workdir, a.device, variant=a.variant).run()
+    return Driver(a.workdir, a.device, variant=a.variant, rc_real=a.real_cutoff, ksq_max=a.ksq_max,
+                  cl_energy=a.cluster_energy).run()
 
 
 if __name__ == "__main__":

@@ -121,6 +121,10 @@ def test_new_run_writes_every_file():
                   "ptens.dat", "magmom.dat", "output.dat", os.path.join("pos_vel", "pos_vel_0.dat")):
             assert os.path.getsize(os.path.join(d, f)) > 0, f
         assert open(os.path.join(d, "Error.dat")).read() == ""
+        # time.dat in the reference's layout, from the GPU kernels' times
+        lines = open(os.path.join(d, "time.dat")).read().splitlines()
+        assert [ln.split(".")[0] for ln in lines] == ["X move time", "Force_ss time", "P move time", "correl"]
+        assert all(float(ln.split("elap:")[1].split()[0]) > 0 for ln in lines[:3])
 
 
 def test_new_run_lattice_is_the_references():
@@ -157,3 +161,28 @@ def test_thermalize_momenta():
     lb = np.einsum("nab,nb->na", st.O, a["l"])  # body frame
     Kr = 0.5 * np.sum(lb ** 2 / I)
     assert abs(2 * Kr / (3 * 3000) - 1.7) < 0.05 * 1.7
+
+
+def test_library_knobs_in_the_run_loop():
+    """The driver's own options -- a real-space cutoff, a spherical k-set,
+    clusters by pair energy -- run the reference's example restart to the
+    end with every file written; the energy criterion changes the labels."""
+    run = os.path.join(GOLD, "run_v251")
+    labels = {}
+    for ce in (0.0, 0.5):
+        with tempfile.TemporaryDirectory() as d:
+            for f in ("conf.dat", "ran_state0F.dat", "ran_state1F.dat", "counters.dat", "correlation.dat"):
+                shutil.copy(os.path.join(run, "init", f), d)
+            shutil.copy(os.path.join(run, "restart", "input.txt"), d)
+            p = F.read_input(os.path.join(d, "input.txt"))
+            length, dia, mass, dip, nd, nd_part = layout(p)
+            box = F.read_conf(os.path.join(d, "conf.dat"), p.n_part, nd_part)["box"]
+            with open(os.devnull, "w") as devnull:
+                drv = Driver(d, out=devnull, variant="v251", rc_real=0.4 * float(min(box)), ksq_max=16,
+                             cl_energy=ce)
+                assert drv.run() == 0, open(os.path.join(d, "Error.dat")).read()
+            c = F.read_conf(os.path.join(d, "conf.dat"), p.n_part, nd_part)
+            assert np.all(np.isfinite(c["r"])) and np.all(np.isfinite(c["p"]))
+            labels[ce] = c["clust"]
+            assert os.path.getsize(os.path.join(d, "output.dat")) > 0
+    assert not np.array_equal(labels[0.0], labels[0.5])
