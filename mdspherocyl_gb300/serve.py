@@ -17,6 +17,7 @@ job, which leaves at the next tick; the others run on undisturbed.
 """
 from __future__ import annotations
 
+import json
 import time
 from collections import deque
 from dataclasses import dataclass, field
@@ -46,6 +47,14 @@ class Job:
     def n(self) -> int:
         return self.spec.n
 
+    def record(self) -> dict:
+        """One line of the server's job log."""
+        rej = isinstance(self.obs, dict) and str(self.obs.get("status", "")).startswith("rejected")
+        return {"job": self.jid, "n": self.n, "steps": self.steps, "done": self.done, "arrival": self.arrival,
+                "start": self.start, "finish": self.finish,
+                "latency": None if self.finish is None else self.finish - self.arrival,
+                "error": self.obs["status"] if rej else self.error}
+
 
 @dataclass
 class ServerStats:
@@ -62,7 +71,9 @@ class ServerStats:
 
 class Server:
     def __init__(self, hbm_budget_bytes: float = 120e9, tick_steps: int = 50, max_systems: int = 512,
-                 device: int = 0, keep_results: bool = False, clock=time.perf_counter):
+                 device: int = 0, keep_results: bool = False, clock=time.perf_counter, log=None):
+        """log: a writable text stream; every finished (or rejected) job adds
+        one JSON line to it (Job.record)."""
         self.budget = float(hbm_budget_bytes)
         self.tick = int(tick_steps)
         self.max_systems = int(max_systems)
@@ -73,6 +84,12 @@ class Server:
         self.running: list[Job] = []
         self.batch: L.Batch | None = None
         self.stats = ServerStats()
+        self.log = log
+
+    def _complete(self, job: Job) -> None:
+        self.stats.completed.append(job)
+        if self.log is not None:
+            self.log.write(json.dumps(job.record()) + "\n")
 
     # -- admission --------------------------------------------------------
     def submit(self, job: Job) -> None:
@@ -117,7 +134,7 @@ class Server:
             if self.keep_results:
                 j.result = self.batch.download(k)
             j.finish = now
-            self.stats.completed.append(j)
+            self._complete(j)
         new = []
         while self.waiting and self.waiting[0].arrival <= now:
             head = self.waiting[0]
@@ -128,7 +145,7 @@ class Server:
                 # larger than the whole budget on its own: it can never run
                 head.finish = now
                 head.obs = {"status": "rejected: exceeds the HBM budget"}
-                self.stats.completed.append(self.waiting.popleft())
+                self._complete(self.waiting.popleft())
             else:
                 break
         if finished or new:

@@ -43,13 +43,22 @@ def test_each_job_alone_equals_in_the_mix():
 
 
 def test_budget_admission_serialises_jobs():
+    import io
+    import json
+
     jobs = _jobs()[:3]
     one = max(L.estimate_bytes([L.desc_from_spec(j.spec, 1)]) for j in jobs)
-    srv = serve.Server(hbm_budget_bytes=one * 1.01, tick_steps=10)
+    log = io.StringIO()
+    srv = serve.Server(hbm_budget_bytes=one * 1.01, tick_steps=10, log=log)
     stats = srv.run(jobs)
     assert len(stats.completed) == 3 and stats.max_running == 1
     lat = stats.latencies()
     assert np.all(lat > 0)
+    # one JSON line per job: its size, steps, times and error
+    recs = [json.loads(x) for x in log.getvalue().splitlines()]
+    assert sorted(r["job"] for r in recs) == [j.jid for j in jobs]
+    for r in recs:
+        assert r["done"] == r["steps"] and r["error"] is None and r["finish"] >= r["start"] >= r["arrival"]
 
 
 def test_a_failing_job_leaves_alone():
