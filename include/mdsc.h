@@ -134,9 +134,11 @@ typedef struct mdsc_batch mdsc_batch;
 mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mdsc_batch** out);
 mdsc_status mdsc_destroy(mdsc_batch* b);
 int mdsc_num_systems(const mdsc_batch* b);
-/* bytes of GPU memory the batch holds */
+/* bytes of GPU memory the batch holds (with the energy criterion's
+   candidate lists once a system of it takes that criterion) */
 size_t mdsc_device_bytes(const mdsc_batch* b);
-/* GPU memory a batch of these systems would need, without creating it */
+/* GPU memory a batch of these systems would need, without creating it.
+   mdsc_set_cluster_energy later adds 260 bytes per particle of the batch. */
 size_t mdsc_estimate_bytes(const mdsc_system_desc* descs, int nsys);
 /* sizeof of the ABI's structures as this library was built (for bindings
    that lay them out by hand): mdsc_system_desc, mdsc_host_state,
@@ -208,7 +210,9 @@ mdsc_status mdsc_clust_conf(mdsc_batch* b, int sys, int* labels, int* n_clusters
    (bare dipole-dipole energy at the minimum image of the dipole sites) is
    below -u_bond_kT * T, T the system's temperature.  Labels are then
    numbered as clust_conf numbers them.  MDSC_ERR_LIST_OVERFLOW from the
-   clustering if a particle has more than 16 such bonds to higher indices. */
+   clustering if a particle has more than 16 such bonds (or 64 screened
+   candidates) to higher indices.  The first call with u_bond_kT > 0 on a
+   batch allocates the candidate lists: 260 bytes per particle of the batch. */
 mdsc_status mdsc_set_cluster_energy(mdsc_batch* b, int sys, double u_bond_kT);
 
 /* Moves system ssys of batch src into slot dsys of batch dst (same device,

@@ -1205,7 +1205,12 @@ mdsc_status mdsc_destroy(mdsc_batch* B) {
 }
 
 int mdsc_num_systems(const mdsc_batch* B) { return B ? B->nsys : 0; }
-size_t mdsc_device_bytes(const mdsc_batch* B) { return B ? B->arena_bytes : 0; }
+size_t mdsc_device_bytes(const mdsc_batch* B) {
+  if (!B) return 0;
+  // + the energy criterion's candidate lists, allocated on first use
+  const size_t n = (size_t)std::max(B->lo.ntot, 1);
+  return B->arena_bytes + (B->b.ecand ? sizeof(int) * n * (kMaxE + 1) : 0);
+}
 int mdsc_launches_per_step(const mdsc_batch* B) { return B ? B->launches : 0; }
 void* mdsc_stream(const mdsc_batch* B) { return B ? (void*)B->st : nullptr; }
 

@@ -101,7 +101,10 @@ class Server:
     def _fits(self, jobs) -> bool:
         if len(jobs) > self.max_systems:
             return False
-        return L.estimate_bytes([self._desc(j) for j in jobs]) <= self.budget
+        need = L.estimate_bytes([self._desc(j) for j in jobs])
+        if any(getattr(j.spec, "cl_energy", 0.0) > 0 for j in jobs):
+            need += 260 * sum(j.n for j in jobs)  # the energy criterion's candidate lists (mdsc_set_cluster_energy)
+        return need <= self.budget
 
     # -- one tick -----------------------------------------------------------
     def _repack(self, keep: list[Job], new: list[Job]) -> None:
