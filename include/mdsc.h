@@ -174,7 +174,9 @@ mdsc_status mdsc_zero_forces(mdsc_batch* b);
    reference's false. */
 mdsc_status mdsc_force_sc(mdsc_batch* b, double* U, double* W, double* PT);
 /* force_dipR (v25/functions.hpp:40-41, v25/functions.cpp:1555-1678):
-   real-space Ewald over all minimum-image dipole pairs, accumulated. */
+   real-space Ewald over all minimum-image dipole pairs, accumulated; for a
+   system with rc_real > 0, force_dipR with its table zeroed beyond rc_real,
+   over the system's neighbour list. */
 mdsc_status mdsc_force_dipR(mdsc_batch* b, double* U, double* PT);
 /* force_dipK (v25/functions.hpp:42-43, v25/functions.cpp:1706-1961):
    reciprocal-space Ewald, accumulated. */
