@@ -12,7 +12,9 @@ Metric: aggregate particle-steps/s.  `value` is device-timed with the
 state resident in HBM (CUDA events around each step, L2 flushed between
 steps); `e2e` goes through the C ABI with host buffers: every step uploads
 the packed state (r, p, O, l, F, T) from pinned memory, steps once and
-downloads it again.
+downloads the observables and the whole updated state again.  The roofline
+of the dominant kernel (real_pairs, FP32-bound) is taken against the FP32
+multiply-add peak measured on the same device (mdsc_fp32_peak).
 
   python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
                   [--workload replica_mix|c0|c1|c2]
@@ -176,14 +178,6 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
-
-
-def measured_peaks():
-    p = os.path.join(HERE, "MEASURED_PEAKS.json")
-    if os.path.exists(p):
-        with open(p) as f:
-            return json.load(f), "measured"
-    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
 
 
 def cpu_sample(states, threads: int, budget_s: float = 20.0, stride: int = 16):
@@ -401,9 +395,13 @@ def run_ours(args):
     cutoff = single and getattr(args, "rc_value", 0.0) > 0
     rp_ms = prof.get("real_pairs", float("nan"))
     achieved = FLOP_PER_PAIR * pairs / (rp_ms * 1e-3) / 1e12 if not cutoff else float("nan")
-    peaks, src = measured_peaks()
-    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
-    fp32_peak = 2 * 128 * 152 * sm_max * 1e6 / 1e12
+    # the FP32 multiply-add peak of this device, measured (mdsc_fp32_peak),
+    # with the SM clock sampled while the probe runs
+    pclk = ClockSampler(device)
+    pclk.start()
+    probe = L.fp32_peak(device, reps=5)
+    probe_clocks = pclk.stop()
+    fp32_peak = max(probe["ffma_tflops"], probe["ffma2_tflops"])
 
     # ---- end to end through the C ABI with host buffers ----
     nd = sts[0].dip.shape[1]
@@ -412,29 +410,37 @@ def run_ours(args):
     h["O"] = pin(ntot, 3, 3)
     bt.download_all(h["r"], h["p"], h["O"], h["l"], h["F"], h["T"])
     # every step: the step's input (the whole state of every system) from
-    # pinned host memory, the step, and the step's result (every system's
-    # energies, pressure tensors, thermostat and status) read back
+    # pinned host memory, the step, and the step's result read back: every
+    # system's observables (energies, pressure tensors, thermostat, status)
+    # and the whole updated state (r, p, O, l, F, T), as a caller of the
+    # reference's per-function boundary needs it
     obs_buf = (L.Observables * len(specs))()
-    bytes_h2d = sum(v.nbytes for v in h.values())
-    bytes_d2h = ctypes.sizeof(obs_buf)
+    bytes_state = sum(v.nbytes for v in h.values())
+    bytes_obs = ctypes.sizeof(obs_buf)
 
-    def e2e_step():
+    def e2e_step(state_back: bool):
         bt.upload_all(h["r"], h["p"], h["O"], h["l"], h["F"], h["T"])
         code = bt.lib.mdsc_step(bt.h, 1, obs_buf)  # ends with the observables in host memory
         if code != 0:
             raise L.MdscError(code, "mdsc_step", bt._err())
+        if state_back:
+            bt.download_all(h["r"], h["p"], h["O"], h["l"], h["F"], h["T"])
 
-    for _ in range(2):
-        e2e_step()
-    e2e_steps = max(3, min(args.steps, 20))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        e2e_step()
-    torch.cuda.synchronize()
-    t_e2e = time.perf_counter() - t0
-    (_,), (t_e2e,) = aggregate_ranks([0], [t_e2e], device=f"cuda:{device}")
-    e2e = ntot_all * e2e_steps / t_e2e
+    def e2e_rate(state_back: bool):
+        for _ in range(2):
+            e2e_step(state_back)
+        nst = max(3, min(args.steps, 20))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(nst):
+            e2e_step(state_back)
+        torch.cuda.synchronize()
+        tt = time.perf_counter() - t0
+        (_,), (tt,) = aggregate_ranks([0], [tt], device=f"cuda:{device}")
+        return ntot_all * nst / tt
+
+    e2e = e2e_rate(True)
+    e2e_obs_only = e2e_rate(False)
     launches = bt.launches_per_step + 1  # + the per-call reset of the noise row
     bt.close()
     serving = run_serving(args, device) if (args.jobs > 0 and ws == 1 and not single) else None
@@ -462,17 +468,20 @@ def run_ours(args):
                        "real_space": real_space(args), "dt": 1e-3,
                        "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{ws}",
                        "graph": "one CUDA graph per step", "launch_mappings": tuning},
-            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": bytes_h2d,
-                    "d2h_bytes_per_step": bytes_d2h},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": bytes_state,
+                    "d2h_bytes_per_step": bytes_state + bytes_obs,
+                    "how": "C ABI, pinned host buffers: the whole state up, one step, observables and the whole "
+                           "updated state (r, p, O, l, F, T) down, every step",
+                    "observables_only": {"value": e2e_obs_only, "d2h_bytes_per_step": bytes_obs}},
             "gpu_launches": launches * args.steps,
             "roofline": None if cutoff else {
                 "bound": "fp32", "kernel": "real_pairs", "achieved": achieved, "peak": fp32_peak,
                 "unit": "TFLOP/s", "frac": achieved / fp32_peak,
                 "traffic": REAL_PAIRS_DRAM_BYTES_PER_PAIR * pairs,
                 "traffic_unit": "bytes per launch (ncu dram read+write, scaled by pairs)",
-                "peak_source": (f"nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 FLOP at "
-                                f"{sm_max:.0f} MHz ({src} max SM clock); MEASURED_PEAKS.json has "
-                                f"HBM and bf16 tensor figures only"),
+                "peak_source": ("measured: mdsc_fp32_peak (independent FFMA / FFMA2 chains on every SM, "
+                                "CUDA events, best of 5), the larger of the two forms, of measured"),
+                "peak_probe": {**probe, "clocks": probe_clocks},
                 "flop_per_pair": FLOP_PER_PAIR, "pairs_per_launch": pairs,
                 "kernel_ms": rp_ms},
             "kernel_ms": prof,

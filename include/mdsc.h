@@ -364,7 +364,11 @@ mdsc_status mdsc_set_tuning(mdsc_batch* b, const int* values);
    on every GPU that loads the library, held until the process exits), so
    ndip may not exceed 4096 (MDSC_ERR_TOO_LARGE otherwise).  The first call
    on a device looks up that array's device address; make it before any
-   stream capture.  Calls share the array and overwrite what they read, so
+   stream capture.  The address is kept per device and CUDA context: after
+   cudaDeviceReset the next call looks it up again (so it, too, must come
+   before any capture).  A CUDA error already pending on the calling thread
+   makes the call return MDSC_ERR_CUDA without launching, and leaves that
+   error pending.  Calls share the array and overwrite what they read, so
    calls whose work overlaps on the GPU race.  No counterpart in the
    reference: it is the GPU form of force_dipR's arithmetic for callers
    without an allocator. */
@@ -373,6 +377,16 @@ mdsc_status mdsc_force_dipR_noalloc(int ndip, const double* d_pos, const double*
                                     double* d_UPT, void* stream);
 
 /* ---- utility ------------------------------------------------------------ */
+/* Measured FP32 multiply-add throughput of a device (the bound of the pair
+   kernels): `reps` timed launches of independent multiply-add chains in
+   scalar (FFMA) and paired (FFMA2, float2 halves) form, best of each, in
+   TFLOP/s at 2 FLOP per multiply-add; ms is the best paired launch's device
+   time, num_sms the device's multiprocessor count.  No counterpart in the
+   reference: it is the roofline denominator of the measurement. */
+mdsc_status mdsc_fp32_peak(int device, int reps, double* tflops_ffma, double* tflops_ffma2, double* ms,
+                           int* num_sms);
+
+
 /* Seeded random non-overlapping placement of n rods in a periodic box
    (sequential rejection on the segment distance, gap added to
    (D_i + D_j)/2): centres r (n*3) and orientation matrices O (n*9).  Host

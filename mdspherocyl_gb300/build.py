@@ -19,7 +19,7 @@ LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libmdsc.so")
 
 SOURCES = ["k_real.cu", "k_kspace.cu", "k_int.cu", "k_wca.cu", "k_obs.cu", "k_render.cu", "k_init.cu", "api.cu",
-           "gen.cpp", "noalloc.cu"]
+           "gen.cpp", "noalloc.cu", "k_probe.cu"]
 # files that repeat the reference's FP64 arithmetic operation by operation
 NO_FMA = ("k_wca.cu", "k_init.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

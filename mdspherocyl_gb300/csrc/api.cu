@@ -493,6 +493,7 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
 
 struct mdsc_batch {
   int device = 0;
+  int num_sms = 0;  // streaming multiprocessors of the device
   int nsys = 0;
   cudaStream_t st = nullptr, s2 = nullptr, s3 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_j2 = nullptr, ev_j3 = nullptr;
@@ -584,9 +585,9 @@ mdsc_status ensure_forces(mdsc_batch* B);
 // class of the batch (tiles, particles, k-vectors: half-octaves), so a
 // server that repacks batches of similar size tunes once.
 struct TuneKey {
-  int tiles, parts, ks, maxnd;
+  int tiles, parts, ks, maxnd, sms;
   bool operator<(const TuneKey& o) const {
-    return std::tie(tiles, parts, ks, maxnd) < std::tie(o.tiles, o.parts, o.ks, o.maxnd);
+    return std::tie(tiles, parts, ks, maxnd, sms) < std::tie(o.tiles, o.parts, o.ks, o.maxnd, o.sms);
   }
 };
 std::mutex g_tune_mu;
@@ -594,7 +595,7 @@ std::map<TuneKey, Tuning> g_tune_cache;
 
 TuneKey tune_key(const mdsc_batch* B) {
   auto cls = [](long long x) { return x <= 0 ? -1 : (int)std::lround(2.0 * std::log2((double)x)); };
-  return TuneKey{cls(B->b.ntiles), cls(B->lo.ntot), cls(B->b.nktot), B->lo.maxnd};
+  return TuneKey{cls(B->b.ntiles), cls(B->lo.ntot), cls(B->b.nktot), B->lo.maxnd, B->num_sms};
 }
 
 // average device time (ms) of `launch` over `reps` runs after one warm-up
@@ -644,7 +645,8 @@ mdsc_status autotune(mdsc_batch* B, int force, int reps) {
   };
   // WCA evaluation grid (the screen runs with it: it refills the work list)
   {
-    const int cand[4] = {152 * 2, 152 * 4, 152 * 8, 152 * 16};
+    const int m = B->num_sms;
+    const int cand[4] = {m * 2, m * 4, m * 8, m * 16};
     pick("wca_blocks", cand, 4, b.tune.wca_blocks, [&] { launch_wca(b, B->st); });
   }
   // real-space tiles per block, then the strip-sum block size
@@ -1064,12 +1066,18 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   B->nsys = nsys;
   B->desc.assign(descs, descs + nsys);
   cudaSetDevice(device);
+  if (cudaDeviceGetAttribute(&B->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      B->num_sms <= 0) {
+    delete B;
+    return MDSC_ERR_NO_DEVICE;
+  }
   make_layout(descs, nsys, B->lo);
   fill_tables(descs, B->lo);
   const Layout& lo = B->lo;
   Arena A;
   carve(A, lo, nsys, B->b, &B->kwork, &B->kowner, B->noise);
   B->arena_bytes = A.off;
+  B->b.tune.wca_blocks = 8 * B->num_sms;
   cudaError_t e = cudaMalloc(&B->arena, B->arena_bytes);
   if (e != cudaSuccess) {
     delete B;
@@ -1596,11 +1604,21 @@ mdsc_status mdsc_clust_conf(mdsc_batch* B, int sys, int* labels, int* n_clusters
 // the candidate lists of the energy screen, for every particle of the batch,
 // allocated when a system of it first takes the energy criterion
 static mdsc_status ensure_energy_lists(mdsc_batch* B) {
-  if (B->b.ecand) return MDSC_OK;
+  if (B->b.ecand && B->b.ecnt) return MDSC_OK;
   const size_t n = (size_t)std::max(B->lo.ntot, 1);
-  CU(cudaMalloc(&B->b.ecand, sizeof(int) * n * kMaxE));
-  CU(cudaMalloc(&B->b.ecnt, sizeof(int) * n));
-  CU(cudaMemsetAsync(B->b.ecnt, 0, sizeof(int) * n, B->st));
+  // both lists or neither: the batch keeps them only once both exist
+  int* cand = nullptr;
+  int* cnt = nullptr;
+  CU(cudaMalloc(&cand, sizeof(int) * n * kMaxE));
+  const cudaError_t e = cudaMalloc(&cnt, sizeof(int) * n);
+  if (e != cudaSuccess) {
+    cudaFree(cand);
+    return fail(B, e == cudaErrorMemoryAllocation ? MDSC_ERR_OOM : MDSC_ERR_CUDA,
+                std::string("energy candidate counts: ") + cudaGetErrorString(e));
+  }
+  B->b.ecand = cand;
+  B->b.ecnt = cnt;
+  CU(cudaMemsetAsync(cnt, 0, sizeof(int) * n, B->st));
   return MDSC_OK;
 }
 

@@ -125,7 +125,7 @@ struct SysObs {
 struct Tuning {
   int rp_warps = 1;          // real-space tiles (warps) per block: 1, 2 or 4
   int rsum_threads = 256;    // strip-sum block size: 128, 256 or 512
-  int wca_blocks = 152 * 8;  // grid of the FP64 WCA evaluation
+  int wca_blocks = 0;        // grid of the FP64 WCA evaluation (8 x the SM count until tuned)
   int kg_scalar = 0;         // k-space gather: 0 two particles per thread, 1 one
 };
 

@@ -18,6 +18,15 @@
 // it reads, so nothing carries over from one call to the next; two calls
 // whose work overlaps on the GPU (different streams, or host threads
 // calling at once) race on the array and give wrong results.
+//
+// The array's device address is looked up on a device's first call and
+// kept, together with the CUDA context it belongs to.  A later call in
+// another context (after cudaDeviceReset, or when the primary context was
+// released and created again) looks it up again.  A CUDA error left
+// pending by earlier, unrelated work on this thread makes the call return
+// MDSC_ERR_CUDA before it launches anything, and the error stays pending
+// for its owner to read.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -160,6 +169,23 @@ __global__ void noalloc_reduce_kernel(const unsigned char* scr, int ndip, double
 
 std::mutex g_mu;
 void* g_scratch_ptr[64] = {nullptr};  // device address of g_scratch, per device
+CUcontext g_scratch_ctx[64] = {nullptr};  // the context that address belongs to
+
+// the calling thread's current context (driver entry point, resolved once)
+CUcontext current_context() {
+  using Fn = CUresult (*)(CUcontext*);
+  static Fn fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return (Fn)f;
+  }();
+  CUcontext c = nullptr;
+  if (!fn || fn(&c) != CUDA_SUCCESS) return nullptr;
+  return c;
+}
 
 }  // namespace
 
@@ -175,17 +201,21 @@ extern "C" mdsc_status mdsc_force_dipR_noalloc(int ndip, const double* d_pos, co
   if (!(box[0] > 0 && box[1] > 0 && box[2] > 0 && alpha > 0)) return MDSC_ERR_BAD_ARG;
   const double hd = 0.5 * std::sqrt(box[0] * box[0] + box[1] * box[1] + box[2] * box[2]);
   if (hd >= 0.5 * 200 * 1.001) return MDSC_ERR_TABLE_RANGE;
+  // an error left pending by earlier work stays with its owner
+  if (cudaPeekAtLastError() != cudaSuccess) return MDSC_ERR_CUDA;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return MDSC_ERR_NO_DEVICE;
   void* scr = nullptr;
   {
-    // set-up, once per device, with that device current: the device
-    // address of the scratch array
+    // set-up, once per device and context, with that device current: the
+    // device address of the scratch array
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_ptr[dev]) {
+    const CUcontext ctx = current_context();
+    if (!g_scratch_ptr[dev] || ctx != g_scratch_ctx[dev]) {
       void* p = nullptr;
       if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) return MDSC_ERR_CUDA;
       g_scratch_ptr[dev] = p;
+      g_scratch_ctx[dev] = current_context();
     }
     scr = g_scratch_ptr[dev];
   }
@@ -196,6 +226,7 @@ extern "C" mdsc_status mdsc_force_dipR_noalloc(int ndip, const double* d_pos, co
   const int nthr = ndip > ntile ? ndip : ntile;
   noalloc_prep_kernel<<<cdiv(nthr, 256), 256, 0, st>>>(base, ndip, d_pos, d_mom, box[0], box[1], box[2],
                                                         alpha);
+  if (cudaGetLastError() != cudaSuccess) return MDSC_ERR_CUDA;
   Batch b{};
   b.nsys = 1;
   b.ntot = ndip;
@@ -209,6 +240,7 @@ extern "C" mdsc_status mdsc_force_dipR_noalloc(int ndip, const double* d_pos, co
   b.rpart = reinterpret_cast<float*>(base + kOffPart);
   b.tileE = reinterpret_cast<float*>(base + kOffTileE);
   launch_real_pairs(b, false, st);
+  if (cudaGetLastError() != cudaSuccess) return MDSC_ERR_CUDA;
   noalloc_reduce_kernel<<<cdiv(ndip, 256) + 1, 256, 0, st>>>(base, ndip, d_F, d_T, d_UPT);
   return cudaGetLastError() == cudaSuccess ? MDSC_OK : MDSC_ERR_CUDA;
 }

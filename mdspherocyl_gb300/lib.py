@@ -41,6 +41,7 @@ EXPORTS = [
     "mdsc_autotune", "mdsc_tuning", "mdsc_set_tuning", "mdsc_correlation_bins", "mdsc_correlations",
     "mdsc_order_params", "mdsc_step_trace", "mdsc_get_rng", "mdsc_set_rng", "mdsc_set_species",
     "mdsc_correlation_size", "mdsc_get_thermostat", "mdsc_render", "mdsc_lattice", "mdsc_thermalize",
+    "mdsc_fp32_peak",
 ]
 
 
@@ -188,6 +189,7 @@ def load(build: bool = True) -> ctypes.CDLL:
                                             c_void_p, c_void_p]),
         "mdsc_profile_steps": (c_int, [c_void_p, c_int, c_int, c_char_p, c_size_t, _dp, _ip]),
         "mdsc_place_rods": (c_int, [c_int, _dp, _dp, _dp, ctypes.c_ulonglong, c_double, c_int, _dp, _dp]),
+        "mdsc_fp32_peak": (c_int, [c_int, c_int, _dp, _dp, _dp, _ip]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -564,3 +566,15 @@ def estimate_bytes(descs) -> int:
     lib = load()
     arr = (SystemDesc * len(descs))(*descs)
     return int(lib.mdsc_estimate_bytes(arr, len(descs)))
+
+
+def fp32_peak(device: int = 0, reps: int = 5) -> dict:
+    """Measured FP32 multiply-add throughput of the device (mdsc_fp32_peak):
+    TFLOP/s of the scalar and paired forms and the best paired launch's ms."""
+    lib = load()
+    a, b, ms = c_double(), c_double(), c_double()
+    sms = c_int()
+    code = lib.mdsc_fp32_peak(device, reps, ctypes.byref(a), ctypes.byref(b), ctypes.byref(ms), ctypes.byref(sms))
+    if code != 0:
+        raise MdscError(code, "mdsc_fp32_peak", "")
+    return {"ffma_tflops": a.value, "ffma2_tflops": b.value, "launch_ms": ms.value, "sms": sms.value}

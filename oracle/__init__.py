@@ -116,11 +116,25 @@ def build_oracle(force: bool = False) -> str:
     return ORACLE_SO
 
 
+def reference_root() -> str:
+    """Where the reference's sources lie: MDSC_REFERENCE, else the default of
+    the build recipe (build_ref.sh --where)."""
+    env = os.environ.get("MDSC_REFERENCE")
+    if env:
+        return env
+    out = subprocess.run(["bash", os.path.join(HERE, "build_ref.sh"), "--where"], capture_output=True, text=True)
+    return out.stdout.strip()
+
+
+def reference_present() -> bool:
+    root = reference_root()
+    return bool(root) and os.path.isdir(os.path.join(root, "v25"))
+
+
 def build_ref() -> str | None:
     """Build oracle/_ref from the reference sources when they are present."""
     script = os.path.join(HERE, "build_ref.sh")
-    ref_root = os.environ.get("MDSC_REFERENCE", "/root/reference")
-    if not os.path.isdir(os.path.join(ref_root, "v25")):
+    if not reference_present():
         return None
     subprocess.check_call(["bash", script])
     return REF_SO if os.path.exists(REF_SO) else None

@@ -19,7 +19,13 @@
 # file is copied.  -ffp-contract=off keeps the arithmetic identical to the
 # reference's own x86 build (no fused multiply-adds) on every host.
 set -euo pipefail
+# where the reference's sources lie: MDSC_REFERENCE, else this container's
+# read-only mount (the one place this repository names that path)
 REF="${MDSC_REFERENCE:-/root/reference}"
+if [ "${1:-}" = "--where" ]; then
+  echo "$REF"
+  exit 0
+fi
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 if [ ! -d "$REF/v25" ]; then

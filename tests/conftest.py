@@ -10,7 +10,17 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 GOLDEN = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "golden_*.npz")))
-REFERENCE = os.environ.get("MDSC_REFERENCE", "/root/reference")
+
+
+def _reference_root():
+    import oracle
+
+    return oracle.reference_root()
+
+
+# where the reference's sources lie (the oracle's build recipe knows); the
+# tests that read them skip when they are absent
+REFERENCE = _reference_root()
 
 
 def pytest_configure(config):

@@ -186,7 +186,7 @@ def run_files():
     shortened: a new run of 2 steps with every output every step (init/),
     then a restart (signal 1) of 3 steps from its files (restart/) and a
     continuation (signal 2) of 2 steps (continue/)."""
-    ref = os.environ.get("MDSC_REFERENCE", "/root/reference")
+    ref = oracle.reference_root()
     src = open(os.path.join(ref, "v25", "input.txt")).read()
     common = {"Histogram bar width=": "Histogram bar width=\t0.1", "corr. sum freq.=": "corr. sum freq.=\t1",
               "DiffCorr. frequency=": "DiffCorr. frequency=    1", "ViscCorr. frequency=": "ViscCorr. frequency=    1",
@@ -198,7 +198,7 @@ def run_files_v251():
     """The same three stages with the later driver (v25/v251) on its own
     example (v25/v251/run1/input.txt: rods of length 9 with an axial dipole
     in a field), at 200 rods and the same density, clustering every step."""
-    ref = os.environ.get("MDSC_REFERENCE", "/root/reference")
+    ref = oracle.reference_root()
     src = open(os.path.join(ref, "v25", "v251", "run1", "input.txt")).read()
     common = {"Histogram bar width=": "Histogram bar width=\t0.5", "corr. sum freq.=": "corr. sum freq.=\t1",
               "DiffCorr. frequency=": "DiffCorr. frequency=    1", "ViscCorr. frequency=": "ViscCorr. frequency=    1",

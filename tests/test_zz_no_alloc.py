@@ -20,28 +20,37 @@ pytestmark = pytest.mark.gpu
 TOL_F = 1e-5  # the tolerance the other GPU tests hold the Ewald forces to
 
 
-def test_noalloc_matches_force_dipR_on_two_calls():
-    import torch
-
-    lib = L.load()
-    spec, st = S.plain_c0(seed=9, n=300)
+def _regular(spec, st):
+    """The regular entry point's answer (mdsc_force_dipR on its own batch)."""
     with L.Batch([spec], [st]) as bt:
         bt.zero_forces()
         U_ref, PT_ref = bt.force_dipR()
         ref = bt.download(0)
-    n = st.n
+    return ref["F"], ref["T"], U_ref[0], PT_ref[0]
+
+
+def test_noalloc_matches_force_dipR_on_two_calls():
+    """Two calls in a row on different systems: first the largest the fixed
+    scratch holds (4096 dipoles, 64 strips, 2080 tiles: every byte of the
+    array in use), then a smaller one with other positions, moments and box.
+    A second call that read partials, energies or tiles the first left
+    behind would differ from its own regular answer."""
+    import torch
+
+    lib = L.load()
+    cases = [S.plain_c0(seed=9, n=4096), S.plain_c0(seed=21, n=700)]
+    assert cases[0][1].n == 4096 and not np.allclose(cases[0][0].box, cases[1][0].box)
+    refs = [_regular(spec, st) for spec, st in cases]
     dev = torch.device("cuda:0")
-    pos = torch.tensor(st.r, dtype=torch.float64, device=dev)
-    mom = torch.tensor(st.dip[:, 0, 4:5] * st.O[:, 2, :], dtype=torch.float64, device=dev)
-    F = torch.empty((n, 3), dtype=torch.float64, device=dev)
-    T = torch.empty((n, 3), dtype=torch.float64, device=dev)
-    UPT = torch.empty(10, dtype=torch.float64, device=dev)
-    box = (ctypes.c_double * 3)(*[float(x) for x in spec.box])
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    for _ in range(2):
-        F.fill_(float("nan"))
-        T.fill_(float("nan"))
-        UPT.fill_(float("nan"))
+    for (spec, st), (F_ref, T_ref, U_ref, PT_ref) in zip(cases, refs):
+        n = st.n
+        pos = torch.tensor(st.r, dtype=torch.float64, device=dev)
+        mom = torch.tensor(st.dip[:, 0, 4:5] * st.O[:, 2, :], dtype=torch.float64, device=dev)
+        F = torch.full((n, 3), float("nan"), dtype=torch.float64, device=dev)
+        T = torch.full((n, 3), float("nan"), dtype=torch.float64, device=dev)
+        UPT = torch.full((10,), float("nan"), dtype=torch.float64, device=dev)
+        box = (ctypes.c_double * 3)(*[float(x) for x in spec.box])
         code = lib.mdsc_force_dipR_noalloc(n, ctypes.c_void_p(pos.data_ptr()), ctypes.c_void_p(mom.data_ptr()),
                                            ctypes.cast(box, ctypes.POINTER(ctypes.c_double)), float(spec.alpha),
                                            ctypes.c_void_p(F.data_ptr()), ctypes.c_void_p(T.data_ptr()),
@@ -49,10 +58,10 @@ def test_noalloc_matches_force_dipR_on_two_calls():
         torch.cuda.synchronize()
         assert code == 0, L.STATUS.get(code, code)
         f, t, upt = F.cpu().numpy(), T.cpu().numpy(), UPT.cpu().numpy()
-        assert rms_rel(f, ref["F"]) < TOL_F
-        assert rms_rel(t, ref["T"]) < TOL_F
-        assert abs(upt[0] - U_ref[0]) < TOL_F * max(1.0, abs(U_ref[0]))
-        assert rms_rel(upt[1:].reshape(3, 3), PT_ref[0]) < TOL_F
+        assert rms_rel(f, F_ref) < TOL_F, (n, rms_rel(f, F_ref))
+        assert rms_rel(t, T_ref) < TOL_F, (n, rms_rel(t, T_ref))
+        assert abs(upt[0] - U_ref) < TOL_F * max(1.0, abs(U_ref)), (n, upt[0], U_ref)
+        assert rms_rel(upt[1:].reshape(3, 3), PT_ref) < TOL_F, n
 
 
 def test_noalloc_rejects_more_dipoles_than_its_scratch_holds():
