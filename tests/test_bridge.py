@@ -31,6 +31,6 @@ def test_bridge_compiles_links_and_round_trips(tmp_path):
            "-L", libdir, "-lmdsc", f"-Wl,-rpath,{libdir}", "-Wl,--no-undefined", "-o", exe]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-4000:]
-    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60, cwd=str(tmp_path))
     assert r.returncode == 0, r.stdout[-4000:] + r.stderr[-2000:]
     assert "round trip OK" in r.stdout
