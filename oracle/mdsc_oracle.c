@@ -301,6 +301,12 @@ int mdsc_or_neigh_list(const mdsc_oracle_state* s, double r_list, int* counts, i
       const double* rj = &s->r[3 * g];
       double rij[3], st[2], dij[3];
       for (int a = 0; a < 3; ++a) rij[a] = mimg(ri[a] - rj[a], s->L[a]);
+      /* screen: the segment distance is at least the centre distance less
+         both half lengths; pairs clearly beyond r_list that way are not
+         listed by the segment test either (the margin is far above
+         rounding), so the list is the same */
+      const double reach = 0.5 * (s->len[f] + s->len[g]) + r_list;
+      if (rij[0] * rij[0] + rij[1] * rij[1] + rij[2] * rij[2] > reach * reach * (1. + 1e-9) + 1e-9) continue;
       double dsq = mdsc_or_seg_dist(s, f, g, rij, dij, st);
       if (dsq < rl_sq) {
         if (tot < cap) idx[tot] = g;
@@ -1147,8 +1153,57 @@ static int bonded(const mdsc_oracle_state* s, int A, int B, const bond_rule* br)
   return (A < B ? mdsc_or_pair_energy(s, A, B) : mdsc_or_pair_energy(s, B, A)) < -br->v;
 }
 
+/* Partners j that the geometric test can bond to A, ascending: the segment
+   distance is at least the centre distance less both half lengths, so a
+   pair whose minimum-image centres lie further apart than
+   (L_A + L_B)/2 + sigma (with a margin far above rounding) cannot pass
+   dist_test.  Only a screen: the bond itself is still dist_test, and the
+   partners come in the order the reference's j loop visits them. */
+static void geometric_candidates(const mdsc_oracle_state* s, double min_s, int** start_out, int** list_out) {
+  const int TP = s->n;
+  int* cnt = (int*)calloc((size_t)TP + 1, sizeof(int));
+  int* tmp_n = (int*)calloc(TP > 0 ? TP : 1, sizeof(int));
+  int** tmp = (int**)calloc(TP > 0 ? TP : 1, sizeof(int*));
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int A = 0; A < TP; ++A) {
+    int cap = 16, m = 0;
+    int* v = (int*)malloc(sizeof(int) * cap);
+    for (int B = 0; B < TP; ++B) {
+      if (B == A) continue;
+      double r2 = 0.;
+      for (int a = 0; a < 3; ++a) {
+        double d = s->r[3 * A + a] - s->r[3 * B + a];
+        d -= s->L[a] * floor(d / s->L[a] + 0.5);
+        r2 += d * d;
+      }
+      const double reach = 0.5 * (s->len[A] + s->len[B]) + (s->dia[A] + s->dia[B]) / 2 + min_s;
+      if (r2 > reach * reach * (1. + 1e-9) + 1e-9) continue;
+      if (m == cap) {
+        cap *= 2;
+        v = (int*)realloc(v, sizeof(int) * cap);
+      }
+      v[m++] = B;
+    }
+    tmp[A] = v;
+    tmp_n[A] = m;
+  }
+  for (int A = 0; A < TP; ++A) cnt[A + 1] = cnt[A] + tmp_n[A];
+  int* list = (int*)malloc(sizeof(int) * (cnt[TP] > 0 ? cnt[TP] : 1));
+  for (int A = 0; A < TP; ++A) {
+    memcpy(list + cnt[A], tmp[A], sizeof(int) * tmp_n[A]);
+    free(tmp[A]);
+  }
+  free(tmp);
+  free(tmp_n);
+  *start_out = cnt;
+  *list_out = list;
+}
+
 static int clust_bfs(mdsc_oracle_state* s, const bond_rule* br, mdsc_mt19937* ran) {
   const int TP = s->n;
+  /* the geometric test visits only the partners within reach (same order) */
+  int *cstart = NULL, *clist = NULL;
+  if (!br->energy) geometric_candidates(s, br->v, &cstart, &clist);
   int* NI = (int*)malloc(sizeof(int) * (TP > 0 ? TP : 1)); /* remaining, ascending */
   int nrem = TP;
   for (int j = 0; j < TP; ++j) NI[j] = j;
@@ -1172,7 +1227,9 @@ static int clust_bfs(mdsc_oracle_state* s, const bond_rule* br, mdsc_mt19937* ra
     /* clust_gen breadth-first growth, :3074-3145 */
     while (qh < qt) {
       int ii = queue[qh];
-      for (int j = 0; j < TP; ++j) {
+      const int jn = cstart ? cstart[ii + 1] - cstart[ii] : TP;
+      for (int q = 0; q < jn; ++q) {
+        const int j = cstart ? clist[cstart[ii] + q] : q;
         if (locadd[j]) continue;
         if (bonded(s, ii, j, br)) {
           if (!added[j]) {
@@ -1200,6 +1257,8 @@ static int clust_bfs(mdsc_oracle_state* s, const bond_rule* br, mdsc_mt19937* ra
   free(added);
   free(locadd);
   free(queue);
+  free(cstart);
+  free(clist);
   return n_clust;
 }
 

@@ -1,0 +1,197 @@
+"""The GPU path against the FP64 oracle on the workloads as they are stated:
+
+  c0  N = 256 rods, phi 0.10, alpha 5.6/L_box, |n|^2 <= 27: 1000 steps,
+      energies and pressure tensor every step;
+  c1  N = 4096, phi 0.20, alpha 7/L_box, |n|^2 <= 64: 200 steps, energies
+      and pressure tensor every step, then the state;
+  c2  N = 32768, phi 0.15, mu^2 5 in a field, |n|^2 <= 100: one force
+      evaluation of every term (force_sc, force_dipR, force_dipK,
+      ext_field) and the reference's geometric cluster labels;
+  c3  every 16th system of the 256-replica mix (seed 3), stepped inside the
+      full batch of 256 systems against the oracle's step of that system
+      alone.
+
+Bars (as in test_gpu_parity.py): Ewald forces and torques RMS relative
+<= 1e-5; total energy of a step E = K + U relative <= 1e-7; U alone <= 1e-6;
+each Ewald energy <= 1e-5; pressure tensors RMS relative <= 1e-5; WCA
+(FP64) <= 1e-12; cluster labels identical.
+
+With MDSC_PARITY_OUT set to a directory, each test writes the errors it
+measured there as JSON (parity_<config>.json)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import rms_rel
+from mdspherocyl_gb300 import lib as L
+from mdspherocyl_gb300 import systems as S
+
+pytestmark = pytest.mark.gpu
+
+TOL_F = 1e-5
+TOL_E_TOTAL = 1e-7
+TOL_U = 1e-6
+TOL_PT = 1e-5
+THREADS = os.cpu_count() or 1
+
+
+def _report(name, data):
+    out = os.environ.get("MDSC_PARITY_OUT")
+    if not out:
+        return
+    os.makedirs(out, exist_ok=True)
+    with open(os.path.join(out, f"parity_{name}.json"), "w") as f:
+        json.dump(data, f, indent=1, default=float)
+
+
+def _osys(st, box):
+    return oracle.System(st.r, st.p, st.O, st.l, st.length, st.dia, st.mass, st.dip, box)
+
+
+def _md(orc, spec, st):
+    return oracle.MDOracle(orc, _osys(st, spec.box), dt=spec.dt, temp=spec.temp, Q=spec.Q, gamma=spec.gamma,
+                           xi0=spec.xi0, sr_cut=3.0, K_max=spec.K_max, ksq_max=spec.ksq_max, alpha=spec.alpha,
+                           B=spec.B, rc_real=spec.rc_real)
+
+
+def _totals(o_gpu, o_or):
+    """(E, U, PT) of a GPU observables record and of the oracle's."""
+    Ug = o_gpu["U_ss"] + o_gpu["U_dipR"] + o_gpu["U_dipK"] + o_gpu["U_ext"] + o_gpu["U_self"]
+    Uo = o_or["Uss"] + o_or["UdipR"] + o_or["UdipK"] + o_or["Uext"] + o_or["Uself"]
+    Kg, Ko = float(np.sum(o_gpu["K"])), float(np.sum(o_or["K"]))
+    PTg = sum(np.asarray(o_gpu[k]).reshape(3, 3) for k in ("PT_kin", "PT_ss", "PT_dipR", "PT_dipK"))
+    PTo = o_or["PTkin"] + o_or["PTss"] + o_or["PTdipR"] + o_or["PTdipK"]
+    return (Kg + Ug, Ko + Uo), (Ug, Uo), (PTg, PTo)
+
+
+def _trajectory(spec, st, steps):
+    """Every step's relative errors of E, U and the pressure tensor, the
+    GPU's step trace against the oracle's driver loop from the same state."""
+    orc = oracle.Oracle()
+    orc.set_threads(THREADS)
+    md = _md(orc, spec, st)
+    with L.Batch([spec], [st]) as bt:
+        trace = bt.step_trace(steps)
+        fin = bt.download(0)
+    eE, eU, ePT, eparts = [], [], [], []
+    for k in range(steps):
+        assert md.step()
+        mo = md.obs()
+        og = trace[k][0]
+        (Eg, Eo), (Ug, Uo), (PTg, PTo) = _totals(og, mo)
+        eE.append(abs(Eg - Eo) / abs(Eo))
+        eU.append(abs(Ug - Uo) / abs(Uo))
+        ePT.append(rms_rel(PTg, PTo))
+        eparts.append(max(abs(og["U_dipR"] - mo["UdipR"]) / max(1.0, abs(mo["UdipR"])),
+                          abs(og["U_dipK"] - mo["UdipK"]) / max(1.0, abs(mo["UdipK"]))))
+    o = md.sys
+    st_err = {f: rms_rel(fin[f], getattr(o, f)) for f in ("p", "l", "F", "T")}
+    st_err["r_max_abs"] = float(np.abs(fin["r"] - o.r).max())
+    md.close()
+    return np.array(eE), np.array(eU), np.array(ePT), np.array(eparts), st_err
+
+
+def test_c0_1000_steps_vs_oracle():
+    spec, st = S.plain_c0()
+    assert st.n == 256
+    eE, eU, ePT, eparts, st_err = _trajectory(spec, st, 1000)
+    _report("c0", {"config": "c0: N=256, 1000 steps, all minimum-image pairs", "steps": 1000,
+                   "rel_E_max": eE.max(), "rel_U_max": eU.max(), "rms_PT_max": ePT.max(),
+                   "ewald_U_max": eparts.max(), "state_after": st_err,
+                   "rel_E_at": {str(k): eE[k - 1] for k in (1, 10, 100, 1000)}})
+    assert eE.max() <= TOL_E_TOTAL, eE.max()
+    assert eU.max() <= TOL_U, eU.max()
+    assert ePT.max() <= TOL_PT, ePT.max()
+    assert eparts.max() <= TOL_F, eparts.max()
+
+
+def test_c1_200_steps_vs_oracle():
+    spec, st = S.plain_c1()
+    assert st.n == 4096
+    eE, eU, ePT, eparts, st_err = _trajectory(spec, st, 200)
+    _report("c1", {"config": "c1: N=4096, 200 steps, all minimum-image pairs", "steps": 200,
+                   "rel_E_max": eE.max(), "rel_U_max": eU.max(), "rms_PT_max": ePT.max(),
+                   "ewald_U_max": eparts.max(), "state_after": st_err,
+                   "rel_E_at": {str(k): eE[k - 1] for k in (1, 10, 100, 200)}})
+    assert eE.max() <= TOL_E_TOTAL, eE.max()
+    assert eU.max() <= TOL_U, eU.max()
+    assert ePT.max() <= TOL_PT, ePT.max()
+    assert eparts.max() <= TOL_F, eparts.max()
+    for f in ("p", "l", "F", "T"):
+        assert st_err[f] <= TOL_F, (f, st_err[f])
+
+
+def test_c2_full_size_every_term_and_geometric_labels():
+    spec, st = S.plain_c2()
+    assert st.n == 32768
+    orc = oracle.Oracle()
+    orc.set_threads(THREADS)
+    rep = {"config": "c2: N=32768, phi 0.15, mu^2 5, field along z, |n|^2 <= 100; one evaluation"}
+    with L.Batch([spec], [st]) as bt:
+        for name, call, ofn in (
+            ("sc", lambda: bt.force_sc(), lambda s: orc.force_sc(s, 3.0, 3.5)[1:]),
+            ("dipR", lambda: bt.force_dipR(), lambda s: orc.force_dipR(s, spec.alpha)),
+            ("dipK", lambda: bt.force_dipK(), lambda s: orc.force_dipK(s, spec.K_max, spec.alpha, spec.ksq_max)),
+        ):
+            bt.zero_forces()
+            res = call()
+            d = bt.download(0)
+            s = _osys(st, spec.box)
+            ores = ofn(s)
+            U, Uo = res[0][0], ores[0]
+            PT, PTo = res[-1][0], ores[-1]
+            rep[name] = {"rms_F": rms_rel(d["F"], s.F), "rms_T": rms_rel(d["T"], s.T),
+                         "rel_U": abs(U - Uo) / abs(Uo), "rms_PT": rms_rel(PT, PTo)}
+        bt.zero_forces()
+        Ue = bt.ext_field()[0]
+        d = bt.download(0)
+        s = _osys(st, spec.box)
+        Ueo = orc.ext_field(s, spec.B)
+        rep["ext"] = {"rel_U": abs(Ue - Ueo) / abs(Ueo), "rms_T": rms_rel(d["T"], s.T)}
+        lab, nc = bt.clust_conf(0)
+    s = _osys(st, spec.box)
+    lo, nco, _ = orc.clust_conf(s, float(spec.min_s), seed=1, skip=0)  # the batch's generator: seed 1
+    rep["labels_equal"] = bool(np.array_equal(lab, lo))
+    rep["clusters"] = int(nc)
+    _report("c2", rep)
+    for a, b in (("sc", 1e-12), ("dipR", TOL_F), ("dipK", TOL_F)):
+        r = rep[a]
+        assert r["rms_F"] <= b and r["rms_T"] <= b, (a, r)
+        assert r["rel_U"] <= b and r["rms_PT"] <= max(b, 1e-12), (a, r)
+    assert rep["ext"]["rel_U"] <= 1e-7 and rep["ext"]["rms_T"] <= 1e-6, rep["ext"]
+    assert rep["labels_equal"] and nc == nco
+
+
+def test_c3_mix_systems_inside_the_full_batch():
+    ds = S.replica_mix_specs(n_systems=256, seed=3)
+    systems = [S.replica_system(d) for d in ds]
+    picks = list(range(0, 256, 16))
+    with L.Batch([s for s, _ in systems], [t for _, t in systems]) as bt:
+        obs = bt.step(1)
+        got = {k: bt.download(k) for k in picks}
+    orc = oracle.Oracle()
+    orc.set_threads(THREADS)
+    rows = []
+    for k in picks:
+        spec, st = systems[k]
+        md = _md(orc, spec, st)
+        assert md.step()
+        mo = md.obs()
+        (Eg, Eo), (Ug, Uo), (PTg, PTo) = _totals(obs[k], mo)
+        o = md.sys
+        row = {"system": k, "n": spec.n, "rel_E": abs(Eg - Eo) / abs(Eo), "rel_U": abs(Ug - Uo) / abs(Uo),
+               "rms_PT": rms_rel(PTg, PTo), "rms_F": rms_rel(got[k]["F"], o.F), "rms_T": rms_rel(got[k]["T"], o.T),
+               "rms_p": rms_rel(got[k]["p"], o.p), "r_max_abs": float(np.abs(got[k]["r"] - o.r).max())}
+        rows.append(row)
+        md.close()
+    worst = {key: max(r[key] for r in rows) for key in rows[0] if key not in ("system", "n")}
+    _report("c3", {"config": "c3: every 16th system of the 256-replica mix (seed 3), one step inside the full "
+                             "batch of 256 systems", "systems": rows, "worst": worst})
+    assert worst["rel_E"] <= TOL_E_TOTAL, worst
+    assert worst["rel_U"] <= TOL_U, worst
+    assert worst["rms_PT"] <= TOL_PT, worst
+    assert worst["rms_F"] <= TOL_F and worst["rms_T"] <= TOL_F, worst
+    assert worst["r_max_abs"] <= 1e-9, worst

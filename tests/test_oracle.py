@@ -135,6 +135,20 @@ def test_clusters_and_neighbour_list_vs_reference(ref, orc):
     assert np.array_equal(ca, cb) and np.array_equal(ia, ib)
 
 
+def test_clusters_at_2048_rods_vs_reference(ref, orc):
+    """The oracle's labelling visits only partners within reach of the
+    geometric test; at 2048 dense polydisperse rods (many clusters, long
+    rods beside short ones) the labels and the generator's position still
+    equal the reference's, which tests every pair."""
+    rng = np.random.default_rng(12)
+    n = 2048
+    st, box = S.make_system(n=n, phi=0.2, lengths=rng.uniform(2, 5, n), mu=np.ones(n), seed=12)
+    for ms in (0.1, 0.8):
+        la, nca, nxa = orc.clust_conf(_sys(st, box), ms, seed=4, skip=2)
+        lb, nxb = ref.clust_conf(_sys(st, box), ms, seed=4, skip=2)
+        assert np.array_equal(la, lb) and nxa == nxb and nca == la.max() + 1
+
+
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
 def test_restatement_matches_golden_fixtures(orc, path):
     g = load_golden(path)
