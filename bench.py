@@ -441,6 +441,23 @@ def run_ours(args):
 
     e2e = e2e_rate(True)
     e2e_obs_only = e2e_rate(False)
+
+    # ---- a forced list rebuild of every system (mdsc_neigh_list: positions
+    # to working copies, the build, a synchronize), on cells and over all
+    # pairs: the two give the same lists ----
+    def rebuild_ms(cells: bool) -> float:
+        bt.set_list_cells(cells)
+        bt.neigh_list()
+        ts = []
+        for _ in range(5):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            bt.neigh_list()
+            ts.append(1e3 * (time.perf_counter() - t0))
+        return statistics.median(ts)
+
+    list_build = {"cells_ms": rebuild_ms(True), "all_pairs_ms": rebuild_ms(False),
+                  "how": "host clock around mdsc_neigh_list (every system rebuilt, then a synchronize), median of 5"}
     launches = bt.launches_per_step + 1  # + the per-call reset of the noise row
     bt.close()
     serving = run_serving(args, device) if (args.jobs > 0 and ws == 1 and not single) else None
@@ -485,6 +502,7 @@ def run_ours(args):
                 "flop_per_pair": FLOP_PER_PAIR, "pairs_per_launch": pairs,
                 "kernel_ms": rp_ms},
             "kernel_ms": prof,
+            "list_build": list_build,
             "plain_gpu": plain,
             "serving": serving,
             "clustering": clustering,

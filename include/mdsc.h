@@ -349,6 +349,14 @@ mdsc_status mdsc_autotune(mdsc_batch* b, int force);
 mdsc_status mdsc_tuning(const mdsc_batch* b, int* values, char* log, size_t len);
 /* Sets the mappings by hand (values[0..3] as above) instead of tuning. */
 mdsc_status mdsc_set_tuning(mdsc_batch* b, const int* values);
+/* List builds (neigh_list, v25/functions.cpp:1298-1334) on cells (on = 1,
+   the default: systems of 256 rods or more whose box holds at least 3
+   cells of the largest list reach along every axis bin their rods and scan
+   the 27 cells around each rod, O(N)) or over all pairs (on = 0, O(N^2)).
+   Both give the same lists, so the same bits; the switch is for timing and
+   tests.  A cell holding more than 64 rods sends its system to the
+   all-pairs scan for that build. */
+mdsc_status mdsc_set_list_cells(mdsc_batch* b, int on);
 
 /* ---- allocation-free variant ------------------------------------------- */
 /* Real-space Ewald forces, torques (without lever arms), energy and

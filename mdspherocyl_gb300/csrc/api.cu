@@ -21,7 +21,8 @@
 namespace mdsc {
 void launch_real_pairs(const Batch& b, bool multi, cudaStream_t s);
 void launch_real_sum(const Batch& b, cudaStream_t s);
-void launch_real_cut(const Batch& b, cudaStream_t s);
+// the cutoff systems' neighbour pass: real space (1), WCA screen (2), both (3)
+void launch_near_pass(const Batch& b, int mode, cudaStream_t s);
 void launch_kspace(const Batch& b, int maxnd, const int4* kwork, int nkwork, const int2* kowner,
                    double* kE, cudaStream_t s);
 void launch_derive(const Batch& b, cudaStream_t s);
@@ -33,7 +34,9 @@ void launch_movex(const Batch& b, cudaStream_t s);
 void launch_renorm(const Batch& b, cudaStream_t s);
 void launch_movep(const Batch& b, const double* xi, int last, cudaStream_t s);
 void launch_list_build(const Batch& b, int force_all, cudaStream_t s);
-void launch_wca(const Batch& b, cudaStream_t s);
+// the WCA screens and FP64 evaluation; near_mode: what the cutoff systems'
+// neighbour pass runs besides its WCA screen (1: also their real space)
+void launch_wca(const Batch& b, int near_mode, cudaStream_t s);
 void launch_cluster_bonds(const Batch& b, cudaStream_t s);
 void launch_ebond(const Batch& b, cudaStream_t s);
 void launch_cluster_hook(const Batch& b, cudaStream_t s);
@@ -74,6 +77,8 @@ struct Layout {
   std::vector<int2> blk, kowner;
   std::vector<int2> bstrips;  // strips of the systems whose tile energies are summed per strip
   std::vector<int2> kgwork;   // (particle block, part) of the k-space gather
+  std::vector<int2> cellblk;  // (system, first cell) of every block of the cell-binned list build
+  int ncellcap = 0;           // cells of capacity over all systems
   long long kgsets = 0;       // partial sets of the split gathers
   int ntot = 0, ndtot = 0, nktot = 0, maxnd = 0, nchunks = 0, nstrips = 0;
   bool any_rc = false;  // some system sums its real space over a neighbour list
@@ -316,6 +321,12 @@ void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
     Lo.nchunks += P.nkchunk;
     for (int ch = 0; ch < P.nkchunk; ++ch)
       for (int kt = 0; kt < cdiv(P.nk, kKBlock); ++kt) Lo.kwork.push_back(make_int4(s, ch, kt, 0));
+    // cell capacity of the list build: at most one cell per 8 rods (the
+    // grid is chosen at upload, when the shapes are known)
+    P.cell_off = Lo.ncellcap;
+    P.cell_cap = d.n >= kCellMinRods ? d.n / 8 : 0;
+    for (int c = 0; c < P.cell_cap; c += 2) Lo.cellblk.push_back(make_int2(s, c));
+    Lo.ncellcap += P.cell_cap;
     P.blk_off = blk;
     P.nblk = cdiv(d.n, kPartBlock);
     for (int k = 0; k < P.nblk; ++k) Lo.blk.push_back(make_int2(s, part + k * kPartBlock));
@@ -440,6 +451,7 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   b.kgdone = A.take<int>(nb);
   b.rnb = A.take<int>(Lo.any_rc ? n * kMaxR : 1);
   b.rnbc = A.take<int>(n);
+  b.rnbw = A.take<int>(n);
   b.rlE = A.take<double>(10 * nb);
   b.tiles = A.take<int4>(nt);
   b.wlist = A.take<int2>(n * kMaxC);
@@ -473,6 +485,10 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   b.dmax = A.take<double>(nb);
   b.obk = A.take<double>(12 * nb);
   b.blk = A.take<int2>(nb);
+  b.ccnt = A.take<int>(std::max(Lo.ncellcap, 1));
+  b.cpos = A.take<uint4>((size_t)std::max(Lo.ncellcap, 1) * kCellSlots);
+  b.cax = A.take<float4>((size_t)std::max(Lo.ncellcap, 1) * kCellSlots);
+  b.cellblk = A.take<int2>(std::max<size_t>(Lo.cellblk.size(), 1));
   b.nb = A.take<int>(n * kMaxNb);
   b.nbc = A.take<int>(n);
   b.fsave = A.take<uint32_t>(3 * n);
@@ -558,8 +574,7 @@ mdsc_status eval_forces(mdsc_batch* B, int force_list) {
   Batch b = batch_with_noise(B, 0);
   launch_derive(b, B->st);
   launch_list_build(b, force_list, B->st);
-  launch_real_cut(b, B->st);
-  launch_wca(b, B->st);
+  launch_wca(b, 1, B->st);  // with the cutoff systems' real space, in the same neighbour pass
   launch_real_pairs(b, B->lo.multi, B->st);
   launch_real_sum(b, B->st);
   launch_kspace(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, B->st);
@@ -647,7 +662,7 @@ mdsc_status autotune(mdsc_batch* B, int force, int reps) {
   {
     const int m = B->num_sms;
     const int cand[4] = {m * 2, m * 4, m * 8, m * 16};
-    pick("wca_blocks", cand, 4, b.tune.wca_blocks, [&] { launch_wca(b, B->st); });
+    pick("wca_blocks", cand, 4, b.tune.wca_blocks, [&] { launch_wca(b, 0, B->st); });
   }
   // real-space tiles per block, then the strip-sum block size
   if (b.ntiles > 0) {
@@ -689,9 +704,10 @@ mdsc_status capture_step(mdsc_batch* B, int which) {
   cudaStreamWaitEvent(B->s3, B->ev_fork, 0);
   launch_order_terms(b, B->st);
   launch_list_build(b, 0, B->st);
-  launch_real_cut(b, B->st);  // systems with a real-space cutoff: after their list
-  launch_wca(b, B->st);
-  launches += 4 + (b.any_rc ? 1 : 0);
+  launch_wca(b, 1, B->st);  // the cutoff systems' real space in their neighbour pass, after their list
+  // order terms, the list build's decision and scan (+ the cell binning),
+  // the WCA screen and evaluation (+ the cutoff pass)
+  launches += 5 + (b.cells && b.ncellblk ? 1 : 0) + (b.any_rc ? 1 : 0);
   launch_real_pairs(b, B->lo.multi, B->s2);
   launch_real_sum(b, B->s2);
   launches += b.ntiles > 0 ? 2 + (b.nbstrips > 0 ? 1 : 0) : 0;
@@ -1096,6 +1112,8 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   b.any_rc = lo.any_rc ? 1 : 0;
   b.nkgwork = (int)lo.kgwork.size();
   b.nblk = (int)lo.blk.size();
+  b.ncellblk = (int)lo.cellblk.size();
+  b.cells = 1;
   b.noise = B->noise[0];
   // The step graph forks the real-space tiles (stream s2) from the WCA and
   // k-space chains (st, s3).  The tiles keep the FP32 pipe busy while the
@@ -1125,6 +1143,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   if (!lo.bstrips.empty()) up(b.bstrips, lo.bstrips.data(), sizeof(int2) * lo.bstrips.size());
   if (!lo.kgwork.empty()) up(b.kgwork, lo.kgwork.data(), sizeof(int2) * lo.kgwork.size());
   up(b.blk, lo.blk.data(), sizeof(int2) * lo.blk.size());
+  if (!lo.cellblk.empty()) up(b.cellblk, lo.cellblk.data(), sizeof(int2) * lo.cellblk.size());
   up(b.kn, lo.kn.data(), sizeof(int4) * lo.kn.size());
   up(b.kv, lo.kv.data(), sizeof(float4) * lo.kv.size());
   up((void*)b.rtab, lo.rtab.data(), sizeof(float4) * lo.rtab.size());
@@ -1152,6 +1171,8 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   cudaMemsetAsync(b.wincnt, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.stripE, 0, sizeof(double) * 10 * std::max(lo.nstrips, 1), B->st);
   cudaMemsetAsync(b.rnbc, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
+  cudaMemsetAsync(b.rnbw, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
+  cudaMemsetAsync(b.ccnt, 0, sizeof(int) * std::max(lo.ncellcap, 1), B->st);
   cudaMemsetAsync(b.kgdone, 0, sizeof(int) * std::max<size_t>(lo.blk.size(), 1), B->st);
   cudaMemsetAsync(b.rlE, 0, sizeof(double) * 10 * std::max<size_t>(lo.blk.size(), 1), B->st);
   cudaMemsetAsync(b.kgcnt, 0, sizeof(int) * std::max(nsys, 1), B->st);
@@ -1228,6 +1249,34 @@ mdsc_status mdsc_last_error(const mdsc_batch* B, char* buf, size_t len) {
   return MDSC_OK;
 }
 
+// The list build's cell grid of a system: cells no smaller than the largest
+// reach of a list entry -- the segment-distance radius plus both rods' half
+// lengths (at most the longest rod), or the real-space neighbour radius --
+// so that every partner of a rod lies in the 27 cells around its own.  At
+// most cell_cap cells (dimensions shrunk, largest first); fewer than 3
+// cells along an axis, or no capacity: ncell = 0, the all-pairs scan.
+static void set_cell_grid(SysDev& P, const double* len) {
+  P.ncell = P.cnx = P.cny = P.cnz = 0;
+  if (P.cell_cap < 27) return;
+  double lmax = 0.0;
+  for (int i = 0; i < P.n; ++i) lmax = std::max(lmax, len[i]);
+  double side = (P.r_list + lmax) * 1.0001 + 1e-4;
+  if (P.rc_real > 0) side = std::max(side, std::sqrt((double)P.rl_r2) * 1.0001 + 1e-4);
+  int c[3];
+  for (int a = 0; a < 3; ++a) c[a] = (int)std::floor(P.L[a] / side);
+  while ((long long)c[0] * c[1] * c[2] > P.cell_cap) {
+    int a = 0;
+    for (int k = 1; k < 3; ++k)
+      if (c[k] > c[a]) a = k;
+    --c[a];
+  }
+  if (c[0] < 3 || c[1] < 3 || c[2] < 3) return;
+  P.cnx = c[0];
+  P.cny = c[1];
+  P.cnz = c[2];
+  P.ncell = c[0] * c[1] * c[2];
+}
+
 static mdsc_status upload_one(mdsc_batch* B, int s, const mdsc_host_state* h, bool sync) {
   const SysDev& P = B->lo.sys[s];
   const int n = P.n;
@@ -1293,6 +1342,7 @@ static mdsc_status upload_one(mdsc_batch* B, int s, const mdsc_host_state* h, bo
       const double rr = (Pm.rc_real + kLh + 2 * e + Pm.skin) * 1.0001 + 1e-4;
       Pm.rl_r2 = (float)(rr * rr);
     }
+    set_cell_grid(Pm, h->len);
     Pm.Uself = Uself;
     CU(up((void*)(b.sys + s), &Pm, sizeof(SysDev)));
     if (B->uploaded[s]) {
@@ -1443,7 +1493,7 @@ mdsc_status mdsc_force_sc(mdsc_batch* B, double* U, double* W, double* PT) {
   if (st) return st;
   launch_derive(B->b, B->st);
   launch_list_build(B->b, 0, B->st);
-  launch_wca(B->b, B->st);
+  launch_wca(B->b, 0, B->st);
   launch_finalize(B->b, kMaskWca | kFlagAccum, B->st);
   launch_order_terms(B->b, B->st);
   launch_reduce_obs(B->b, kRedEnergies, B->st);
@@ -1462,7 +1512,7 @@ mdsc_status mdsc_force_dipR(mdsc_batch* B, double* U, double* PT) {
   if (st) return st;
   launch_derive(B->b, B->st);
   if (B->b.any_rc) launch_list_build(B->b, 0, B->st);
-  launch_real_cut(B->b, B->st);
+  launch_near_pass(B->b, 1, B->st);
   launch_real_pairs(B->b, B->lo.multi, B->st);
   launch_real_sum(B->b, B->st);
   launch_finalize(B->b, kMaskReal | kFlagAccum, B->st);
@@ -1939,6 +1989,10 @@ mdsc_status mdsc_transfer(mdsc_batch* D, int dsys, mdsc_batch* S, int ssys) {
   Pd.Uself = Ps.Uself;
   Pd.cl_mode = Ps.cl_mode;
   Pd.rl_r2 = Ps.rl_r2;
+  Pd.ncell = Ps.ncell;
+  Pd.cnx = Ps.cnx;
+  Pd.cny = Ps.cny;
+  Pd.cnz = Ps.cnz;
   if (Pd.cl_mode == 1) {
     const mdsc_status est = ensure_energy_lists(D);
     if (est) return est;
@@ -2095,6 +2149,18 @@ mdsc_status mdsc_autotune(mdsc_batch* B, int force) {
   return MDSC_OK;
 }
 
+mdsc_status mdsc_set_list_cells(mdsc_batch* B, int on) {
+  if (!B || (on != 0 && on != 1)) return MDSC_ERR_BAD_ARG;
+  B->b.cells = on;
+  B->launches = 0;
+  for (int w = 0; w < 2; ++w)
+    if (B->graph[w]) {
+      cudaGraphExecDestroy(B->graph[w]);
+      B->graph[w] = nullptr;
+    }
+  return MDSC_OK;
+}
+
 mdsc_status mdsc_set_tuning(mdsc_batch* B, const int* values) {
   if (!B || !values) return MDSC_ERR_BAD_ARG;
   const int w = values[0], rt = values[1], wb = values[2], kg = values[3];
@@ -2143,7 +2209,8 @@ mdsc_status mdsc_profile_steps(mdsc_batch* B, int nsteps, int max_kernels, char*
   mdsc_status st = ensure_forces(B);
   if (st) return st;
   const char* kn[12] = {"integrate_first", "order_terms", "list_build", "wca", "real_pairs", "real_sum",
-                        "real_cut", "kspace_sum", "kspace_combine", "kspace_gather", "finalize", "reduce_obs"};
+                        "near_pass_real", "kspace_sum", "kspace_combine", "kspace_gather", "finalize",
+                        "reduce_obs"};
   const int nk = 12;
   std::vector<cudaEvent_t> ev(nk + 1);
   for (auto& e : ev) cudaEventCreate(&e);
@@ -2160,13 +2227,13 @@ mdsc_status mdsc_profile_steps(mdsc_batch* B, int nsteps, int max_kernels, char*
     cudaEventRecord(ev[2], B->st);
     launch_list_build(b, 0, B->st);
     cudaEventRecord(ev[3], B->st);
-    launch_wca(b, B->st);
+    launch_wca(b, 0, B->st);
     cudaEventRecord(ev[4], B->st);
     launch_real_pairs(b, B->lo.multi, B->st);
     cudaEventRecord(ev[5], B->st);
     launch_real_sum(b, B->st);
     cudaEventRecord(ev[6], B->st);
-    launch_real_cut(b, B->st);
+    launch_near_pass(b, 1, B->st);
     cudaEventRecord(ev[7], B->st);
     // the three k-space kernels, timed one by one
     launch_kspace_parts(b, B->lo.maxnd, B->kwork, (int)B->lo.kwork.size(), B->kowner, b.kE, 0, B->st);

@@ -55,6 +55,7 @@
 // reference's table is there to FP32 precision.
 #include "mdsc_dev.cuh"
 #include "reduce.cuh"
+#include "wca_screen.cuh"
 
 namespace mdsc {
 
@@ -513,25 +514,62 @@ __global__ void __launch_bounds__(32 * W, 20 / W) real_pairs_kernel(Batch b) {
   }
 }
 
-// Real space over a neighbour list, for systems with a real-space cutoff:
-// the reference's force_dipR with its table zeroed beyond rc_real, where
-// pairs beyond rc_real + Lh add nothing, so only the rods the list holds
-// (centres within rc_real + Lh + the dipoles' offsets + the skin) are
-// visited.  A group of kCutLanes lanes per dipole i takes its partner
-// dipoles -- the listed rods' dipoles, rods in ascending order -- two at a
-// time through the tiles' pair step (both halves holding dipole i), lane j
-// the pair steps j, j + kCutLanes, ...; a fixed shuffle tree adds the
-// lanes' sums.  Only i's own force and torque are kept, so every pair is met
-// from both ends and the energy and pressure tensor take half of each
-// meeting.  No atomics: the same bits alone and in any batch.  Writes each
-// dipole's force and torque where real_sum writes them, and its block's
-// energy and pressure tensor (float-float block sums) for the per-system sum.
+// The neighbour pass of the systems with a real-space cutoff: the
+// real-space sum and the WCA screen over one list per rod (list_build's
+// union list: the real-space partners at its head, the Verlet list's other
+// partners after them).
+//
+// Real space (mode kNearReal): the reference's force_dipR with its table
+// zeroed beyond rc_real, where pairs beyond rc_real + Lh add nothing, so
+// only the head of the list is visited -- the rods whose centres are within
+// rc_real + Lh + the dipoles' offsets + the skin.  A group of kCutLanes
+// lanes per dipole i takes its partner dipoles -- the listed rods' dipoles,
+// rods in ascending order -- two at a time through the tiles' pair step
+// (both halves holding dipole i), lane j the pair steps j, j + kCutLanes,
+// ...; a fixed shuffle tree adds the lanes' sums.  Only i's own force and
+// torque are kept, so every pair is met from both ends and the energy and
+// pressure tensor take half of each meeting.  No atomics: the same bits
+// alone and in any batch.  Writes each dipole's force and torque where
+// real_sum writes them, and its block's energy and pressure tensor
+// (float-float block sums) for the per-system sum.
+//
+// WCA screen (mode kNearWca): the first kPartBlock threads, a particle
+// each, merge the list's Verlet-list partners (flagged head entries, then
+// the tail: two ascending runs) into ascending order and screen them as the
+// WCA screen kernel screens its Verlet list (wca_screen.cuh); the FP64
+// evaluation follows in wca_eval.
 constexpr int kCutLanes = 4;
-__global__ void __launch_bounds__(kPartBlock * kCutLanes) real_cut_kernel(Batch b) {
+enum : int { kNearReal = 1, kNearWca = 2 };
+
+__device__ __forceinline__ void near_wca_screen(const Batch& b, const int2 bk, const SysDev& P) {
+  if (threadIdx.x >= kPartBlock) return;  // whole warps
+  const int i = bk.y + threadIdx.x;
+  const bool ok = i < P.part_off + P.n;
+  const int* r = b.rnb + (long long)(ok ? i : bk.y) * kMaxR;
+  const int na = ok ? b.rnbc[i] : 0;
+  const int tend = ok ? na + b.rnbw[i] : 0;
+  int a = 0, t = na;
+  wca_screen_one(b, P, bk.x, i, ok, [&]() -> int {
+    while (a < na && !(r[a] & kRnbWca)) ++a;
+    const int qa = a < na ? (r[a] & kRnbIdx) : 0x7fffffff;
+    const int qt = t < tend ? r[t] : 0x7fffffff;
+    if (qa == 0x7fffffff && qt == 0x7fffffff) return -1;
+    if (qa < qt) {
+      ++a;
+      return qa;
+    }
+    ++t;
+    return qt;
+  });
+}
+
+__global__ void __launch_bounds__(kPartBlock * kCutLanes) near_pass_kernel(Batch b, int mode) {
   __shared__ double sh[10 * kPartBlock * kCutLanes / 32];
   const int2 bk = b.blk[blockIdx.x];
   const SysDev& P = b.sys[bk.x];
   if (P.rc_real <= 0.0) return;  // the same for the whole block
+  if (mode & kNearWca) near_wca_screen(b, bk, P);
+  if (!(mode & kNearReal)) return;
   const int nd = P.nd;
   const int p0 = bk.y - P.part_off;
   const int np = min(kPartBlock, P.n - p0);
@@ -589,8 +627,8 @@ __global__ void __launch_bounds__(kPartBlock * kCutLanes) real_cut_kernel(Batch 
     for (int k = 2 * lane; k < nj; k += 2 * kCutLanes) {
       const bool two = k + 1 < nj;
       const int k1 = two ? k + 1 : k;
-      const int ga = P.dip_off + (lst[k / nd] - P.part_off) * nd + k % nd;
-      const int gb = P.dip_off + (lst[k1 / nd] - P.part_off) * nd + k1 % nd;
+      const int ga = P.dip_off + ((lst[k / nd] & kRnbIdx) - P.part_off) * nd + k % nd;
+      const int gb = P.dip_off + ((lst[k1 / nd] & kRnbIdx) - P.part_off) * nd + k1 % nd;
       const uint4 jpa = make_uint4(b.dfx[ga], b.dfx[ND + ga], b.dfx[2 * ND + ga], 0u);
       const uint4 jpb = make_uint4(b.dfx[gb], b.dfx[ND + gb], b.dfx[2 * ND + gb], 0u);
       const float4 jma = make_float4(b.dm[ga], b.dm[ND + ga], b.dm[2 * ND + ga], 0.f);
@@ -710,8 +748,8 @@ __global__ void __launch_bounds__(128) strip_energy_kernel(Batch b) {
   }
 }
 
-void launch_real_cut(const Batch& b, cudaStream_t s) {
-  if (b.any_rc && b.nblk) real_cut_kernel<<<b.nblk, kPartBlock * kCutLanes, 0, s>>>(b);
+void launch_near_pass(const Batch& b, int mode, cudaStream_t s) {
+  if (b.any_rc && b.nblk && mode) near_pass_kernel<<<b.nblk, kPartBlock * kCutLanes, 0, s>>>(b, mode);
 }
 
 void launch_real_sum(const Batch& b, cudaStream_t s) {

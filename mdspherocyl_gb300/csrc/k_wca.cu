@@ -10,7 +10,16 @@
 // the length times the axis change); the reference's own test looks at the
 // centres only (v25/functions.cpp:1386-1387), which is not enough once the
 // list radius is tight.  The build scans every particle of the system in
-// FP32 (fixed-point separations, exact minimum image).
+// FP32 (fixed-point separations, exact minimum image).  Systems of
+// kCellMinRods rods or more whose box holds at least 3 cells along every
+// axis bin their rods into cells no smaller than the largest reach of a
+// list entry and scan only the 27 cells around each rod's own: O(N) per
+// build instead of O(N^2).  A cell's rods are staged in cell order (the
+// fixed-point position with the rod's index, and the axis with the
+// length), and the two warps of a cell read each neighbour cell's slots
+// together, the same address across the warp.  The tests are the same FP32
+// expressions on the same values as the all-pairs scan, and each list is
+// sorted by index before it is written, so both scans give the same lists.
 //
 // WCA: the force is non-zero only for segment distance < 2^(1/6) sigma_ij.
 // A pair is first screened in FP32; pairs that pass are evaluated exactly as
@@ -21,25 +30,192 @@
 #include "mdsc_dev.cuh"
 #include "reduce.cuh"
 #include "seg_dist.cuh"
+#include "wca_screen.cuh"
 
 namespace mdsc {
 
-__global__ void __launch_bounds__(kPartBlock) list_build_kernel(Batch b, int force_all) {
-  __shared__ uint32_t sx[kPartBlock], sy[kPartBlock], sz[kPartBlock];
-  __shared__ float4 sa[kPartBlock];
+// Rebuild decision of every system (the same in every block of a system),
+// and, for a system that rebuilds on cells, its cell counts zeroed.
+__global__ void __launch_bounds__(kPartBlock) list_prep_kernel(Batch b, int force_all) {
   const int2 bk = b.blk[blockIdx.x];
-  const int s = bk.x;
-  const SysDev& P = b.sys[s];
-  SysState& S = b.st[s];
-  // rebuild decision, identical in every block of the system
+  const SysDev& P = b.sys[bk.x];
+  SysState& S = b.st[bk.x];
   bool need = force_all || S.force_list;
   if (!need) {
     double m = 0.0;
     for (int k = 0; k < P.nblk; ++k) m = fmax(m, b.dmax[P.blk_off + k]);
     need = 2.0 * m > P.skin;
   }
-  if (blk_slot(P, bk) == P.blk_off) S.rebuild = need ? 1 : 0;
-  if (!need) return;
+  const int j = blk_slot(P, bk) - P.blk_off;
+  if (j == 0 && threadIdx.x == 0) {
+    S.rebuild = need ? 1 : 0;
+    S.cell_ovf = 0;
+  }
+  if (!need || P.ncell == 0) return;
+  for (int c = j * kPartBlock + threadIdx.x; c < P.ncell; c += P.nblk * kPartBlock) b.ccnt[P.cell_off + c] = 0;
+}
+
+// cell of a fixed-point position: floor(fraction x cells), exact
+__device__ __forceinline__ int cell_of(const SysDev& P, uint32_t ux, uint32_t uy, uint32_t uz) {
+  const int cx = (int)(((unsigned long long)ux * (unsigned)P.cnx) >> 32);
+  const int cy = (int)(((unsigned long long)uy * (unsigned)P.cny) >> 32);
+  const int cz = (int)(((unsigned long long)uz * (unsigned)P.cnz) >> 32);
+  return (cz * P.cny + cy) * P.cnx + cx;
+}
+
+// Each rod of a rebuilding cell system into a slot of its cell (any order).
+__global__ void __launch_bounds__(kPartBlock) cell_bin_kernel(Batch b) {
+  const int2 bk = b.blk[blockIdx.x];
+  const SysDev& P = b.sys[bk.x];
+  SysState& S = b.st[bk.x];
+  if (!S.rebuild || P.ncell == 0) return;
+  const int i = bk.y + threadIdx.x;
+  if (i >= P.part_off + P.n) return;
+  const int N = b.ntot;
+  const uint32_t ux = b.pfx[i], uy = b.pfx[N + i], uz = b.pfx[2 * N + i];
+  const int c = P.cell_off + cell_of(P, ux, uy, uz);
+  const int slot = atomicAdd(&b.ccnt[c], 1);
+  if (slot < kCellSlots) {
+    b.cpos[(long long)c * kCellSlots + slot] = make_uint4(ux, uy, uz, (uint32_t)i);
+    b.cax[(long long)c * kCellSlots + slot] = b.pax[i];
+  } else {
+    atomicExch(&S.cell_ovf, 1);
+  }
+}
+
+// ascending insertion sort of a short list
+template <class A>
+__device__ __forceinline__ void sort_small(A& v, int n) {
+  for (int a = 1; a < n; ++a) {
+    const int x = v[a];
+    int c = a - 1;
+    while (c >= 0 && v[c] > x) {
+      v[c + 1] = v[c];
+      --c;
+    }
+    v[c + 1] = x;
+  }
+}
+
+// A cutoff system's neighbour-pass list: the real-space partners (centres
+// within the real-space radius, ascending) stay at the head, those also on
+// the Verlet list flagged kRnbWca; the Verlet list's other partners follow,
+// ascending.  One list then serves both the real-space sum and the WCA
+// screen of the neighbour pass.
+__device__ void rnb_merge(const Batch& b, int i, int cnt, int rcnt, int& err) {
+  const int* w = b.nb + (long long)i * kMaxNb;
+  int* r = b.rnb + (long long)i * kMaxR;
+  int a = 0, tail = rcnt;
+  for (int k = 0; k < cnt; ++k) {
+    const int q = w[k];
+    while (a < rcnt && (r[a] & kRnbIdx) < q) ++a;
+    if (a < rcnt && (r[a] & kRnbIdx) == q) {
+      r[a] |= kRnbWca;
+    } else {
+      if (tail < kMaxR) r[tail] = q;
+      ++tail;
+    }
+  }
+  if (tail > kMaxR) err |= kErrListOverflow;
+  b.rnbw[i] = min(tail, kMaxR) - rcnt;
+}
+
+// The cell scan: blocks of two cells (two warps each), a thread per slot.
+__device__ void list_cells(const Batch& b) {
+  const int2 cb = b.cellblk[blockIdx.x - b.nblk];
+  const SysDev& P = b.sys[cb.x];
+  SysState& S = b.st[cb.x];
+  if (!S.rebuild || P.ncell == 0 || S.cell_ovf) return;
+  const int c = cb.y + (threadIdx.x >> 6);
+  if (c >= P.ncell) return;
+  const int t = threadIdx.x & 63;
+  const int cnt0 = b.ccnt[P.cell_off + c];
+  const bool ok = t < cnt0;
+  uint4 me = make_uint4(0u, 0u, 0u, 0u);
+  float4 ai = make_float4(0.f, 0.f, 1.f, 0.f);
+  if (ok) {
+    me = b.cpos[(long long)(P.cell_off + c) * kCellSlots + t];
+    ai = b.cax[(long long)(P.cell_off + c) * kCellSlots + t];
+  }
+  const int i = (int)me.w;
+  const float rl = (float)P.r_list;
+  const float rl2 = rl * rl;
+  const float Lx = P.Lfix[0], Ly = P.Lfix[1], Lz = P.Lfix[2];
+  const bool rcut = P.rc_real > 0.0;
+  int lst[kMaxNb];
+  int cnt = 0, rcnt = 0;
+  int* rout = b.rnb + (long long)i * kMaxR;
+  const int cx = c % P.cnx, cy = (c / P.cnx) % P.cny, cz = c / (P.cnx * P.cny);
+  for (int dz = -1; dz <= 1; ++dz) {
+    const int qz = (cz + dz + P.cnz) % P.cnz;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int qy = (cy + dy + P.cny) % P.cny;
+      for (int dx0 = -1; dx0 <= 1; ++dx0) {
+        const int qx = (cx + dx0 + P.cnx) % P.cnx;
+        const long long q = P.cell_off + (qz * P.cny + qy) * P.cnx + qx;
+        const int m = b.ccnt[q];
+        const uint4* cp = b.cpos + q * kCellSlots;
+        const float4* ca = b.cax + q * kCellSlots;
+        for (int k = 0; k < m; ++k) {
+          const uint4 pj = cp[k];
+          const float4 aj = ca[k];
+          if (!ok || pj.w == me.w) continue;
+          const float dx = fix_diff(me.x, pj.x, Lx);
+          const float dy = fix_diff(me.y, pj.y, Ly);
+          const float dz2 = fix_diff(me.z, pj.z, Lz);
+          const float r2 = dx * dx + dy * dy + dz2 * dz2;
+          if (rcut && r2 < P.rl_r2) {
+            if (rcnt < kMaxR) rout[rcnt] = (int)pj.w;
+            ++rcnt;
+          }
+          const float reach = rl + 0.5f * (ai.w + aj.w);
+          if (!(r2 < reach * reach)) continue;
+          const float d2 = seg_dist_fast(dx, dy, dz2, ai.x, ai.y, ai.z, ai.w, aj.x, aj.y, aj.z, aj.w);
+          if (d2 < rl2) {
+            if (cnt < kMaxNb) lst[cnt] = (int)pj.w;
+            ++cnt;
+          }
+        }
+      }
+    }
+  }
+  if (!ok) return;
+  int err = (cnt > kMaxNb || rcnt > kMaxR) ? kErrListOverflow : 0;
+  cnt = min(cnt, kMaxNb);
+  sort_small(lst, cnt);
+  int* out = b.nb + (long long)i * kMaxNb;
+  for (int k = 0; k < cnt; ++k) out[k] = lst[k];
+  b.nbc[i] = cnt;
+  if (rcut) {
+    rcnt = min(rcnt, kMaxR);
+    sort_small(rout, rcnt);
+    b.rnbc[i] = rcnt;
+    rnb_merge(b, i, cnt, rcnt, err);
+  }
+  if (err) atomicOr(&S.status, err);
+  const int N = b.ntot;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    b.fsave[3 * i + a] = b.pfx[a * N + i];
+    b.usave[3 * i + a] = a == 0 ? ai.x : (a == 1 ? ai.y : ai.z);
+  }
+}
+
+// The list build: blocks below nblk scan all pairs of their particle block
+// (systems without cells, or whose cells overflowed this build); the rest
+// scan cells.
+__global__ void __launch_bounds__(kPartBlock) list_build_kernel(Batch b) {
+  __shared__ uint32_t sx[kPartBlock], sy[kPartBlock], sz[kPartBlock];
+  __shared__ float4 sa[kPartBlock];
+  if ((int)blockIdx.x >= b.nblk) {
+    list_cells(b);
+    return;
+  }
+  const int2 bk = b.blk[blockIdx.x];
+  const int s = bk.x;
+  const SysDev& P = b.sys[s];
+  SysState& S = b.st[s];
+  if (!S.rebuild || (b.cells && P.ncell > 0 && !S.cell_ovf)) return;
   const int i = bk.y + threadIdx.x;
   const bool ok = i < P.part_off + P.n;
   const int N = b.ntot;
@@ -124,9 +300,13 @@ __global__ void __launch_bounds__(kPartBlock) list_build_kernel(Batch b, int for
     }
   }
   if (!ok) return;
-  if (cnt > kMaxNb || rcnt > kMaxR) atomicOr(&S.status, kErrListOverflow);
+  int err = (cnt > kMaxNb || rcnt > kMaxR) ? kErrListOverflow : 0;
   b.nbc[i] = min(cnt, kMaxNb);
-  if (rcut) b.rnbc[i] = min(rcnt, kMaxR);
+  if (rcut) {
+    b.rnbc[i] = min(rcnt, kMaxR);
+    rnb_merge(b, i, min(cnt, kMaxNb), min(rcnt, kMaxR), err);
+  }
+  if (err) atomicOr(&S.status, err);
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     b.fsave[3 * i + a] = b.pfx[a * N + i];
@@ -235,60 +415,13 @@ __global__ void __launch_bounds__(kPartBlock) wca_screen_kernel(Batch b) {
   const int2 bk = b.blk[blockIdx.x];
   const int s = bk.x;
   const SysDev& P = b.sys[s];
-  const int lane = threadIdx.x & 31;
+  if (P.rc_real > 0.0) return;  // screened in the cutoff systems' neighbour pass (near_pass)
   const int i = bk.y + threadIdx.x;
   const bool ok = i < P.part_off + P.n;
-  const int N = b.ntot;
-  int err = 0;
-  int nc = 0;
-  if (ok) {
-    const uint32_t ux = b.pfx[i], uy = b.pfx[N + i], uz = b.pfx[2 * N + i];
-    const float4 ai = b.pax[i];
-    const float di = b.pdia[i];
-    const int nl = b.nbc[i];
-    const int* lst = b.nb + (long long)i * kMaxNb;
-    for (int k = 0; k < nl; ++k) {
-      const int q = lst[k];
-      if (q < i) continue;
-      const float dx = fix_diff(ux, b.pfx[q], P.Lfix[0]);
-      const float dy = fix_diff(uy, b.pfx[N + q], P.Lfix[1]);
-      const float dz = fix_diff(uz, b.pfx[2 * N + q], P.Lfix[2]);
-      const float4 aj = b.pax[q];
-      const float sg = 0.5f * (di + b.pdia[q]);
-      const float d2 = seg_dist_fast(dx, dy, dz, ai.x, ai.y, ai.z, ai.w, aj.x, aj.y, aj.z, aj.w);
-      // 2^(1/3) sigma^2, with a margin for the FP32 screen
-      if (d2 >= 1.2599211f * sg * sg * 1.002f) continue;
-      if (nc < kMaxC) {
-        b.wcand[(long long)i * kMaxC + nc] = q;
-        // the partner learns where its share of this pair will be
-        const int k = atomicAdd(&b.wincnt[q], 1);
-        if (k < kMaxC)
-          b.win[(long long)q * kMaxC + k] = i * kMaxC + nc;
-        else
-          err |= kErrListOverflow;
-      }
-      ++nc;
-    }
-    if (nc > kMaxC) {
-      err |= kErrListOverflow;
-      nc = kMaxC;
-    }
-    b.wcnt[i] = nc;
-  }
-  // room on the work list for the warp's candidates: one atomic per warp
-  int inc = nc;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const int v = __shfl_up_sync(0xffffffffu, inc, d);
-    if (lane >= d) inc += v;
-  }
-  const int wtot = __shfl_sync(0xffffffffu, inc, 31);
-  int base = 0;
-  if (lane == 31 && wtot > 0) base = atomicAdd(b.wlist_n, wtot);
-  base = __shfl_sync(0xffffffffu, base, 31);
-  const int off = base + inc - nc;
-  for (int kk = 0; kk < nc; ++kk) b.wlist[off + kk] = make_int2(i * kMaxC + kk, s);
-  if (err) atomicOr(&b.st[s].status, err);
+  const int nl = ok ? b.nbc[i] : 0;
+  const int* lst = b.nb + (long long)i * kMaxNb;
+  int k = 0;
+  wca_screen_one(b, P, s, i, ok, [&]() { return k < nl ? lst[k++] : -1; });
 }
 
 __global__ void __launch_bounds__(128) wca_eval_kernel(Batch b) {
@@ -559,12 +692,21 @@ __global__ void __launch_bounds__(kPartBlock) cluster_compress_kernel(Batch b) {
 }
 
 void launch_list_build(const Batch& b, int force_all, cudaStream_t s) {
-  if (b.nblk) list_build_kernel<<<b.nblk, kPartBlock, 0, s>>>(b, force_all);
+  if (!b.nblk) return;
+  list_prep_kernel<<<b.nblk, kPartBlock, 0, s>>>(b, force_all);
+  const int ncb = b.cells ? b.ncellblk : 0;
+  if (ncb) cell_bin_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
+  list_build_kernel<<<b.nblk + ncb, kPartBlock, 0, s>>>(b);
 }
-void launch_wca(const Batch& b, cudaStream_t s) {
+void launch_near_pass(const Batch& b, int mode, cudaStream_t s);  // k_real.cu
+
+void launch_wca(const Batch& b, int near_mode, cudaStream_t s) {
   if (!b.nblk) return;
   cudaMemsetAsync(b.wlist_n, 0, sizeof(int), s);
   cudaMemsetAsync(b.wincnt, 0, sizeof(int) * b.ntot, s);
+  // cutoff systems: the WCA screen over their neighbour-pass list (with
+  // their real space when near_mode says so); the others: over the Verlet list
+  launch_near_pass(b, 2 | near_mode, s);
   wca_screen_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
   // a fixed grid (chosen by the autotuner); each thread loops over the list
   wca_eval_kernel<<<b.tune.wca_blocks, 128, 0, s>>>(b);

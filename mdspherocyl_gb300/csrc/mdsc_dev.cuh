@@ -18,9 +18,19 @@ constexpr int kKChunk = 256;     // particles per block of the structure-factor 
 // systems of more strips than this sum their real-space tile energies per
 // strip first (real_sum); smaller ones are summed tile by tile
 constexpr int kStripRows = 32;
-constexpr int kMaxR = 256;       // real-space neighbours per rod (systems with a real-space cutoff)
+constexpr int kMaxR = 256;       // neighbour-pass list entries per rod (systems with a real-space cutoff)
+// entries of the neighbour-pass list: the real-space partners first
+// (ascending; kRnbWca marks those also on the Verlet list), then the Verlet
+// list's other partners (ascending)
+constexpr int kRnbWca = 1 << 30;
+constexpr int kRnbIdx = kRnbWca - 1;
 constexpr int kMaxE = 64;        // energy-criterion candidates (higher index) per rod
 constexpr int kMaxC = 16;        // WCA contact candidates of higher index per particle
+// cell-binned list builds: rods per cell slot range (a cell with more rods
+// sends its system to the all-pairs scan for that build); systems of fewer
+// rods than kCellMinRods always scan all pairs
+constexpr int kCellSlots = 64;
+constexpr int kCellMinRods = 256;
 
 // status bits (OR-ed per system; mapped to mdsc_status on the host)
 enum : int {
@@ -62,6 +72,12 @@ struct SysDev {
   int blk_off, nblk;        // per-particle block range
   int cl_fr;
   int cl_mode;     // cluster bonds: 0 the reference's geometric test, 1 pair energy
+  // cell grid of the list build (set at upload from the shapes): ncell = 0
+  // scans all pairs; else cnx x cny x cnz cells of at least the largest
+  // reach of a list entry, at cell_off .. cell_off + cell_cap - 1 of the
+  // batch's cell arrays
+  int ncell, cnx, cny, cnz;
+  int cell_off, cell_cap;
   float rl_r2;     // rc_real > 0: squared centre-distance radius of the real-space neighbour list
   double rc_real;  // real-space cutoff (0: all minimum-image pairs, the tiles)
   double cl_ubond; // mode 1: a bond is U_pair < -cl_ubond (the threshold times T)
@@ -103,6 +119,7 @@ struct SysState {
   int list_builds;
   int iter;          // step index within the current mdsc_step call (noise row)
   int force_list;    // rebuild the Verlet list at the next check regardless of the skin
+  int cell_ovf;      // this build: a cell held more than kCellSlots rods (all-pairs scan instead)
   double K_first[2]; // kinetic energies after the first half kick
   double xi_mid[2];  // xi used by the second half kick
 };
@@ -170,7 +187,8 @@ struct Batch {
   int nbstrips;
   int any_rc;     // some system has a real-space cutoff
   int* rnb;       // n * kMaxR: real-space neighbour rods (both directions, ascending) of rc_real systems
-  int* rnbc;      // n: their number
+  int* rnbc;      // n: the real-space partners among them (the head of the list)
+  int* rnbw;      // n: the Verlet-list partners after them (the tail)
   double* rlE;    // 10 per particle block: U, PT of the block's real-space neighbour pairs (rc_real systems)
   int4* tiles;   // (sys, I, J, 0)
   int2* wlist;   // WCA work list: (candidate slot, system), n * kMaxC at most
@@ -209,6 +227,15 @@ struct Batch {
   double* dmax;  // 1 per block: largest displacement measure since the last list build
   double* obk;   // 12 per block: the order-parameter terms of SysObs::osum
   int2* blk;     // (sys, first particle) per block
+  // cell bins of the list build: per cell its count, and kCellSlots slots
+  // of (fixed-point position, batch index) and (axis, length), filled in
+  // any order by the binning kernel
+  int* ccnt;     // ncellcap
+  uint4* cpos;   // ncellcap * kCellSlots
+  float4* cax;   // ncellcap * kCellSlots
+  int2* cellblk; // per pair of cells of capacity: (system, first cell)
+  int ncellblk;
+  int cells;     // 1: systems with a cell grid build their lists on it; 0: every system scans all pairs
   // neighbour list
   int* nb;       // n * kMaxNb
   int* nbc;      // n

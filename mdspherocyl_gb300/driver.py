@@ -340,7 +340,7 @@ class Driver:
         t = lambda *names: sum(ms.get(x, 0.0) for x in names) * 1e-3  # noqa: E731
         rows = [("X move time", t("integrate_first")), ("Force_ss time", t("list_build", "wca"))]
         if self.v251:
-            rows += [("Force_dipR time", t("real_pairs", "real_sum", "real_cut")),
+            rows += [("Force_dipR time", t("real_pairs", "real_sum", "near_pass_real")),
                      ("Force_dipK time", t("kspace_sum", "kspace_combine", "kspace_gather"))]
         rows.append(("P move time", t("finalize", "reduce_obs")))
         cor = self._cor_s / (V * cor_cont) if cor_cont > 0 else 0.0

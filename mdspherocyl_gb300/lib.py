@@ -41,7 +41,7 @@ EXPORTS = [
     "mdsc_autotune", "mdsc_tuning", "mdsc_set_tuning", "mdsc_correlation_bins", "mdsc_correlations",
     "mdsc_order_params", "mdsc_step_trace", "mdsc_get_rng", "mdsc_set_rng", "mdsc_set_species",
     "mdsc_correlation_size", "mdsc_get_thermostat", "mdsc_render", "mdsc_lattice", "mdsc_thermalize",
-    "mdsc_fp32_peak",
+    "mdsc_fp32_peak", "mdsc_set_list_cells",
 ]
 
 
@@ -190,6 +190,7 @@ def load(build: bool = True) -> ctypes.CDLL:
         "mdsc_profile_steps": (c_int, [c_void_p, c_int, c_int, c_char_p, c_size_t, _dp, _ip]),
         "mdsc_place_rods": (c_int, [c_int, _dp, _dp, _dp, ctypes.c_ulonglong, c_double, c_int, _dp, _dp]),
         "mdsc_fp32_peak": (c_int, [c_int, c_int, _dp, _dp, _dp, _ip]),
+        "mdsc_set_list_cells": (c_int, [c_void_p, c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -493,6 +494,10 @@ class Batch:
         """Pin the launch mappings (mdsc_set_tuning) instead of tuning them."""
         v = np.array([rp_warps, rsum_threads, wca_blocks, kg_scalar], dtype=np.int32)
         self._check(self.lib.mdsc_set_tuning(self.h, v.ctypes.data_as(_ip)), "mdsc_set_tuning")
+
+    def set_list_cells(self, on: bool) -> None:
+        """List builds on cells (the default) or over all pairs; same lists."""
+        self._check(self.lib.mdsc_set_list_cells(self.h, int(bool(on))), "mdsc_set_list_cells")
 
     def tuning(self) -> dict:
         """The launch mappings in use and the last tuning's timings."""
