@@ -180,11 +180,14 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_sample(states, threads: int, budget_s: float = 20.0, stride: int = 16):
+def cpu_sample(states, threads: int, budget_s: float = 20.0, stride: int = 16, keep: dict | None = None):
     """Times the oracle's MD step (the reference's routines restated in C,
     OpenMP over `threads` host threads) on every `stride`-th system of the
     mix -- a sample that spans the mix's N distribution -- one step each,
-    until `budget_s` is spent.  Returns particle-steps/s and the sample."""
+    until `budget_s` is spent.  Returns particle-steps/s and the sample.
+    With `keep`, each stepped system's results (observables, F, T, r, p)
+    are stored there by system index: the oracle's answers for the parity
+    block."""
     import oracle
 
     orc = oracle.Oracle()
@@ -201,10 +204,101 @@ def cpu_sample(states, threads: int, budget_s: float = 20.0, stride: int = 16):
         t_tot += time.perf_counter() - t0
         done_p += spec.n
         used.append(spec.n)
+        if keep is not None:
+            keep[k] = {"obs": md.obs(), "F": o.F.copy(), "T": o.T.copy(), "r": o.r.copy(), "p": o.p.copy()}
         md.close()
         if t_tot > budget_s:
             break
     return done_p / t_tot, used, t_tot
+
+
+# ---- parity of the GPU path against the oracle (the CPU leg's checker) ----
+# bars: Ewald forces and torques RMS relative 1e-5; total energy of a step
+# 1e-7; U alone 1e-6; pressure tensor RMS relative 1e-5; WCA (FP64) 1e-12;
+# cluster labels identical
+BARS = {"rms_F": 1e-5, "rms_T": 1e-5, "rel_E": 1e-7, "rel_U": 1e-6, "rms_PT": 1e-5}
+
+
+def _rms_rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    den = float(np.sqrt(np.mean(b ** 2)))
+    return float(np.sqrt(np.mean((a - b) ** 2)) / den) if den > 0 else float(np.abs(a).max())
+
+
+def _step_errors(gobs, gstate, oobs, ostate):
+    """Errors of one GPU step against the oracle's step of the same system."""
+    Ug = gobs["U_ss"] + gobs["U_dipR"] + gobs["U_dipK"] + gobs["U_ext"] + gobs["U_self"]
+    Uo = oobs["Uss"] + oobs["UdipR"] + oobs["UdipK"] + oobs["Uext"] + oobs["Uself"]
+    Kg, Ko = float(np.sum(gobs["K"])), float(np.sum(oobs["K"]))
+    PTg = sum(np.asarray(gobs[k]).reshape(3, 3) for k in ("PT_kin", "PT_ss", "PT_dipR", "PT_dipK"))
+    PTo = oobs["PTkin"] + oobs["PTss"] + oobs["PTdipR"] + oobs["PTdipK"]
+    return {"rms_F": _rms_rel(gstate["F"], ostate["F"]), "rms_T": _rms_rel(gstate["T"], ostate["T"]),
+            "rel_E": abs((Kg + Ug) - (Ko + Uo)) / abs(Ko + Uo), "rel_U": abs(Ug - Uo) / abs(Uo),
+            "rms_PT": _rms_rel(PTg, PTo), "max_dr": float(np.abs(gstate["r"] - ostate["r"]).max())}
+
+
+def _worst(rows):
+    w = {k: max(r[k] for r in rows) for k in rows[0]}
+    w["within_bars"] = all(w[k] <= v for k, v in BARS.items() if k in w)
+    return w
+
+
+def parity_block(mix_first, mix_oracle, device: int, threads: int, with_c2: bool = True) -> dict:
+    """One step of c0 (N=256) and c1 (N=4096) from their seeded states, the
+    sampled systems of the mix (c3, stepped inside the full batch), and one
+    evaluation of every force term of c2 (N=32768) with its geometric
+    cluster labels: GPU against the oracle."""
+    import oracle
+    from mdspherocyl_gb300 import lib as L
+    from mdspherocyl_gb300 import systems as S
+
+    orc = oracle.Oracle()
+    orc.set_threads(threads)
+    out = {"bars": BARS}
+    rows = [_step_errors(mix_first[k][0], mix_first[k][1], mix_oracle[k]["obs"], mix_oracle[k])
+            for k in sorted(mix_oracle) if k in mix_first]
+    if rows:
+        out["c3"] = {"systems": len(rows), "what": "every 16th system of the mix, one step inside the full batch",
+                     **_worst(rows)}
+    for name, fn in (("c0", "plain_c0"), ("c1", "plain_c1")):
+        spec, st = getattr(S, fn)(seed=3)
+        with L.Batch([spec], [st], device=device) as b1:
+            gobs = b1.step(1)[0]
+            gst = b1.download(0)
+        o = oracle.System(st.r, st.p, st.O, st.l, st.length, st.dia, st.mass, st.dip, spec.box)
+        md = oracle.MDOracle(orc, o, dt=spec.dt, temp=spec.temp, Q=spec.Q, gamma=spec.gamma, xi0=spec.xi0,
+                             sr_cut=3.0, K_max=spec.K_max, ksq_max=spec.ksq_max, alpha=spec.alpha, B=spec.B)
+        md.step()
+        e = _step_errors(gobs, gst, md.obs(), {"F": o.F, "T": o.T, "r": o.r})
+        md.close()
+        out[name] = {"n": spec.n, "what": "one step from the seeded state", **e,
+                     "within_bars": all(e[k] <= v for k, v in BARS.items())}
+    if with_c2:
+        spec, st = S.plain_c2(seed=3)
+        c2 = {"n": spec.n, "what": "one evaluation of each force term; geometric cluster labels"}
+        with L.Batch([spec], [st], device=device) as b1:
+            for name, call, ofn in (
+                ("sc", b1.force_sc, lambda s: orc.force_sc(s, 3.0, 3.5)[1:]),
+                ("dipR", b1.force_dipR, lambda s: orc.force_dipR(s, spec.alpha)),
+                ("dipK", b1.force_dipK, lambda s: orc.force_dipK(s, spec.K_max, spec.alpha, spec.ksq_max)),
+            ):
+                b1.zero_forces()
+                res = call()
+                d = b1.download(0)
+                so = oracle.System(st.r, st.p, st.O, st.l, st.length, st.dia, st.mass, st.dip, spec.box)
+                ores = ofn(so)
+                c2[name] = {"rms_F": _rms_rel(d["F"], so.F), "rms_T": _rms_rel(d["T"], so.T),
+                            "rel_U": abs(res[0][0] - ores[0]) / abs(ores[0]), "rms_PT": _rms_rel(res[-1][0], ores[-1])}
+            lab, nc = b1.clust_conf(0)
+        so = oracle.System(st.r, st.p, st.O, st.l, st.length, st.dia, st.mass, st.dip, spec.box)
+        lo, nco, _ = orc.clust_conf(so, float(spec.min_s), seed=1, skip=0)
+        c2["labels_equal"] = bool(np.array_equal(lab, lo)) and nc == nco
+        c2["clusters"] = int(nc)
+        c2["within_bars"] = (c2["labels_equal"] and max(c2["sc"][k] for k in ("rms_F", "rms_T", "rel_U")) <= 1e-12
+                             and all(c2[t][k] <= 1e-5 for t in ("dipR", "dipK") for k in ("rms_F", "rms_T", "rel_U",
+                                                                                         "rms_PT")))
+        out["c2"] = c2
+    return out
 
 
 def run_reference(args):
@@ -318,6 +412,12 @@ def run_ours(args):
         bt.set_cluster_energy(0, u_bond)
     stream = torch.cuda.ExternalStream(bt.lib.mdsc_stream(bt.h), device=device)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{device}")
+
+    # ---- the first step of the sampled systems, kept for the parity block ----
+    mix_first = {}
+    if not single and not args.no_cpu and not args.no_parity and ws == 1:
+        first = bt.step(1)
+        mix_first = {k: (first[k], bt.download(k)) for k in range(0, len(specs), 16)}
 
     # ---- device-resident throughput ----
     bt.step(max(args.warmup, 3))
@@ -467,7 +567,9 @@ def run_ours(args):
         cpu = None
         if not args.no_cpu and ws == 1:
             threads = os.cpu_count() or 1
-            v, used, tt = cpu_sample(states, threads, budget_s=args.cpu_budget, stride=1 if single else 16)
+            mix_oracle = {}
+            v, used, tt = cpu_sample(states, threads, budget_s=args.cpu_budget, stride=1 if single else 16,
+                                     keep=mix_oracle)
             cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": (f"oracle MD step (reference routines restated in C, OpenMP, {threads} threads) "
                               f"on every 16th system of the mix ({len(used)} systems, N={min(used)}..{max(used)}, "
@@ -511,6 +613,11 @@ def run_ours(args):
         }
         if cpu is not None:
             out["cpu_baseline"] = cpu
+            if not args.no_parity and not single:
+                t0 = time.perf_counter()
+                par = parity_block(mix_first, mix_oracle, device, threads, with_c2=not args.no_parity_c2)
+                par["seconds"] = time.perf_counter() - t0
+                out["parity"] = par
         print(json.dumps(out), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
@@ -533,6 +640,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the parity block of the CPU leg")
+    ap.add_argument("--no-parity-c2", action="store_true", help="parity block without the N=32768 evaluation")
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--jobs", type=int, default=200, help="serving leg: jobs (0 = skip)")
     ap.add_argument("--rate", type=float, default=40.0, help="serving leg: arrivals per second")

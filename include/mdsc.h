@@ -223,6 +223,21 @@ mdsc_status mdsc_set_cluster_energy(mdsc_batch* b, int sys, double u_bond_kT);
    continuous-batching server uses it to repack running systems when jobs
    finish or arrive.  No counterpart in the reference (one system per run). */
 mdsc_status mdsc_transfer(mdsc_batch* dst, int dsys, mdsc_batch* src, int ssys);
+/* The same for count systems at once (slot dsys[k] of dst from slot
+   ssys[k] of src), without a host synchronization: the copies are ordered
+   after src's queued work and before dst's next work, in one kernel
+   launch per 256 systems.  src may be destroyed as soon as it returns.
+   No counterpart in the reference. */
+mdsc_status mdsc_transfer_many(mdsc_batch* dst, mdsc_batch* src, const int* dsys, const int* ssys, int count);
+/* System sys takes no more steps once its step count (steps since the
+   batch was created, carried by mdsc_transfer) reaches `limit`; limit <= 0
+   removes the limit.  In mdsc_step a system at its limit costs nothing:
+   every kernel of the step returns at once for it, its state, observables
+   and generators stay as they were, and the others go on.  The server uses
+   it so that a job that finishes within a tick stops at exactly its step
+   count while the batch runs the whole tick.  No counterpart in the
+   reference (one system per run). */
+mdsc_status mdsc_set_step_limit(mdsc_batch* b, int sys, long long limit);
 
 /* ---- the fused step ---------------------------------------------------- */
 /* Advances every system by nsteps steps of the reference's loop body
@@ -350,7 +365,7 @@ mdsc_status mdsc_tuning(const mdsc_batch* b, int* values, char* log, size_t len)
 /* Sets the mappings by hand (values[0..3] as above) instead of tuning. */
 mdsc_status mdsc_set_tuning(mdsc_batch* b, const int* values);
 /* List builds (neigh_list, v25/functions.cpp:1298-1334) on cells (on = 1,
-   the default: systems of 256 rods or more whose box holds at least 3
+   the default: systems of 4096 rods or more whose box holds at least 3
    cells of the largest list reach along every axis bin their rods and scan
    the 27 cells around each rod, O(N)) or over all pairs (on = 0, O(N^2)).
    Both give the same lists, so the same bits; the switch is for timing and

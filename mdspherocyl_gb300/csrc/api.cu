@@ -1,6 +1,7 @@
 // Host implementation of the C ABI in include/mdsc.h: batch layout, memory,
 // the CUDA-graph step, thermostat noise and cluster-label replay.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstddef>
 #include <cstdio>
@@ -20,6 +21,7 @@
 
 namespace mdsc {
 void launch_real_pairs(const Batch& b, bool multi, cudaStream_t s);
+cudaError_t prepare_real_pairs();
 void launch_real_sum(const Batch& b, cudaStream_t s);
 // the cutoff systems' neighbour pass: real space (1), WCA screen (2), both (3)
 void launch_near_pass(const Batch& b, int mode, cudaStream_t s);
@@ -42,6 +44,8 @@ void launch_ebond(const Batch& b, cudaStream_t s);
 void launch_cluster_hook(const Batch& b, cudaStream_t s);
 void launch_cluster_compress(const Batch& b, cudaStream_t s);
 void launch_reset_iter(const Batch& b, cudaStream_t s);
+// copies systems (dst slot, src slot) between batches on the destination's stream
+cudaError_t launch_transfer(const Batch& dst, const Batch& src, const std::vector<int2>& pairs, cudaStream_t s);
 void launch_kspace_parts(const Batch& b, int maxnd, const int4* kwork, int nkwork, const int2* kowner,
                          double* kE, int part, cudaStream_t s);
 void launch_correlations(const Batch& b, const CorrSys* cs, const unsigned char* species, double bar_w,
@@ -78,6 +82,9 @@ struct Layout {
   std::vector<int2> bstrips;  // strips of the systems whose tile energies are summed per strip
   std::vector<int2> kgwork;   // (particle block, part) of the k-space gather
   std::vector<int2> cellblk;  // (system, first cell) of every block of the cell-binned list build
+  std::vector<int4> rpwork;   // runs of tiles whose table is staged in shared memory
+  std::vector<int> gtile;     // tiles read from the table in global memory
+  int smem_tn = 0;
   int ncellcap = 0;           // cells of capacity over all systems
   long long kgsets = 0;       // partial sets of the split gathers
   int ntot = 0, ndtot = 0, nktot = 0, maxnd = 0, nchunks = 0, nstrips = 0;
@@ -381,6 +388,20 @@ void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
     Lo.maxnd = std::max(Lo.maxnd, d.nd);
     if (d.nd > 1) Lo.multi = true;
   }
+  // real-space tiles: systems whose table fits a block's shared memory in
+  // runs of kSmemChunk tiles (the longest runs first), the others one by one
+  for (int s = 0; s < nsys; ++s) {
+    const SysDev& P = Lo.sys[s];
+    if (P.ntile == 0) continue;
+    if (P.rt_n > 0 && P.rt_n <= kSmemTableMax) {
+      for (int t = 0; t < P.ntile; t += kSmemChunk)
+        Lo.rpwork.push_back(make_int4(s, P.tile_off + t, std::min(kSmemChunk, P.ntile - t), 0));
+      Lo.smem_tn = std::max(Lo.smem_tn, P.rt_n);
+    } else {
+      for (int t = 0; t < P.ntile; ++t) Lo.gtile.push_back(P.tile_off + t);
+    }
+  }
+  std::stable_sort(Lo.rpwork.begin(), Lo.rpwork.end(), [](const int4& u, const int4& v) { return u.z > v.z; });
   // launch the particle blocks of the largest systems first: their blocks
   // run longest (real-space partials over more strips), so they must not
   // be the last wave on the GPU.  Kernels find a block's partial-sum slot
@@ -454,6 +475,8 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   b.rnbw = A.take<int>(n);
   b.rlE = A.take<double>(10 * nb);
   b.tiles = A.take<int4>(nt);
+  b.rpwork = A.take<int4>(std::max<size_t>(Lo.rpwork.size(), 1));
+  b.gtile = A.take<int>(std::max<size_t>(Lo.gtile.size(), 1));
   b.wlist = A.take<int2>(n * kMaxC);
   b.wlist_n = A.take<int>(1);
   b.wown = A.take<double>(n * kMaxC * 6);
@@ -527,6 +550,7 @@ struct mdsc_batch {
   std::vector<Mt19937> thermo_rng;  // 2 per system
   std::vector<Mt19937> clus_rng;    // 1 per system
   std::vector<long long> step_h;
+  std::vector<long long> stop_h;  // the systems' step limits (LLONG_MAX: none)
   std::vector<std::vector<int>> labels;
   std::vector<int> n_clusters;
   std::vector<char> uploaded, built, have_forces;
@@ -694,6 +718,7 @@ mdsc_status autotune(mdsc_batch* B, int force, int reps) {
 
 mdsc_status capture_step(mdsc_batch* B, int which) {
   Batch b = batch_with_noise(B, which);
+  b.honor_stop = 1;  // systems at their step limit take no step
   cudaGraph_t g = nullptr;
   CU(cudaStreamBeginCapture(B->st, cudaStreamCaptureModeThreadLocal));
   int launches = 0;
@@ -736,6 +761,7 @@ void draw_noise(mdsc_batch* B, int steps) {
   double* h = B->h_noise;
   for (int k = 0; k < steps; ++k)
     for (int s = 0; s < B->nsys; ++s) {
+      if (B->step_h[s] + k >= B->stop_h[s]) continue;  // at its step limit: no step, no draw
       double* o = h + ((size_t)k * B->nsys + s) * 4;
       for (int t = 0; t < 2; ++t) {
         Mt19937& g = B->thermo_rng[2 * s + t];
@@ -1083,7 +1109,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   B->desc.assign(descs, descs + nsys);
   cudaSetDevice(device);
   if (cudaDeviceGetAttribute(&B->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
-      B->num_sms <= 0) {
+      B->num_sms <= 0 || prepare_real_pairs() != cudaSuccess) {
     delete B;
     return MDSC_ERR_NO_DEVICE;
   }
@@ -1113,6 +1139,9 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   b.nkgwork = (int)lo.kgwork.size();
   b.nblk = (int)lo.blk.size();
   b.ncellblk = (int)lo.cellblk.size();
+  b.nrpwork = (int)lo.rpwork.size();
+  b.ngtile = (int)lo.gtile.size();
+  b.smem_tn = lo.smem_tn;
   b.cells = 1;
   b.noise = B->noise[0];
   // The step graph forks the real-space tiles (stream s2) from the WCA and
@@ -1140,6 +1169,8 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   };
   up((void*)b.sys, lo.sys.data(), sizeof(SysDev) * nsys);
   up(b.tiles, lo.tiles.data(), sizeof(int4) * lo.tiles.size());
+  if (!lo.rpwork.empty()) up(b.rpwork, lo.rpwork.data(), sizeof(int4) * lo.rpwork.size());
+  if (!lo.gtile.empty()) up(b.gtile, lo.gtile.data(), sizeof(int) * lo.gtile.size());
   if (!lo.bstrips.empty()) up(b.bstrips, lo.bstrips.data(), sizeof(int2) * lo.bstrips.size());
   if (!lo.kgwork.empty()) up(b.kgwork, lo.kgwork.data(), sizeof(int2) * lo.kgwork.size());
   up(b.blk, lo.blk.data(), sizeof(int2) * lo.blk.size());
@@ -1161,6 +1192,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   for (int s = 0; s < nsys; ++s) {
     st[s].xi[0] = st[s].xi[1] = descs[s].xi0;
     st[s].force_list = 1;
+    st[s].stop = LLONG_MAX;
   }
   up(b.st, st.data(), sizeof(SysState) * nsys);
   cudaMemsetAsync(b.obs, 0, sizeof(SysObs) * nsys, B->st);
@@ -1191,6 +1223,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
     B->clus_rng.back().discard(descs[s].cluster_skip);
   }
   B->step_h.assign(nsys, 0);
+  B->stop_h.assign(nsys, LLONG_MAX);
   B->labels.assign(nsys, std::vector<int>());
   for (int s = 0; s < nsys; ++s) B->labels[s].assign(descs[s].n, 0);
   B->n_clusters.assign(nsys, 0);
@@ -2010,11 +2043,75 @@ mdsc_status mdsc_transfer(mdsc_batch* D, int dsys, mdsc_batch* S, int ssys) {
   D->thermo_rng[2 * dsys + 1] = S->thermo_rng[2 * ssys + 1];
   D->clus_rng[dsys] = S->clus_rng[ssys];
   D->step_h[dsys] = S->step_h[ssys];
+  D->stop_h[dsys] = S->stop_h[ssys];
   D->labels[dsys] = S->labels[ssys];
   D->n_clusters[dsys] = S->n_clusters[ssys];
   D->uploaded[dsys] = 1;
   D->built[dsys] = 0;
   D->have_forces[dsys] = S->have_forces[ssys];
+  return MDSC_OK;
+}
+
+mdsc_status mdsc_transfer_many(mdsc_batch* D, mdsc_batch* S, const int* dsys, const int* ssys, int count) {
+  if (!D || !S || count < 0 || (count > 0 && (!dsys || !ssys))) return MDSC_ERR_BAD_ARG;
+  mdsc_batch* B = D;
+  if (S->device != D->device) return fail(D, MDSC_ERR_BAD_ARG, "mdsc_transfer_many: batches on different devices");
+  std::vector<int2> pairs(count);
+  bool energy = false;
+  for (int k = 0; k < count; ++k) {
+    const int d = dsys[k], q = ssys[k];
+    if (d < 0 || d >= D->nsys || q < 0 || q >= S->nsys) return MDSC_ERR_BAD_ARG;
+    const SysDev& Ps = S->lo.sys[q];
+    const SysDev& Pd = D->lo.sys[d];
+    if (Ps.n != Pd.n || Ps.nd != Pd.nd)
+      return fail(D, MDSC_ERR_BAD_ARG, "mdsc_transfer_many: systems differ in size");
+    if (!S->uploaded[q]) return fail(D, MDSC_ERR_STATE, "mdsc_transfer_many: a source system has no state");
+    energy |= Ps.cl_mode == 1;
+    pairs[k] = make_int2(d, q);
+  }
+  if (count == 0) return MDSC_OK;
+  cudaSetDevice(D->device);
+  if (energy) {
+    const mdsc_status est = ensure_energy_lists(D);
+    if (est) return est;
+  }
+  // the source's work is done before its state is read
+  CU(cudaEventRecord(S->ev_fork, S->st));
+  CU(cudaStreamWaitEvent(D->st, S->ev_fork, 0));
+  for (const int2& pr : pairs) {
+    const SysDev& Ps = S->lo.sys[pr.y];
+    SysDev& Pd = D->lo.sys[pr.x];
+    Pd.sig_max = Ps.sig_max;
+    Pd.skin = Ps.skin;
+    Pd.r_list = Ps.r_list;
+    Pd.Uself = Ps.Uself;
+    Pd.cl_mode = Ps.cl_mode;
+    Pd.rl_r2 = Ps.rl_r2;
+    Pd.ncell = Ps.ncell;
+    Pd.cnx = Ps.cnx;
+    Pd.cny = Ps.cny;
+    Pd.cnz = Ps.cnz;
+    Pd.cl_ubond = Ps.cl_ubond;
+  }
+  // the whole constant table once (the host copy stays alive with the batch)
+  CU(cudaMemcpyAsync((void*)D->b.sys, D->lo.sys.data(), sizeof(SysDev) * D->nsys, cudaMemcpyHostToDevice, D->st));
+  CU(launch_transfer(D->b, S->b, pairs, D->st));
+  for (const int2& pr : pairs) {
+    const int d = pr.x, q = pr.y;
+    D->thermo_rng[2 * d] = S->thermo_rng[2 * q];
+    D->thermo_rng[2 * d + 1] = S->thermo_rng[2 * q + 1];
+    D->clus_rng[d] = S->clus_rng[q];
+    D->step_h[d] = S->step_h[q];
+    D->stop_h[d] = S->stop_h[q];
+    D->labels[d] = S->labels[q];
+    D->n_clusters[d] = S->n_clusters[q];
+    D->uploaded[d] = 1;
+    D->built[d] = 0;
+    D->have_forces[d] = S->have_forces[q];
+  }
+  // the source may be destroyed once this returns: its reads are ordered
+  // before anything that follows on the destination's stream, and a
+  // destroy synchronizes the device first
   return MDSC_OK;
 }
 
@@ -2077,9 +2174,10 @@ static mdsc_status run_steps(mdsc_batch* B, int nsteps, mdsc_observables* trace)
     std::vector<int> due;
     for (int s = 0; s < B->nsys; ++s) {
       const int fr = B->desc[s].cl_fr;
-      const long long last = B->step_h[s] + chunk - 1;
-      if (fr > 0 && last % fr == 0) due.push_back(s);
-      B->step_h[s] += chunk;
+      const long long took = std::max(0LL, std::min<long long>(chunk, B->stop_h[s] - B->step_h[s]));
+      const long long last = B->step_h[s] + took - 1;
+      if (fr > 0 && took == chunk && last % fr == 0) due.push_back(s);
+      B->step_h[s] += took;
     }
     if (trace)  // cluster counts as they stood before this chunk's clustering step
       for (int k = 0; k < chunk; ++k)
@@ -2146,6 +2244,17 @@ mdsc_status mdsc_autotune(mdsc_batch* B, int force) {
       cudaGraphExecDestroy(B->graph[w]);
       B->graph[w] = nullptr;
     }
+  return MDSC_OK;
+}
+
+mdsc_status mdsc_set_step_limit(mdsc_batch* B, int sys, long long limit) {
+  if (!B || sys < 0 || sys >= B->nsys) return MDSC_ERR_BAD_ARG;
+  cudaSetDevice(B->device);
+  const long long v = limit > 0 ? limit : LLONG_MAX;
+  B->stop_h[sys] = v;
+  SysState* d = B->b.st + sys;
+  CU(cudaMemcpyAsync((char*)d + offsetof(SysState, stop), &v, sizeof v, cudaMemcpyHostToDevice, B->st));
+  CU(cudaStreamSynchronize(B->st));
   return MDSC_OK;
 }
 

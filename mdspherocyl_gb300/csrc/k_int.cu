@@ -11,6 +11,9 @@
 // FP32 *relative* precision (|D| ~ 1e-3 -> ~1e-10 absolute), and is applied
 // to the FP64 orientation as O += D O.  Kicks, drifts and the thermostat
 // scalars stay in FP64.
+#include <algorithm>
+#include <vector>
+
 #include "mdsc_dev.cuh"
 #include "reduce.cuh"
 
@@ -200,6 +203,7 @@ __global__ void __launch_bounds__(kPartBlock) integrate_first_kernel(Batch b) {
   __shared__ double sfac[2];
   const int2 bk = b.blk[blockIdx.x];
   const int s = bk.x;
+  if (at_limit(b, s)) return;
   const SysDev& P = b.sys[s];
   const SysState& S = b.st[s];
   const int i = bk.y + threadIdx.x;
@@ -285,6 +289,7 @@ __global__ void __launch_bounds__(kPartBlock, 6) finalize_kernel(Batch b, int mo
   __shared__ double sh[20 * kPartBlock / 32];
   const int2 bk = b.blk[blockIdx.x];
   const int s = bk.x;
+  if (at_limit(b, s)) return;
   const SysDev& P = b.sys[s];
   const SysState& S = b.st[s];
   const int i = bk.y + threadIdx.x;
@@ -473,6 +478,7 @@ __global__ void __launch_bounds__(kPartBlock, 6) finalize_kernel(Batch b, int mo
 __global__ void __launch_bounds__(kPartBlock) order_terms_kernel(Batch b) {
   __shared__ double sh[12 * kPartBlock / 32];
   const int2 bk = b.blk[blockIdx.x];
+  if (at_limit(b, bk.x)) return;
   const SysDev& P = b.sys[bk.x];
   const int i = bk.y + threadIdx.x;
   FF v[12];
@@ -506,6 +512,7 @@ constexpr int kRedThreads = 128;
 __global__ void __launch_bounds__(kRedThreads) reduce_obs_kernel(Batch b, int mode) {
   __shared__ double sh[12 * kRedThreads / 32];
   const int s = blockIdx.x / kRedGroups, grp = blockIdx.x % kRedGroups;
+  if (at_limit(b, s)) return;
   const SysDev& P = b.sys[s];
   SysState& S = b.st[s];
   SysObs& ob = b.obs[s];
@@ -731,6 +738,79 @@ void launch_renorm(const Batch& b, cudaStream_t s) {
 }
 void launch_movep(const Batch& b, const double* xi, int last, cudaStream_t s) {
   if (b.nblk) movep_kernel<<<b.nblk, kPartBlock, 0, s>>>(b, xi, last);
+}
+
+}  // namespace mdsc
+
+// ---------------------------------------------------------------------
+// systems moved between batches (mdsc_transfer_many): the particle state,
+// forces, shapes and dipoles of each (destination slot, source slot) pair,
+// the dipole owners for the destination's layout, and the mutable state
+// with a list rebuild requested.  One launch per kTransferChunk pairs,
+// grid.y over the pairs.
+// ---------------------------------------------------------------------
+namespace mdsc {
+
+constexpr int kTransferChunk = 256;
+struct TransferPairs {
+  int n;
+  int2 p[kTransferChunk];  // (destination system, source system)
+};
+
+__global__ void transfer_kernel(Batch dst, Batch src, TransferPairs tp) {
+  const int k = blockIdx.y;
+  if (k >= tp.n) return;
+  const int d = tp.p[k].x, q = tp.p[k].y;
+  const SysDev& Pd = dst.sys[d];
+  const SysDev& Ps = src.sys[q];
+  const int n = Pd.n, ndip = Pd.ndip;
+  const long long is = Ps.part_off, id = Pd.part_off, gs = Ps.dip_off, gd = Pd.dip_off;
+  const int stride = gridDim.x * blockDim.x;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < 9 * n; t += stride) {
+    dst.O[9 * id + t] = src.O[9 * is + t];
+    if (t < 3 * n) {
+      dst.r[3 * id + t] = src.r[3 * is + t];
+      dst.p[3 * id + t] = src.p[3 * is + t];
+      dst.l[3 * id + t] = src.l[3 * is + t];
+      dst.F[3 * id + t] = src.F[3 * is + t];
+      dst.T[3 * id + t] = src.T[3 * is + t];
+      dst.inert[3 * id + t] = src.inert[3 * is + t];
+      dst.invI[3 * id + t] = src.invI[3 * is + t];
+    }
+    if (t < n) {
+      dst.len[id + t] = src.len[is + t];
+      dst.dia[id + t] = src.dia[is + t];
+      dst.mass[id + t] = src.mass[is + t];
+      dst.invm[id + t] = src.invm[is + t];
+    }
+    if (t < 3 * ndip) dst.dob[3 * gd + t] = src.dob[3 * gs + t];
+    if (t < ndip) {
+      dst.dpc[gd + t] = src.dpc[gs + t];
+      dst.dmu[gd + t] = src.dmu[gs + t];
+      dst.downer[gd + t] = (int)id + t / max(Pd.nd, 1);
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    SysState st = src.st[q];
+    st.force_list = 1;
+    st.rebuild = 0;
+    st.iter = 0;
+    dst.st[d] = st;
+  }
+}
+
+cudaError_t launch_transfer(const Batch& dst, const Batch& src, const std::vector<int2>& pairs, cudaStream_t s) {
+  for (size_t k0 = 0; k0 < pairs.size(); k0 += kTransferChunk) {
+    TransferPairs tp;
+    tp.n = (int)std::min<size_t>(kTransferChunk, pairs.size() - k0);
+    for (int k = 0; k < tp.n; ++k) tp.p[k] = pairs[k0 + k];
+    // enough threads for the largest system of the batch: 9 values per rod
+    const int grid_x = std::min(64, cdiv(9 * std::max(dst.ntot, 1), 256));
+    transfer_kernel<<<dim3(grid_x, tp.n), 256, 0, s>>>(dst, src, tp);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 }  // namespace mdsc

@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(kKBlock) ksum_kernel(Batch b, const int4* __re
   __shared__ double shG[6 * kKBlock / 32];
   const int4 w = kwork[blockIdx.x];
   const SysDev& P = b.sys[w.x];
-  if (ND > 1 && P.nd <= 1) return;  // single-dipole systems: ksum1_kernel
+  if ((ND > 1 && P.nd <= 1) || at_limit(b, w.x)) return;  // single-dipole systems: ksum1_kernel
   const int chunk = w.y;
   const int kl = w.z * kKBlock + threadIdx.x;
   const int ND_all = b.ndtot;
@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(kKBlock / 2) ksum1_kernel(Batch b, const int4*
   __shared__ double shG[6 * (kKBlock / 2) / 32];
   const int4 w = kwork[blockIdx.x];
   const SysDev& P = b.sys[w.x];
-  if (P.nd != 1) return;  // other systems: ksum_kernel<ND>
+  if (P.nd != 1 || at_limit(b, w.x)) return;  // other systems: ksum_kernel<ND>
   const int chunk = w.y;
   const int t = threadIdx.x;
   const int kl0 = w.z * kKBlock + t, kl1 = kl0 + kKBlock / 2;
@@ -227,6 +227,7 @@ __global__ void kcombine_kernel(Batch b, const int2* __restrict__ kowner, double
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= b.nktot) return;
   const int2 ow = kowner[k];  // (system, k index within the system)
+  if (at_limit(b, ow.x)) return;
   const SysDev& P = b.sys[ow.x];
   const int kl = ow.y;
   // single-dipole systems (all of them when ND = 1): 6 sums per chunk and
@@ -309,7 +310,7 @@ __global__ void __launch_bounds__(kPartBlock) kgather_kernel(Batch b) {
   __shared__ float2 sks[kKBlock];
   const int2 bk = b.blk[blockIdx.x];
   const SysDev& P = b.sys[bk.x];
-  if (ND > 1 && P.nd <= 1) return;  // single-dipole systems: kgather1 / kgather1s
+  if ((ND > 1 && P.nd <= 1) || at_limit(b, bk.x)) return;  // single-dipole systems: kgather1 / kgather1s
   const int i = bk.y + threadIdx.x;  // batch particle index
   const bool ok = i < P.part_off + P.n;
   const int nd = P.nd;
@@ -455,7 +456,7 @@ __global__ void __launch_bounds__(kPartBlock / 2) kgather1_kernel(Batch b) {
   const int2 wk = b.kgwork[blockIdx.x];  // (particle block, part)
   const int2 bk = b.blk[wk.x];
   const SysDev& P = b.sys[bk.x];
-  if (P.nd != 1) return;  // other systems: kgather_kernel<ND>
+  if (P.nd != 1 || at_limit(b, bk.x)) return;  // other systems: kgather_kernel<ND>
   int kb, ke;
   kpart_range(P, wk.y, kb, ke);
   const int t = threadIdx.x;
@@ -563,7 +564,7 @@ __global__ void __launch_bounds__(kPartBlock) kgather1s_kernel(Batch b) {
   const int2 wk = b.kgwork[blockIdx.x];  // (particle block, part)
   const int2 bk = b.blk[wk.x];
   const SysDev& P = b.sys[bk.x];
-  if (P.nd != 1) return;  // other systems: kgather_kernel<ND>
+  if (P.nd != 1 || at_limit(b, bk.x)) return;  // other systems: kgather_kernel<ND>
   int kb, ke;
   kpart_range(P, wk.y, kb, ke);
   const int t = threadIdx.x;

@@ -122,8 +122,16 @@ struct PairConst {
   f2 invLh, halfLh2, nsixthLh3;
   f2 Lhx, Lhy, Lhz, Llx, Lly, Llz;  // L / 2^32 per axis as float-float pairs
   f2 ihh, ihl;                      // 1 / Lh as a float-float pair
-  const float4* tab;                // the system's table entries (TAB kernels)
+  const float4* tab;                // the system's table entries in global memory (MODE 1)
+  const float4* stab;               // its values in shared memory (MODE 2): A, B, C, A' - A per entry
   int tn;                           // its number of entries
+};
+
+// how a tile kernel gets the reference's interpolation
+enum : int {
+  kAnalytic = 0,   // analytic terms plus the table's interpolation error (no table)
+  kTabGlobal = 1,  // the system's table in global memory, one 256-bit load per lookup
+  kTabShared = 2,  // the system's table staged in shared memory, two 128-bit loads per lookup
 };
 
 struct Lane2 {
@@ -143,7 +151,7 @@ struct JOut {
 // one step of a tile loop: the lane's two i-dipoles against j0 (half 0)
 // and j1 (half 1) -- the same j in off-diagonal tiles.  Pairs masked off
 // (a0, a1 false) contribute exactly zero.
-template <bool MASKED, bool TAB>
+template <bool MASKED, int MODE>
 __device__ __forceinline__ void tile_step(const PairConst& K, Lane2& s, const uint4 jp0, const float4 jm0,
                                           const uint4 jp1, const float4 jm1, bool a0, bool a1, JOut& o) {
   f2 mix = s.mx, miy = s.my, miz = s.mz;
@@ -167,7 +175,19 @@ __device__ __forceinline__ void tile_step(const PairConst& K, Lane2& s, const ui
   const f2 rinv3 = mul2(rinv2, rinv);
 
   f2 Ac, Bc, Cc;
-  if (TAB) {
+  if (MODE == kTabShared) {
+    // the same interpolation, entries from the block's shared copy: A and
+    // A's difference as stored, B and C's differences from the next entry
+    const f2 uu = fma2(r, K.ihh, mul2(r, K.ihl));
+    const float fl0 = floorf(uu.x), fl1 = floorf(uu.y);
+    const f2 fr = add2(fma2(r, K.ihh, make_float2(-fl0, -fl1)), mul2(r, K.ihl));
+    const int e0 = min(max((int)fl0 - 1, 0), K.tn - 1), e1 = min(max((int)fl1 - 1, 0), K.tn - 1);
+    const float4 p0 = K.stab[e0], n0 = K.stab[e0 + 1];
+    const float4 p1 = K.stab[e1], n1 = K.stab[e1 + 1];
+    Ac = fma2(fr, make_float2(p0.w, p1.w), make_float2(p0.x, p1.x));
+    Bc = fma2(fr, make_float2(n0.y - p0.y, n1.y - p1.y), make_float2(p0.y, p1.y));
+    Cc = fma2(fr, make_float2(n0.z - p0.z, n1.z - p1.z), make_float2(p0.z, p1.z));
+  } else if (MODE == kTabGlobal) {
     // the reference's own method: linear interpolation in its table
     // (v25/functions.cpp:1606-1614), entry ri - 1 and ri for ri = floor(r/Lh);
     // r/Lh from a float-float 1/Lh, the fraction by one FMA against the
@@ -278,7 +298,7 @@ __device__ __forceinline__ void tile_step(const PairConst& K, Lane2& s, const ui
 // Off-diagonal tile (strips I < J): 64 steps, at step t lane l pairs both
 // its i-dipoles with j = (l + t) mod 64; the two halves' j-side terms are
 // added into that j's sums.
-template <bool MASKED, bool MULTI, bool TAB>
+template <bool MASKED, bool MULTI, int MODE>
 __device__ __forceinline__ void tile_loop(const PairConst& K, Lane2& s, const uint4* sj, const float4* smj,
                                           float4* sa4, float2* sa2, int lane, int jvalid) {
 #pragma unroll 2
@@ -297,7 +317,7 @@ __device__ __forceinline__ void tile_loop(const PairConst& K, Lane2& s, const ui
       }
     }
     JOut o;
-    tile_step<MASKED, TAB>(K, s, jp, jm, jp, jm, a0, a1, o);
+    tile_step<MASKED, MODE>(K, s, jp, jm, jp, jm, a0, a1, o);
     float4 ja4 = sa4[lj];
     float2 ja2 = sa2[lj];
     ja4.x -= o.fx.x + o.fx.y;
@@ -317,7 +337,7 @@ __device__ __forceinline__ void tile_loop(const PairConst& K, Lane2& s, const ui
 // x = l + 32 (half 1) pair with (x + t) mod 64: each pair at cyclic distance
 // d < 32 is met once from its lower end, d > 32 once from its upper end,
 // and d = 32 from half 0 only.  The 64 j's of a step are distinct.
-template <bool MULTI, bool TAB>
+template <bool MULTI, int MODE>
 __device__ __forceinline__ void diag_loop(const PairConst& K, Lane2& s, const uint4* sj, const float4* smj,
                                           float4* sa4, float2* sa2, int lane, int jvalid) {
 #pragma unroll 1
@@ -332,7 +352,7 @@ __device__ __forceinline__ void diag_loop(const PairConst& K, Lane2& s, const ui
       a1 = a1 && (s.own1 != (int)jp1.w);
     }
     JOut o;
-    tile_step<true, TAB>(K, s, jp0, jm0, jp1, jm1, a0, a1, o);
+    tile_step<true, MODE>(K, s, jp0, jm0, jp1, jm1, a0, a1, o);
     float4 ja4 = sa4[j0];
     float2 ja2 = sa2[j0];
     ja4.x -= o.fx.x;
@@ -359,36 +379,8 @@ __device__ __forceinline__ void diag_loop(const PairConst& K, Lane2& s, const ui
 
 }  // namespace
 
-// W warps per block, one tile per warp (tile = W * blockIdx.x + warp): the
-// block size changes how tiles are grouped for scheduling, never what a
-// tile computes, so every W gives the same bits (the autotuner picks W).
-// TAB: interpolate in the reference's table (the batch path); otherwise the
-// analytic terms with the table's error added (callers without the table).
-// 20 warps per SM hold the kernel to 96 registers (16 B of spills) from
-// 126: the table lookups' latency is hidden by warps, and 21 warps instead
-// of 16 made the table form 3% faster on the 256-replica mix.
-template <bool MULTI, int W, bool TAB>
-__global__ void __launch_bounds__(32 * W, 20 / W) real_pairs_kernel(Batch b) {
-  __shared__ uint4 sj_all[W][kTile];    // fixed-point x, y, z and owner of the j-dipoles
-  __shared__ float4 smj_all[W][kTile];  // their moments
-  __shared__ float4 sa4_all[W][kTile];  // j-side sums: F x, y, z and T x
-  __shared__ float2 sa2_all[W][kTile];  // T y, z
-  const int wid = threadIdx.x >> 5;
-  const int tile = W * blockIdx.x + wid;
-  if (tile >= b.ntiles) return;
-  uint4* sj = sj_all[wid];
-  float4* smj = smj_all[wid];
-  float4* sa4 = sa4_all[wid];
-  float2* sa2 = sa2_all[wid];
-
-  const int4 tl = b.tiles[tile];
-  const SysDev& P = b.sys[tl.x];
-  const int I = tl.y, J = tl.z;
-  const bool diag = (I == J);
-  const int lane = threadIdx.x & 31;
-  const int ndip = P.ndip;
-  const int ND = b.ndtot;
-
+// per-system constants of the pair step
+__device__ __forceinline__ PairConst pair_consts(const Batch& b, const SysDev& P, int mode, const float4* stab) {
   PairConst K;
   K.xh = b2(P.xh);
   K.xlo = b2(P.xlo);
@@ -405,10 +397,27 @@ __global__ void __launch_bounds__(32 * W, 20 / W) real_pairs_kernel(Batch b) {
   K.invLh = b2(P.invLh);
   K.ihh = b2(kInvLhHi);
   K.ihl = b2(kInvLhLo);
-  K.tab = TAB ? b.rtab + 2 * (long long)P.rt_off : nullptr;
+  K.tab = mode == kTabGlobal ? b.rtab + 2 * (long long)P.rt_off : nullptr;
+  K.stab = stab;
   K.tn = P.rt_n;
   K.halfLh2 = b2(P.halfLh2);
   K.nsixthLh3 = b2(-P.sixthLh3);
+  return K;
+}
+
+// One tile (strips I <= J of one system) by one warp: the j-strip staged in
+// the warp's shared arrays, the i-strip in registers, the pair loop, the
+// partial slots and the tile's energy and pressure tensor.
+template <bool MULTI, int MODE>
+__device__ __forceinline__ void tile_work(const Batch& b, int tile, const PairConst& K, uint4* sj, float4* smj,
+                                          float4* sa4, float2* sa2) {
+  const int4 tl = b.tiles[tile];
+  const SysDev& P = b.sys[tl.x];
+  const int I = tl.y, J = tl.z;
+  const bool diag = (I == J);
+  const int lane = threadIdx.x & 31;
+  const int ndip = P.ndip;
+  const int ND = b.ndtot;
 
   for (int k = lane; k < kTile; k += 32) {
     const int jj = J * kTile + k;
@@ -450,13 +459,12 @@ __global__ void __launch_bounds__(32 * W, 20 / W) real_pairs_kernel(Batch b) {
   // no pair of this tile is skipped: the fast loop without masks
   const bool full = !MULTI && !diag && jvalid == kTile;
   if (diag)
-    diag_loop<MULTI, TAB>(K, s, sj, smj, sa4, sa2, lane, jvalid);
+    diag_loop<MULTI, MODE>(K, s, sj, smj, sa4, sa2, lane, jvalid);
   else if (full)
-    tile_loop<false, MULTI, TAB>(K, s, sj, smj, sa4, sa2, lane, jvalid);
+    tile_loop<false, MULTI, MODE>(K, s, sj, smj, sa4, sa2, lane, jvalid);
   else
-    tile_loop<true, MULTI, TAB>(K, s, sj, smj, sa4, sa2, lane, jvalid);
+    tile_loop<true, MULTI, MODE>(K, s, sj, smj, sa4, sa2, lane, jvalid);
   __syncwarp();
-
   // partial slots: (strip X, strip Y, component c, local index)
   const int ns = P.nstrip;
   float* base_ij = b.rpart + P.pp_off + ((long long)(I * ns + J) * 6) * kTile;
@@ -514,6 +522,64 @@ __global__ void __launch_bounds__(32 * W, 20 / W) real_pairs_kernel(Batch b) {
   }
 }
 
+// W warps per block, one tile per warp (tile = W * blockIdx.x + warp, or
+// the warp's entry of the list `gtile` of tiles that read the table from
+// global memory): the block size changes how tiles are grouped for
+// scheduling, never what a tile computes, so every W gives the same bits
+// (the autotuner picks W).  MODE kTabGlobal: interpolate in the reference's
+// table (systems whose table does not fit a block's shared memory);
+// kAnalytic: the analytic terms with the table's error added (callers
+// without the table).  20 warps per SM hold the kernel to 96 registers
+// (16 B of spills) from 126: the table lookups' latency is hidden by warps,
+// and 21 warps instead of 16 made the table form 3% faster on the
+// 256-replica mix.
+template <bool MULTI, int W, int MODE>
+__global__ void __launch_bounds__(32 * W, 20 / W) real_pairs_kernel(Batch b, const int* gtile, int ntile) {
+  __shared__ uint4 sj_all[W][kTile];    // fixed-point x, y, z and owner of the j-dipoles
+  __shared__ float4 smj_all[W][kTile];  // their moments
+  __shared__ float4 sa4_all[W][kTile];  // j-side sums: F x, y, z and T x
+  __shared__ float2 sa2_all[W][kTile];  // T y, z
+  const int wid = threadIdx.x >> 5;
+  const int k = W * blockIdx.x + wid;
+  if (k >= ntile) return;
+  const int tile = gtile ? gtile[k] : k;
+  if (at_limit(b, b.tiles[tile].x)) return;
+  const SysDev& P = b.sys[b.tiles[tile].x];
+  const PairConst K = pair_consts(b, P, MODE, nullptr);
+  tile_work<MULTI, MODE>(b, tile, K, sj_all[wid], smj_all[wid], sa4_all[wid], sa2_all[wid]);
+}
+
+// Tiles of systems whose table fits a block's shared memory: a block takes
+// a run of one system's tiles (rpwork: system, first tile, tiles), stages
+// the system's interpolation table once -- A, B, C and A's difference per
+// entry, 16 bytes, plus a copy of the last entry -- and its kSmemWarps
+// warps take the run's tiles in turn.  A lookup is two 128-bit shared
+// loads (entries k and k + 1, for the differences of B and C) instead of a
+// scattered 256-bit global load: the table lookups no longer queue on the
+// L1's tag stage behind misses to L2.  One block of kSmemWarps warps per SM.
+template <bool MULTI>
+__global__ void __launch_bounds__(32 * kSmemWarps, 1) real_pairs_smem_kernel(Batch b) {
+  extern __shared__ float4 dyn[];
+  const int4 wk = b.rpwork[blockIdx.x];
+  if (at_limit(b, wk.x)) return;
+  const SysDev& P = b.sys[wk.x];
+  const int tn = P.rt_n;
+  float4* stab = dyn;
+  const float4* g = b.rtab + 2 * (long long)P.rt_off;
+  for (int e = threadIdx.x; e <= tn; e += blockDim.x) stab[e] = __ldg(g + 2 * min(e, tn - 1));
+  // per warp: 64 x (uint4 + float4 + float4) + 64 float2, after the table
+  const int wid = threadIdx.x >> 5;
+  float4* wbase = dyn + (tn + 1) + wid * (3 * kTile + kTile / 2);
+  uint4* sj = reinterpret_cast<uint4*>(wbase);
+  float4* smj = wbase + kTile;
+  float4* sa4 = wbase + 2 * kTile;
+  float2* sa2 = reinterpret_cast<float2*>(wbase + 3 * kTile);
+  __syncthreads();
+  const PairConst K = pair_consts(b, P, kTabShared, stab);
+  for (int t = wk.y + wid; t < wk.y + wk.z; t += kSmemWarps)
+    tile_work<MULTI, kTabShared>(b, t, K, sj, smj, sa4, sa2);
+}
+
 // The neighbour pass of the systems with a real-space cutoff: the
 // real-space sum and the WCA screen over one list per rod (list_build's
 // union list: the real-space partners at its head, the Verlet list's other
@@ -567,7 +633,7 @@ __global__ void __launch_bounds__(kPartBlock * kCutLanes) near_pass_kernel(Batch
   __shared__ double sh[10 * kPartBlock * kCutLanes / 32];
   const int2 bk = b.blk[blockIdx.x];
   const SysDev& P = b.sys[bk.x];
-  if (P.rc_real <= 0.0) return;  // the same for the whole block
+  if (P.rc_real <= 0.0 || at_limit(b, bk.x)) return;  // the same for the whole block
   if (mode & kNearWca) near_wca_screen(b, bk, P);
   if (!(mode & kNearReal)) return;
   const int nd = P.nd;
@@ -634,7 +700,7 @@ __global__ void __launch_bounds__(kPartBlock * kCutLanes) near_pass_kernel(Batch
       const float4 jma = make_float4(b.dm[ga], b.dm[ND + ga], b.dm[2 * ND + ga], 0.f);
       const float4 jmb = make_float4(b.dm[gb], b.dm[ND + gb], b.dm[2 * ND + gb], 0.f);
       JOut o;
-      tile_step<true, true>(K, s, jpa, jma, jpb, jmb, true, two, o);
+      tile_step<true, kTabGlobal>(K, s, jpa, jma, jpb, jmb, true, two, o);
     }
     // a lane's sums, then the group's (xor tree over the kCutLanes lanes)
     float v[17];
@@ -693,7 +759,7 @@ __global__ void __launch_bounds__(kPartBlock * kCutLanes) near_pass_kernel(Batch
 __global__ void __launch_bounds__(512) real_sum_kernel(Batch b) {
   const int2 bk = b.blk[blockIdx.x];
   const SysDev& P = b.sys[bk.x];
-  if (P.rc_real > 0.0) return;  // summed by the neighbour pass (real_cut)
+  if (P.rc_real > 0.0 || at_limit(b, bk.x)) return;  // cutoff systems: summed by their neighbour pass
   const int nd = P.nd;
   const int p0 = bk.y - P.part_off;
   const int np = min(kPartBlock, P.n - p0);
@@ -728,6 +794,7 @@ __global__ void __launch_bounds__(128) strip_energy_kernel(Batch b) {
   const int w = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (w >= b.nbstrips) return;
   const int2 sx = b.bstrips[w];
+  if (at_limit(b, sx.x)) return;
   const SysDev& P = b.sys[sx.x];
   const int X = sx.y, ns = P.nstrip;
   const long long t0 = P.tile_off + (long long)X * ns - (long long)X * (X - 1) / 2;
@@ -758,22 +825,44 @@ void launch_real_sum(const Batch& b, cudaStream_t s) {
   if (b.nbstrips) strip_energy_kernel<<<cdiv(b.nbstrips, 4), 128, 0, s>>>(b);
 }
 
+size_t real_pairs_smem_bytes(int tn) {
+  return sizeof(float4) * ((size_t)tn + 1 + (size_t)kSmemWarps * (3 * kTile + kTile / 2));
+}
+
+// Once per device, outside any stream capture: the largest dynamic shared
+// memory a shared-table tile launch may ask for.
+cudaError_t prepare_real_pairs() {
+  const int most = (int)real_pairs_smem_bytes(kSmemTableMax);
+  cudaError_t e = cudaFuncSetAttribute(real_pairs_smem_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(real_pairs_smem_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+  return e;
+}
+
 void launch_real_pairs(const Batch& b, bool multi, cudaStream_t s) {
   if (b.ntiles == 0) return;
-  const int W = b.tune.rp_warps;
-  const int grid = cdiv(b.ntiles, W);
   if (b.rtab == nullptr) {  // no table: the analytic form, one tile per block
-    if (multi) real_pairs_kernel<true, 1, false><<<b.ntiles, 32, 0, s>>>(b);
-    else real_pairs_kernel<false, 1, false><<<b.ntiles, 32, 0, s>>>(b);
-  } else if (W == 4) {
-    if (multi) real_pairs_kernel<true, 4, true><<<grid, 128, 0, s>>>(b);
-    else real_pairs_kernel<false, 4, true><<<grid, 128, 0, s>>>(b);
+    if (multi) real_pairs_kernel<true, 1, kAnalytic><<<b.ntiles, 32, 0, s>>>(b, nullptr, b.ntiles);
+    else real_pairs_kernel<false, 1, kAnalytic><<<b.ntiles, 32, 0, s>>>(b, nullptr, b.ntiles);
+    return;
+  }
+  if (b.nrpwork) {
+    const size_t bytes = real_pairs_smem_bytes(b.smem_tn);
+    if (multi) real_pairs_smem_kernel<true><<<b.nrpwork, 32 * kSmemWarps, bytes, s>>>(b);
+    else real_pairs_smem_kernel<false><<<b.nrpwork, 32 * kSmemWarps, bytes, s>>>(b);
+  }
+  if (b.ngtile == 0) return;
+  const int W = b.tune.rp_warps;
+  const int grid = cdiv(b.ngtile, W);
+  if (W == 4) {
+    if (multi) real_pairs_kernel<true, 4, kTabGlobal><<<grid, 128, 0, s>>>(b, b.gtile, b.ngtile);
+    else real_pairs_kernel<false, 4, kTabGlobal><<<grid, 128, 0, s>>>(b, b.gtile, b.ngtile);
   } else if (W == 2) {
-    if (multi) real_pairs_kernel<true, 2, true><<<grid, 64, 0, s>>>(b);
-    else real_pairs_kernel<false, 2, true><<<grid, 64, 0, s>>>(b);
+    if (multi) real_pairs_kernel<true, 2, kTabGlobal><<<grid, 64, 0, s>>>(b, b.gtile, b.ngtile);
+    else real_pairs_kernel<false, 2, kTabGlobal><<<grid, 64, 0, s>>>(b, b.gtile, b.ngtile);
   } else {
-    if (multi) real_pairs_kernel<true, 1, true><<<b.ntiles, 32, 0, s>>>(b);
-    else real_pairs_kernel<false, 1, true><<<b.ntiles, 32, 0, s>>>(b);
+    if (multi) real_pairs_kernel<true, 1, kTabGlobal><<<b.ngtile, 32, 0, s>>>(b, b.gtile, b.ngtile);
+    else real_pairs_kernel<false, 1, kTabGlobal><<<b.ngtile, 32, 0, s>>>(b, b.gtile, b.ngtile);
   }
 }
 

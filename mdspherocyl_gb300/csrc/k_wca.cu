@@ -40,8 +40,8 @@ __global__ void __launch_bounds__(kPartBlock) list_prep_kernel(Batch b, int forc
   const int2 bk = b.blk[blockIdx.x];
   const SysDev& P = b.sys[bk.x];
   SysState& S = b.st[bk.x];
-  bool need = force_all || S.force_list;
-  if (!need) {
+  bool need = (force_all || S.force_list) && !at_limit(b, bk.x);
+  if (!need && !at_limit(b, bk.x)) {
     double m = 0.0;
     for (int k = 0; k < P.nblk; ++k) m = fmax(m, b.dmax[P.blk_off + k]);
     need = 2.0 * m > P.skin;
@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(kPartBlock) wca_screen_kernel(Batch b) {
   const int2 bk = b.blk[blockIdx.x];
   const int s = bk.x;
   const SysDev& P = b.sys[s];
-  if (P.rc_real > 0.0) return;  // screened in the cutoff systems' neighbour pass (near_pass)
+  if (P.rc_real > 0.0 || at_limit(b, s)) return;  // cutoff systems: screened in their neighbour pass
   const int i = bk.y + threadIdx.x;
   const bool ok = i < P.part_off + P.n;
   const int nl = ok ? b.nbc[i] : 0;

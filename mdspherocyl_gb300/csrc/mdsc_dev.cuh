@@ -10,6 +10,11 @@
 namespace mdsc {
 
 constexpr int kTile = 64;        // real-space tile edge, in dipoles
+// real-space tiles with the table in shared memory: warps per block, the
+// largest table (entries) a block stages, tiles per block
+constexpr int kSmemWarps = 16;
+constexpr int kSmemTableMax = 10000;
+constexpr int kSmemChunk = 32;
 constexpr int kMaxNb = 64;       // Verlet-list capacity per particle
 constexpr int kMaxD = 4;         // dipoles per particle (MDSC_MAX_DIPOLES)
 constexpr int kPartBlock = 128;  // threads per block of the per-particle kernels
@@ -28,9 +33,11 @@ constexpr int kMaxE = 64;        // energy-criterion candidates (higher index) p
 constexpr int kMaxC = 16;        // WCA contact candidates of higher index per particle
 // cell-binned list builds: rods per cell slot range (a cell with more rods
 // sends its system to the all-pairs scan for that build); systems of fewer
-// rods than kCellMinRods always scan all pairs
+// rods than kCellMinRods always scan all pairs (the shared-memory all-pairs
+// scan of a 2048-rod system took half the time of its cell scan on GB300;
+// at 32,768 rods the cells are 8.7x faster)
 constexpr int kCellSlots = 64;
-constexpr int kCellMinRods = 256;
+constexpr int kCellMinRods = 4096;
 
 // status bits (OR-ed per system; mapped to mdsc_status on the host)
 enum : int {
@@ -120,6 +127,7 @@ struct SysState {
   int iter;          // step index within the current mdsc_step call (noise row)
   int force_list;    // rebuild the Verlet list at the next check regardless of the skin
   int cell_ovf;      // this build: a cell held more than kCellSlots rods (all-pairs scan instead)
+  long long stop;    // the step count at which the system stops taking steps (mdsc_set_step_limit)
   double K_first[2]; // kinetic energies after the first half kick
   double xi_mid[2];  // xi used by the second half kick
 };
@@ -191,6 +199,11 @@ struct Batch {
   int* rnbw;      // n: the Verlet-list partners after them (the tail)
   double* rlE;    // 10 per particle block: U, PT of the block's real-space neighbour pairs (rc_real systems)
   int4* tiles;   // (sys, I, J, 0)
+  int4* rpwork;  // (sys, first tile, tiles, 0): runs of the tiles whose system's table fits shared memory
+  int nrpwork;
+  int smem_tn;   // the largest of those tables (entries)
+  int* gtile;    // the other tiles (their table is read from global memory)
+  int ngtile;
   int2* wlist;   // WCA work list: (candidate slot, system), n * kMaxC at most
   int* wlist_n;  // its length this step
   double* wown;  // n * kMaxC * 6: the lower index's force and torque of each candidate
@@ -236,6 +249,7 @@ struct Batch {
   int2* cellblk; // per pair of cells of capacity: (system, first cell)
   int ncellblk;
   int cells;     // 1: systems with a cell grid build their lists on it; 0: every system scans all pairs
+  int honor_stop; // the step graph: kernels skip the systems at their step limit
   // neighbour list
   int* nb;       // n * kMaxNb
   int* nbc;      // n
@@ -261,6 +275,13 @@ struct CorrSys {
 };
 
 // ---- small helpers ----------------------------------------------------
+// A system at its step limit takes no step: every kernel of the step graph
+// returns at once for it (the check is uniform over a block or a warp of
+// that system), so it costs nothing until it leaves the batch.
+__device__ __forceinline__ bool at_limit(const Batch& b, int s) {
+  return b.honor_stop && b.st[s].step >= b.st[s].stop;
+}
+
 __host__ __device__ inline int cdiv(int a, int b) { return (a + b - 1) / b; }
 
 // fixed-point image of a coordinate: fraction of the box in [0, 2^32),

@@ -41,7 +41,7 @@ EXPORTS = [
     "mdsc_autotune", "mdsc_tuning", "mdsc_set_tuning", "mdsc_correlation_bins", "mdsc_correlations",
     "mdsc_order_params", "mdsc_step_trace", "mdsc_get_rng", "mdsc_set_rng", "mdsc_set_species",
     "mdsc_correlation_size", "mdsc_get_thermostat", "mdsc_render", "mdsc_lattice", "mdsc_thermalize",
-    "mdsc_fp32_peak", "mdsc_set_list_cells",
+    "mdsc_fp32_peak", "mdsc_set_list_cells", "mdsc_transfer_many", "mdsc_set_step_limit",
 ]
 
 
@@ -191,6 +191,8 @@ def load(build: bool = True) -> ctypes.CDLL:
         "mdsc_place_rods": (c_int, [c_int, _dp, _dp, _dp, ctypes.c_ulonglong, c_double, c_int, _dp, _dp]),
         "mdsc_fp32_peak": (c_int, [c_int, c_int, _dp, _dp, _dp, _ip]),
         "mdsc_set_list_cells": (c_int, [c_void_p, c_int]),
+        "mdsc_transfer_many": (c_int, [c_void_p, c_void_p, _ip, _ip, c_int]),
+        "mdsc_set_step_limit": (c_int, [c_void_p, c_int, c_longlong]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -494,6 +496,17 @@ class Batch:
         """Pin the launch mappings (mdsc_set_tuning) instead of tuning them."""
         v = np.array([rp_warps, rsum_threads, wca_blocks, kg_scalar], dtype=np.int32)
         self._check(self.lib.mdsc_set_tuning(self.h, v.ctypes.data_as(_ip)), "mdsc_set_tuning")
+
+    def transfer_many(self, src: "Batch", pairs) -> None:
+        """Slots (k, ks) of this batch from src, all at once (mdsc_transfer_many)."""
+        d = np.ascontiguousarray([p[0] for p in pairs], dtype=np.int32)
+        q = np.ascontiguousarray([p[1] for p in pairs], dtype=np.int32)
+        self._check(self.lib.mdsc_transfer_many(self.h, src.h, d.ctypes.data_as(_ip), q.ctypes.data_as(_ip), len(d)),
+                    "mdsc_transfer_many")
+
+    def set_step_limit(self, k: int, limit: int) -> None:
+        """System k stops taking steps at step count `limit` (<= 0: no limit)."""
+        self._check(self.lib.mdsc_set_step_limit(self.h, k, int(limit)), "mdsc_set_step_limit")
 
     def set_list_cells(self, on: bool) -> None:
         """List builds on cells (the default) or over all pairs; same lists."""

@@ -18,8 +18,8 @@ pytestmark = pytest.mark.gpu
 def _systems():
     rs = np.random.default_rng(41)
     out = []
-    for k, (n, nd, rc) in enumerate(((300, 1, 0.0), (1200, 1, 0.0), (90, 1, 0.0), (600, 2, 0.0),
-                                     (2048, 1, 3.5))):
+    for k, (n, nd, rc) in enumerate(((4200, 1, 0.0), (5000, 1, 0.0), (90, 1, 0.0), (4400, 2, 0.0),
+                                     (4096, 1, 3.5))):
         mu = np.full(n, float(rs.uniform(0.8, 1.8)))
         st, box = S.make_system(n=n, phi=float(rs.uniform(0.08, 0.22)), lengths=rs.uniform(2, 4, n), mu=mu,
                                 seed=500 + k, temp=1.1)
@@ -34,8 +34,8 @@ def _systems():
         if rc > 0:
             spec.alpha = 3.3 / rc
         out.append((spec, st))
-    # a dense cluster of 400 rods in a box 3x wider: its cells overflow
-    n = 400
+    # a dense cluster of 4096 rods in a box 3x wider: its cells overflow
+    n = 4096
     st, box = S.make_system(n=n, phi=0.25, lengths=np.full(n, 2.0), mu=np.full(n, 1.0), seed=590)
     big = box * 3.0
     spec = S.SystemSpec(n=n, box=big, alpha=6.0 / big[0], K_max=5, ksq_max=16)

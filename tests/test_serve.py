@@ -115,3 +115,28 @@ def test_cutoff_and_energy_cluster_jobs_as_alone():
         assert j.done == j.steps and j.error is None
         for f in ("r", "p", "O", "l", "F", "T", "clust"):
             assert np.array_equal(j.result[f], alone[j.jid][f]), (j.jid, f)
+
+
+def test_step_limits_stop_systems_exactly():
+    """mdsc_set_step_limit: in one batch stepped 20 steps, systems limited
+    to 5 and 12 steps stop there (their step counts, states and observables
+    those of 5 and 12 steps alone, bit for bit) while the third takes all 20;
+    the limited ones cost no steps afterwards."""
+    jobs = _jobs()[:3]
+    limits = (5, 12, 0)
+    alone = []
+    for j, lim in zip(jobs, limits):
+        with L.Batch([j.spec], [j.state]) as bt:
+            o = bt.step(lim or 20)[0]
+            alone.append((o, bt.download(0)))
+    with L.Batch([j.spec for j in jobs], [j.state for j in jobs]) as bt:
+        for k, lim in enumerate(limits):
+            bt.set_step_limit(k, lim)
+        obs = bt.step(20)
+        for k, lim in enumerate(limits):
+            assert obs[k]["step"] == (lim or 20)
+            d = bt.download(k)
+            for f in ("r", "p", "O", "l", "F", "T"):
+                assert np.array_equal(d[f], alone[k][1][f]), (k, f)
+            for key in ("U_dipR", "U_dipK", "U_ss", "K", "xi"):
+                assert np.array_equal(np.asarray(obs[k][key]), np.asarray(alone[k][0][key])), (k, key)
