@@ -2096,6 +2096,16 @@ mdsc_status mdsc_transfer_many(mdsc_batch* D, mdsc_batch* S, const int* dsys, co
   // the whole constant table once (the host copy stays alive with the batch)
   CU(cudaMemcpyAsync((void*)D->b.sys, D->lo.sys.data(), sizeof(SysDev) * D->nsys, cudaMemcpyHostToDevice, D->st));
   CU(launch_transfer(D->b, S->b, pairs, D->st));
+  // the source's stream waits for the copies, so destroying the source
+  // (which synchronizes its stream before freeing) cannot free what they read
+  {
+    cudaEvent_t copied = nullptr;
+    CU(cudaEventCreateWithFlags(&copied, cudaEventDisableTiming));
+    const cudaError_t e1 = cudaEventRecord(copied, D->st);
+    const cudaError_t e2 = e1 == cudaSuccess ? cudaStreamWaitEvent(S->st, copied, 0) : e1;
+    cudaEventDestroy(copied);
+    CU(e2);
+  }
   for (const int2& pr : pairs) {
     const int d = pr.x, q = pr.y;
     D->thermo_rng[2 * d] = S->thermo_rng[2 * q];
@@ -2109,9 +2119,6 @@ mdsc_status mdsc_transfer_many(mdsc_batch* D, mdsc_batch* S, const int* dsys, co
     D->built[d] = 0;
     D->have_forces[d] = S->have_forces[q];
   }
-  // the source may be destroyed once this returns: its reads are ordered
-  // before anything that follows on the destination's stream, and a
-  // destroy synchronizes the device first
   return MDSC_OK;
 }
 
