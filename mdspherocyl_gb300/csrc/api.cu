@@ -337,11 +337,12 @@ void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
     P.blk_off = blk;
     P.nblk = cdiv(d.n, kPartBlock);
     for (int k = 0; k < P.nblk; ++k) Lo.blk.push_back(make_int2(s, part + k * kPartBlock));
-    // the k-space gather of a large single-dipole system runs its k tiles in
-    // parts on separate blocks (a function of the system only, so the same
-    // bits alone and in any batch); smaller systems fill the GPU as they are
+    // the k-space gather of a single-dipole system runs its k tiles in parts
+    // on separate blocks (a function of the system only, so the same bits
+    // alone and in any batch): several times the blocks of one-part
+    // gathers, whose few warps per SM left the gather latency-bound
     const int ktiles = cdiv(P.nk, kKBlock);
-    P.kgs = (d.nd == 1 && d.n >= 4096 && ktiles > 1) ? std::min(8, ktiles) : 1;
+    P.kgs = (d.nd == 1 && ktiles > 1) ? std::min(8, ktiles) : 1;
     P.kgp_off = (int)Lo.kgsets;
     if (P.kgs > 1) Lo.kgsets += (long long)P.nblk * P.kgs;
     blk += P.nblk;
@@ -390,10 +391,14 @@ void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
   }
   // real-space tiles: systems whose table fits a block's shared memory in
   // runs of kSmemChunk tiles (the longest runs first), the others one by one
+  // (MDSC_SMEM_TABLE=0: every system reads its table from global memory, for
+  // timing the two forms against each other)
+  const char* smem_env = std::getenv("MDSC_SMEM_TABLE");
+  const bool smem_ok = !(smem_env && smem_env[0] == '0');
   for (int s = 0; s < nsys; ++s) {
     const SysDev& P = Lo.sys[s];
     if (P.ntile == 0) continue;
-    if (P.rt_n > 0 && P.rt_n <= kSmemTableMax) {
+    if (smem_ok && P.rt_n > 0 && P.rt_n <= kSmemTableMax) {
       for (int t = 0; t < P.ntile; t += kSmemChunk)
         Lo.rpwork.push_back(make_int4(s, P.tile_off + t, std::min(kSmemChunk, P.ntile - t), 0));
       Lo.smem_tn = std::max(Lo.smem_tn, P.rt_n);

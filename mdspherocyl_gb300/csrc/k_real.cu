@@ -566,7 +566,12 @@ __global__ void __launch_bounds__(32 * kSmemWarps, 1) real_pairs_smem_kernel(Bat
   const int tn = P.rt_n;
   float4* stab = dyn;
   const float4* g = b.rtab + 2 * (long long)P.rt_off;
-  for (int e = threadIdx.x; e <= tn; e += blockDim.x) stab[e] = __ldg(g + 2 * min(e, tn - 1));
+  // asynchronous 16-byte copies global -> shared, all in flight at once
+  for (int e = threadIdx.x; e <= tn; e += blockDim.x) {
+    const unsigned dst = (unsigned)__cvta_generic_to_shared(stab + e);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(g + 2 * min(e, tn - 1)) : "memory");
+  }
+  asm volatile("cp.async.wait_all;" ::: "memory");
   // per warp: 64 x (uint4 + float4 + float4) + 64 float2, after the table
   const int wid = threadIdx.x >> 5;
   float4* wbase = dyn + (tn + 1) + wid * (3 * kTile + kTile / 2);
