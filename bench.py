@@ -360,7 +360,7 @@ def run_reference(args):
     return 0
 
 
-def run_serving(args, device: int) -> dict:
+def run_serving(args, device: int, jobs_n: int, rate: float, seed_off: int = 0) -> dict:
     """Poisson stream of jobs (one system each) through the continuous-
     batching server; job configurations are generated before the clock
     starts (they are the clients' inputs)."""
@@ -369,21 +369,21 @@ def run_serving(args, device: int) -> dict:
     from mdspherocyl_gb300 import serve
     from mdspherocyl_gb300 import systems as S
 
-    arr = serve.poisson_arrivals(args.jobs, args.rate, seed=args.seed + 7)
+    arr = serve.poisson_arrivals(jobs_n, rate, seed=args.seed + 7 + seed_off)
     t0 = time.time()
+    ids = [seed_off * 100_000 + k for k in range(jobs_n)]
     with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
-        made = pool.map(S.serving_job, range(args.jobs), chunksize=1)
-    log(f"serving: {args.jobs} jobs generated in {time.time() - t0:.1f}s")
+        made = pool.map(S.serving_job, ids, chunksize=1)
+    log(f"serving: {jobs_n} jobs generated in {time.time() - t0:.1f}s")
     jobs = [serve.Job(k, spec, st, spec.steps, arrival=float(arr[k])) for k, (spec, st) in enumerate(made)]
     srv = serve.Server(hbm_budget_bytes=120e9, tick_steps=args.tick, device=device)
     t0 = time.perf_counter()
     stats = srv.run(jobs)
     wall = time.perf_counter() - t0
-    out = serve.summarize(stats, wall)
-    out.update({"rate_per_s": args.rate, "hbm_budget_bytes": 120e9, "tick_steps": args.tick,
+    out = serve.summarize(stats, wall, jobs)
+    out.update({"rate_per_s": rate, "hbm_budget_bytes": 120e9, "tick_steps": args.tick,
                 "jobs_spec": "N log-U[64,8192], steps U[500,5000], phi U[.05,.25], mu^2 U[.5,5], T U[.8,1.5], "
-                             "L ~ N(3, 0.3); alpha = 6/L_box, |n|^2 <= 36",
-                "note": f"{args.jobs} jobs of the 2000-job stream's distribution, same arrival rate"})
+                             "L ~ N(3, 0.3); alpha = 6/L_box, |n|^2 <= 36"})
     return out
 
 
@@ -558,9 +558,31 @@ def run_ours(args):
 
     list_build = {"cells_ms": rebuild_ms(True), "all_pairs_ms": rebuild_ms(False),
                   "how": "host clock around mdsc_neigh_list (every system rebuilt, then a synchronize), median of 5"}
+    bt.set_list_cells(True)
     launches = bt.launches_per_step + 1  # + the per-call reset of the noise row
+
+    # ---- the step graph's own cost: the same graph with every system held
+    # at its step limit, so every kernel returns at once (launch, fork/join
+    # and block-scheduling overhead per step) ----
+    cur = [o["step"] for o in bt.observe()]
+    for k in range(len(specs)):
+        bt.set_step_limit(k, cur[k])
+    bt.step(5)
+    ov = []
+    for _ in range(3):
+        bt.lib.mdsc_step(bt.h, 50, None)
+        ov.append(bt.lib.mdsc_last_device_ms(bt.h) / 50)
+    for k in range(len(specs)):
+        bt.set_step_limit(k, 0)
+    graph_overhead = {"us_per_step": 1e3 * statistics.median(ov), "launches_per_step": launches,
+                      "how": "device time of 50 graph launches with every system at its step limit, median of 3"}
     bt.close()
-    serving = run_serving(args, device) if (args.jobs > 0 and ws == 1 and not single) else None
+    serving = None
+    if args.jobs > 0 and ws == 1 and not single:
+        # the configured stream (2000 jobs at 40/s), then a rate the GPU sustains
+        serving = run_serving(args, device, args.jobs, args.rate)
+        if args.stable_jobs > 0:
+            serving["at_sustainable_rate"] = run_serving(args, device, args.stable_jobs, args.stable_rate, seed_off=1)
 
     out = None
     if rank == 0:
@@ -605,6 +627,7 @@ def run_ours(args):
                 "kernel_ms": rp_ms},
             "kernel_ms": prof,
             "list_build": list_build,
+            "graph_overhead": graph_overhead,
             "plain_gpu": plain,
             "serving": serving,
             "clustering": clustering,
@@ -643,8 +666,11 @@ def main():
     ap.add_argument("--no-parity", action="store_true", help="skip the parity block of the CPU leg")
     ap.add_argument("--no-parity-c2", action="store_true", help="parity block without the N=32768 evaluation")
     ap.add_argument("--plain-steps", type=int, default=3)
-    ap.add_argument("--jobs", type=int, default=200, help="serving leg: jobs (0 = skip)")
+    ap.add_argument("--jobs", type=int, default=2000, help="serving leg: jobs (0 = skip)")
     ap.add_argument("--rate", type=float, default=40.0, help="serving leg: arrivals per second")
+    ap.add_argument("--stable-jobs", type=int, default=400,
+                    help="serving leg: jobs of a second stream at a rate the GPU sustains (0 = skip)")
+    ap.add_argument("--stable-rate", type=float, default=10.0, help="arrivals per second of that stream")
     ap.add_argument("--tick", type=int, default=50, help="serving leg: steps between admissions")
     args = ap.parse_args()
     if args.impl == "reference":

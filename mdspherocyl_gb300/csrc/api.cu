@@ -389,12 +389,14 @@ void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
     Lo.maxnd = std::max(Lo.maxnd, d.nd);
     if (d.nd > 1) Lo.multi = true;
   }
-  // real-space tiles: systems whose table fits a block's shared memory in
-  // runs of kSmemChunk tiles (the longest runs first), the others one by one
-  // (MDSC_SMEM_TABLE=0: every system reads its table from global memory, for
-  // timing the two forms against each other)
+  // real-space tiles: one by one, each reading its system's table from
+  // global memory.  With MDSC_SMEM_TABLE=1, systems whose table fits a
+  // block's shared memory run in runs of kSmemChunk tiles (the longest runs
+  // first) on the shared-table form instead: 11% faster alone, but its
+  // whole-SM blocks wait for free SMs beside the step's other chains, and
+  // the step was 10% slower on the 256-replica mix (both stream priorities)
   const char* smem_env = std::getenv("MDSC_SMEM_TABLE");
-  const bool smem_ok = !(smem_env && smem_env[0] == '0');
+  const bool smem_ok = smem_env && smem_env[0] == '1';
   for (int s = 0; s < nsys; ++s) {
     const SysDev& P = Lo.sys[s];
     if (P.ntile == 0) continue;

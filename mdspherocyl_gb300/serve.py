@@ -296,4 +296,17 @@ def summarize(stats: ServerStats, wall_s: float, jobs: list[Job] | None = None) 
         tr = np.array(stats.trace, dtype=np.float64)
         out["queue"] = {"max_waiting": int(tr[:, 1].max()), "max_running": int(tr[:, 2].max()),
                         "mean_running_particles": float(tr[:, 3].mean())}
+        # ticks: the GPU's time and the host's, and what a repack added
+        out["tick"] = {"mean_device_ms": float(tr[:, 4].mean()), "mean_wall_ms": float(tr[:, 5].mean()),
+                       "mean_wall_ms_with_repack": float(tr[tr[:, 6] == 1, 5].mean()) if (tr[:, 6] == 1).any()
+                       else None,
+                       "mean_wall_ms_without": float(tr[tr[:, 6] == 0, 5].mean()) if (tr[:, 6] == 0).any() else None}
+        # the queue over time: (seconds, waiting, running, running particles)
+        # about every 5 s
+        pts, nxt = [], 0.0
+        for row in stats.trace:
+            if row[0] >= nxt:
+                pts.append([round(row[0], 2), int(row[1]), int(row[2]), int(row[3])])
+                nxt = row[0] + 5.0
+        out["queue_over_time"] = pts
     return out
