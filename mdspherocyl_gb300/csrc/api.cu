@@ -337,12 +337,14 @@ void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
     P.blk_off = blk;
     P.nblk = cdiv(d.n, kPartBlock);
     for (int k = 0; k < P.nblk; ++k) Lo.blk.push_back(make_int2(s, part + k * kPartBlock));
-    // the k-space gather of a single-dipole system runs its k tiles in parts
-    // on separate blocks (a function of the system only, so the same bits
-    // alone and in any batch): several times the blocks of one-part
-    // gathers, whose few warps per SM left the gather latency-bound
+    // the k-space gather of a large single-dipole system runs its k tiles in
+    // parts on separate blocks (a function of the system only, so the same
+    // bits alone and in any batch); smaller systems fill the GPU as they
+    // are (split for every single-dipole system, the 256-replica mix's
+    // gather went from 0.107 to 0.117 ms: the parts' partial sums and their
+    // combination cost more than the added blocks gained)
     const int ktiles = cdiv(P.nk, kKBlock);
-    P.kgs = (d.nd == 1 && ktiles > 1) ? std::min(8, ktiles) : 1;
+    P.kgs = (d.nd == 1 && d.n >= 4096 && ktiles > 1) ? std::min(8, ktiles) : 1;
     P.kgp_off = (int)Lo.kgsets;
     if (P.kgs > 1) Lo.kgsets += (long long)P.nblk * P.kgs;
     blk += P.nblk;
@@ -1430,18 +1432,27 @@ mdsc_status mdsc_upload_all(mdsc_batch* B, const mdsc_host_state* h) {
     CU(cudaStreamSynchronize(B->st));
     return MDSC_OK;
   }
-  // state only: one copy per array for the whole batch
+  // state only: one copy per array for the whole batch, the arrays spread
+  // over the batch's three streams so that several copy engines share the
+  // host link, joined back into the main stream
   const size_t n = B->lo.ntot;
   Batch& b = B->b;
-  CU(cudaMemcpyAsync(b.r, h->r, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->st));
-  CU(cudaMemcpyAsync(b.p, h->p, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->st));
-  CU(cudaMemcpyAsync(b.O, h->O, sizeof(double) * 9 * n, cudaMemcpyHostToDevice, B->st));
-  CU(cudaMemcpyAsync(b.l, h->l, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->st));
   const bool forces = h->F && h->T;
+  CU(cudaEventRecord(B->ev_fork, B->st));
+  CU(cudaStreamWaitEvent(B->s2, B->ev_fork, 0));
+  CU(cudaStreamWaitEvent(B->s3, B->ev_fork, 0));
+  CU(cudaMemcpyAsync(b.O, h->O, sizeof(double) * 9 * n, cudaMemcpyHostToDevice, B->st));
+  CU(cudaMemcpyAsync(b.r, h->r, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->s2));
+  CU(cudaMemcpyAsync(b.p, h->p, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->s2));
+  CU(cudaMemcpyAsync(b.l, h->l, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->s3));
   if (forces) {
-    CU(cudaMemcpyAsync(b.F, h->F, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->st));
-    CU(cudaMemcpyAsync(b.T, h->T, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->st));
+    CU(cudaMemcpyAsync(b.F, h->F, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->s2));
+    CU(cudaMemcpyAsync(b.T, h->T, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->s3));
   }
+  CU(cudaEventRecord(B->ev_j2, B->s2));
+  CU(cudaEventRecord(B->ev_j3, B->s3));
+  CU(cudaStreamWaitEvent(B->st, B->ev_j2, 0));
+  CU(cudaStreamWaitEvent(B->st, B->ev_j3, 0));
   for (int s = 0; s < B->nsys; ++s) B->have_forces[s] = forces ? 1 : 0;
   return MDSC_OK;
 }
@@ -1449,15 +1460,21 @@ mdsc_status mdsc_upload_all(mdsc_batch* B, const mdsc_host_state* h) {
 static mdsc_status download_range(mdsc_batch* B, int i0, int n, int s_first, int s_last,
                                   mdsc_host_state* h) {
   Batch& b = B->b;
-  auto dn = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
-    return (dst && bytes) ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, B->st) : cudaSuccess;
+  // after the main stream's work, the arrays spread over the three streams
+  CU(cudaEventRecord(B->ev_fork, B->st));
+  CU(cudaStreamWaitEvent(B->s2, B->ev_fork, 0));
+  CU(cudaStreamWaitEvent(B->s3, B->ev_fork, 0));
+  auto dn = [&](void* dst, const void* src, size_t bytes, cudaStream_t st) -> cudaError_t {
+    return (dst && bytes) ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st) : cudaSuccess;
   };
-  CU(dn(h->r, b.r + 3 * i0, sizeof(double) * 3 * n));
-  CU(dn(h->p, b.p + 3 * i0, sizeof(double) * 3 * n));
-  CU(dn(h->O, b.O + 9 * i0, sizeof(double) * 9 * n));
-  CU(dn(h->l, b.l + 3 * i0, sizeof(double) * 3 * n));
-  CU(dn(h->F, b.F + 3 * i0, sizeof(double) * 3 * n));
-  CU(dn(h->T, b.T + 3 * i0, sizeof(double) * 3 * n));
+  CU(dn(h->O, b.O + 9 * i0, sizeof(double) * 9 * n, B->st));
+  CU(dn(h->r, b.r + 3 * i0, sizeof(double) * 3 * n, B->s2));
+  CU(dn(h->p, b.p + 3 * i0, sizeof(double) * 3 * n, B->s2));
+  CU(dn(h->F, b.F + 3 * i0, sizeof(double) * 3 * n, B->s2));
+  CU(dn(h->l, b.l + 3 * i0, sizeof(double) * 3 * n, B->s3));
+  CU(dn(h->T, b.T + 3 * i0, sizeof(double) * 3 * n, B->s3));
+  CU(cudaStreamSynchronize(B->s2));
+  CU(cudaStreamSynchronize(B->s3));
   CU(cudaStreamSynchronize(B->st));
   if (h->clust) {
     int off = 0;
