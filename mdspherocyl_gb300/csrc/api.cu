@@ -83,8 +83,9 @@ struct Layout {
   std::vector<int2> kgwork;   // (particle block, part) of the k-space gather
   std::vector<int2> cellblk;  // (system, first cell) of every block of the cell-binned list build
   std::vector<int4> rpwork;   // runs of tiles whose table is staged in shared memory
-  std::vector<int> gtile;     // tiles read from the table in global memory
+  std::vector<int> gtile;     // tiles of the one-tile-per-warp kernel (analytic or global table)
   int smem_tn = 0;
+  bool rp_table = false;      // the tiles interpolate in the table (MDSC_REAL_FORM=table)
   int ncellcap = 0;           // cells of capacity over all systems
   long long kgsets = 0;       // partial sets of the split gathers
   int ntot = 0, ndtot = 0, nktot = 0, maxnd = 0, nchunks = 0, nstrips = 0;
@@ -219,7 +220,7 @@ void fill_tables(const mdsc_system_desc* descs, Layout& Lo) {
     std::lock_guard<std::mutex> g(g_tables.mu);
     std::map<std::tuple<uint64_t, uint64_t, int>, int> first;
     for (int s = 0; s < nsys; ++s) {
-      if (descs[s].nd <= 0) continue;
+      if (Lo.sys[s].rt_n <= 0) continue;
       const auto k = key_of(s);
       auto it = g_tables.m.find(k);
       if (it != g_tables.m.end()) {
@@ -260,7 +261,7 @@ void fill_tables(const mdsc_system_desc* descs, Layout& Lo) {
   // every system, in order, from the cache or a sibling with the same key
   std::lock_guard<std::mutex> g(g_tables.mu);
   for (int s = 0; s < nsys; ++s) {
-    if (descs[s].nd <= 0) continue;
+    if (Lo.sys[s].rt_n <= 0) continue;
     auto it = g_tables.m.find(key_of(s));
     if (it != g_tables.m.end()) {
       std::copy(it->second.first.begin(), it->second.first.end(), Lo.rtab.begin() + 2 * (size_t)Lo.sys[s].rt_off);
@@ -273,6 +274,8 @@ void fill_tables(const mdsc_system_desc* descs, Layout& Lo) {
 
 void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
   Lo.sys.resize(nsys);
+  const char* form_env = std::getenv("MDSC_REAL_FORM");
+  Lo.rp_table = form_env && std::strcmp(form_env, "table") == 0;
   int part = 0, dip = 0, blk = 0;
   long long pp = 0, kp = 0;
   for (int s = 0; s < nsys; ++s) {
@@ -377,11 +380,15 @@ void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
     P.sixthLh3 = (float)(kLh * kLh * kLh / 6.0);
     set_pair_consts(P);
     // the reference's interpolation table (tabul, v25/functions.cpp:1680-1704)
-    // over the distances this box can hold, in FP64 as tabul computes it,
-    // stored as FP32 values and differences to the next entry
+    // in FP64 as tabul computes it, stored as FP32 values and differences to
+    // the next entry: over the distances the box can hold for the neighbour
+    // pass of a system with a real-space cutoff and for tiles that read it
+    // (MDSC_REAL_FORM=table); up to r = kNearTab for the analytic tiles,
+    // which interpolate in it for near-contact pairs only
     if (d.nd > 0) {
       const double hd = 0.5 * std::sqrt(d.box[0] * d.box[0] + d.box[1] * d.box[1] + d.box[2] * d.box[2]);
-      const int n = std::min((int)std::floor(hd / kLh) + 3, 32767);
+      int n = std::min((int)std::floor(hd / kLh) + 3, 32767);
+      if (!Lo.rp_table && !(d.rc_real > 0)) n = std::min(n, (int)std::ceil(kNearTab / kLh) + 3);
       P.rt_off = (int)(Lo.rtab_n / 2);
       P.rt_n = n;
       Lo.rtab_n += 2 * (size_t)n;
@@ -391,14 +398,17 @@ void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
     Lo.maxnd = std::max(Lo.maxnd, d.nd);
     if (d.nd > 1) Lo.multi = true;
   }
-  // real-space tiles: one by one, each reading its system's table from
-  // global memory.  With MDSC_SMEM_TABLE=1, systems whose table fits a
+  // real-space tiles: one by one, each evaluating the analytic terms with
+  // the table's interpolation error added (no lookups: bound by the FP32
+  // pipe alone).  MDSC_REAL_FORM=table reads the system's table from
+  // global memory instead (one scattered 32-byte lookup per pair, bound by
+  // the L1).  With that and MDSC_SMEM_TABLE=1, systems whose table fits a
   // block's shared memory run in runs of kSmemChunk tiles (the longest runs
-  // first) on the shared-table form instead: 11% faster alone, but its
-  // whole-SM blocks wait for free SMs beside the step's other chains, and
-  // the step was 10% slower on the 256-replica mix (both stream priorities)
+  // first) on the shared-table form: 11% faster than the global table
+  // alone, but its whole-SM blocks wait for free SMs beside the step's
+  // other chains, and the step was 10% slower on the 256-replica mix
   const char* smem_env = std::getenv("MDSC_SMEM_TABLE");
-  const bool smem_ok = smem_env && smem_env[0] == '1';
+  const bool smem_ok = Lo.rp_table && smem_env && smem_env[0] == '1';
   for (int s = 0; s < nsys; ++s) {
     const SysDev& P = Lo.sys[s];
     if (P.ntile == 0) continue;
@@ -1151,6 +1161,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   b.nrpwork = (int)lo.rpwork.size();
   b.ngtile = (int)lo.gtile.size();
   b.smem_tn = lo.smem_tn;
+  b.rp_table = lo.rp_table ? 1 : 0;
   b.cells = 1;
   b.noise = B->noise[0];
   // The step graph forks the real-space tiles (stream s2) from the WCA and

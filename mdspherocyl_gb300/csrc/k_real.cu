@@ -30,22 +30,24 @@
 // (v25/functions.cpp:1563,1606-1614,1680-1697), which differs from the
 // analytic B(r), C(r) by up to ~5e-5 near contact.  Two forms reproduce it:
 //
-// TAB (the batch path): the same interpolation, in the system's own table.
+// TAB (the neighbour pass of cutoff systems, and the tiles with
+// MDSC_REAL_FORM=table): the same interpolation, in the system's own table.
 // The host builds it once per system with tabul's expressions in FP64 over
 // the distances the box can hold and stores each entry as FP32 A, B, C and
 // the differences to the next entry, 32 bytes, read with one 256-bit load
 // (one L1 wavefront per lane per lookup).  The lookups are scattered, so
-// the kernel leans on L2 as well as on the FP32 pipe.
+// the kernel leans on the L1 and L2 as well as on the FP32 pipe.
 //
-// Analytic (callers without a table, mdsc_force_dipR_noalloc): the kernel
-// evaluates the analytic terms and adds the table's own interpolation error to second
-// and third order, h2 f''(r) + h3 f'''(r) with a = r - r0, b = r1 - r,
-// h2 = ab/2, h3 = ab(b - a)/6, using the closed forms (A, B, C as the
+// Analytic (the tiles by default, and callers without a table such as
+// mdsc_force_dipR_noalloc): the kernel evaluates the analytic terms and
+// adds the table's own interpolation error to second order, h2 f''(r) with
+// a = r - r0, b = r1 - r, h2 = ab/2, using the closed forms (A, B, C as the
 // reference's table columns, s = 5B + C)
-//   A'' = 4B + C,                A''' = -4s/r - 2a^2 r C
-//   B'' = 6s/r^2 + 2a^2 C,       B''' = -42s/r^3 - 12a^2 C/r - 4a^4 r C
-//   C'' = 2a^2 C (2a^2 r^2 - 1), C''' = 4a^4 r C (3 - 2a^2 r^2)
-// which matches the table to ~2e-9 without reading it.
+//   A'' = 4B + C,   B'' = 6s/r^2 + 2a^2 C,   C'' = 2a^2 C (2a^2 r^2 - 1)
+// which matches the table to 2e-7 of each value at r = 0.8 and to 1e-8
+// beyond r = 3 (alpha <= 0.55) without reading it; what remains is the
+// third-order term h3 f'''(r), h3 = ab(b - a)/6.  The pair step is then
+// bound by the FP32 pipe alone.
 //
 // erfc(x) = exp(-x^2) t Q(t), t = 1/(1 + x/2), with Q a degree-9 polynomial
 // fitted to erfcx(x)/t by weighted least squares on Chebyshev nodes over
@@ -139,27 +141,35 @@ struct Lane2 {
   f2 mx, my, mz;                    // their moments (0 for a missing dipole)
   int own0, own1;
   bool ok0, ok1;
-  f2 F[3], T[3], pt[9], U, Uc;
+  // sums over the lane's pairs: force, the dipolar field of the partners
+  // (the torque is mi x field, taken once at the end), pressure tensor and
+  // energy (Kahan)
+  f2 F[3], E[3], pt[9], U, Uc;
 };
 
 // j-side results of one step for the two halves (half 0 pairs i-dipole
-// lane with j0, half 1 pairs lane + 32 with j1)
+// lane with j0, half 1 pairs lane + 32 with j1): the force on i (j gets
+// minus it) and the field of i at j
 struct JOut {
-  f2 fx, fy, fz, tx, ty, tz;
+  f2 fx, fy, fz, ex, ey, ez;
 };
 
 // one step of a tile loop: the lane's two i-dipoles against j0 (half 0)
 // and j1 (half 1) -- the same j in off-diagonal tiles.  Pairs masked off
-// (a0, a1 false) contribute exactly zero.
+// (a0, a1 false) contribute exactly zero: both moments are scaled by 0.
 template <bool MASKED, int MODE>
 __device__ __forceinline__ void tile_step(const PairConst& K, Lane2& s, const uint4 jp0, const float4 jm0,
                                           const uint4 jp1, const float4 jm1, bool a0, bool a1, JOut& o) {
   f2 mix = s.mx, miy = s.my, miz = s.mz;
+  f2 mjx = make_float2(jm0.x, jm1.x), mjy = make_float2(jm0.y, jm1.y), mjz = make_float2(jm0.z, jm1.z);
   if (MASKED) {
     const f2 on = make_float2(a0 ? 1.f : 0.f, a1 ? 1.f : 0.f);
     mix = mul2(mix, on);
     miy = mul2(miy, on);
     miz = mul2(miz, on);
+    mjx = mul2(mjx, on);
+    mjy = mul2(mjy, on);
+    mjz = mul2(mjz, on);
   }
   const f2 dx = fix_diff2(s.x0, s.x1, jp0.x, jp1.x, K.Lhx, K.Llx);
   const f2 dy = fix_diff2(s.y0, s.y1, jp0.y, jp1.y, K.Lhy, K.Lly);
@@ -172,7 +182,6 @@ __device__ __forceinline__ void tile_step(const PairConst& K, Lane2& s, const ui
   const f2 rinv = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
   const f2 r = mul2(r2, rinv);
   const f2 rinv2 = mul2(rinv, rinv);
-  const f2 rinv3 = mul2(rinv2, rinv);
 
   f2 Ac, Bc, Cc;
   if (MODE == kTabShared) {
@@ -222,30 +231,54 @@ __device__ __forceinline__ void tile_step(const PairConst& K, Lane2& s, const ui
     q = fma2(q, tt, b2(kQ0));
     const f2 E = mul2(mul2(ex, tt), q);
     const f2 G = mul2(ex, K.gpref);
-    const f2 Er3 = mul2(E, rinv3);
-    const f2 A = fma2(G, rinv2, Er3);
-    const f2 B = mul2(fma2(G, fma2(b2(3.f), rinv2, K.a2), mul2(b2(3.f), Er3)), rinv2);
+    // A = erfc/r^3 + G/r^2, B = (3 A + 2 alpha^2 G) / r^2, C = 4 alpha^4 G
+    const f2 A = mul2(fma2(E, rinv, G), rinv2);
+    const f2 B = mul2(fma2(b2(3.f), A, mul2(K.a2, G)), rinv2);
     const f2 C = mul2(G, K.a4x4);
 
-    // the table's interpolation error, second and third order
+    // the table's linear-interpolation error to second order, (ab/2) f''(r)
+    // with a = r - r0, b = r1 - r (the third-order term is below 3e-7 of
+    // each value at r >= 0.8 for alpha <= 0.55)
     const f2 uu = mul2(r, K.invLh);
     const f2 fr = sub2(uu, make_float2(floorf(uu.x), floorf(uu.y)));
-    const f2 ab = mul2(fr, fma2(fr, b2(-1.f), b2(1.f)));
-    const f2 h2 = mul2(ab, K.halfLh2);
-    const f2 nh3 = mul2(mul2(ab, K.nsixthLh3), fma2(fr, b2(-2.f), b2(1.f)));  // -h3
-    const f2 s5 = fma2(b2(5.f), B, C);
+    const f2 hh = mul2(fma2(neg2(fr), fr, fr), K.halfLh2);
     const f2 a2C = mul2(K.a2, C);
-    const f2 a2rC = mul2(a2C, r);
-    const f2 a2a2rC = mul2(K.a2, a2rC);
-    const f2 a2r2 = mul2(K.a2, r2);
-    Ac = fma2(h2, fma2(b2(4.f), B, C), fma2(nh3, fma2(mul2(b2(4.f), s5), rinv, a2rC), A));
-    Bc = fma2(h2, fma2(mul2(b2(6.f), s5), rinv2, a2C),
-                       fma2(nh3, fma2(mul2(b2(42.f), s5), rinv3, fma2(mul2(b2(6.f), a2C), rinv, a2a2rC)), B));
-    Cc = fma2(h2, mul2(a2C, add2(a2r2, b2(-1.f))), fma2(nh3, mul2(a2a2rC, add2(a2r2, b2(-3.f))), C));
+    Ac = fma2(hh, fma2(b2(4.f), B, C), A);
+    Bc = fma2(hh, fma2(mul2(b2(6.f), fma2(b2(5.f), B, C)), rinv2, a2C), B);
+    Cc = fma2(hh, mul2(a2C, fma2(K.a2, r2, b2(-1.f))), C);
+    // near contact (r < kNearTab) the pair terms are largest, and the
+    // rounding of the FP32 erfc chain (a few ulp, against one for a table
+    // entry) would dominate the error of energy sums that cancel between
+    // pairs: such pairs interpolate in the system's short table, as the
+    // reference does.  A warp takes the lookups only when one of its pairs
+    // is that close, and only those lanes load.
+    const bool nr0 = a0 && r.x < kNearTab, nr1 = a1 && r.y < kNearTab;
+    if (K.tab != nullptr && __any_sync(0xffffffffu, nr0 || nr1)) {
+      const f2 ut = fma2(r, K.ihh, mul2(r, K.ihl));
+      const float fl0 = floorf(ut.x), fl1 = floorf(ut.y);
+      const f2 ft = add2(fma2(r, K.ihh, make_float2(-fl0, -fl1)), mul2(r, K.ihl));
+      const int e0 = min(max((int)fl0 - 1, 0), K.tn - 1), e1 = min(max((int)fl1 - 1, 0), K.tn - 1);
+      if (nr0) {
+        float4 p0, q0;
+        ld_entry(K.tab + 2 * e0, p0, q0);
+        Ac.x = fmaf(ft.x, p0.w, p0.x);
+        Bc.x = fmaf(ft.x, q0.x, p0.y);
+        Cc.x = fmaf(ft.x, q0.y, p0.z);
+      }
+      if (nr1) {
+        float4 p1, q1;
+        ld_entry(K.tab + 2 * e1, p1, q1);
+        Ac.y = fmaf(ft.y, p1.w, p1.x);
+        Bc.y = fmaf(ft.y, q1.x, p1.y);
+        Cc.y = fmaf(ft.y, q1.y, p1.z);
+      }
+    }
   }
 
-  // dipole-dipole energy, force on i, torques without lever arm
-  const f2 mjx = make_float2(jm0.x, jm1.x), mjy = make_float2(jm0.y, jm1.y), mjz = make_float2(jm0.z, jm1.z);
+  // dipole-dipole energy, force on i, and the fields of the pair at each
+  // other: the torque on a dipole is its moment crossed with the field
+  // (v25/functions.cpp:1640-1661 without lever arms), so the fields are
+  // summed and crossed once per tile
   const f2 mimj = fma2(miz, mjz, fma2(miy, mjy, mul2(mix, mjx)));
   const f2 mir = fma2(miz, dz, fma2(miy, dy, mul2(mix, dx)));
   const f2 mjr = fma2(mjz, dz, fma2(mjy, dy, mul2(mjx, dx)));
@@ -257,28 +290,21 @@ __device__ __forceinline__ void tile_step(const PairConst& K, Lane2& s, const ui
   const f2 fx = fma2(fact, dx, fma2(mirB, mjx, mul2(mjrB, mix)));
   const f2 fy = fma2(fact, dy, fma2(mirB, mjy, mul2(mjrB, miy)));
   const f2 fz = fma2(fact, dz, fma2(mirB, mjz, mul2(mjrB, miz)));
-  const f2 wx = mul2(Ac, fma2(miy, mjz, mul2(neg2(miz), mjy)));
-  const f2 wy = mul2(Ac, fma2(miz, mjx, mul2(neg2(mix), mjz)));
-  const f2 wz = mul2(Ac, fma2(mix, mjy, mul2(neg2(miy), mjx)));
-  const f2 tix = fma2(mjrB, fma2(miy, dz, mul2(neg2(miz), dy)), neg2(wx));
-  const f2 tiy = fma2(mjrB, fma2(miz, dx, mul2(neg2(mix), dz)), neg2(wy));
-  const f2 tiz = fma2(mjrB, fma2(mix, dy, mul2(neg2(miy), dx)), neg2(wz));
-  const f2 tjx = fma2(mirB, fma2(mjy, dz, mul2(neg2(mjz), dy)), wx);
-  const f2 tjy = fma2(mirB, fma2(mjz, dx, mul2(neg2(mjx), dz)), wy);
-  const f2 tjz = fma2(mirB, fma2(mjx, dy, mul2(neg2(mjy), dx)), wz);
+  // field of j at i, (mj.r) B r - A mj, into the lane's sums; field of i at j
+  const f2 nA = neg2(Ac);
+  s.E[0] = fma2(nA, mjx, fma2(mjrB, dx, s.E[0]));
+  s.E[1] = fma2(nA, mjy, fma2(mjrB, dy, s.E[1]));
+  s.E[2] = fma2(nA, mjz, fma2(mjrB, dz, s.E[2]));
+  o.ex = fma2(mirB, dx, mul2(nA, mix));
+  o.ey = fma2(mirB, dy, mul2(nA, miy));
+  o.ez = fma2(mirB, dz, mul2(nA, miz));
 
   s.F[0] = add2(s.F[0], fx);
   s.F[1] = add2(s.F[1], fy);
   s.F[2] = add2(s.F[2], fz);
-  s.T[0] = add2(s.T[0], tix);
-  s.T[1] = add2(s.T[1], tiy);
-  s.T[2] = add2(s.T[2], tiz);
   o.fx = fx;
   o.fy = fy;
   o.fz = fz;
-  o.tx = tjx;
-  o.ty = tjy;
-  o.tz = tjz;
   // Kahan: U += u
   const f2 yk = sub2(u, s.Uc);
   const f2 tk = add2(s.U, yk);
@@ -323,9 +349,9 @@ __device__ __forceinline__ void tile_loop(const PairConst& K, Lane2& s, const ui
     ja4.x -= o.fx.x + o.fx.y;
     ja4.y -= o.fy.x + o.fy.y;
     ja4.z -= o.fz.x + o.fz.y;
-    ja4.w += o.tx.x + o.tx.y;
-    ja2.x += o.ty.x + o.ty.y;
-    ja2.y += o.tz.x + o.tz.y;
+    ja4.w += o.ex.x + o.ex.y;
+    ja2.x += o.ey.x + o.ey.y;
+    ja2.y += o.ez.x + o.ez.y;
     sa4[lj] = ja4;
     sa2[lj] = ja2;
     __syncwarp();
@@ -358,9 +384,9 @@ __device__ __forceinline__ void diag_loop(const PairConst& K, Lane2& s, const ui
     ja4.x -= o.fx.x;
     ja4.y -= o.fy.x;
     ja4.z -= o.fz.x;
-    ja4.w += o.tx.x;
-    ja2.x += o.ty.x;
-    ja2.y += o.tz.x;
+    ja4.w += o.ex.x;
+    ja2.x += o.ey.x;
+    ja2.y += o.ez.x;
     sa4[j0] = ja4;
     sa2[j0] = ja2;
     ja4 = sa4[j1];
@@ -368,9 +394,9 @@ __device__ __forceinline__ void diag_loop(const PairConst& K, Lane2& s, const ui
     ja4.x -= o.fx.y;
     ja4.y -= o.fy.y;
     ja4.z -= o.fz.y;
-    ja4.w += o.tx.y;
-    ja2.x += o.ty.y;
-    ja2.y += o.tz.y;
+    ja4.w += o.ex.y;
+    ja2.x += o.ey.y;
+    ja2.y += o.ez.y;
     sa4[j1] = ja4;
     sa2[j1] = ja2;
     __syncwarp();
@@ -397,7 +423,9 @@ __device__ __forceinline__ PairConst pair_consts(const Batch& b, const SysDev& P
   K.invLh = b2(P.invLh);
   K.ihh = b2(kInvLhHi);
   K.ihl = b2(kInvLhLo);
-  K.tab = mode == kTabGlobal ? b.rtab + 2 * (long long)P.rt_off : nullptr;
+  K.tab = (mode == kTabGlobal || mode == kAnalytic) && b.rtab != nullptr && P.rt_n > 0
+              ? b.rtab + 2 * (long long)P.rt_off
+              : nullptr;
   K.stab = stab;
   K.tn = P.rt_n;
   K.halfLh2 = b2(P.halfLh2);
@@ -448,7 +476,7 @@ __device__ __forceinline__ void tile_work(const Batch& b, int tile, const PairCo
     s.own0 = b.downer[g0];
     s.own1 = b.downer[g1];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) s.F[c] = s.T[c] = b2(0.f);
+    for (int c = 0; c < 3; ++c) s.F[c] = s.E[c] = b2(0.f);
 #pragma unroll
     for (int c = 0; c < 9; ++c) s.pt[c] = b2(0.f);
     s.U = s.Uc = b2(0.f);
@@ -472,11 +500,11 @@ __device__ __forceinline__ void tile_work(const Batch& b, int tile, const PairCo
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     const int li = lane + 32 * h;
-    float fv[3], tv[3];
+    float fv[3], ev[3], tv[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       fv[c] = h ? s.F[c].y : s.F[c].x;
-      tv[c] = h ? s.T[c].y : s.T[c].x;
+      ev[c] = h ? s.E[c].y : s.E[c].x;
     }
     if (diag) {
       const float4 a4 = sa4[li];
@@ -484,10 +512,15 @@ __device__ __forceinline__ void tile_work(const Batch& b, int tile, const PairCo
       fv[0] += a4.x;
       fv[1] += a4.y;
       fv[2] += a4.z;
-      tv[0] += a4.w;
-      tv[1] += a2.x;
-      tv[2] += a2.y;
+      ev[0] += a4.w;
+      ev[1] += a2.x;
+      ev[2] += a2.y;
     }
+    // torque without lever arm: moment x field
+    const float mx = h ? s.mx.y : s.mx.x, my = h ? s.my.y : s.my.x, mz = h ? s.mz.y : s.mz.x;
+    tv[0] = my * ev[2] - mz * ev[1];
+    tv[1] = mz * ev[0] - mx * ev[2];
+    tv[2] = mx * ev[1] - my * ev[0];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       base_ij[c * kTile + li] = fv[c];
@@ -498,12 +531,13 @@ __device__ __forceinline__ void tile_work(const Batch& b, int tile, const PairCo
     for (int k = lane; k < kTile; k += 32) {
       const float4 a4 = sa4[k];
       const float2 a2 = sa2[k];
+      const float4 mj = smj[k];
       base_ji[0 * kTile + k] = a4.x;
       base_ji[1 * kTile + k] = a4.y;
       base_ji[2 * kTile + k] = a4.z;
-      base_ji[3 * kTile + k] = a4.w;
-      base_ji[4 * kTile + k] = a2.x;
-      base_ji[5 * kTile + k] = a2.y;
+      base_ji[3 * kTile + k] = mj.y * a2.y - mj.z * a2.x;
+      base_ji[4 * kTile + k] = mj.z * a4.w - mj.x * a2.y;
+      base_ji[5 * kTile + k] = mj.x * a2.x - mj.y * a4.w;
     }
   }
   // tile energy and pressure tensor
@@ -523,22 +557,22 @@ __device__ __forceinline__ void tile_work(const Batch& b, int tile, const PairCo
 }
 
 // W warps per block, one tile per warp (tile = W * blockIdx.x + warp, or
-// the warp's entry of the list `gtile` of tiles that read the table from
-// global memory): the block size changes how tiles are grouped for
-// scheduling, never what a tile computes, so every W gives the same bits
-// (the autotuner picks W).  MODE kTabGlobal: interpolate in the reference's
-// table (systems whose table does not fit a block's shared memory);
-// kAnalytic: the analytic terms with the table's error added (callers
-// without the table).  20 warps per SM hold the kernel to 96 registers
-// (16 B of spills) from 126: the table lookups' latency is hidden by warps,
-// and 21 warps instead of 16 made the table form 3% faster on the
-// 256-replica mix.
+// the warp's entry of the list `gtile`): the block size changes how tiles
+// are grouped for scheduling, never what a tile computes, so every W gives
+// the same bits (the autotuner picks W).  MODE kAnalytic: the analytic
+// terms with the table's interpolation error added (the default);
+// kTabGlobal: interpolate in the reference's table in global memory.  20
+// warps per SM hold the kernel to 96 registers (no spills in the analytic
+// form, 12 B in the table form).  Measured on the 256-replica mix (CUDA
+// events, one box): analytic 0.436 ms per launch at 20 warps per SM, 0.446
+// at 16 (124 registers), 0.453 at 24 (80 registers, 120 B of spills); the
+// table form 0.485 ms.
 template <bool MULTI, int W, int MODE>
 __global__ void __launch_bounds__(32 * W, 20 / W) real_pairs_kernel(Batch b, const int* gtile, int ntile) {
   __shared__ uint4 sj_all[W][kTile];    // fixed-point x, y, z and owner of the j-dipoles
   __shared__ float4 smj_all[W][kTile];  // their moments
-  __shared__ float4 sa4_all[W][kTile];  // j-side sums: F x, y, z and T x
-  __shared__ float2 sa2_all[W][kTile];  // T y, z
+  __shared__ float4 sa4_all[W][kTile];  // j-side sums: force x, y, z and field x
+  __shared__ float2 sa2_all[W][kTile];  // field y, z
   const int wid = threadIdx.x >> 5;
   const int k = W * blockIdx.x + wid;
   if (k >= ntile) return;
@@ -689,7 +723,7 @@ __global__ void __launch_bounds__(kPartBlock * kCutLanes) near_pass_kernel(Batch
     s.own0 = s.own1 = ip;
     s.ok0 = s.ok1 = true;
 #pragma unroll
-    for (int c = 0; c < 3; ++c) s.F[c] = s.T[c] = b2(0.f);
+    for (int c = 0; c < 3; ++c) s.F[c] = s.E[c] = b2(0.f);
 #pragma unroll
     for (int c = 0; c < 9; ++c) s.pt[c] = b2(0.f);
     s.U = s.Uc = b2(0.f);
@@ -709,10 +743,17 @@ __global__ void __launch_bounds__(kPartBlock * kCutLanes) near_pass_kernel(Batch
     }
     // a lane's sums, then the group's (xor tree over the kCutLanes lanes)
     float v[17];
+    {
+      // both halves hold dipole i: its field, then the torque mi x field
+      float ev[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      v[c] = s.F[c].x + s.F[c].y;
-      v[3 + c] = s.T[c].x + s.T[c].y;
+      for (int c = 0; c < 3; ++c) {
+        v[c] = s.F[c].x + s.F[c].y;
+        ev[c] = s.E[c].x + s.E[c].y;
+      }
+      v[3] = s.my.x * ev[2] - s.mz.x * ev[1];
+      v[4] = s.mz.x * ev[0] - s.mx.x * ev[2];
+      v[5] = s.mx.x * ev[1] - s.my.x * ev[0];
     }
     v[6] = (s.U.x + (-s.Uc.x)) + (s.U.y + (-s.Uc.y));
 #pragma unroll
@@ -844,11 +885,26 @@ cudaError_t prepare_real_pairs() {
   return e;
 }
 
+// one tile per warp over `list` (all tiles when null), W warps per block
+template <int MODE>
+void launch_tiles(const Batch& b, bool multi, int W, const int* list, int n, cudaStream_t s) {
+  const int grid = cdiv(n, W);
+  if (W == 4) {
+    if (multi) real_pairs_kernel<true, 4, MODE><<<grid, 128, 0, s>>>(b, list, n);
+    else real_pairs_kernel<false, 4, MODE><<<grid, 128, 0, s>>>(b, list, n);
+  } else if (W == 2) {
+    if (multi) real_pairs_kernel<true, 2, MODE><<<grid, 64, 0, s>>>(b, list, n);
+    else real_pairs_kernel<false, 2, MODE><<<grid, 64, 0, s>>>(b, list, n);
+  } else {
+    if (multi) real_pairs_kernel<true, 1, MODE><<<n, 32, 0, s>>>(b, list, n);
+    else real_pairs_kernel<false, 1, MODE><<<n, 32, 0, s>>>(b, list, n);
+  }
+}
+
 void launch_real_pairs(const Batch& b, bool multi, cudaStream_t s) {
   if (b.ntiles == 0) return;
-  if (b.rtab == nullptr) {  // no table: the analytic form, one tile per block
-    if (multi) real_pairs_kernel<true, 1, kAnalytic><<<b.ntiles, 32, 0, s>>>(b, nullptr, b.ntiles);
-    else real_pairs_kernel<false, 1, kAnalytic><<<b.ntiles, 32, 0, s>>>(b, nullptr, b.ntiles);
+  if (b.rtab == nullptr) {  // no table (callers without one): the analytic form, one tile per block
+    launch_tiles<kAnalytic>(b, multi, 1, nullptr, b.ntiles, s);
     return;
   }
   if (b.nrpwork) {
@@ -857,18 +913,8 @@ void launch_real_pairs(const Batch& b, bool multi, cudaStream_t s) {
     else real_pairs_smem_kernel<false><<<b.nrpwork, 32 * kSmemWarps, bytes, s>>>(b);
   }
   if (b.ngtile == 0) return;
-  const int W = b.tune.rp_warps;
-  const int grid = cdiv(b.ngtile, W);
-  if (W == 4) {
-    if (multi) real_pairs_kernel<true, 4, kTabGlobal><<<grid, 128, 0, s>>>(b, b.gtile, b.ngtile);
-    else real_pairs_kernel<false, 4, kTabGlobal><<<grid, 128, 0, s>>>(b, b.gtile, b.ngtile);
-  } else if (W == 2) {
-    if (multi) real_pairs_kernel<true, 2, kTabGlobal><<<grid, 64, 0, s>>>(b, b.gtile, b.ngtile);
-    else real_pairs_kernel<false, 2, kTabGlobal><<<grid, 64, 0, s>>>(b, b.gtile, b.ngtile);
-  } else {
-    if (multi) real_pairs_kernel<true, 1, kTabGlobal><<<b.ngtile, 32, 0, s>>>(b, b.gtile, b.ngtile);
-    else real_pairs_kernel<false, 1, kTabGlobal><<<b.ngtile, 32, 0, s>>>(b, b.gtile, b.ngtile);
-  }
+  if (b.rp_table) launch_tiles<kTabGlobal>(b, multi, b.tune.rp_warps, b.gtile, b.ngtile, s);
+  else launch_tiles<kAnalytic>(b, multi, b.tune.rp_warps, b.gtile, b.ngtile, s);
 }
 
 }  // namespace mdsc

@@ -15,6 +15,9 @@ constexpr int kTile = 64;        // real-space tile edge, in dipoles
 constexpr int kSmemWarps = 16;
 constexpr int kSmemTableMax = 10000;
 constexpr int kSmemChunk = 32;
+// the analytic tiles interpolate in the reference's table below this
+// distance (a short table per system, up to r = kNearTab)
+constexpr float kNearTab = 2.0f;
 constexpr int kMaxNb = 64;       // Verlet-list capacity per particle
 constexpr int kMaxD = 4;         // dipoles per particle (MDSC_MAX_DIPOLES)
 constexpr int kPartBlock = 128;  // threads per block of the per-particle kernels
@@ -202,8 +205,9 @@ struct Batch {
   int4* rpwork;  // (sys, first tile, tiles, 0): runs of the tiles whose system's table fits shared memory
   int nrpwork;
   int smem_tn;   // the largest of those tables (entries)
-  int* gtile;    // the other tiles (their table is read from global memory)
+  int* gtile;    // the other tiles, one per warp
   int ngtile;
+  int rp_table;  // those tiles read the table from global memory (else the analytic form)
   int2* wlist;   // WCA work list: (candidate slot, system), n * kMaxC at most
   int* wlist_n;  // its length this step
   double* wown;  // n * kMaxC * 6: the lower index's force and torque of each candidate
