@@ -14,8 +14,13 @@ builds it while the GPU runs the tick: the allocation, the new jobs'
 uploads and step limits.  When the tick ends the running systems move into
 it on the GPU (mdsc_transfer_many, one kernel, no host round trip) and the
 next tick starts; the GPU waits only for those copies.  Admission is by an
-HBM budget: mdsc_estimate_bytes of the planned batch must fit it (during a
-repack the old and the new batch are both resident).
+HBM budget: the planned batch must fit it (during a repack the old and the
+new batch are both resident).  A batch's device bytes are a sum over its
+systems (every array is per system, per particle, per tile or per k), so the
+server sums each job's own mdsc_estimate_bytes, taken once when the job is
+first considered: never below the batch's estimate (each job's share carries
+its own alignment) and within 1% of it on the 256-replica mix, with no
+layout of the whole batch inside the tick loop.
 
 A job's result is independent of the jobs it shares the GPU with: every
 kernel works per system and sums in a fixed order, so a system gives the
@@ -51,6 +56,7 @@ class Job:
     result: dict | None = None
     obs: dict | None = None
     error: str | None = None  # the status of a system that failed (overlap, NaN, ...)
+    nbytes: int | None = None  # its device bytes alone (mdsc_estimate_bytes), once
 
     @property
     def n(self) -> int:
@@ -117,7 +123,10 @@ class Server:
     def _fits(self, jobs) -> bool:
         if len(jobs) > self.max_systems:
             return False
-        need = L.estimate_bytes([self._desc(j) for j in jobs])
+        for j in jobs:
+            if j.nbytes is None:
+                j.nbytes = L.estimate_bytes([self._desc(j)])
+        need = sum(j.nbytes for j in jobs)
         if any(getattr(j.spec, "cl_energy", 0.0) > 0 for j in jobs):
             need += 260 * sum(j.n for j in jobs)  # the energy criterion's candidate lists (mdsc_set_cluster_energy)
         return need <= self.budget
@@ -192,24 +201,24 @@ class Server:
         t_wall = self.clock()
         arr = (L.Observables * len(self.running))()
         code = self.batch.lib.mdsc_step(self.batch.h, self.tick, arr)
-        obs = [o.as_dict() for o in arr]
         dev_ms = self.batch.lib.mdsc_last_device_ms(self.batch.h)
         failed = []
         if code != 0:
             # a system's own error fails its job only; anything else is the server's
-            bad = [k for k, o in enumerate(obs) if o["status"] != 0]
+            bad = [k for k, o in enumerate(arr) if o.status != 0]
             if not bad:
                 if fut is not None:
                     fut.result().close()
                 raise L.MdscError(code, "mdsc_step", self.batch._err())
             for k in bad:
-                self.running[k].error = L.STATUS.get(obs[k]["status"], str(obs[k]["status"]))
+                self.running[k].error = L.STATUS.get(arr[k].status, str(arr[k].status))
                 failed.append(self.running[k])
         steps_taken = 0
-        for j, o in zip(self.running, obs):
-            steps_taken += (int(o["step"]) - j.done) * j.n
-            j.done = int(o["step"])
-            j.obs = o
+        for j, o in zip(self.running, arr):
+            steps_taken += (int(o.step) - j.done) * j.n
+            j.done = int(o.step)
+            if j.done >= j.steps or j.error:
+                j.obs = o.as_dict()  # a finished job's last observables
         self.stats.gpu_ms += dev_ms
         self.stats.ticks += 1
         self.stats.particle_steps += steps_taken

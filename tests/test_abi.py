@@ -52,6 +52,16 @@ def test_estimate_bytes_without_gpu():
     assert L.estimate_bytes([d, d]) > nb
 
 
+def test_estimate_bytes_sum_of_jobs_bounds_the_batch():
+    """The server admits against the sum of its jobs' own estimates: that sum
+    must never be below the batch's estimate, and close to it."""
+    jobs = [S.serving_job(k) for k in range(24)]
+    descs = [L.desc_from_spec(spec, 1) for spec, _ in jobs]
+    batch = L.estimate_bytes(descs)
+    singles = sum(L.estimate_bytes([d]) for d in descs)
+    assert batch <= singles <= 1.02 * batch
+
+
 def test_estimate_bytes_counts_the_cutoff_lists_and_gather_parts():
     """The HBM a batch needs (what the server admits against) includes the
     real-space neighbour lists of a cutoff system (256 ints per rod) and the
