@@ -453,7 +453,7 @@ struct Arena {
 
 // carves every buffer of a batch out of one allocation (or only sizes it)
 void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** kowner,
-           double** noise2) {
+           double** noise2, int** skip) {
   const size_t n = std::max(Lo.ntot, 1), nd = std::max(Lo.ndtot, 1), nk = std::max(Lo.nktot, 1);
   const size_t nt = std::max<size_t>(Lo.tiles.size(), 1), nb = std::max<size_t>(Lo.blk.size(), 1);
   b.sys = A.take<SysDev>(nsys);
@@ -545,6 +545,7 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   *kowner = A.take<int2>(nk);
   noise2[0] = A.take<double>((size_t)kNoiseChunk * nsys * 4);
   noise2[1] = A.take<double>((size_t)kNoiseChunk * nsys * 4);
+  *skip = A.take<int>(std::max(nsys, 1));
 }
 
 }  // namespace
@@ -561,6 +562,7 @@ struct mdsc_batch {
   int4* kwork = nullptr;
   int2* kowner = nullptr;
   double* noise[2] = {nullptr, nullptr};
+  int* d_skip = nullptr;      // per system: skipped by a force evaluation of the others
   double* h_noise = nullptr;  // pinned
   SysObs* h_obs = nullptr;    // pinned
   SysObs* h_trace = nullptr;  // pinned, kNoiseChunk x nsys: per-step observables of mdsc_step_trace
@@ -612,9 +614,11 @@ Batch batch_with_noise(const mdsc_batch* B, int which) {
   return b;
 }
 
-// every force term, F and T set from scratch, energies reduced
-mdsc_status eval_forces(mdsc_batch* B, int force_list) {
+// every force term, F and T set from scratch, energies reduced; with a
+// skip mask (device, per system) the flagged systems are left as they are
+mdsc_status eval_forces(mdsc_batch* B, int force_list, const int* skip = nullptr) {
   Batch b = batch_with_noise(B, 0);
+  b.skip = skip;
   launch_derive(b, B->st);
   launch_list_build(b, force_list, B->st);
   launch_wca(b, 1, B->st);  // with the cutoff systems' real space, in the same neighbour pass
@@ -902,10 +906,19 @@ mdsc_status read_obs(mdsc_batch* B, mdsc_observables* out) {
 mdsc_status ensure_forces(mdsc_batch* B) {
   for (int s = 0; s < B->nsys; ++s)
     if (!B->uploaded[s]) return fail(B, MDSC_ERR_STATE, "system " + std::to_string(s) + " has no state yet");
-  bool need = false;
-  for (int s = 0; s < B->nsys; ++s) need |= !B->have_forces[s];
-  if (!need) return MDSC_OK;
-  return eval_forces(B, 0);
+  int missing = 0;
+  for (int s = 0; s < B->nsys; ++s) missing += !B->have_forces[s];
+  if (missing == 0) return MDSC_OK;
+  if (missing == B->nsys) return eval_forces(B, 0);
+  // only the systems without forces (those a server just added beside
+  // systems moved in with theirs): every kernel returns at once for the
+  // others, which keep their forces, lists and bits
+  std::vector<int> skip(B->nsys);
+  for (int s = 0; s < B->nsys; ++s) skip[s] = B->have_forces[s] ? 1 : 0;
+  CU(cudaMemcpyAsync(B->d_skip, skip.data(), sizeof(int) * B->nsys, cudaMemcpyHostToDevice, B->st));
+  const mdsc_status st = eval_forces(B, 0, B->d_skip);
+  CU(cudaStreamSynchronize(B->st));  // the host flags are read by the copy
+  return st;
 }
 
 // host-side derived per-particle data of system s from its shape arrays
@@ -1101,7 +1114,8 @@ size_t mdsc_estimate_bytes(const mdsc_system_desc* descs, int nsys) {
   int4* kw;
   int2* ko;
   double* nz[2];
-  carve(A, lo, nsys, b, &kw, &ko, nz);
+  int* sk;
+  carve(A, lo, nsys, b, &kw, &ko, nz, &sk);
   return A.off;
 }
 
@@ -1136,7 +1150,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   fill_tables(descs, B->lo);
   const Layout& lo = B->lo;
   Arena A;
-  carve(A, lo, nsys, B->b, &B->kwork, &B->kowner, B->noise);
+  carve(A, lo, nsys, B->b, &B->kwork, &B->kowner, B->noise, &B->d_skip);
   B->arena_bytes = A.off;
   B->b.tune.wca_blocks = 8 * B->num_sms;
   cudaError_t e = cudaMalloc(&B->arena, B->arena_bytes);
@@ -1146,7 +1160,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   }
   A.off = 0;
   A.base = B->arena;
-  carve(A, lo, nsys, B->b, &B->kwork, &B->kowner, B->noise);
+  carve(A, lo, nsys, B->b, &B->kwork, &B->kowner, B->noise, &B->d_skip);
   Batch& b = B->b;
   b.nsys = nsys;
   b.ntot = lo.ntot;

@@ -254,6 +254,8 @@ struct Batch {
   int ncellblk;
   int cells;     // 1: systems with a cell grid build their lists on it; 0: every system scans all pairs
   int honor_stop; // the step graph: kernels skip the systems at their step limit
+  const int* skip; // per system, or null: kernels skip the flagged systems (a force evaluation
+                   // for the systems that joined a batch, beside systems that arrived with forces)
   // neighbour list
   int* nb;       // n * kMaxNb
   int* nbc;      // n
@@ -283,7 +285,7 @@ struct CorrSys {
 // returns at once for it (the check is uniform over a block or a warp of
 // that system), so it costs nothing until it leaves the batch.
 __device__ __forceinline__ bool at_limit(const Batch& b, int s) {
-  return b.honor_stop && b.st[s].step >= b.st[s].stop;
+  return (b.honor_stop && b.st[s].step >= b.st[s].stop) || (b.skip && b.skip[s]);
 }
 
 __host__ __device__ inline int cdiv(int a, int b) { return (a + b - 1) / b; }
