@@ -443,6 +443,10 @@ def run_ours(args):
     (ntot_all,), (t_dev,) = aggregate_ranks([ntot], [t_dev], device=f"cuda:{device}")
     value = ntot_all * args.steps / t_dev
     obs = bt.observe()
+    # kernels per graph-launched step, as captured for the timed steps (a
+    # later mdsc_set_list_cells drops the graphs and the count with them),
+    # + the per-call reset of the noise row
+    launches = bt.launches_per_step + 1
     st_ok = all(o["status"] == 0 for o in obs)
     clustering = None
     if single and specs[0].cl_fr > 0:
@@ -559,7 +563,6 @@ def run_ours(args):
     list_build = {"cells_ms": rebuild_ms(True), "all_pairs_ms": rebuild_ms(False),
                   "how": "host clock around mdsc_neigh_list (every system rebuilt, then a synchronize), median of 5"}
     bt.set_list_cells(True)
-    launches = bt.launches_per_step + 1  # + the per-call reset of the noise row
 
     # ---- the step graph's own cost: the same graph with every system held
     # at its step limit, so every kernel returns at once (launch, fork/join
