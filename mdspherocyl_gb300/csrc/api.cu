@@ -491,7 +491,6 @@ void carve(Arena& A, const Layout& Lo, int nsys, Batch& b, int4** kwork, int2** 
   b.kgdone = A.take<int>(nb);
   b.rnb = A.take<int>(Lo.any_rc ? n * kMaxR : 1);
   b.rnbc = A.take<int>(n);
-  b.rnbw = A.take<int>(n);
   b.rlE = A.take<double>(10 * nb);
   b.tiles = A.take<int4>(nt);
   b.rpwork = A.take<int4>(std::max<size_t>(Lo.rpwork.size(), 1));
@@ -1237,7 +1236,6 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
   cudaMemsetAsync(b.wincnt, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.stripE, 0, sizeof(double) * 10 * std::max(lo.nstrips, 1), B->st);
   cudaMemsetAsync(b.rnbc, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
-  cudaMemsetAsync(b.rnbw, 0, sizeof(int) * std::max(lo.ntot, 1), B->st);
   cudaMemsetAsync(b.ccnt, 0, sizeof(int) * std::max(lo.ncellcap, 1), B->st);
   cudaMemsetAsync(b.kgdone, 0, sizeof(int) * std::max<size_t>(lo.blk.size(), 1), B->st);
   cudaMemsetAsync(b.rlE, 0, sizeof(double) * 10 * std::max<size_t>(lo.blk.size(), 1), B->st);

@@ -619,15 +619,14 @@ __global__ void __launch_bounds__(32 * kSmemWarps, 1) real_pairs_smem_kernel(Bat
     tile_work<MULTI, kTabShared>(b, t, K, sj, smj, sa4, sa2);
 }
 
-// The neighbour pass of the systems with a real-space cutoff: the
-// real-space sum and the WCA screen over one list per rod (list_build's
-// union list: the real-space partners at its head, the Verlet list's other
-// partners after them).
+// The neighbour pass of the systems with a real-space cutoff, over the two
+// lists one scan of list_build wrote for each rod.
 //
 // Real space (mode kNearReal): the reference's force_dipR with its table
-// zeroed beyond rc_real, where pairs beyond rc_real + Lh add nothing, so
-// only the head of the list is visited -- the rods whose centres are within
-// rc_real + Lh + the dipoles' offsets + the skin.  A group of kCutLanes
+// zeroed beyond rc_real, where pairs
+// beyond rc_real + Lh add nothing, so only the rods on the system's
+// real-space list are visited -- those whose centres are within rc_real +
+// Lh + the dipoles' offsets + the skin (list_build).  A group of kCutLanes
 // lanes per dipole i takes its partner dipoles -- the listed rods' dipoles,
 // rods in ascending order -- two at a time through the tiles' pair step
 // (both halves holding dipole i), lane j the pair steps j, j + kCutLanes,
@@ -638,42 +637,26 @@ __global__ void __launch_bounds__(32 * kSmemWarps, 1) real_pairs_smem_kernel(Bat
 // real_sum writes them, and its block's energy and pressure tensor
 // (float-float block sums) for the per-system sum.
 //
-// WCA screen (mode kNearWca): the first kPartBlock threads, a particle
-// each, merge the list's Verlet-list partners (flagged head entries, then
-// the tail: two ascending runs) into ascending order and screen them as the
-// WCA screen kernel screens its Verlet list (wca_screen.cuh); the FP64
-// evaluation follows in wca_eval.
+// WCA screen (mode kNearWca): in the same blocks, the first kPartBlock
+// threads, a particle each, screen its Verlet list as the WCA screen kernel
+// does for the other systems (wca_screen.cuh), feeding the same FP64
+// evaluation.
 constexpr int kCutLanes = 4;
 enum : int { kNearReal = 1, kNearWca = 2 };
-
-__device__ __forceinline__ void near_wca_screen(const Batch& b, const int2 bk, const SysDev& P) {
-  if (threadIdx.x >= kPartBlock) return;  // whole warps
-  const int i = bk.y + threadIdx.x;
-  const bool ok = i < P.part_off + P.n;
-  const int* r = b.rnb + (long long)(ok ? i : bk.y) * kMaxR;
-  const int na = ok ? b.rnbc[i] : 0;
-  const int tend = ok ? na + b.rnbw[i] : 0;
-  int a = 0, t = na;
-  wca_screen_one(b, P, bk.x, i, ok, [&]() -> int {
-    while (a < na && !(r[a] & kRnbWca)) ++a;
-    const int qa = a < na ? (r[a] & kRnbIdx) : 0x7fffffff;
-    const int qt = t < tend ? r[t] : 0x7fffffff;
-    if (qa == 0x7fffffff && qt == 0x7fffffff) return -1;
-    if (qa < qt) {
-      ++a;
-      return qa;
-    }
-    ++t;
-    return qt;
-  });
-}
 
 __global__ void __launch_bounds__(kPartBlock * kCutLanes) near_pass_kernel(Batch b, int mode) {
   __shared__ double sh[10 * kPartBlock * kCutLanes / 32];
   const int2 bk = b.blk[blockIdx.x];
   const SysDev& P = b.sys[bk.x];
   if (P.rc_real <= 0.0 || at_limit(b, bk.x)) return;  // the same for the whole block
-  if (mode & kNearWca) near_wca_screen(b, bk, P);
+  if ((mode & kNearWca) && threadIdx.x < kPartBlock) {  // whole warps
+    const int i = bk.y + threadIdx.x;
+    const bool ok = i < P.part_off + P.n;
+    const int nl = ok ? b.nbc[i] : 0;
+    const int* lst = b.nb + (long long)(ok ? i : bk.y) * kMaxNb;
+    int k = 0;
+    wca_screen_one(b, P, bk.x, i, ok, [&]() { return k < nl ? lst[k++] : -1; });
+  }
   if (!(mode & kNearReal)) return;
   const int nd = P.nd;
   const int p0 = bk.y - P.part_off;
@@ -732,8 +715,8 @@ __global__ void __launch_bounds__(kPartBlock * kCutLanes) near_pass_kernel(Batch
     for (int k = 2 * lane; k < nj; k += 2 * kCutLanes) {
       const bool two = k + 1 < nj;
       const int k1 = two ? k + 1 : k;
-      const int ga = P.dip_off + ((lst[k / nd] & kRnbIdx) - P.part_off) * nd + k % nd;
-      const int gb = P.dip_off + ((lst[k1 / nd] & kRnbIdx) - P.part_off) * nd + k1 % nd;
+      const int ga = P.dip_off + (lst[k / nd] - P.part_off) * nd + k % nd;
+      const int gb = P.dip_off + (lst[k1 / nd] - P.part_off) * nd + k1 % nd;
       const uint4 jpa = make_uint4(b.dfx[ga], b.dfx[ND + ga], b.dfx[2 * ND + ga], 0u);
       const uint4 jpb = make_uint4(b.dfx[gb], b.dfx[ND + gb], b.dfx[2 * ND + gb], 0u);
       const float4 jma = make_float4(b.dm[ga], b.dm[ND + ga], b.dm[2 * ND + ga], 0.f);

@@ -97,29 +97,6 @@ __device__ __forceinline__ void sort_small(A& v, int n) {
   }
 }
 
-// A cutoff system's neighbour-pass list: the real-space partners (centres
-// within the real-space radius, ascending) stay at the head, those also on
-// the Verlet list flagged kRnbWca; the Verlet list's other partners follow,
-// ascending.  One list then serves both the real-space sum and the WCA
-// screen of the neighbour pass.
-__device__ void rnb_merge(const Batch& b, int i, int cnt, int rcnt, int& err) {
-  const int* w = b.nb + (long long)i * kMaxNb;
-  int* r = b.rnb + (long long)i * kMaxR;
-  int a = 0, tail = rcnt;
-  for (int k = 0; k < cnt; ++k) {
-    const int q = w[k];
-    while (a < rcnt && (r[a] & kRnbIdx) < q) ++a;
-    if (a < rcnt && (r[a] & kRnbIdx) == q) {
-      r[a] |= kRnbWca;
-    } else {
-      if (tail < kMaxR) r[tail] = q;
-      ++tail;
-    }
-  }
-  if (tail > kMaxR) err |= kErrListOverflow;
-  b.rnbw[i] = min(tail, kMaxR) - rcnt;
-}
-
 // The cell scan: blocks of two cells (two warps each), a thread per slot.
 __device__ void list_cells(const Batch& b) {
   const int2 cb = b.cellblk[blockIdx.x - b.nblk];
@@ -190,7 +167,6 @@ __device__ void list_cells(const Batch& b) {
     rcnt = min(rcnt, kMaxR);
     sort_small(rout, rcnt);
     b.rnbc[i] = rcnt;
-    rnb_merge(b, i, cnt, rcnt, err);
   }
   if (err) atomicOr(&S.status, err);
   const int N = b.ntot;
@@ -304,7 +280,6 @@ __global__ void __launch_bounds__(kPartBlock) list_build_kernel(Batch b) {
   b.nbc[i] = min(cnt, kMaxNb);
   if (rcut) {
     b.rnbc[i] = min(rcnt, kMaxR);
-    rnb_merge(b, i, min(cnt, kMaxNb), min(rcnt, kMaxR), err);
   }
   if (err) atomicOr(&S.status, err);
 #pragma unroll
@@ -704,8 +679,9 @@ void launch_wca(const Batch& b, int near_mode, cudaStream_t s) {
   if (!b.nblk) return;
   cudaMemsetAsync(b.wlist_n, 0, sizeof(int), s);
   cudaMemsetAsync(b.wincnt, 0, sizeof(int) * b.ntot, s);
-  // cutoff systems: the WCA screen over their neighbour-pass list (with
-  // their real space when near_mode says so); the others: over the Verlet list
+  // cutoff systems: the WCA screen over their Verlet list in their
+  // neighbour pass (with their real space when near_mode says so); the
+  // others: in the screen kernel
   launch_near_pass(b, 2 | near_mode, s);
   wca_screen_kernel<<<b.nblk, kPartBlock, 0, s>>>(b);
   // a fixed grid (chosen by the autotuner); each thread loops over the list

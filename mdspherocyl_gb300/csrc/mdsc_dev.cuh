@@ -27,11 +27,6 @@ constexpr int kKChunk = 256;     // particles per block of the structure-factor 
 // strip first (real_sum); smaller ones are summed tile by tile
 constexpr int kStripRows = 32;
 constexpr int kMaxR = 256;       // neighbour-pass list entries per rod (systems with a real-space cutoff)
-// entries of the neighbour-pass list: the real-space partners first
-// (ascending; kRnbWca marks those also on the Verlet list), then the Verlet
-// list's other partners (ascending)
-constexpr int kRnbWca = 1 << 30;
-constexpr int kRnbIdx = kRnbWca - 1;
 constexpr int kMaxE = 64;        // energy-criterion candidates (higher index) per rod
 constexpr int kMaxC = 16;        // WCA contact candidates of higher index per particle
 // cell-binned list builds: rods per cell slot range (a cell with more rods
@@ -198,8 +193,7 @@ struct Batch {
   int nbstrips;
   int any_rc;     // some system has a real-space cutoff
   int* rnb;       // n * kMaxR: real-space neighbour rods (both directions, ascending) of rc_real systems
-  int* rnbc;      // n: the real-space partners among them (the head of the list)
-  int* rnbw;      // n: the Verlet-list partners after them (the tail)
+  int* rnbc;      // n: their number
   double* rlE;    // 10 per particle block: U, PT of the block's real-space neighbour pairs (rc_real systems)
   int4* tiles;   // (sys, I, J, 0)
   int4* rpwork;  // (sys, first tile, tiles, 0): runs of the tiles whose system's table fits shared memory

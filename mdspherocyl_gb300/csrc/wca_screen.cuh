@@ -1,6 +1,6 @@
-// The FP32 screen of force_sc's pairs (v25/functions.cpp:1397-1553), shared
-// by the WCA screen kernel (partners from the Verlet list) and by the
-// cutoff systems' neighbour pass (partners from its union list).
+// The FP32 screen of force_sc's pairs (v25/functions.cpp:1397-1553),
+// partners from the Verlet list: in the WCA screen kernel, and in the
+// neighbour pass of the systems with a real-space cutoff.
 //
 // Each thread screens its particle i against the partners q > i the
 // iterator yields in ascending order: FP32 segment distance against
