@@ -523,12 +523,9 @@ def run_ours(args):
     bytes_obs = ctypes.sizeof(obs_buf)
 
     def e2e_step(state_back: bool):
-        bt.upload_all(h["r"], h["p"], h["O"], h["l"], h["F"], h["T"])
-        code = bt.lib.mdsc_step(bt.h, 1, obs_buf)  # ends with the observables in host memory
-        if code != 0:
-            raise L.MdscError(code, "mdsc_step", bt._err())
-        if state_back:
-            bt.download_all(h["r"], h["p"], h["O"], h["l"], h["F"], h["T"])
+        # mdsc_step_io: the state up, one step, the observables and (state_back)
+        # the updated state down into the same host arrays
+        bt.step_io(h, 1, h if state_back else None, obs_buf)
 
     def e2e_rate(state_back: bool):
         for _ in range(2):
@@ -614,8 +611,9 @@ def run_ours(args):
                        "graph": "one CUDA graph per step", "launch_mappings": tuning},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": bytes_state,
                     "d2h_bytes_per_step": bytes_state + bytes_obs,
-                    "how": "C ABI, pinned host buffers: the whole state up, one step, observables and the whole "
-                           "updated state (r, p, O, l, F, T) down, every step",
+                    "how": "C ABI (mdsc_step_io), pinned host buffers: the whole state up, one step, observables "
+                           "and the whole updated state (r, p, O, l, F, T) down, every step; r and O travel while "
+                           "the step's forces are computed",
                     "observables_only": {"value": e2e_obs_only, "d2h_bytes_per_step": bytes_obs}},
             "gpu_launches": launches * args.steps,
             "roofline": None if cutoff else {

@@ -247,6 +247,18 @@ mdsc_status mdsc_set_step_limit(mdsc_batch* b, int sys, long long limit);
    Thermostat noise is drawn on the host from each system's MT19937 pair
    exactly as moveTher does (v25/functions.cpp:2193-2213). */
 mdsc_status mdsc_step(mdsc_batch* b, int nsteps, mdsc_observables* obs);
+/* A step loop that keeps its state in host memory (the reference's driver
+   around its per-function boundary, v25/main.cpp:558-708, with part and
+   its Dynvecs on the host): uploads `in` (r, p, O, l and F, T of every
+   system, as mdsc_upload_all; NULL keeps the device state), takes nsteps
+   steps as mdsc_step, and downloads the updated state into `out` (as
+   mdsc_download_all; NULL fields are skipped, NULL out downloads nothing).
+   Positions and orientations are final once the last step has moved the
+   particles, so they travel to the host while that step's forces are
+   computed; momenta, angular momenta, forces and torques follow the step.
+   Observables of the last step go to obs (may be NULL). */
+mdsc_status mdsc_step_io(mdsc_batch* b, const mdsc_host_state* in, int nsteps, mdsc_host_state* out,
+                         mdsc_observables* obs);
 /* Observables of the last step without stepping. */
 mdsc_status mdsc_observe(mdsc_batch* b, mdsc_observables* obs);
 /* mdsc_step that also returns every step's observables: trace holds

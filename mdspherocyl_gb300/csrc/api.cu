@@ -555,6 +555,11 @@ struct mdsc_batch {
   int nsys = 0;
   cudaStream_t st = nullptr, s2 = nullptr, s3 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_j2 = nullptr, ev_j3 = nullptr;
+  // mdsc_step_io: the stream that takes positions and orientations home
+  // while a step's forces are computed, and the event its graph records
+  // once they are final
+  cudaStream_t sio = nullptr;
+  cudaEvent_t ev_x = nullptr;
   std::vector<mdsc_system_desc> desc;
   Layout lo;
   Batch b{};
@@ -576,6 +581,7 @@ struct mdsc_batch {
   std::vector<char> uploaded, built, have_forces;
   std::vector<std::vector<int>> species;  // per system: particles per species (contiguous blocks)
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  cudaGraphExec_t graph_io[2] = {nullptr, nullptr};  // the same step, with ev_x after the first half-step
   cudaEvent_t t_beg = nullptr, t_end = nullptr;  // device time of the last mdsc_step
   double last_ms = 0.0;
   int launches = 0;
@@ -738,7 +744,10 @@ mdsc_status autotune(mdsc_batch* B, int force, int reps) {
   return MDSC_OK;
 }
 
-mdsc_status capture_step(mdsc_batch* B, int which) {
+// io: the variant for mdsc_step_io, which also records ev_x (an event
+// outside the graph) once the first half-step has moved every particle:
+// positions and orientations are final from there on
+mdsc_status capture_step(mdsc_batch* B, int which, bool io = false) {
   Batch b = batch_with_noise(B, which);
   b.honor_stop = 1;  // systems at their step limit take no step
   cudaGraph_t g = nullptr;
@@ -746,6 +755,7 @@ mdsc_status capture_step(mdsc_batch* B, int which) {
   int launches = 0;
   launch_integrate_first(b, B->st);
   ++launches;
+  if (io) cudaEventRecordWithFlags(B->ev_x, B->st, cudaEventRecordExternal);
   cudaEventRecord(B->ev_fork, B->st);
   cudaStreamWaitEvent(B->s2, B->ev_fork, 0);
   cudaStreamWaitEvent(B->s3, B->ev_fork, 0);
@@ -769,11 +779,21 @@ mdsc_status capture_step(mdsc_batch* B, int which) {
   launches += 2;
   cudaError_t e = cudaStreamEndCapture(B->st, &g);
   if (e != cudaSuccess) return fail(B, MDSC_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-  e = cudaGraphInstantiate(&B->graph[which], g, cudaGraphInstantiateFlagUseNodePriority);
+  e = cudaGraphInstantiate(io ? &B->graph_io[which] : &B->graph[which], g, cudaGraphInstantiateFlagUseNodePriority);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return fail(B, MDSC_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-  B->launches = launches;
+  if (!io) B->launches = launches;
   return MDSC_OK;
+}
+
+// every step graph, to be captured again (new launch mappings or list mode)
+void drop_graphs(mdsc_batch* B) {
+  for (cudaGraphExec_t* set : {B->graph, B->graph_io})
+    for (int w = 0; w < 2; ++w)
+      if (set[w]) {
+        cudaGraphExecDestroy(set[w]);
+        set[w] = nullptr;
+      }
 }
 
 // thermostat noise of `steps` steps for every system, drawn as moveTher
@@ -1190,6 +1210,8 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
       cudaEventCreateWithFlags(&B->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&B->ev_j2, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&B->ev_j3, cudaEventDisableTiming) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&B->sio, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&B->ev_x, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreate(&B->t_beg) != cudaSuccess || cudaEventCreate(&B->t_end) != cudaSuccess ||
       cudaMallocHost(&B->h_noise, sizeof(double) * kNoiseChunk * nsys * 4) != cudaSuccess ||
       cudaMallocHost(&B->h_obs, sizeof(SysObs) * nsys) != cudaSuccess) {
@@ -1280,6 +1302,8 @@ mdsc_status mdsc_destroy(mdsc_batch* B) {
   if (B->st) cudaStreamSynchronize(B->st);
   for (auto& g : B->graph)
     if (g) cudaGraphExecDestroy(g);
+  for (auto& g : B->graph_io)
+    if (g) cudaGraphExecDestroy(g);
   if (B->arena) cudaFree(B->arena);
   if (B->b.ecand) cudaFree(B->b.ecand);
   if (B->b.ecnt) cudaFree(B->b.ecnt);
@@ -1289,6 +1313,8 @@ mdsc_status mdsc_destroy(mdsc_batch* B) {
   if (B->ev_fork) cudaEventDestroy(B->ev_fork);
   if (B->ev_j2) cudaEventDestroy(B->ev_j2);
   if (B->ev_j3) cudaEventDestroy(B->ev_j3);
+  if (B->ev_x) cudaEventDestroy(B->ev_x);
+  if (B->sio) cudaStreamDestroy(B->sio);
   if (B->t_beg) cudaEventDestroy(B->t_beg);
   if (B->t_end) cudaEventDestroy(B->t_end);
   if (B->st) cudaStreamDestroy(B->st);
@@ -1455,27 +1481,22 @@ mdsc_status mdsc_upload_all(mdsc_batch* B, const mdsc_host_state* h) {
     CU(cudaStreamSynchronize(B->st));
     return MDSC_OK;
   }
-  // state only: one copy per array for the whole batch, the arrays spread
-  // over the batch's three streams so that several copy engines share the
-  // host link, joined back into the main stream
+  // state only: one copy per array for the whole batch, one after another on
+  // the main stream.  Each copy runs at the host link's rate (~205 GB/s to
+  // the device on this GB300); spreading the arrays over several streams
+  // made the copies share the link and the whole no faster (the same e2e
+  // within 1%, 175 GB/s for 4 concurrent copies against 207 for one)
   const size_t n = B->lo.ntot;
   Batch& b = B->b;
   const bool forces = h->F && h->T;
-  CU(cudaEventRecord(B->ev_fork, B->st));
-  CU(cudaStreamWaitEvent(B->s2, B->ev_fork, 0));
-  CU(cudaStreamWaitEvent(B->s3, B->ev_fork, 0));
   CU(cudaMemcpyAsync(b.O, h->O, sizeof(double) * 9 * n, cudaMemcpyHostToDevice, B->st));
-  CU(cudaMemcpyAsync(b.r, h->r, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->s2));
-  CU(cudaMemcpyAsync(b.p, h->p, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->s2));
-  CU(cudaMemcpyAsync(b.l, h->l, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->s3));
+  CU(cudaMemcpyAsync(b.r, h->r, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->st));
+  CU(cudaMemcpyAsync(b.p, h->p, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->st));
+  CU(cudaMemcpyAsync(b.l, h->l, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->st));
   if (forces) {
-    CU(cudaMemcpyAsync(b.F, h->F, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->s2));
-    CU(cudaMemcpyAsync(b.T, h->T, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->s3));
+    CU(cudaMemcpyAsync(b.F, h->F, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->st));
+    CU(cudaMemcpyAsync(b.T, h->T, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, B->st));
   }
-  CU(cudaEventRecord(B->ev_j2, B->s2));
-  CU(cudaEventRecord(B->ev_j3, B->s3));
-  CU(cudaStreamWaitEvent(B->st, B->ev_j2, 0));
-  CU(cudaStreamWaitEvent(B->st, B->ev_j3, 0));
   for (int s = 0; s < B->nsys; ++s) B->have_forces[s] = forces ? 1 : 0;
   return MDSC_OK;
 }
@@ -1483,21 +1504,17 @@ mdsc_status mdsc_upload_all(mdsc_batch* B, const mdsc_host_state* h) {
 static mdsc_status download_range(mdsc_batch* B, int i0, int n, int s_first, int s_last,
                                   mdsc_host_state* h) {
   Batch& b = B->b;
-  // after the main stream's work, the arrays spread over the three streams
-  CU(cudaEventRecord(B->ev_fork, B->st));
-  CU(cudaStreamWaitEvent(B->s2, B->ev_fork, 0));
-  CU(cudaStreamWaitEvent(B->s3, B->ev_fork, 0));
-  auto dn = [&](void* dst, const void* src, size_t bytes, cudaStream_t st) -> cudaError_t {
-    return (dst && bytes) ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st) : cudaSuccess;
+  // after the main stream's work, one copy per array on that stream (as
+  // the uploads: concurrent copies share the host link)
+  auto dn = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+    return (dst && bytes) ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, B->st) : cudaSuccess;
   };
-  CU(dn(h->O, b.O + 9 * i0, sizeof(double) * 9 * n, B->st));
-  CU(dn(h->r, b.r + 3 * i0, sizeof(double) * 3 * n, B->s2));
-  CU(dn(h->p, b.p + 3 * i0, sizeof(double) * 3 * n, B->s2));
-  CU(dn(h->F, b.F + 3 * i0, sizeof(double) * 3 * n, B->s2));
-  CU(dn(h->l, b.l + 3 * i0, sizeof(double) * 3 * n, B->s3));
-  CU(dn(h->T, b.T + 3 * i0, sizeof(double) * 3 * n, B->s3));
-  CU(cudaStreamSynchronize(B->s2));
-  CU(cudaStreamSynchronize(B->s3));
+  CU(dn(h->O, b.O + 9 * i0, sizeof(double) * 9 * n));
+  CU(dn(h->r, b.r + 3 * i0, sizeof(double) * 3 * n));
+  CU(dn(h->p, b.p + 3 * i0, sizeof(double) * 3 * n));
+  CU(dn(h->F, b.F + 3 * i0, sizeof(double) * 3 * n));
+  CU(dn(h->l, b.l + 3 * i0, sizeof(double) * 3 * n));
+  CU(dn(h->T, b.T + 3 * i0, sizeof(double) * 3 * n));
   CU(cudaStreamSynchronize(B->st));
   if (h->clust) {
     int off = 0;
@@ -2173,7 +2190,10 @@ mdsc_status mdsc_transfer_many(mdsc_batch* D, mdsc_batch* S, const int* dsys, co
 // nsteps steps; trace (nsteps x nsys, may be NULL) gets every step's
 // observables: a copy of the device observables after each graph launch into
 // pinned staging, converted after the chunk
-static mdsc_status run_steps(mdsc_batch* B, int nsteps, mdsc_observables* trace) {
+// out (mdsc_step_io): the host state the last step's results go to, the
+// positions and orientations while that step's forces are computed
+static mdsc_status run_steps(mdsc_batch* B, int nsteps, mdsc_observables* trace,
+                             const mdsc_host_state* out = nullptr) {
   mdsc_status st = ensure_forces(B);
   if (st) return st;
   if (!B->tuned && !B->graph[0]) {
@@ -2189,6 +2209,11 @@ static mdsc_status run_steps(mdsc_batch* B, int nsteps, mdsc_observables* trace)
   for (int w = 0; w < 2; ++w)
     if (!B->graph[w]) {
       st = capture_step(B, w);
+      if (st) return st;
+    }
+  for (int w = 0; out && w < 2; ++w)
+    if (!B->graph_io[w]) {
+      st = capture_step(B, w, true);
       if (st) return st;
     }
   if (trace && !B->h_trace) CU(cudaMallocHost(&B->h_trace, sizeof(SysObs) * kNoiseChunk * B->nsys));
@@ -2213,12 +2238,34 @@ static mdsc_status run_steps(mdsc_batch* B, int nsteps, mdsc_observables* trace)
                        cudaMemcpyHostToDevice, B->st));
     launch_reset_iter(B->b, B->st);
     for (int k = 0; k < chunk; ++k) {
-      CU(cudaGraphLaunch(B->graph[which], B->st));
+      const bool io = out && done + k == nsteps - 1;
+      CU(cudaGraphLaunch(io ? B->graph_io[which] : B->graph[which], B->st));
+      if (io) {
+        // r and O are final after the first half-step (moveX; renorm every
+        // 100 steps before it): they go home while the forces are computed
+        const size_t n = B->lo.ntot;
+        CU(cudaStreamWaitEvent(B->sio, B->ev_x, 0));
+        if (out->r) CU(cudaMemcpyAsync(out->r, B->b.r, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, B->sio));
+        if (out->O) CU(cudaMemcpyAsync(out->O, B->b.O, sizeof(double) * 9 * n, cudaMemcpyDeviceToHost, B->sio));
+      }
       if (trace)
         CU(cudaMemcpyAsync(B->h_trace + (size_t)k * B->nsys, B->b.obs, sizeof(SysObs) * B->nsys,
                            cudaMemcpyDeviceToHost, B->st));
     }
     CU(cudaEventRecord(B->t_end, B->st));
+    if (out && done + chunk == nsteps) {
+      // the last step's momenta, angular momenta, forces and torques (the
+      // force assembly writing them into mapped host memory itself made the
+      // end-to-end step 11% slower: small remote writes, not a copy engine)
+      const size_t n = B->lo.ntot;
+      auto dn = [&](double* dst, const double* src) -> cudaError_t {
+        return dst ? cudaMemcpyAsync(dst, src, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, B->st) : cudaSuccess;
+      };
+      CU(dn(out->p, B->b.p));
+      CU(dn(out->l, B->b.l));
+      CU(dn(out->F, B->b.F));
+      CU(dn(out->T, B->b.T));
+    }
     {
       CU(cudaEventSynchronize(B->t_end));
       float t = 0.f;
@@ -2259,6 +2306,35 @@ mdsc_status mdsc_step(mdsc_batch* B, int nsteps, mdsc_observables* obs) {
   return read_obs(B, obs);
 }
 
+mdsc_status mdsc_step_io(mdsc_batch* B, const mdsc_host_state* in, int nsteps, mdsc_host_state* out,
+                         mdsc_observables* obs) {
+  if (!B || nsteps < 0) return MDSC_ERR_BAD_ARG;
+  cudaSetDevice(B->device);
+  mdsc_status st = MDSC_OK;
+  if (in) {
+    st = mdsc_upload_all(B, in);
+    if (st) return st;
+  }
+  if (nsteps == 0) {
+    if (out) st = mdsc_download_all(B, out);
+    return st ? st : read_obs(B, obs);
+  }
+  st = run_steps(B, nsteps, nullptr, out);
+  if (st) return st;
+  if (out) {
+    CU(cudaStreamSynchronize(B->sio));
+    CU(cudaStreamSynchronize(B->st));
+    if (out->clust) {
+      int off = 0;
+      for (int s = 0; s < B->nsys; ++s) {
+        std::copy(B->labels[s].begin(), B->labels[s].end(), out->clust + off);
+        off += (int)B->labels[s].size();
+      }
+    }
+  }
+  return read_obs(B, obs);
+}
+
 mdsc_status mdsc_step_trace(mdsc_batch* B, int nsteps, mdsc_observables* trace) {
   if (!B || nsteps < 0 || (nsteps > 0 && !trace)) return MDSC_ERR_BAD_ARG;
   cudaSetDevice(B->device);
@@ -2293,11 +2369,7 @@ mdsc_status mdsc_autotune(mdsc_batch* B, int force) {
   const mdsc_status st = autotune(B, force, 5);
   if (st) return st;
   // the step graphs hold the old mappings: capture them again at the next step
-  for (int w = 0; w < 2; ++w)
-    if (B->graph[w]) {
-      cudaGraphExecDestroy(B->graph[w]);
-      B->graph[w] = nullptr;
-    }
+  drop_graphs(B);
   return MDSC_OK;
 }
 
@@ -2315,12 +2387,7 @@ mdsc_status mdsc_set_step_limit(mdsc_batch* B, int sys, long long limit) {
 mdsc_status mdsc_set_list_cells(mdsc_batch* B, int on) {
   if (!B || (on != 0 && on != 1)) return MDSC_ERR_BAD_ARG;
   B->b.cells = on;
-  B->launches = 0;
-  for (int w = 0; w < 2; ++w)
-    if (B->graph[w]) {
-      cudaGraphExecDestroy(B->graph[w]);
-      B->graph[w] = nullptr;
-    }
+  drop_graphs(B);
   return MDSC_OK;
 }
 
@@ -2336,11 +2403,7 @@ mdsc_status mdsc_set_tuning(mdsc_batch* B, const int* values) {
   B->b.tune.wca_blocks = wb;
   B->b.tune.kg_scalar = kg;
   B->tuned = 1;
-  for (int k = 0; k < 2; ++k)
-    if (B->graph[k]) {
-      cudaGraphExecDestroy(B->graph[k]);
-      B->graph[k] = nullptr;
-    }
+  drop_graphs(B);
   return MDSC_OK;
 }
 

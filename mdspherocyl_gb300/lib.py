@@ -35,7 +35,7 @@ EXPORTS = [
     "mdsc_force_dipK", "mdsc_ext_field", "mdsc_self_ener", "mdsc_moveX", "mdsc_moveP",
     "mdsc_renorm", "mdsc_neigh_list", "mdsc_check_list", "mdsc_clust_conf", "mdsc_set_cluster_energy",
     "mdsc_abi_sizes",
-    "mdsc_step",
+    "mdsc_step", "mdsc_step_io",
     "mdsc_observe", "mdsc_launches_per_step", "mdsc_stream", "mdsc_profile_steps",
     "mdsc_place_rods", "mdsc_last_device_ms", "mdsc_force_dipR_noalloc", "mdsc_transfer",
     "mdsc_autotune", "mdsc_tuning", "mdsc_set_tuning", "mdsc_correlation_bins", "mdsc_correlations",
@@ -165,6 +165,7 @@ def load(build: bool = True) -> ctypes.CDLL:
         "mdsc_set_cluster_energy": (c_int, [c_void_p, c_int, c_double]),
         "mdsc_abi_sizes": (None, [P(c_size_t), P(c_size_t), P(c_size_t), P(c_size_t)]),
         "mdsc_step": (c_int, [c_void_p, c_int, P(Observables)]),
+        "mdsc_step_io": (c_int, [c_void_p, P(HostState), c_int, P(HostState), P(Observables)]),
         "mdsc_observe": (c_int, [c_void_p, P(Observables)]),
         "mdsc_launches_per_step": (c_int, [c_void_p]),
         "mdsc_stream": (c_void_p, [c_void_p]),
@@ -324,6 +325,15 @@ class Batch:
     def download_all(self, r, p, O, l, F=None, T=None) -> None:
         hs = self._hoststate(r, p, O, l, F, T)
         self._check(self.lib.mdsc_download_all(self.h, ctypes.byref(hs)), "mdsc_download_all")
+
+    def step_io(self, state_in: dict | None, nsteps: int, state_out: dict | None, obs=None) -> None:
+        """mdsc_step_io: upload state_in (arrays r, p, O, l, F, T for the
+        whole batch; None keeps the device state), take nsteps steps and
+        download into state_out (None: nothing); obs: an Observables array
+        of nsys entries or None."""
+        hi = None if state_in is None else ctypes.byref(self._hoststate(*(state_in.get(k) for k in "rpOlFT")))
+        ho = None if state_out is None else ctypes.byref(self._hoststate(*(state_out.get(k) for k in "rpOlFT")))
+        self._check(self.lib.mdsc_step_io(self.h, hi, int(nsteps), ho, obs), "mdsc_step_io")
 
     def set_thermostat(self, k: int, xi, strn=None) -> None:
         x = np.ascontiguousarray(xi, dtype=np.float64)
