@@ -567,7 +567,9 @@ struct mdsc_batch {
   int2* kowner = nullptr;
   double* noise[2] = {nullptr, nullptr};
   int* d_skip = nullptr;      // per system: skipped by a force evaluation of the others
-  double* h_noise = nullptr;  // pinned
+  double* h_noise = nullptr;  // pinned, the draws of a run of steps (noise buffer 0)
+  double* h_noise2 = nullptr; // the same for noise buffer 1: the host draws a run while the last one's copy runs
+  cudaEvent_t ev_noise[2] = {nullptr, nullptr};  // the last copy out of each
   SysObs* h_obs = nullptr;    // pinned
   SysObs* h_trace = nullptr;  // pinned, kNoiseChunk x nsys: per-step observables of mdsc_step_trace
   char* arena = nullptr;
@@ -799,8 +801,7 @@ void drop_graphs(mdsc_batch* B) {
 // thermostat noise of `steps` steps for every system, drawn as moveTher
 // mode 0 draws it (v25/functions.cpp:2194-2197): two uniforms per
 // thermostat, Box-Muller, first value now, second stored for mode 2
-void draw_noise(mdsc_batch* B, int steps) {
-  double* h = B->h_noise;
+void draw_noise(mdsc_batch* B, int steps, double* h) {
   for (int k = 0; k < steps; ++k)
     for (int s = 0; s < B->nsys; ++s) {
       if (B->step_h[s] + k >= B->stop_h[s]) continue;  // at its step limit: no step, no draw
@@ -909,9 +910,8 @@ void convert_obs(const SysObs& o, int n, int n_clusters, mdsc_observables& r) {
   order_params(o.osum, n, &r.G1, &r.G2, r.M);
 }
 
-mdsc_status read_obs(mdsc_batch* B, mdsc_observables* out) {
-  CU(cudaMemcpyAsync(B->h_obs, B->b.obs, sizeof(SysObs) * B->nsys, cudaMemcpyDeviceToHost, B->st));
-  CU(cudaStreamSynchronize(B->st));
+// the observables copied to h_obs, to the caller's form and status
+mdsc_status finish_obs(mdsc_batch* B, mdsc_observables* out) {
   int bits = 0;
   for (int s = 0; s < B->nsys; ++s) {
     bits |= B->h_obs[s].status;
@@ -920,6 +920,12 @@ mdsc_status read_obs(mdsc_batch* B, mdsc_observables* out) {
   const mdsc_status st = status_from_bits(bits);
   if (st != MDSC_OK) return fail(B, st, "a system reported an error (see mdsc_observables.status)");
   return MDSC_OK;
+}
+
+mdsc_status read_obs(mdsc_batch* B, mdsc_observables* out) {
+  CU(cudaMemcpyAsync(B->h_obs, B->b.obs, sizeof(SysObs) * B->nsys, cudaMemcpyDeviceToHost, B->st));
+  CU(cudaStreamSynchronize(B->st));
+  return finish_obs(B, out);
 }
 
 mdsc_status ensure_forces(mdsc_batch* B) {
@@ -1214,6 +1220,9 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
       cudaEventCreateWithFlags(&B->ev_x, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreate(&B->t_beg) != cudaSuccess || cudaEventCreate(&B->t_end) != cudaSuccess ||
       cudaMallocHost(&B->h_noise, sizeof(double) * kNoiseChunk * nsys * 4) != cudaSuccess ||
+      cudaMallocHost(&B->h_noise2, sizeof(double) * kNoiseChunk * nsys * 4) != cudaSuccess ||
+      cudaEventCreateWithFlags(&B->ev_noise[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&B->ev_noise[1], cudaEventDisableTiming) != cudaSuccess ||
       cudaMallocHost(&B->h_obs, sizeof(SysObs) * nsys) != cudaSuccess) {
     mdsc_destroy(B);
     return MDSC_ERR_CUDA;
@@ -1308,6 +1317,9 @@ mdsc_status mdsc_destroy(mdsc_batch* B) {
   if (B->b.ecand) cudaFree(B->b.ecand);
   if (B->b.ecnt) cudaFree(B->b.ecnt);
   if (B->h_noise) cudaFreeHost(B->h_noise);
+  if (B->h_noise2) cudaFreeHost(B->h_noise2);
+  for (cudaEvent_t e : B->ev_noise)
+    if (e) cudaEventDestroy(e);
   if (B->h_obs) cudaFreeHost(B->h_obs);
   if (B->h_trace) cudaFreeHost(B->h_trace);
   if (B->ev_fork) cudaEventDestroy(B->ev_fork);
@@ -2230,12 +2242,15 @@ static mdsc_status run_steps(mdsc_batch* B, int nsteps, mdsc_observables* trace,
       const long long next = ((k0 + fr - 1) / fr) * fr;  // first k >= k0 with k % fr == 0
       chunk = (int)std::min<long long>(chunk, next - k0 + 1);
     }
-    // noise for this chunk; the other buffer may still be read by the GPU
-    CU(cudaStreamSynchronize(B->st));
-    draw_noise(B, chunk);
+    // noise for this chunk, into the host buffer of this noise buffer once
+    // its last copy has gone (no wait for the GPU's other work: an upload or
+    // the last chunk's steps run meanwhile)
+    double* hn = which ? B->h_noise2 : B->h_noise;
+    CU(cudaEventSynchronize(B->ev_noise[which]));
+    draw_noise(B, chunk, hn);
     CU(cudaEventRecord(B->t_beg, B->st));
-    CU(cudaMemcpyAsync(B->noise[which], B->h_noise, sizeof(double) * chunk * B->nsys * 4,
-                       cudaMemcpyHostToDevice, B->st));
+    CU(cudaMemcpyAsync(B->noise[which], hn, sizeof(double) * chunk * B->nsys * 4, cudaMemcpyHostToDevice, B->st));
+    CU(cudaEventRecord(B->ev_noise[which], B->st));
     launch_reset_iter(B->b, B->st);
     for (int k = 0; k < chunk; ++k) {
       const bool io = out && done + k == nsteps - 1;
@@ -2321,9 +2336,11 @@ mdsc_status mdsc_step_io(mdsc_batch* B, const mdsc_host_state* in, int nsteps, m
   }
   st = run_steps(B, nsteps, nullptr, out);
   if (st) return st;
+  // the observables behind the state on the same stream, one wait for both
+  CU(cudaMemcpyAsync(B->h_obs, B->b.obs, sizeof(SysObs) * B->nsys, cudaMemcpyDeviceToHost, B->st));
+  CU(cudaStreamSynchronize(B->sio));
+  CU(cudaStreamSynchronize(B->st));
   if (out) {
-    CU(cudaStreamSynchronize(B->sio));
-    CU(cudaStreamSynchronize(B->st));
     if (out->clust) {
       int off = 0;
       for (int s = 0; s < B->nsys; ++s) {
@@ -2332,7 +2349,7 @@ mdsc_status mdsc_step_io(mdsc_batch* B, const mdsc_host_state* in, int nsteps, m
       }
     }
   }
-  return read_obs(B, obs);
+  return finish_obs(B, obs);
 }
 
 mdsc_status mdsc_step_trace(mdsc_batch* B, int nsteps, mdsc_observables* trace) {
@@ -2441,7 +2458,8 @@ mdsc_status mdsc_profile_steps(mdsc_batch* B, int nsteps, int max_kernels, char*
   std::vector<cudaEvent_t> ev(nk + 1);
   for (auto& e : ev) cudaEventCreate(&e);
   std::vector<double> acc(nk, 0.0);
-  draw_noise(B, 1);
+  CU(cudaEventSynchronize(B->ev_noise[0]));
+  draw_noise(B, 1, B->h_noise);
   Batch b = batch_with_noise(B, 0);
   for (int it = 0; it < nsteps; ++it) {
     CU(cudaMemcpyAsync(B->noise[0], B->h_noise, sizeof(double) * B->nsys * 4, cudaMemcpyHostToDevice, B->st));
