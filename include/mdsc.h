@@ -255,7 +255,8 @@ mdsc_status mdsc_step(mdsc_batch* b, int nsteps, mdsc_observables* obs);
    mdsc_download_all; NULL fields are skipped, NULL out downloads nothing).
    Positions and orientations are final once the last step has moved the
    particles, so they travel to the host while that step's forces are
-   computed; momenta, angular momenta, forces and torques follow the step.
+   computed; momenta, angular momenta, forces and torques as soon as its
+   force assembly has written them.
    Observables of the last step go to obs (may be NULL). */
 mdsc_status mdsc_step_io(mdsc_batch* b, const mdsc_host_state* in, int nsteps, mdsc_host_state* out,
                          mdsc_observables* obs);

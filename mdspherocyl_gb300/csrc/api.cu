@@ -560,6 +560,7 @@ struct mdsc_batch {
   // once they are final
   cudaStream_t sio = nullptr;
   cudaEvent_t ev_x = nullptr;
+  cudaEvent_t ev_f = nullptr;  // recorded by the same graph once the force assembly has run
   std::vector<mdsc_system_desc> desc;
   Layout lo;
   Batch b{};
@@ -777,6 +778,7 @@ mdsc_status capture_step(mdsc_batch* B, int which, bool io = false) {
   cudaStreamWaitEvent(B->st, B->ev_j2, 0);
   cudaStreamWaitEvent(B->st, B->ev_j3, 0);
   launch_finalize(b, kMaskAll | kFlagMoveP, B->st);
+  if (io) cudaEventRecordWithFlags(B->ev_f, B->st, cudaEventRecordExternal);
   launch_reduce_obs(b, kRedStep, B->st);
   launches += 2;
   cudaError_t e = cudaStreamEndCapture(B->st, &g);
@@ -1218,6 +1220,7 @@ mdsc_status mdsc_create(const mdsc_system_desc* descs, int nsys, int device, mds
       cudaEventCreateWithFlags(&B->ev_j3, cudaEventDisableTiming) != cudaSuccess ||
       cudaStreamCreateWithFlags(&B->sio, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&B->ev_x, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&B->ev_f, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreate(&B->t_beg) != cudaSuccess || cudaEventCreate(&B->t_end) != cudaSuccess ||
       cudaMallocHost(&B->h_noise, sizeof(double) * kNoiseChunk * nsys * 4) != cudaSuccess ||
       cudaMallocHost(&B->h_noise2, sizeof(double) * kNoiseChunk * nsys * 4) != cudaSuccess ||
@@ -1326,6 +1329,7 @@ mdsc_status mdsc_destroy(mdsc_batch* B) {
   if (B->ev_j2) cudaEventDestroy(B->ev_j2);
   if (B->ev_j3) cudaEventDestroy(B->ev_j3);
   if (B->ev_x) cudaEventDestroy(B->ev_x);
+  if (B->ev_f) cudaEventDestroy(B->ev_f);
   if (B->sio) cudaStreamDestroy(B->sio);
   if (B->t_beg) cudaEventDestroy(B->t_beg);
   if (B->t_end) cudaEventDestroy(B->t_end);
@@ -2257,30 +2261,27 @@ static mdsc_status run_steps(mdsc_batch* B, int nsteps, mdsc_observables* trace,
       CU(cudaGraphLaunch(io ? B->graph_io[which] : B->graph[which], B->st));
       if (io) {
         // r and O are final after the first half-step (moveX; renorm every
-        // 100 steps before it): they go home while the forces are computed
+        // 100 steps before it): they go home while the forces are computed;
+        // p, l, F, T once the force assembly has written them, beside the
+        // per-system sums
         const size_t n = B->lo.ntot;
+        auto dn = [&](double* dst, const double* src, size_t w) -> cudaError_t {
+          return dst ? cudaMemcpyAsync(dst, src, sizeof(double) * w * n, cudaMemcpyDeviceToHost, B->sio) : cudaSuccess;
+        };
         CU(cudaStreamWaitEvent(B->sio, B->ev_x, 0));
-        if (out->r) CU(cudaMemcpyAsync(out->r, B->b.r, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, B->sio));
-        if (out->O) CU(cudaMemcpyAsync(out->O, B->b.O, sizeof(double) * 9 * n, cudaMemcpyDeviceToHost, B->sio));
+        CU(dn(out->r, B->b.r, 3));
+        CU(dn(out->O, B->b.O, 9));
+        CU(cudaStreamWaitEvent(B->sio, B->ev_f, 0));
+        CU(dn(out->p, B->b.p, 3));
+        CU(dn(out->l, B->b.l, 3));
+        CU(dn(out->F, B->b.F, 3));
+        CU(dn(out->T, B->b.T, 3));
       }
       if (trace)
         CU(cudaMemcpyAsync(B->h_trace + (size_t)k * B->nsys, B->b.obs, sizeof(SysObs) * B->nsys,
                            cudaMemcpyDeviceToHost, B->st));
     }
     CU(cudaEventRecord(B->t_end, B->st));
-    if (out && done + chunk == nsteps) {
-      // the last step's momenta, angular momenta, forces and torques (the
-      // force assembly writing them into mapped host memory itself made the
-      // end-to-end step 11% slower: small remote writes, not a copy engine)
-      const size_t n = B->lo.ntot;
-      auto dn = [&](double* dst, const double* src) -> cudaError_t {
-        return dst ? cudaMemcpyAsync(dst, src, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, B->st) : cudaSuccess;
-      };
-      CU(dn(out->p, B->b.p));
-      CU(dn(out->l, B->b.l));
-      CU(dn(out->F, B->b.F));
-      CU(dn(out->T, B->b.T));
-    }
     {
       CU(cudaEventSynchronize(B->t_end));
       float t = 0.f;
