@@ -103,7 +103,10 @@ void k_vectors(const mdsc_system_desc& d, std::vector<int4>& kn) {
         const bool half = nz > 0 || (nz == 0 && ny > 0) || (nz == 0 && ny == 0 && nx > 0);
         if (!half) continue;
         if (d.ksq_max > 0 && nx * nx + ny * ny + nz * nz > d.ksq_max) continue;
-        kn.push_back(make_int4(nx, ny, nz, 0));
+        // w = 1: n is the previous k-vector's n + (1, 0, 0), so the gathers'
+        // phase n . u advances by u_x alone (exactly, modulo 2^32)
+        const bool next = !kn.empty() && kn.back().x == nx - 1 && kn.back().y == ny && kn.back().z == nz;
+        kn.push_back(make_int4(nx, ny, nz, next ? 1 : 0));
       }
 }
 

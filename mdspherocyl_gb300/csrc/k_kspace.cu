@@ -26,13 +26,25 @@
 
 namespace mdsc {
 
-__device__ __forceinline__ void phase_exp(uint32_t ux, uint32_t uy, uint32_t uz, int4 n, float& c,
-                                          float& s) {
-  const uint32_t ph = (uint32_t)n.x * ux + (uint32_t)n.y * uy + (uint32_t)n.z * uz;
+__device__ __forceinline__ void phase_cs(uint32_t ph, float& c, float& s) {
   // (int)ph * 2^-31 * pi: the phase, already reduced to [-pi, pi); the
   // hardware sine/cosine is accurate to ~4e-7 absolute on that range
   const float x = (float)(int32_t)ph * 1.4629180792671596e-09f;
   __sincosf(x, &s, &c);
+}
+__device__ __forceinline__ uint32_t phase_of(uint32_t ux, uint32_t uy, uint32_t uz, int4 n) {
+  return (uint32_t)n.x * ux + (uint32_t)n.y * uy + (uint32_t)n.z * uz;
+}
+__device__ __forceinline__ void phase_exp(uint32_t ux, uint32_t uy, uint32_t uz, int4 n, float& c,
+                                          float& s) {
+  phase_cs(phase_of(ux, uy, uz, n), c, s);
+}
+// the gathers walk their k-vectors in order: where a k-vector is the last
+// one plus (1, 0, 0) (n.w = 1, marked at layout) the phase advances by u_x,
+// the same integer modulo 2^32 as the three products
+__device__ __forceinline__ uint32_t phase_next(uint32_t ph, bool have, uint32_t ux, uint32_t uy, uint32_t uz,
+                                               int4 n) {
+  return (have && n.w) ? ph + ux : phase_of(ux, uy, uz, n);
 }
 
 // grid: one block per (system, particle chunk, k tile); work list kwork.
@@ -336,6 +348,10 @@ __global__ void __launch_bounds__(kPartBlock) kgather_kernel(Batch b) {
 #pragma unroll
     for (int c = 0; c < 6; ++c) fo[d][c] = fc[d][c] = 0.f;
 
+  uint32_t ph[ND];
+#pragma unroll
+  for (int d = 0; d < ND; ++d) ph[d] = 0u;
+  bool have = false;
   for (int k0 = 0; k0 < P.nk; k0 += kKBlock) {
     const int nk = min(kKBlock, P.nk - k0);
     __syncthreads();
@@ -359,12 +375,14 @@ __global__ void __launch_bounds__(kPartBlock) kgather_kernel(Batch b) {
 #pragma unroll
       for (int d = 0; d < ND; ++d) {
         if (d < nd) {
-          phase_exp(ux[d], uy[d], uz[d], n, Ec[d], Es[d]);
+          ph[d] = phase_next(ph[d], have, ux[d], uy[d], uz[d], n);
+          phase_cs(ph[d], Ec[d], Es[d]);
           a[d] = mx[d] * kv.x + my[d] * kv.y + mz[d] * kv.z;
           Sr += a[d] * Ec[d];
           Si -= a[d] * Es[d];
         }
       }
+      have = true;
       // D = conj(val S) - val conj(S_i)
       const float Dr = vS.x - kv.w * Sr;
       const float Di = -vS.y + kv.w * Si;
@@ -477,6 +495,8 @@ __global__ void __launch_bounds__(kPartBlock / 2) kgather1_kernel(Batch b) {
 #pragma unroll
   for (int c = 0; c < 6; ++c) fo[c] = fc[c] = bc(0.f);
 
+  uint32_t ph0 = 0u, ph1 = 0u;
+  bool have = false;  // a phase from the previous k-vector (the first of the range computes its own)
   for (int k0 = kb; k0 < ke; k0 += kKBlock) {
     const int nk = min(kKBlock, ke - k0);
     __syncthreads();
@@ -495,8 +515,11 @@ __global__ void __launch_bounds__(kPartBlock / 2) kgather1_kernel(Batch b) {
       const float4 kv = skv[q];  // kx, ky, kz, val
       const float2 vS = sks[q];  // val * S(k)
       float c0, s0, c1, s1;
-      phase_exp(ux0, uy0, uz0, n, c0, s0);
-      phase_exp(ux1, uy1, uz1, n, c1, s1);
+      ph0 = phase_next(ph0, have, ux0, uy0, uz0, n);
+      ph1 = phase_next(ph1, have, ux1, uy1, uz1, n);
+      have = true;
+      phase_cs(ph0, c0, s0);
+      phase_cs(ph1, c1, s1);
       const float2 c = pk(c0, c1), sn = pk(s0, s1);
       const float2 a = __ffma2_rn(mz, bc(kv.z), __ffma2_rn(my, bc(kv.y), __fmul2_rn(mx, bc(kv.x))));
       const float2 va = __fmul2_rn(bc(kv.w), a);
@@ -578,6 +601,8 @@ __global__ void __launch_bounds__(kPartBlock) kgather1s_kernel(Batch b) {
   float fo[6], fc[6];
 #pragma unroll
   for (int c = 0; c < 6; ++c) fo[c] = fc[c] = 0.f;
+  uint32_t ph = 0u;
+  bool have = false;
   for (int k0 = kb; k0 < ke; k0 += kKBlock) {
     const int nk = min(kKBlock, ke - k0);
     __syncthreads();
@@ -596,7 +621,9 @@ __global__ void __launch_bounds__(kPartBlock) kgather1s_kernel(Batch b) {
       const float4 kv = skv[q];
       const float2 vS = sks[q];
       float c, sn;
-      phase_exp(ux0, uy0, uz0, n, c, sn);
+      ph = phase_next(ph, have, ux0, uy0, uz0, n);
+      have = true;
+      phase_cs(ph, c, sn);
       const float a = __fmaf_rn(mz, kv.z, __fmaf_rn(my, kv.y, __fmul_rn(mx, kv.x)));
       const float va = __fmul_rn(kv.w, a);
       const float Dr = __fmaf_rn(-va, c, vS.x);
