@@ -68,3 +68,28 @@ def test_step_io_equals_upload_step_download(nsteps, pinned):
             for x, y in zip(oa, ob):
                 for key in ("U_ss", "U_dipR", "U_dipK", "K", "step"):
                     assert np.array_equal(np.asarray(x[key]), np.asarray(y[key])), key
+
+
+def test_step_io_without_state_or_steps():
+    """nsteps = 0 moves the state only; no `in` steps the device state; no
+    `out` leaves the host arrays alone."""
+    systems = _mix()
+    specs, states = [s for s, _ in systems], [t for _, t in systems]
+    with L.Batch(specs, states) as a, L.Batch(specs, states) as b:
+        a.step(2)
+        b.step(2)
+        h = _arrays(a)
+        g = {k: np.full_like(v, np.nan) for k, v in h.items()}
+        b.step_io(h, 0, g)  # up and down, no step
+        for k in "rpOlFT":
+            assert np.array_equal(g[k], h[k]), k
+        a.step(3)
+        b.step_io(None, 3, None)  # three steps of the device state
+        b.step_io(None, 0, g)
+        ref = _arrays(a)
+        for k in "rpOlFT":
+            assert np.array_equal(g[k], ref[k]), k
+        keep = {k: v.copy() for k, v in g.items()}
+        b.step_io(None, 1, None)  # no `out`: the host arrays are not written
+        for k in "rpOlFT":
+            assert np.array_equal(g[k], keep[k]), k
