@@ -164,27 +164,26 @@ void table_values(double alpha, int n, double* T) {
   }
 }
 
-void set_pair_consts(SysDev& P) {
-  const double xa = P.alpha * 1.2011224087864498;  // sqrt(log2 e)
-  P.xh = (float)xa;
-  P.xlo = (float)(xa - (double)P.xh);
-  for (int a = 0; a < 3; ++a) {
-    const double h = P.L[a] / 4294967296.0;
-    P.Lhi[a] = (float)h;
-    P.Llo[a] = (float)(h - (double)P.Lhi[a]);
-  }
-}
-
 // One system's table as stored on the device: per entry (A, B, C, dA) and
 // (dB, dC, 0, 0), the differences to the next entry.  rc > 0: the entries
 // beyond the real-space cutoff zeroed (Lh (k + 1) > rc), before the
-// differences are taken.
-std::vector<float4> table_entries(double alpha, int n, double rc) {
+// differences are taken.  scaled: the short table of the analytic tiles,
+// whose pair step measures lengths in units of 1/s (set_real_consts):
+// A / s^3, B / s^5 and C / s^5, in FP64 before rounding.
+std::vector<float4> table_entries(double alpha, int n, double rc, bool scaled) {
   std::vector<double> T(3 * (size_t)(n + 1));
   table_values(alpha, n + 1, T.data());
   if (rc > 0)
     for (int k = 0; k <= n; ++k)
       if (0.5 * (200 * 1.001) * (k + 1) / 32768 > rc) T[3 * (size_t)k] = T[3 * (size_t)k + 1] = T[3 * (size_t)k + 2] = 0.0;
+  if (scaled) {
+    const double s = alpha * 1.2011224087864498, s3 = s * s * s, s5 = s3 * s * s;
+    for (int k = 0; k <= n; ++k) {
+      T[3 * (size_t)k] /= s3;
+      T[3 * (size_t)k + 1] /= s5;
+      T[3 * (size_t)k + 2] /= s5;
+    }
+  }
   std::vector<float4> e(2 * (size_t)n);
   for (int k = 0; k < n; ++k) {
     const double* a = &T[3 * (size_t)k];
@@ -202,7 +201,7 @@ std::vector<float4> table_entries(double alpha, int n, double rc) {
 constexpr size_t kTableCacheBytes = size_t(256) << 20;
 struct TableCache {
   std::mutex mu;
-  std::map<std::tuple<uint64_t, uint64_t, int>, std::pair<std::vector<float4>, uint64_t>> m;  // -> (entries, last use)
+  std::map<std::tuple<uint64_t, uint64_t, int, bool>, std::pair<std::vector<float4>, uint64_t>> m;  // -> (entries, last use)
   uint64_t clock = 0;
   size_t bytes = 0;
 };
@@ -211,17 +210,19 @@ TableCache g_tables;
 void fill_tables(const mdsc_system_desc* descs, Layout& Lo) {
   Lo.rtab.assign(Lo.rtab_n, make_float4(0.f, 0.f, 0.f, 0.f));
   const int nsys = (int)Lo.sys.size();
+  // the analytic tiles' short tables are stored scaled (table_entries)
+  auto scaled = [&](int s) { return !Lo.rp_table && !(descs[s].rc_real > 0); };
   auto key_of = [&](int s) {
     uint64_t a, c;
     memcpy(&a, &descs[s].alpha, 8);
     memcpy(&c, &descs[s].rc_real, 8);
-    return std::make_tuple(a, c, Lo.sys[s].rt_n);
+    return std::make_tuple(a, c, Lo.sys[s].rt_n, scaled(s));
   };
   // systems whose table is not cached: build them on all host threads
   std::vector<int> miss;
   {
     std::lock_guard<std::mutex> g(g_tables.mu);
-    std::map<std::tuple<uint64_t, uint64_t, int>, int> first;
+    std::map<std::tuple<uint64_t, uint64_t, int, bool>, int> first;
     for (int s = 0; s < nsys; ++s) {
       if (Lo.sys[s].rt_n <= 0) continue;
       const auto k = key_of(s);
@@ -240,7 +241,7 @@ void fill_tables(const mdsc_system_desc* descs, Layout& Lo) {
     std::atomic<int> next{0};
     auto work = [&] {
       for (int q; (q = next.fetch_add(1)) < (int)miss.size();)
-        built[q] = table_entries(descs[miss[q]].alpha, Lo.sys[miss[q]].rt_n, descs[miss[q]].rc_real);
+        built[q] = table_entries(descs[miss[q]].alpha, Lo.sys[miss[q]].rt_n, descs[miss[q]].rc_real, scaled(miss[q]));
     };
     std::vector<std::thread> th;
     for (int t = 1; t < nth; ++t) th.emplace_back(work);
@@ -269,7 +270,7 @@ void fill_tables(const mdsc_system_desc* descs, Layout& Lo) {
     if (it != g_tables.m.end()) {
       std::copy(it->second.first.begin(), it->second.first.end(), Lo.rtab.begin() + 2 * (size_t)Lo.sys[s].rt_off);
     } else {  // evicted at once (cache smaller than this batch's tables): build here
-      const std::vector<float4> e = table_entries(descs[s].alpha, Lo.sys[s].rt_n, descs[s].rc_real);
+      const std::vector<float4> e = table_entries(descs[s].alpha, Lo.sys[s].rt_n, descs[s].rc_real, scaled(s));
       std::copy(e.begin(), e.end(), Lo.rtab.begin() + 2 * (size_t)Lo.sys[s].rt_off);
     }
   }
@@ -373,15 +374,7 @@ void make_layout(const mdsc_system_desc* descs, int nsys, Layout& Lo) {
     P.cnoise = std::sqrt(2. * d.temp * d.gamma * d.dt / d.Q);
     P.ntemp3 = 3. * d.n * d.temp;
     P.min_s = d.min_s;
-    P.alphaf = (float)d.alpha;
-    P.alpha2x2 = (float)(2. * d.alpha * d.alpha);
-    P.gpref = (float)(2. * d.alpha / std::sqrt(M_PI));
-    P.alpha4x4 = (float)(4. * d.alpha * d.alpha * d.alpha * d.alpha);
-    P.invLh = (float)(1.0 / kLh);
-    P.halfLh2 = (float)(0.5 * kLh * kLh);
-    P.rmax_table = (float)kTableRmax;
-    P.sixthLh3 = (float)(kLh * kLh * kLh / 6.0);
-    set_pair_consts(P);
+    set_real_consts(P, kLh);
     // the reference's interpolation table (tabul, v25/functions.cpp:1680-1704)
     // in FP64 as tabul computes it, stored as FP32 values and differences to
     // the next entry: over the distances the box can hold for the neighbour

@@ -115,15 +115,27 @@ constexpr double kInvLhD = 32768.0 / (0.5 * (200 * 1.001));
 constexpr float kInvLhHi = (float)kInvLhD;
 constexpr float kInvLhLo = (float)(kInvLhD - (double)kInvLhHi);
 
-// per-system constants, the same value in both halves
+// The analytic form in units of 1/s, s = alpha sqrt(log2 e) (lengths r~ =
+// s r, x = alpha r = r~ / sqrt(log2 e)): exp(-x^2) = 2^(-r~^2), and with
+// g = 2 / sqrt(pi log2 e) and E = exp(-x^2)
+//   A = s^3 (erfc(x)/r~^3 + g E/r~^2),  B = s^5 (3 A~ + (2g/log2 e) E)/r~^2,
+//   C = s^5 (4g/log2 e^2) E,  2 alpha^2 = s^2 (2/log2 e)
+// so the pair step holds no per-system factor but the length unit; the
+// tile's sums go back to length units once, at its end.
+constexpr float kHalfX = 0.41627730557884884f;  // 1 / (2 sqrt(log2 e)): x / 2 = kHalfX r~
+constexpr float kGq = 0.9394372786996514f;      // g
+constexpr float kGB = 1.3023366020871419f;      // 2 g / log2 e
+constexpr float kGC = 1.8054218877534436f;      // 4 g / log2 e^2
+constexpr float kGC2 = 2.502846182435027f;      // 8 g / log2 e^3
+constexpr float kA2 = 1.3862943611198906f;      // 2 / log2 e
+
+// per-system constants, the same value in both halves; lengths in the
+// step's unit (1/s for the analytic form, 1 for the table forms)
 struct PairConst {
-  f2 xh, xlo;    // alpha sqrt(log2 e) as a float-float pair: 2^(-(x r)^2) = exp(-alpha^2 r^2)
-  f2 ahalf;      // alpha / 2
-  f2 gpref;      // 2 alpha / sqrt(pi)
-  f2 a2, a4x4;   // 2 alpha^2, 4 alpha^4
-  f2 invLh, halfLh2, nsixthLh3;
-  f2 Lhx, Lhy, Lhz, Llx, Lly, Llz;  // L / 2^32 per axis as float-float pairs
-  f2 ihh, ihl;                      // 1 / Lh as a float-float pair
+  f2 invLh, halfLh2;                // 1 / Lh and Lh^2 / 2
+  f2 Lhx, Lhy, Lhz, Llx, Lly, Llz;  // the fixed-point unit per axis as float-float pairs
+  f2 ihh, ihl;                      // 1 / Lh as a float-float pair (table index)
+  float rnear;                      // kNearTab
   const float4* tab;                // the system's table entries in global memory (MODE 1)
   const float4* stab;               // its values in shared memory (MODE 2): A, B, C, A' - A per entry
   int tn;                           // its number of entries
@@ -212,13 +224,11 @@ __device__ __forceinline__ void tile_step(const PairConst& K, Lane2& s, const ui
     Bc = fma2(fr, make_float2(q0.x, q1.x), make_float2(p0.y, p1.y));
     Cc = fma2(fr, make_float2(q0.y, q1.y), make_float2(p0.z, p1.z));
   } else {
-    // exp(-x^2) and erfc(x), x = alpha r; the exponent from a once-rounded
-    // product (x up to ~5 puts it near -40, where a biased constant would
-    // shift every far pair's weight alike)
-    const f2 xr = fma2(r, K.xh, mul2(r, K.xlo));
-    const f2 y = mul2(xr, xr);
-    const f2 ex = make_float2(ex2_approx(-y.x), ex2_approx(-y.y));
-    const f2 den = fma2(r, K.ahalf, b2(1.f));
+    // exp(-x^2) = 2^(-r~^2) and erfc(x) (lengths in units of 1/s: the
+    // exponent is the squared distance itself, with no rounded constant
+    // that would shift every far pair's weight alike)
+    const f2 ex = make_float2(ex2_approx(-r2.x), ex2_approx(-r2.y));
+    const f2 den = fma2(r, b2(kHalfX), b2(1.f));
     const f2 tt = make_float2(rcp_approx(den.x), rcp_approx(den.y));
     f2 q = fma2(b2(kQ9), tt, b2(kQ8));
     q = fma2(q, tt, b2(kQ7));
@@ -229,30 +239,31 @@ __device__ __forceinline__ void tile_step(const PairConst& K, Lane2& s, const ui
     q = fma2(q, tt, b2(kQ2));
     q = fma2(q, tt, b2(kQ1));
     q = fma2(q, tt, b2(kQ0));
-    const f2 E = mul2(mul2(ex, tt), q);
-    const f2 G = mul2(ex, K.gpref);
-    // A = erfc/r^3 + G/r^2, B = (3 A + 2 alpha^2 G) / r^2, C = 4 alpha^4 G
-    const f2 A = mul2(fma2(E, rinv, G), rinv2);
-    const f2 B = mul2(fma2(b2(3.f), A, mul2(K.a2, G)), rinv2);
-    const f2 C = mul2(G, K.a4x4);
+    // A~ = E (t Q(t) / r~ + g) / r~^2, B~ = (3 A~ + (2g/log2 e) E) / r~^2,
+    // C~ = (4g/log2 e^2) E
+    const f2 A = mul2(mul2(ex, fma2(mul2(tt, q), rinv, b2(kGq))), rinv2);
+    const f2 B = mul2(fma2(b2(3.f), A, mul2(b2(kGB), ex)), rinv2);
+    const f2 C = mul2(b2(kGC), ex);
 
     // the table's linear-interpolation error to second order, (ab/2) f''(r)
     // with a = r - r0, b = r1 - r (the third-order term is below 3e-7 of
-    // each value at r >= 0.8 for alpha <= 0.55)
+    // each value at r >= 0.8 for alpha <= 0.55); in the step's units
+    // 2 alpha^2 is kA2 and 2 alpha^2 C is kGC2 E
     const f2 uu = mul2(r, K.invLh);
     const f2 fr = sub2(uu, make_float2(floorf(uu.x), floorf(uu.y)));
     const f2 hh = mul2(fma2(neg2(fr), fr, fr), K.halfLh2);
-    const f2 a2C = mul2(K.a2, C);
+    const f2 a2C = mul2(b2(kGC2), ex);
     Ac = fma2(hh, fma2(b2(4.f), B, C), A);
     Bc = fma2(hh, fma2(mul2(b2(6.f), fma2(b2(5.f), B, C)), rinv2, a2C), B);
-    Cc = fma2(hh, mul2(a2C, fma2(K.a2, r2, b2(-1.f))), C);
+    Cc = fma2(hh, mul2(a2C, fma2(b2(kA2), r2, b2(-1.f))), C);
     // near contact (r < kNearTab) the pair terms are largest, and the
     // rounding of the FP32 erfc chain (a few ulp, against one for a table
     // entry) would dominate the error of energy sums that cancel between
     // pairs: such pairs interpolate in the system's short table, as the
     // reference does.  A warp takes the lookups only when one of its pairs
-    // is that close, and only those lanes load.
-    const bool nr0 = a0 && r.x < kNearTab, nr1 = a1 && r.y < kNearTab;
+    // is that close, and only those lanes load.  The short table holds A /
+    // s^3, B / s^5, C / s^5 (the step's units); r / Lh is r~ / (s Lh).
+    const bool nr0 = a0 && r.x < K.rnear, nr1 = a1 && r.y < K.rnear;
     if (K.tab != nullptr && __any_sync(0xffffffffu, nr0 || nr1)) {
       const f2 ut = fma2(r, K.ihh, mul2(r, K.ihl));
       const float fl0 = floorf(ut.x), fl1 = floorf(ut.y);
@@ -405,32 +416,37 @@ __device__ __forceinline__ void diag_loop(const PairConst& K, Lane2& s, const ui
 
 }  // namespace
 
-// per-system constants of the pair step
+// per-system constants of the pair step: lengths in units of 1/s for the
+// analytic form, in length units for the table forms
 __device__ __forceinline__ PairConst pair_consts(const Batch& b, const SysDev& P, int mode, const float4* stab) {
   PairConst K;
-  K.xh = b2(P.xh);
-  K.xlo = b2(P.xlo);
-  K.Lhx = b2(P.Lhi[0]);
-  K.Llx = b2(P.Llo[0]);
-  K.Lhy = b2(P.Lhi[1]);
-  K.Lly = b2(P.Llo[1]);
-  K.Lhz = b2(P.Lhi[2]);
-  K.Llz = b2(P.Llo[2]);
-  K.ahalf = b2(0.5f * P.alphaf);
-  K.gpref = b2(P.gpref);
-  K.a2 = b2(P.alpha2x2);
-  K.a4x4 = b2(P.alpha4x4);
-  K.invLh = b2(P.invLh);
-  K.ihh = b2(kInvLhHi);
-  K.ihl = b2(kInvLhLo);
+  const bool an = (mode == kAnalytic);
+  K.Lhx = b2(an ? P.Shi[0] : P.Lhi[0]);
+  K.Llx = b2(an ? P.Slo[0] : P.Llo[0]);
+  K.Lhy = b2(an ? P.Shi[1] : P.Lhi[1]);
+  K.Lly = b2(an ? P.Slo[1] : P.Llo[1]);
+  K.Lhz = b2(an ? P.Shi[2] : P.Lhi[2]);
+  K.Llz = b2(an ? P.Slo[2] : P.Llo[2]);
+  K.invLh = b2(P.sihh);
+  K.halfLh2 = b2(P.shalfLh2);
+  K.ihh = b2(an ? P.sihh : kInvLhHi);
+  K.ihl = b2(an ? P.sihl : kInvLhLo);
+  K.rnear = P.snear;
   K.tab = (mode == kTabGlobal || mode == kAnalytic) && b.rtab != nullptr && P.rt_n > 0
               ? b.rtab + 2 * (long long)P.rt_off
               : nullptr;
   K.stab = stab;
   K.tn = P.rt_n;
-  K.halfLh2 = b2(P.halfLh2);
-  K.nsixthLh3 = b2(-P.sixthLh3);
   return K;
+}
+
+// A tile's sum back to length units: the analytic form's forces by s^4 and
+// its fields, torques, energy and pressure tensor by s^3 (float-float
+// factors); the table forms' sums are in length units already.
+template <int MODE>
+__device__ __forceinline__ float to_len(float v, const float* sc) {
+  if (MODE != kAnalytic) return v;
+  return fmaf(v, sc[0], v * sc[1]);
 }
 
 // One tile (strips I <= J of one system) by one warp: the j-strip staged in
@@ -523,8 +539,8 @@ __device__ __forceinline__ void tile_work(const Batch& b, int tile, const PairCo
     tv[2] = mx * ev[1] - my * ev[0];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      base_ij[c * kTile + li] = fv[c];
-      base_ij[(3 + c) * kTile + li] = tv[c];
+      base_ij[c * kTile + li] = to_len<MODE>(fv[c], P.sc4);
+      base_ij[(3 + c) * kTile + li] = to_len<MODE>(tv[c], P.sc3);
     }
   }
   if (!diag) {
@@ -532,12 +548,12 @@ __device__ __forceinline__ void tile_work(const Batch& b, int tile, const PairCo
       const float4 a4 = sa4[k];
       const float2 a2 = sa2[k];
       const float4 mj = smj[k];
-      base_ji[0 * kTile + k] = a4.x;
-      base_ji[1 * kTile + k] = a4.y;
-      base_ji[2 * kTile + k] = a4.z;
-      base_ji[3 * kTile + k] = mj.y * a2.y - mj.z * a2.x;
-      base_ji[4 * kTile + k] = mj.z * a4.w - mj.x * a2.y;
-      base_ji[5 * kTile + k] = mj.x * a2.x - mj.y * a4.w;
+      base_ji[0 * kTile + k] = to_len<MODE>(a4.x, P.sc4);
+      base_ji[1 * kTile + k] = to_len<MODE>(a4.y, P.sc4);
+      base_ji[2 * kTile + k] = to_len<MODE>(a4.z, P.sc4);
+      base_ji[3 * kTile + k] = to_len<MODE>(mj.y * a2.y - mj.z * a2.x, P.sc3);
+      base_ji[4 * kTile + k] = to_len<MODE>(mj.z * a4.w - mj.x * a2.y, P.sc3);
+      base_ji[5 * kTile + k] = to_len<MODE>(mj.x * a2.x - mj.y * a4.w, P.sc3);
     }
   }
   // tile energy and pressure tensor
@@ -552,7 +568,7 @@ __device__ __forceinline__ void tile_work(const Batch& b, int tile, const PairCo
   }
   if (lane == 0) {
 #pragma unroll
-    for (int c = 0; c < 10; ++c) b.tileE[(long long)tile * 10 + c] = red[c];
+    for (int c = 0; c < 10; ++c) b.tileE[(long long)tile * 10 + c] = to_len<MODE>(red[c], P.sc3);
   }
 }
 
@@ -663,26 +679,7 @@ __global__ void __launch_bounds__(kPartBlock * kCutLanes) near_pass_kernel(Batch
   const int np = min(kPartBlock, P.n - p0);
   const int ND = b.ndtot;
   const int lane = threadIdx.x % kCutLanes;
-  PairConst K;
-  K.xh = b2(P.xh);
-  K.xlo = b2(P.xlo);
-  K.Lhx = b2(P.Lhi[0]);
-  K.Llx = b2(P.Llo[0]);
-  K.Lhy = b2(P.Lhi[1]);
-  K.Lly = b2(P.Llo[1]);
-  K.Lhz = b2(P.Lhi[2]);
-  K.Llz = b2(P.Llo[2]);
-  K.ahalf = b2(0.5f * P.alphaf);
-  K.gpref = b2(P.gpref);
-  K.a2 = b2(P.alpha2x2);
-  K.a4x4 = b2(P.alpha4x4);
-  K.invLh = b2(P.invLh);
-  K.ihh = b2(kInvLhHi);
-  K.ihl = b2(kInvLhLo);
-  K.tab = b.rtab + 2 * (long long)P.rt_off;
-  K.tn = P.rt_n;
-  K.halfLh2 = b2(P.halfLh2);
-  K.nsixthLh3 = b2(-P.sixthLh3);
+  const PairConst K = pair_consts(b, P, kTabGlobal, nullptr);
   FF e[10];
 #pragma unroll
   for (int c = 0; c < 10; ++c) e[c] = ff_of(0.f);

@@ -103,16 +103,40 @@ struct SysDev {
   double Uself;
   float Lfix[3];   // L / 2^32: fixed-point units to length
   float Lf[3];
-  // real-space Ewald constants (FP32)
-  float alphaf, alpha2x2;  // alpha, 2 alpha^2
-  float gpref;             // 2 alpha / sqrt(pi)
-  float alpha4x4;          // 4 alpha^4
-  float invLh, halfLh2;    // table spacing of the reference: Lh = 0.5*200.2/32768
-  float rmax_table;        // 100.1: the reference's table covers r <= 100.1
-  float sixthLh3;          // Lh^3 / 6
-  float xh, xlo;           // alpha sqrt(log2 e) as a float-float pair
+  // real-space Ewald constants (FP32; set_real_consts).  The analytic tiles
+  // measure lengths in units of 1/s, s = alpha sqrt(log2 e), where
+  // exp(-alpha^2 r^2) = 2^(-(s r)^2) and every per-system factor of the
+  // pair terms leaves them: A = s^3 A~, B = s^5 B~, C = s^5 C~.
   float Lhi[3], Llo[3];    // L / 2^32 per axis as float-float pairs
+  float Shi[3], Slo[3];    // s L / 2^32 per axis as float-float pairs
+  float sihh, sihl;        // 1 / (s Lh) as a float-float pair, Lh = 0.5*200.2/32768 (the reference's table spacing)
+  float shalfLh2;          // (s Lh)^2 / 2
+  float snear;             // s kNearTab
+  float sc3[2], sc4[2];    // s^3 and s^4 as float-float pairs: fields, energy, pressure tensor and forces to length units
 };
+
+// The real-space constants of a system from its alpha and box (FP64
+// arithmetic, on the host or in a kernel).
+__host__ __device__ inline void set_real_consts(SysDev& P, double Lh) {
+  const double s = P.alpha * 1.2011224087864498;  // alpha sqrt(log2 e)
+  for (int a = 0; a < 3; ++a) {
+    const double h = P.L[a] / 4294967296.0;
+    P.Lhi[a] = (float)h;
+    P.Llo[a] = (float)(h - (double)P.Lhi[a]);
+    P.Shi[a] = (float)(s * h);
+    P.Slo[a] = (float)(s * h - (double)P.Shi[a]);
+  }
+  const double il = 1.0 / (s * Lh);
+  P.sihh = (float)il;
+  P.sihl = (float)(il - (double)P.sihh);
+  P.shalfLh2 = (float)(0.5 * (s * Lh) * (s * Lh));
+  P.snear = (float)(s * (double)kNearTab);
+  const double s3 = s * s * s, s4 = s3 * s;
+  P.sc3[0] = (float)s3;
+  P.sc3[1] = (float)(s3 - (double)P.sc3[0]);
+  P.sc4[0] = (float)s4;
+  P.sc4[1] = (float)(s4 - (double)P.sc4[0]);
+}
 
 // Per-system mutable state.
 struct SysState {

@@ -93,24 +93,7 @@ __global__ void noalloc_prep_kernel(unsigned char* scr, int ndip, const double* 
       d.Lf[a] = (float)L[a];
     }
     d.alpha = alpha;
-    d.alphaf = (float)alpha;
-    d.alpha2x2 = (float)(2. * alpha * alpha);
-    d.gpref = (float)(2. * alpha / sqrt(M_PI));
-    d.alpha4x4 = (float)(4. * alpha * alpha * alpha * alpha);
-    d.invLh = (float)(1.0 / kLh);
-    d.halfLh2 = (float)(0.5 * kLh * kLh);
-    d.sixthLh3 = (float)(kLh * kLh * kLh / 6.0);
-    {
-      const double xa = alpha * 1.2011224087864498;  // sqrt(log2 e)
-      d.xh = (float)xa;
-      d.xlo = (float)(xa - (double)d.xh);
-      for (int a = 0; a < 3; ++a) {
-        const double h = L[a] / 4294967296.0;
-        d.Lhi[a] = (float)h;
-        d.Llo[a] = (float)(h - (double)d.Lhi[a]);
-      }
-    }
-    d.rmax_table = (float)(0.5 * 200 * 1.001);
+    set_real_consts(d, kLh);
     *P = d;
   }
   if (t < ntile) {
