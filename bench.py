@@ -52,11 +52,11 @@ UNIT = "particle-steps/s"
 # pressure tensor 18, accumulation 13 -> ~180, the figure of the survey)
 FLOP_PER_PAIR = 180.0
 # DRAM bytes (read + write) per dipole pair of real_pairs_kernel from one
-# cold-cache ncu capture: 3.744 MB + 0.014 MB over the 47,281,855 pairs of the
+# cold-cache ncu capture: 3.751 MB + 0.003 MB over the 47,281,855 pairs of the
 # 128-replica mix (profiles/real_pairs_replica_mix128.md, the analytic form).
 # The kernel reads each tile's dipoles and writes its partial slots, so its
 # traffic scales with the work a launch processes.
-REAL_PAIRS_DRAM_BYTES_PER_PAIR = 3.758e6 / 47_281_855
+REAL_PAIRS_DRAM_BYTES_PER_PAIR = 3.754e6 / 47_281_855
 
 
 def log(*a):
